@@ -1,0 +1,197 @@
+/* marx_gb300 — GB300-native photon trace for the MARX stage pipeline
+ * (aspect dither -> HRMA mirror -> HETG grating -> ACIS detector).
+ *
+ * C ABI: plain pointers, sizes and POD structs.  Every entry point returns
+ * 0 on success and a negative MX_E* code on failure; mx_last_error() gives
+ * the message.  Nothing aborts or traps across this boundary.
+ *
+ * Reference interfaces this ABI stands in for (paths inside MARX 5.5.3):
+ *   marx_mirror_reflect   marx/libsrc/mirror.c:93   (marx.h:358)
+ *   marx_grating_diffract marx/libsrc/grating.c:88  (marx.h:362)
+ *   marx_detect           marx/libsrc/detector.c:361 (marx.h:355)
+ *   _marx_dither_photons  marx/libsrc/dither.c:630  (_marx.h:142)
+ *   marx_prune_photons    marx/libsrc/photon.c:40   (marx.h:155)
+ * and the *_init(Param_File_Type*) functions beside them, whose parameters
+ * (marx/par/marx.par) are the fields of mx_config.
+ */
+#ifndef MARX_GB300_H
+#define MARX_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ status -- */
+#define MX_OK            0
+#define MX_EINVAL       -1   /* bad argument or configuration */
+#define MX_ENOMEM       -2   /* device or host allocation failed */
+#define MX_ECUDA        -3   /* a CUDA call failed */
+#define MX_EPACK        -4   /* table pack missing or malformed */
+#define MX_ERANGE       -5   /* size beyond a stated limit */
+#define MX_EVARIATE     -6   /* a stage needed more pre-drawn variates than its slots */
+#define MX_EWATCHDOG    -7   /* device-side iteration limit hit; photons flagged */
+
+/* Per-photon flag bits: same values as marx.h:65-75 (PHOTON_*). */
+#define MX_PHOTON_UNDETECTED        0x01u
+#define MX_PHOTON_UNREFLECTED       0x02u
+#define MX_PHOTON_UNDIFFRACTED      0x04u
+#define MX_PHOTON_MISSED_DETECTOR   0x08u
+#define MX_PHOTON_MIRROR_VBLOCKED   0x10u
+#define MX_PHOTON_DRAKE_BLOCKED     0x20u
+#define MX_PHOTON_GRATING_VBLOCKED  0x40u
+#define MX_BAD_PHOTON_MASK          0xFFu
+#define MX_PHOTON_DRAKE_REFLECTED   0x100u
+#define MX_PHOTON_ACIS_STREAKED     0x200u
+/* Engine-only bit: a stage ran out of pre-drawn variate slots. */
+#define MX_PHOTON_VARIATE_OVERRUN   0x10000u
+
+/* Stage mask for mx_trace. */
+#define MX_STAGE_DITHER   0x1u   /* _marx_dither_photons (dither.c:630)   */
+#define MX_STAGE_MIRROR   0x2u   /* marx_mirror_reflect  (mirror.c:93)    */
+#define MX_STAGE_GRATING  0x4u   /* marx_grating_diffract (grating.c:88)  */
+#define MX_STAGE_DETECT   0x8u   /* marx_detect          (detector.c:361) */
+#define MX_STAGE_ALL      0xFu
+
+/* Pre-drawn variate slots per photon.  Each stage reads its uniforms and
+ * normals from a fixed slot range, in the order the reference draws them:
+ *   mirror  U[0..11]: [vignetting] shell radius theta,
+ *                     per optic P then H: [blur phi] [reflectivity] [wfold p, sign]
+ *           N[2..3] : per optic [blur angle]
+ *   grating U[12..13]: vignetting, order;  N[4..5]: dtheta, dP/P
+ *   detect  U[14..15]: [QE] [streak row];  N[6..7]: reserved (pulse height)
+ *   dither  N[0..1]  : aspect blur ra, dec
+ * Slot arrays are slot-major: U[k * n + i] is uniform k of photon i. */
+#define MX_NUM_U 16
+#define MX_NUM_N 8
+#define MX_U_MIRROR   0
+#define MX_U_GRATING 12
+#define MX_U_DETECT  14
+#define MX_N_DITHER   0
+#define MX_N_MIRROR   2
+#define MX_N_GRATING  4
+#define MX_N_DETECT   6
+
+enum { MX_GRATING_NONE = 0, MX_GRATING_HETG = 1 };
+enum { MX_DETECTOR_NONE = 0, MX_DETECTOR_ACIS_I = 1, MX_DETECTOR_ACIS_S = 2 };
+enum { MX_DITHER_NONE = 0, MX_DITHER_INTERNAL = 1 };
+
+/* Simulation parameters.  Names follow marx.par; units are marx.par's. */
+typedef struct mx_config {
+  /* HRMA (hrma.c:244-286) */
+  double hrma_cap_x;          /* HRMA_Cap_X (mm) */
+  double shell_xoffset[4];    /* HRMA_P1H1_XOffset .. P6H6 (mm), shells 1,3,4,6 */
+  double blur_p[4], blur_h[4];/* P1Blur..P6Blur, H1Blur..H6Blur (arcsec) */
+  double scat_p[4], scat_h[4];/* P1ScatFactor.., H1ScatFactor.. */
+  double hrma_vig;            /* HRMAVig */
+  int32_t hrma_ideal;         /* HRMA_Ideal */
+  int32_t use_blur;           /* HRMA_Use_Blur */
+  int32_t use_wfold;          /* HRMA_Use_WFold */
+  int32_t use_struts;         /* HRMA_Use_Struts */
+  int32_t use_scale_factors;  /* HRMA_Use_Scale_Factors */
+  uint32_t shutters[4];       /* Shutters1..6 as open-quadrant bitmaps ("0000" -> 0xF) */
+  double source_distance;     /* Marx_Photon_Type.source_distance (mm, 0 = infinite) */
+  /* Grating (diffract.c:550-614, marx.par HETG_Shell*) */
+  int32_t grating;            /* MX_GRATING_* */
+  int32_t use_sector_files;   /* Use_HETG_Sector_Files */
+  double hetg_theta[4];       /* HETG_Shell{1,3,4,6}_Theta (deg) */
+  double hetg_dtheta[4];      /* HETG_Shell*_dTheta (arcmin, sigma) */
+  double hetg_period[4];      /* HETG_Shell*_Period (um) */
+  double hetg_dpp[4];         /* HETG_Shell*_dPoverP */
+  double hetg_vig[4];         /* HETG_Shell*_Vig */
+  double meg_rowland, heg_rowland; /* MEG/HEGRowlandDiameter (mm) */
+  int32_t max_order;          /* 0: every order in the table; m>0: keep |order|<=m, renormalised */
+  int32_t aperture_area_uniform; /* 0: radius uniform in [rmin,rmax] as hrma.c:1005;
+                                    1: uniform in area over each shell annulus */
+  /* Dither (dither.c:85-110) */
+  int32_t dither;             /* MX_DITHER_* */
+  int32_t reserved1;
+  double dither_amp[3];       /* DitherAmp_RA, _Dec, _Roll (arcsec) */
+  double dither_period[3];    /* DitherPeriod_* (s) */
+  double dither_phase[3];     /* DitherPhase_* (rad) */
+  double roll_nom;            /* Roll_Nom (deg) */
+  double aspect_blur;         /* AspectBlur (arcsec, sigma) */
+  /* Detector (detector.c:45-52, acis-i.c:170-176) */
+  int32_t detector;           /* MX_DETECTOR_* */
+  int32_t det_extend;         /* DetExtendFlag */
+  double det_offset[3];       /* DetOffsetX/Y/Z (mm) */
+  double acis_exposure_time;  /* ACIS_Exposure_Time (s) */
+  double acis_frame_transfer_time; /* ACIS_Frame_Transfer_Time (s) */
+  double focal_length;        /* Marx_Focal_Length (detpix.c:41) (mm) */
+  double start_time;          /* Marx_Photon_Type.start_time (s) */
+} mx_config;
+
+/* Structure-of-arrays photon list.  3-vectors are component-major:
+ * x[0*n + i], x[1*n + i], x[2*n + i].  Which pointers must be set depends
+ * on the stages run; unused outputs may be NULL. */
+typedef struct mx_photons {
+  uint32_t n;
+  uint32_t reserved;
+  double   *energy;        /* keV */
+  double   *x;             /* 3n, mm (output of the mirror) */
+  double   *p;             /* 3n, unit direction (input and output) */
+  double   *arrival_time;  /* s, relative to start_time */
+  uint32_t *flags;         /* MX_PHOTON_* */
+  uint32_t *tag;           /* per-photon generator counter (Philox mode) */
+  int8_t   *mirror_shell;  /* 0..3 */
+  int8_t   *order;         /* grating order */
+  int8_t   *ccd_num;       /* chip id, -1 if missed */
+  int8_t   *reserved8;
+  float    *y_pixel;       /* chip x (0-based) */
+  float    *z_pixel;       /* chip y (0-based) */
+  float    *dither_state;  /* 3n: ra, dec, roll (rad), as Marx_Dither_Type */
+} mx_photons;
+
+/* Pre-drawn variates (device pointers for mx_trace).  When both are NULL
+ * the variates come from Philox4x32-10 keyed by (seed, tag). */
+typedef struct mx_variates {
+  const double *U;         /* MX_NUM_U * n, slot-major, uniforms in [0,1) */
+  const double *N;         /* MX_NUM_N * n, slot-major, unit normals */
+} mx_variates;
+
+typedef struct mx_context mx_context;
+
+/* Defaults = marx.par 5.5 values (HRMA, HETG, INTERNAL dither, ACIS-S). */
+void mx_config_default(mx_config *cfg);
+
+/* Load the table pack (see marx_gb300/caldb/pack.py), derive every model
+ * table for cfg and upload it to the current CUDA device.  Replaces the
+ * marx_mirror_init / marx_grating_init / marx_detector_init / dither init
+ * sequence (mirror.c:48, grating.c:44, detector.c:298, dither.c:508). */
+mx_context *mx_create(const char *pack_path, const mx_config *cfg);
+int  mx_configure(mx_context *ctx, const mx_config *cfg);
+void mx_destroy(mx_context *ctx);
+const char *mx_last_error(const mx_context *ctx);  /* ctx may be NULL */
+
+/* Trace photons in place on the device (pointers in ph are device
+ * pointers).  Stages run back to back per photon inside one fused kernel;
+ * a photon whose flags carry a MX_BAD_PHOTON_MASK bit is left untouched, as
+ * marx_prune_photons leaves it out of sorted_index.  Asynchronous on
+ * stream (a cudaStream_t, NULL = default stream). */
+int mx_trace(mx_context *ctx, const mx_photons *ph, uint32_t stages,
+             const mx_variates *var, uint64_t seed, void *stream);
+
+/* Same trace on HOST buffers: copies inputs to the device, traces and
+ * copies results back; blocks until done. */
+int mx_trace_host(mx_context *ctx, const mx_photons *host, uint32_t stages,
+                  const mx_variates *host_var, uint64_t seed);
+
+/* Survivor compaction (marx_prune_photons, photon.c:40): writes the indices
+ * of photons without MX_BAD_PHOTON_MASK bits to idx_out (device, n entries)
+ * in ascending order and their count to *count_out (host). */
+int mx_compact(mx_context *ctx, const uint32_t *flags, uint32_t n,
+               uint32_t *idx_out, uint32_t *count_out, void *stream);
+
+/* Device table summary, for tests: number of bytes staged per block in
+ * shared memory and resident in global memory. */
+int mx_table_bytes(const mx_context *ctx, size_t *shared_bytes, size_t *global_bytes);
+
+/* Number of kernel launches issued by this context since creation. */
+uint64_t mx_launch_count(const mx_context *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MARX_GB300_H */

@@ -1,0 +1,168 @@
+"""ctypes bindings for the CPU checkers (test infrastructure only)."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from marx_gb300.config import MxConfig, to_par
+from marx_gb300.photons import MxPhotons, PhotonList, NUM_U, NUM_N
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "_build", "libmx_oracle.so")
+REF_SLOTS_SO = os.path.join(HERE, "_ref", "libmxref_slots.so")
+REF_NATIVE_SO = os.path.join(HERE, "_ref", "libmxref_native.so")
+REF_ROOT = os.environ.get("MARX_REFERENCE_ROOT", "/root/reference")
+
+
+def build_port() -> str:
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+    return PORT_SO
+
+
+def reference_available() -> bool:
+    return os.path.isdir(os.path.join(REF_ROOT, "marx", "libsrc"))
+
+
+def build_reference() -> bool:
+    if not reference_available():
+        return False
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_ROOT}"], check=True)
+    return True
+
+
+def _p(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else C.c_void_p(0)
+
+
+class Oracle:
+    """The C++ restatement (oracle/mx_oracle_core.hpp)."""
+
+    def __init__(self, cfg: MxConfig, pack: str | None = None):
+        if not os.path.exists(PORT_SO):
+            build_port()
+        self.lib = C.CDLL(PORT_SO)
+        L = self.lib
+        L.mxo_create.restype = C.c_void_p
+        L.mxo_create.argtypes = [C.c_char_p, C.POINTER(MxConfig)]
+        L.mxo_last_error.restype = C.c_char_p
+        L.mxo_trace.argtypes = [C.c_void_p, C.POINTER(MxPhotons), C.c_uint32, C.c_void_p, C.c_void_p,
+                                C.c_uint64, C.c_int]
+        L.mxo_count_flops.argtypes = [C.c_void_p, C.POINTER(MxPhotons), C.c_uint32, C.c_uint64, C.c_void_p]
+        L.mxo_detector_geometry.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        L.mxo_destroy.argtypes = [C.c_void_p]
+        L.mxo_philox_uniform.restype = C.c_double
+        L.mxo_philox_uniform.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32]
+        L.mxo_philox_normal.restype = C.c_double
+        L.mxo_philox_normal.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32]
+        if pack is None:
+            from marx_gb300.caldb.pack import DEFAULT_PACK
+            pack = DEFAULT_PACK
+        self.cfg = cfg
+        self.h = L.mxo_create(pack.encode(), C.byref(cfg))
+        if not self.h:
+            raise RuntimeError("oracle: " + L.mxo_last_error().decode())
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.mxo_destroy(self.h)
+            self.h = None
+
+    def trace(self, ph: PhotonList, stages: int = 15, U=None, N=None, seed: int = 0, threads: int = 0) -> int:
+        s = ph.struct()
+        r = self.lib.mxo_trace(self.h, C.byref(s), stages, _p(U), _p(N), seed, threads)
+        if r < 0:
+            raise RuntimeError(f"oracle trace failed: {r}")
+        return r
+
+    def count_flops(self, ph: PhotonList, stages: int = 15, seed: int = 0):
+        s = ph.struct()
+        out = np.zeros(2)
+        self.lib.mxo_count_flops(self.h, C.byref(s), stages, seed, _p(out))
+        return out[0], out[1]
+
+    def detector_geometry(self) -> np.ndarray:
+        g = np.zeros((10, 20))
+        n = self.lib.mxo_detector_geometry(self.h, _p(g), 10)
+        return g[:n]
+
+    def philox_uniform(self, seed, tag, slot):
+        return self.lib.mxo_philox_uniform(seed, tag, slot)
+
+    def philox_normal(self, seed, tag, slot):
+        return self.lib.mxo_philox_normal(seed, tag, slot)
+
+
+class Reference:
+    """The reference MARX library compiled from its own sources (only in a
+    checkout that has them).  ``native=True`` keeps its own generator."""
+
+    def __init__(self, cfg: MxConfig, native: bool = False, seed: int = 1):
+        so = REF_NATIVE_SO if native else REF_SLOTS_SO
+        if not os.path.exists(so):
+            if not build_reference():
+                raise RuntimeError("reference sources not available")
+        self.native = native
+        self.lib = C.CDLL(so)
+        L = self.lib
+        L.mxref_last_error.restype = C.c_char_p
+        L.mxref_focal_length.restype = C.c_double
+        par = to_par(cfg)
+        names = (C.c_char_p * len(par))(*[k.encode() for k in par])
+        vals = (C.c_char_p * len(par))(*[v.encode() for v in par.values()])
+        parfile = os.path.join(REF_ROOT, "marx", "par", "marx.par").encode()
+        datadir = os.path.join(REF_ROOT, "marx", "data").encode()
+        if native:
+            L.mxref_seed(C.c_ulong(seed))
+        r = L.mxref_setup(parfile, datadir, len(par), names, vals)
+        if r != 0:
+            raise RuntimeError("reference setup: " + L.mxref_last_error().decode())
+
+    def detector_geometry(self) -> np.ndarray:
+        g = np.zeros((10, 20))
+        n = self.lib.mxref_detector_geometry(_p(g), 10)
+        return g[:n]
+
+    def _outs(self, n):
+        return dict(x=np.zeros((n, 3)), p=np.zeros((n, 3)), flags=np.zeros(n, np.uint32),
+                    shell=np.zeros(n, np.int32), order=np.zeros(n, np.int32), ccd=np.zeros(n, np.int32),
+                    ypix=np.zeros(n, np.float32), zpix=np.zeros(n, np.float32),
+                    dith=np.zeros((n, 3), np.float32))
+
+    def _to_list(self, ph: PhotonList, o: dict) -> PhotonList:
+        q = ph.copy()
+        q.x[:] = o["x"].T; q.p[:] = o["p"].T; q.flags[:] = o["flags"]
+        q.mirror_shell[:] = o["shell"]; q.order[:] = o["order"]; q.ccd_num[:] = o["ccd"]
+        q.y_pixel[:] = o["ypix"]; q.z_pixel[:] = o["zpix"]; q.dither_state[:] = o["dith"].T
+        return q
+
+    def trace_slots(self, ph: PhotonList, U, N, stages: int = 15):
+        """Per-photon run with pre-drawn slot variates (slot-major U, N)."""
+        assert not self.native
+        n = ph.n
+        E = np.ascontiguousarray(ph.energy); P = np.ascontiguousarray(ph.p.T); T = np.ascontiguousarray(ph.arrival_time)
+        Up = np.ascontiguousarray(U.T); Np = np.ascontiguousarray(N.T)
+        o = self._outs(n)
+        used = np.zeros((n, 8), np.int32)
+        r = self.lib.mxref_trace_slots(n, _p(E), _p(P), _p(T), _p(Up), _p(Np), stages,
+                                       _p(o["x"]), _p(o["p"]), _p(o["flags"]), _p(o["shell"]), _p(o["order"]),
+                                       _p(o["ccd"]), _p(o["ypix"]), _p(o["zpix"]), _p(o["dith"]), _p(used))
+        if r < 0:
+            raise RuntimeError("reference trace: " + self.lib.mxref_last_error().decode())
+        return self._to_list(ph, o), used, r
+
+    def trace_batch(self, ph: PhotonList, stages: int = 15):
+        """Whole batch with the reference's own generator; returns (list, seconds)."""
+        assert self.native
+        n = ph.n
+        E = np.ascontiguousarray(ph.energy); P = np.ascontiguousarray(ph.p.T); T = np.ascontiguousarray(ph.arrival_time)
+        o = self._outs(n)
+        f = self.lib.mxref_trace_batch
+        f.restype = C.c_double
+        secs = f(n, _p(E), _p(P), _p(T), stages, _p(o["x"]), _p(o["p"]), _p(o["flags"]), _p(o["shell"]),
+                 _p(o["order"]), _p(o["ccd"]), _p(o["ypix"]), _p(o["zpix"]), _p(o["dith"]))
+        if secs < 0:
+            raise RuntimeError("reference batch trace failed")
+        return self._to_list(ph, o), secs

@@ -1,0 +1,370 @@
+/* Test harness around the reference MARX library (compiled in place from the
+ * reference's own sources by oracle/Makefile).  Test infrastructure only.
+ *
+ * It drives the reference's stage functions over a photon list:
+ *   _marx_dither_photons  (marx/libsrc/dither.c:630)
+ *   marx_mirror_reflect   (marx/libsrc/mirror.c:93)
+ *   marx_grating_diffract (marx/libsrc/grating.c:88)
+ * and the per-photon body of _marx_acis_i_detect / _marx_acis_s_detect
+ * (marx/libsrc/acis-i.c:96-160, acis-s.c:177-248) through the exported
+ * pieces that body calls (_marx_transform_ray, _marx_intersect_with_detector,
+ * _marx_acis_apply_streak).  marx_detector_init itself cannot run here: it
+ * loads the ACIS FEF calibration file unconditionally and that file is not
+ * shipped with the reference, so QE and pulse height are not exercised
+ * (DetIdeal semantics; pulse height left at 0).
+ *
+ * Built twice:
+ *   MXREF_INTERPOSE=1  the jdmath generator is replaced by per-photon
+ *                      pre-drawn variates.  Each stage reads its uniforms
+ *                      and normals from fixed slot ranges of the current
+ *                      photon (MX_U_* / MX_N_* below), so the same variates
+ *                      can be handed to any other implementation.
+ *   MXREF_INTERPOSE=0  the reference's own generator (jdmath random.c,
+ *                      gaussrnd.c), seeded with mxref_seed(); photons are
+ *                      processed as one batch exactly as marx.c does.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#include <time.h>
+
+#include <jdmath.h>
+#include <pfile.h>
+#include "marx.h"
+#include "_marx.h"
+
+/* Variate slot layout, shared with the engine and the port. */
+#define MX_NU 16
+#define MX_NN 8
+#define MX_U_MIRROR 0
+#define MX_U_MIRROR_N 12
+#define MX_U_GRATING 12
+#define MX_U_GRATING_N 2
+#define MX_U_DETECT 14
+#define MX_U_DETECT_N 2
+#define MX_N_DITHER 0
+#define MX_N_DITHER_N 2
+#define MX_N_MIRROR 2
+#define MX_N_MIRROR_N 2
+#define MX_N_GRATING 4
+#define MX_N_GRATING_N 2
+#define MX_N_DETECT 6
+#define MX_N_DETECT_N 2
+
+static char Err[1024];
+static void set_err(const char *s) { strncpy(Err, s, sizeof(Err) - 1); }
+const char *mxref_last_error(void) { return Err; }
+
+/* ---------------------------------------------------------------- RNG -- */
+#if MXREF_INTERPOSE
+static const double *Cur_U, *Cur_N;
+static int U_pos, U_end, N_pos, N_end;
+static int Rng_Overrun, Rng_Unexpected;
+
+static void rng_window(const double *u, int ubase, int ucount,
+                       const double *n, int nbase, int ncount)
+{
+   Cur_U = u; U_pos = ubase; U_end = ubase + ucount;
+   Cur_N = n; N_pos = nbase; N_end = nbase + ncount;
+}
+
+double JDMrandom(void)
+{
+   if (Cur_U == NULL || U_pos >= U_end) { Rng_Overrun++; return 0.5; }
+   return Cur_U[U_pos++];
+}
+double JDMgaussian_random(void)
+{
+   if (Cur_N == NULL || N_pos >= N_end) { Rng_Overrun++; return 0.0; }
+   return Cur_N[N_pos++];
+}
+double JDMexpn_random(void) { Rng_Unexpected++; return 1.0; }
+int JDMsrandom(unsigned long s) { (void) s; return 0; }
+uint32 JDMuint32_random(void) { Rng_Unexpected++; return 0; }
+int JDMseed_random(JDMRandom_Type *rt, unsigned long s) { (void) rt; (void) s; Rng_Unexpected++; return 0; }
+uint32 JDMgenerate_uint32_random(JDMRandom_Type *rt) { (void) rt; Rng_Unexpected++; return 0; }
+double JDMgenerate_random(JDMRandom_Type *rt) { (void) rt; Rng_Unexpected++; return 0.5; }
+JDMRandom_Type *JDMcreate_random(void) { Rng_Unexpected++; return NULL; }
+void JDMfree_random(JDMRandom_Type *rt) { (void) rt; }
+void JDMseed_fast_random(unsigned long s) { (void) s; }
+uint32 JDMfast_uint32_random(void) { Rng_Unexpected++; return 0; }
+double JDMfast_random(void) { Rng_Unexpected++; return 0.5; }
+#endif
+
+/* ------------------------------------------------------------- set-up -- */
+static Param_File_Type *Pf;
+static int Have_Dither, Have_Grating, Det_Kind;   /* 0 none, 1 ACIS-I, 2 ACIS-S */
+static Marx_Detector_Type *Det;
+
+int mxref_setup(const char *parfile, const char *datadir, int nover,
+                const char **names, const char **values)
+{
+   char buf[PF_MAX_LINE_LEN];
+   double yoff, zoff;
+   int i;
+
+   Err[0] = 0;
+   if (Pf != NULL) { pf_close_parameter_file(Pf); Pf = NULL; }
+   if (NULL == (Pf = pf_open_parameter_file((char *) parfile, "rQ")))
+     { set_err("cannot open parameter file"); return -1; }
+   for (i = 0; i < nover; i++)
+     if (-1 == pf_set_value(Pf, (char *) names[i], (char *) values[i]))
+       { snprintf(Err, sizeof(Err), "cannot set %s=%s", names[i], values[i]); return -1; }
+
+   if (-1 == marx_set_data_directory((char *) datadir))
+     { set_err("bad data directory"); return -1; }
+
+   if (-1 == _marx_init_dither(Pf, 0, &yoff, &zoff))
+     { set_err("dither init failed"); return -1; }
+   if (-1 == pf_get_string(Pf, "DitherModel", buf, sizeof(buf)))
+     return -1;
+   Have_Dither = (0 == strcmp(buf, "INTERNAL"));
+
+   if (-1 == marx_mirror_init(Pf)) { set_err("mirror init failed"); return -1; }
+   if (-1 == marx_grating_init(Pf)) { set_err("grating init failed"); return -1; }
+   if (-1 == pf_get_string(Pf, "GratingType", buf, sizeof(buf))) return -1;
+   Have_Grating = (0 != strcmp(buf, "NONE"));
+
+   /* Detector: the part of marx_detector_init (detector.c:298-357) that does
+    * not depend on the missing FEF file. */
+   if (-1 == pf_get_string(Pf, "DetectorType", buf, sizeof(buf))) return -1;
+   Det_Kind = 0; Det = NULL;
+   if (0 == strcmp(buf, "ACIS-I")) Det_Kind = 1;
+   else if (0 == strcmp(buf, "ACIS-S")) Det_Kind = 2;
+   else if (0 != strcmp(buf, "NONE")) { set_err("unsupported DetectorType"); return -1; }
+   if (Det_Kind)
+     {
+        double *m = _Marx_Det_XForm_Matrix.matrix;
+        m[0] = 1; m[1] = 0; m[2] = 0; m[3] = 0; m[4] = 1; m[5] = 0; m[6] = 0; m[7] = 0; m[8] = 1;
+        if ((-1 == pf_get_double(Pf, "DetOffsetX", &_Marx_Det_XForm_Matrix.dx))
+            || (-1 == pf_get_double(Pf, "DetOffsetY", &_Marx_Det_XForm_Matrix.dy))
+            || (-1 == pf_get_double(Pf, "DetOffsetZ", &_Marx_Det_XForm_Matrix.dz))
+            || (-1 == pf_get_boolean(Pf, "DetExtendFlag", &_Marx_Det_Extend_Flag)))
+          { set_err("detector parameters"); return -1; }
+        _Marx_Det_Ideal_Flag = 1;
+        if (-1 == _marx_acis_get_generic_parms(Pf)) { set_err("ACIS parameters"); return -1; }
+        if (NULL == (Det = marx_get_detector_info(Det_Kind == 1 ? "ACIS-I" : "ACIS-S", 0)))
+          { set_err("detector geometry"); return -1; }
+     }
+   return 0;
+}
+
+/* Chip facets after the reference's CALDB patching: per chip
+ * id, x_ll[3], xhat[3], yhat[3], normal[3], xlen, ylen, xpix, ypix,
+ * xpixel_offset, ypixel_offset  (20 doubles). */
+int mxref_detector_geometry(double *out, int max_chips)
+{
+   Marx_Detector_Geometry_Type *g;
+   int n = 0;
+   if (Det == NULL) return 0;
+   for (g = Det->facet_list; g != NULL && n < max_chips; g = g->next, n++)
+     {
+        double *o = out + 20 * n;
+        o[0] = g->id;
+        o[1] = g->x_ll.x; o[2] = g->x_ll.y; o[3] = g->x_ll.z;
+        o[4] = g->xhat.x; o[5] = g->xhat.y; o[6] = g->xhat.z;
+        o[7] = g->yhat.x; o[8] = g->yhat.y; o[9] = g->yhat.z;
+        o[10] = g->normal.x; o[11] = g->normal.y; o[12] = g->normal.z;
+        o[13] = g->xlen; o[14] = g->ylen;
+        o[15] = g->x_pixel_size; o[16] = g->y_pixel_size;
+        o[17] = g->xpixel_offset; o[18] = g->ypixel_offset;
+        o[19] = 0;
+     }
+   return n;
+}
+
+double mxref_focal_length(void) { return Marx_Focal_Length; }
+
+/* ---------------------------------------------------------- detection -- */
+/* Per-photon body of _marx_acis_i_detect (acis-i.c:124-157); the acis-s
+ * body is the same with chip ids 4..9.  QE is skipped (DetIdeal) and the
+ * pulse-height function is not available, so the streak follows every hit. */
+static void detect_photons(Marx_Photon_Type *pt)
+{
+   unsigned int i;
+   marx_prune_photons(pt);
+   for (i = 0; i < pt->num_sorted; i++)
+     {
+        Marx_Photon_Attr_Type *at = pt->attributes + pt->sorted_index[i];
+        Marx_Detector_Geometry_Type *d;
+        double dx, dy;
+
+        _marx_dither_detector(&at->dither_state);
+        _marx_transform_ray(&at->x, &at->p, &_Marx_Det_XForm_Matrix);
+        d = _marx_intersect_with_detector(at->x, at->p, Det->facet_list,
+                                          &at->x, &dx, &dy, _Marx_Det_Extend_Flag);
+        if (d == NULL)
+          {
+             at->flags |= PHOTON_MISSED_DETECTOR;
+             at->ccd_num = -1;
+          }
+        else
+          {
+             at->ccd_num = d->id;
+             at->y_pixel = dx / d->x_pixel_size;
+             at->z_pixel = dy / d->y_pixel_size;
+             _marx_acis_apply_streak(pt->start_time, at, d);
+          }
+        _marx_transform_ray_reverse(&at->x, &at->p, &_Marx_Det_XForm_Matrix);
+        _marx_undither_detector(&at->dither_state);
+     }
+}
+
+/* --------------------------------------------------------------- trace -- */
+typedef struct
+{
+   double *x, *p;           /* n*3 */
+   unsigned int *flags;
+   int *shell, *order, *ccd;
+   float *ypix, *zpix;
+   float *dither;           /* n*3: ra, dec, roll */
+} Out_Type;
+
+static void fill_attr(Marx_Photon_Attr_Type *at, double e, const double *p, double t,
+                      unsigned int tag)
+{
+   memset(at, 0, sizeof(*at));
+   at->energy = e;
+   at->p.x = p[0]; at->p.y = p[1]; at->p.z = p[2];
+   at->arrival_time = t;
+   at->tag = tag;
+   at->ccd_num = -1;
+}
+
+static void store_attr(const Marx_Photon_Attr_Type *at, int i, double *x, double *p,
+                       unsigned int *flags, int *shell, int *order, int *ccd,
+                       float *ypix, float *zpix, float *dith)
+{
+   x[3*i] = at->x.x; x[3*i+1] = at->x.y; x[3*i+2] = at->x.z;
+   p[3*i] = at->p.x; p[3*i+1] = at->p.y; p[3*i+2] = at->p.z;
+   flags[i] = at->flags;
+   shell[i] = (int) at->mirror_shell;
+   order[i] = at->order;
+   ccd[i] = at->ccd_num;
+   ypix[i] = at->y_pixel; zpix[i] = at->z_pixel;
+   dith[3*i] = at->dither_state.ra; dith[3*i+1] = at->dither_state.dec;
+   dith[3*i+2] = at->dither_state.roll;
+}
+
+#define ST_DITHER 1
+#define ST_MIRROR 2
+#define ST_GRATING 4
+#define ST_DETECT 8
+
+#if MXREF_INTERPOSE
+/* One photon at a time with its own pre-drawn variates.  U is n x MX_NU and
+ * N is n x MX_NN, photon-major.  used[] receives, per photon, the number of
+ * uniforms and normals each stage consumed (8 ints).  Returns the number of
+ * photons whose stage ran past its slot range, or -1. */
+int mxref_trace_slots(int n, const double *energy, const double *p_in, const double *t,
+                      const double *U, const double *N, int stages,
+                      double *x, double *p, unsigned int *flags, int *shell, int *order,
+                      int *ccd, float *ypix, float *zpix, float *dith, int *used)
+{
+   Marx_Photon_Type pt;
+   Marx_Photon_Attr_Type at;
+   unsigned int sidx;
+   double sen;
+   int i, bad = 0;
+
+   for (i = 0; i < n; i++)
+     {
+        const double *u = U + (size_t) i * MX_NU;
+        const double *g = N + (size_t) i * MX_NN;
+        int *us = used + 8 * i;
+        unsigned int num;
+
+        fill_attr(&at, energy[i], p_in + 3 * i, t[i], (unsigned int) i);
+        memset(&pt, 0, sizeof(pt));
+        pt.attributes = &at;
+        pt.n_photons = 1; pt.max_n_photons = 1;
+        pt.sorted_index = &sidx; pt.sorted_energies = &sen;
+        pt.num_sorted = 1; sidx = 0; sen = energy[i];
+        pt.history = MARX_ENERGY_OK | MARX_TIME_OK | MARX_P_VECTOR_OK | MARX_TAG_OK;
+        Rng_Overrun = 0;
+
+        memset(us, 0, 8 * sizeof(int));
+        if ((stages & ST_DITHER) && Have_Dither)
+          {
+             rng_window(u, 0, 0, g, MX_N_DITHER, MX_N_DITHER_N);
+             _marx_dither_photons(&pt, &num);
+             us[1] = N_pos - MX_N_DITHER;
+          }
+        if (stages & ST_MIRROR)
+          {
+             rng_window(u, MX_U_MIRROR, MX_U_MIRROR_N, g, MX_N_MIRROR, MX_N_MIRROR_N);
+             if (-1 == marx_mirror_reflect(&pt, 0)) { set_err("mirror"); return -1; }
+             us[2] = U_pos - MX_U_MIRROR; us[3] = N_pos - MX_N_MIRROR;
+          }
+        if ((stages & ST_GRATING) && Have_Grating)
+          {
+             rng_window(u, MX_U_GRATING, MX_U_GRATING_N, g, MX_N_GRATING, MX_N_GRATING_N);
+             if (-1 == marx_grating_diffract(&pt, 0)) { set_err("grating"); return -1; }
+             us[4] = U_pos - MX_U_GRATING; us[5] = N_pos - MX_N_GRATING;
+          }
+        if ((stages & ST_DETECT) && Det_Kind)
+          {
+             rng_window(u, MX_U_DETECT, MX_U_DETECT_N, g, MX_N_DETECT, MX_N_DETECT_N);
+             detect_photons(&pt);
+             us[6] = U_pos - MX_U_DETECT; us[7] = N_pos - MX_N_DETECT;
+          }
+        rng_window(NULL, 0, 0, NULL, 0, 0);
+        if (Rng_Overrun) bad++;
+        store_attr(&at, i, x, p, flags, shell, order, ccd, ypix, zpix, dith);
+     }
+   if (Rng_Unexpected) { set_err("unexpected generator call"); return -1; }
+   return bad;
+}
+#else
+void mxref_seed(unsigned long seed) { JDMsrandom(seed); }
+
+static const double *Sort_E;
+static int cmp_energy(const void *a, const void *b)
+{
+   double ea = Sort_E[*(const unsigned int *) a], eb = Sort_E[*(const unsigned int *) b];
+   return (ea > eb) - (ea < eb);
+}
+
+/* All photons as one batch with the reference's own generator, in energy
+ * order as marx_create_photons leaves them (source.c:366).  Returns the
+ * seconds spent inside the stage calls, or -1. */
+double mxref_trace_batch(int n, const double *energy, const double *p_in, const double *t,
+                         int stages, double *x, double *p, unsigned int *flags, int *shell,
+                         int *order, int *ccd, float *ypix, float *zpix, float *dith)
+{
+   Marx_Photon_Type *pt;
+   unsigned int i, num;
+   struct timespec t0, t1;
+   double secs;
+
+   if (NULL == (pt = marx_alloc_photon_type((unsigned int) n))) return -1;
+   pt->sorted_index = (unsigned int *) malloc(n * sizeof(unsigned int));
+   for (i = 0; i < (unsigned int) n; i++)
+     {
+        fill_attr(pt->attributes + i, energy[i], p_in + 3 * i, t[i], i);
+        pt->sorted_index[i] = i;
+     }
+   Sort_E = energy;
+   qsort(pt->sorted_index, n, sizeof(unsigned int), cmp_energy);
+   for (i = 0; i < (unsigned int) n; i++) pt->sorted_energies[i] = energy[pt->sorted_index[i]];
+   pt->n_photons = n; pt->num_sorted = n;
+   pt->history = MARX_ENERGY_OK | MARX_TIME_OK | MARX_P_VECTOR_OK | MARX_TAG_OK;
+
+   clock_gettime(CLOCK_MONOTONIC, &t0);
+   if ((stages & ST_DITHER) && Have_Dither) _marx_dither_photons(pt, &num);
+   if ((stages & ST_MIRROR) && (-1 == marx_mirror_reflect(pt, 0))) goto fail;
+   if ((stages & ST_GRATING) && Have_Grating && (-1 == marx_grating_diffract(pt, 0))) goto fail;
+   if ((stages & ST_DETECT) && Det_Kind) detect_photons(pt);
+   clock_gettime(CLOCK_MONOTONIC, &t1);
+   secs = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
+
+   for (i = 0; i < (unsigned int) n; i++)
+     store_attr(pt->attributes + i, i, x, p, flags, shell, order, ccd, ypix, zpix, dith);
+   marx_dealloc_photon_type(pt);
+   return secs;
+fail:
+   marx_dealloc_photon_type(pt);
+   return -1;
+}
+#endif
