@@ -1,0 +1,300 @@
+"""Throughput of the fused photon trace on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl reference]
+
+A step is one pass of the hot path (aspect dither -> HRMA mirror -> grating
+-> ACIS detector) over one batch of synthetic photons of the named workload
+(default plain_scatter: 1e7 photons, 0.3-8 keV log-uniform, 0-10 arcmin off
+axis, 8 arcsec Lissajous dither, mirror blur and WFold scattering, ACIS-I).
+
+value     photons/s with the batch resident in HBM (inputs > L2, so no flush);
+          each step restores the batch's input directions and flags, then
+          launches the fused trace kernel.
+e2e       the same metric through mx_trace_host: pinned host buffers in,
+          host buffers out, copies inside the timed region.
+roofline  the trace kernel against the measured FP64 FMA peak (it is FP64
+          bound); algorithmic FP64 operations per photon come from the
+          oracle's counting arithmetic on a sample of the same batch.
+cpu_baseline  the CPU oracle (a restatement of the reference) on a bounded
+          sample, all host threads.
+
+With --gpus N > 1 (torchrun, one rank per GPU) every rank traces its own
+batch (no collective on the data path) and value = all photons / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "photons/s HRMA+grating+ACIS trace"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default="plain_scatter")
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--n", type=int, default=0, help="photons per step (default: the workload's size)")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index, self.proc, self.lines = index, None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0])); mx = float(f[1])
+            except ValueError:
+                continue
+            for k, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(k)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init(gpus):
+    import torch
+    rank, world = int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        dist.init_process_group("nccl")
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(w, n, threads):
+    """Oracle throughput (photons/s) on n photons of the workload."""
+    from oracle.bindings import Oracle
+    o = Oracle(w.cfg)
+    ph = w.photons(n, seed=w.seed + 7)
+    o.trace(ph.copy(), seed=1, threads=threads)          # warm
+    t0 = time.perf_counter()
+    o.trace(ph, seed=2, threads=threads)
+    return n / (time.perf_counter() - t0)
+
+
+def run_reference(a):
+    """Reference arm: the CPU implementation of the path on the host cores."""
+    from marx_gb300 import workloads as W
+    rank, world = int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+    if rank != 0:
+        return
+    w = W.PLAIN[a.workload]()
+    threads = os.cpu_count() or 1
+    n = 400_000
+    for _ in range(max(a.warmup, 0)):
+        cpu_sample(w, 50_000, threads)
+    rates = [cpu_sample(w, n, threads) for _ in range(a.steps)]
+    v = statistics.median(rates)
+    line = {"metric": METRIC, "value": v, "unit": "photons/s", "impl": "reference", "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": n / v * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": a.workload, "photons_per_step": n, "sample_of": w.n},
+            "cpu_baseline": {"value": v, "unit": "photons/s", "cores": threads, "kind": "port",
+                             "sample": f"{n} photons of {a.workload} per step"},
+            "e2e": {"value": v, "unit": "photons/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        return run_reference(a)
+    import numpy as np
+    import torch
+    from marx_gb300 import workloads as W
+    from marx_gb300._native import Engine, DevicePhotons, probe_fp64
+    from marx_gb300.photons import PhotonList
+    from oracle.bindings import Oracle
+
+    rank, world = dist_init(a.gpus)
+    dev = torch.cuda.current_device()
+    w = W.PLAIN[a.workload]()
+    n = a.n or w.n
+    eng = Engine(w.cfg)
+
+    host = w.photons(n, seed=w.seed + rank)
+    host.tag[:] = np.arange(n, dtype=np.uint64).astype(np.uint32) + np.uint32(rank * n)
+    d = DevicePhotons.from_host(host)
+    p0, flags0 = d.p.clone(), d.flags.clone()
+    stream = torch.cuda.current_stream()
+
+    def step(seed):
+        d.p.copy_(p0)
+        d.flags.copy_(flags0)
+        eng.trace(d, stages=w.stages, seed=seed)
+
+    for s in range(a.warmup):
+        step(1000 + s)
+    torch.cuda.synchronize()
+    # kernel-only timing of the same launches for the roofline
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    launches0 = eng.launch_count()
+    with ClockSampler(dev) as clocks:
+        barrier(world)
+        torch.cuda.synchronize()
+        t_start = torch.cuda.Event(enable_timing=True); t_stop = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for s in range(a.steps):
+            d.p.copy_(p0)
+            d.flags.copy_(flags0)
+            ev[s][0].record(stream)
+            eng.trace(d, stages=w.stages, seed=s)
+            ev[s][1].record(stream)
+        t_stop.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+    launches = eng.launch_count() - launches0
+    ms_total = t_start.elapsed_time(t_stop)
+    kernel_ms = statistics.mean(e0.elapsed_time(e1) for e0, e1 in ev)
+    ms_total = max_over_ranks(ms_total, world)
+    value = world * n * a.steps / (ms_total * 1e-3)
+    good = float(((d.flags & 0xFF) == 0).float().mean().item())
+
+    # end to end through the host entry point, pinned buffers
+    e2e = None
+    if not a.no_e2e:
+        pin = {}
+        for k in ("energy", "p", "arrival_time", "flags", "tag", "x", "mirror_shell", "order", "ccd_num",
+                  "y_pixel", "z_pixel", "dither_state"):
+            src = getattr(host, k)
+            t = torch.empty(src.shape, dtype=getattr(torch, str(src.dtype).replace("uint32", "int32")), pin_memory=True)
+            t.numpy()[...] = src.view(np.int32) if src.dtype == np.uint32 else src
+            pin[k] = t
+        hp = PhotonList.__new__(PhotonList)
+        hp.n = n
+        for k, t in pin.items():
+            arr = t.numpy()
+            setattr(hp, k, arr.view(np.uint32) if k in ("flags", "tag") else arr)
+        p_in = pin["p"].clone()
+        in_b = sum(pin[k].numel() * pin[k].element_size() for k in ("energy", "p", "arrival_time", "flags", "tag"))
+        out_b = sum(pin[k].numel() * pin[k].element_size() for k in ("x", "p", "flags", "mirror_shell", "order",
+                                                                     "ccd_num", "y_pixel", "z_pixel", "dither_state"))
+        for s in range(max(1, a.warmup)):
+            pin["p"].copy_(p_in); pin["flags"].zero_()
+            eng.trace_host(hp, stages=w.stages, seed=2000 + s)
+        barrier(world)
+        t0 = time.perf_counter()
+        for s in range(a.steps):
+            pin["p"].copy_(p_in); pin["flags"].zero_()
+            eng.trace_host(hp, stages=w.stages, seed=s)
+        e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+        barrier(world)
+        e2e = {"value": world * n * a.steps / e2e_s, "unit": "photons/s",
+               "h2d_bytes_per_step": in_b, "d2h_bytes_per_step": out_b,
+               "note": "pinned host buffers; wall clock around blocking mx_trace_host calls"}
+
+    if rank != 0:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+
+    # roofline: algorithmic FP64 operations per photon from the oracle's counting arithmetic
+    sample = w.photons(20_000, seed=w.seed + 99)
+    ops, cnt = Oracle(w.cfg).count_flops(sample, seed=5)
+    flops_per_photon = ops / cnt
+    fp64_peak = probe_fp64()
+    achieved = flops_per_photon * n / (kernel_ms * 1e-3) / 1e12
+    bytes_per_photon = 8 + 24 + 8 + 4 + 4 + 24 + 24 + 4 + 3 + 8 + 12 + 24   # SoA columns read + written
+    hbm_peak = None
+    try:
+        hbm_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    except (OSError, KeyError, ValueError):
+        hbm_peak = 6800.0
+    hbm_achieved = bytes_per_photon * n / (kernel_ms * 1e-3) / 1e9
+    cpu_rate = cpu_sample(w, 200_000, os.cpu_count() or 1)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "photons/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms_total / a.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": a.workload, "photons_per_step": n, "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2 (no flush)", "variates": "philox4x32-10",
+                   "detected_fraction": good},
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "kernel_ms": kernel_ms,
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp64_peak, "traffic": None,
+                     "algorithmic_flops_per_photon": flops_per_photon,
+                     "peak_source": "measured live: mx_probe_fp64 DFMA kernel (MEASURED_PEAKS.json has no FP64 figure)",
+                     "hbm": {"achieved_gbs": hbm_achieved, "peak_gbs": hbm_peak, "frac": hbm_achieved / hbm_peak,
+                             "bytes_per_photon": bytes_per_photon}},
+        "cpu_baseline": {"value": cpu_rate, "unit": "photons/s", "cores": os.cpu_count() or 1, "kind": "port",
+                         "sample": f"200000 photons of {a.workload}"},
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -162,6 +162,10 @@ void mx_config_default(mx_config *cfg);
  * sequence (mirror.c:48, grating.c:44, detector.c:298, dither.c:508). */
 mx_context *mx_create(const char *pack_path, const mx_config *cfg);
 int  mx_configure(mx_context *ctx, const mx_config *cfg);
+
+/* Check a configuration against a table pack without touching the GPU:
+ * MX_OK, or MX_EPACK / MX_EINVAL with the reason in mx_last_error(NULL). */
+int  mx_validate_config(const char *pack_path, const mx_config *cfg);
 void mx_destroy(mx_context *ctx);
 const char *mx_last_error(const mx_context *ctx);  /* ctx may be NULL */
 
@@ -190,6 +194,16 @@ int mx_table_bytes(const mx_context *ctx, size_t *shared_bytes, size_t *global_b
 
 /* Number of kernel launches issued by this context since creation. */
 uint64_t mx_launch_count(const mx_context *ctx);
+
+/* The context's own stream (a cudaStream_t), on which mx_trace_host runs. */
+void *mx_stream(mx_context *ctx);
+
+/* Photons flagged MX_PHOTON_VARIATE_OVERRUN since the last reset. */
+int mx_overrun_count(mx_context *ctx, unsigned long long *count, int reset);
+
+/* Measured FP64 fused-multiply-add throughput of the current device
+ * (TFLOP/s), the denominator of the trace kernels' roofline. */
+int mx_probe_fp64(double *tflops, double *ms);
 
 #ifdef __cplusplus
 }

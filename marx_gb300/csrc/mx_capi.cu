@@ -1,0 +1,304 @@
+// Trace kernels and the C ABI of libmarx_gb300 (include/marx_gb300.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "mx_device.cuh"
+#include "mx_host.h"
+#include "mx_kernels.cuh"
+
+using namespace mx;
+
+static thread_local std::string g_create_err;
+
+struct DevBuf {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t need) {
+    if (need <= bytes) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr; bytes = 0;
+    cudaError_t e = cudaMalloc(&ptr, need);
+    if (e == cudaSuccess) bytes = need;
+    return e;
+  }
+  void release() { if (ptr) cudaFree(ptr); ptr = nullptr; bytes = 0; }
+};
+
+struct mx_context {
+  int device = 0;
+  int num_sms = 0;
+  std::string err;
+  mx_config cfg;
+  Pack pack;
+  HostModel hm;
+  MxTables T;              // launch copy with device pointers
+  DevBuf tables;           // every table in one allocation
+  size_t shared_bytes = 0;
+  int trace_blocks[2] = {0, 0};   // resident blocks per SM for the slot / Philox kernels
+  cudaStream_t stream = nullptr;
+  DevBuf io[14];           // staging for mx_trace_host
+  DevBuf scan;             // compaction block counts
+  unsigned long long *d_overrun = nullptr;
+  unsigned long long launches = 0;
+};
+
+static int fail(mx_context *c, int code, const std::string &msg) {
+  if (c) c->err = msg; else g_create_err = msg;
+  return code;
+}
+static int cuda_fail(mx_context *c, cudaError_t e, const char *what) {
+  return fail(c, MX_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// ------------------------------------------------------------ uploading --
+template <class T> static size_t put(std::vector<char> &blob, const std::vector<T> &v) {
+  size_t off = (blob.size() + 255) & ~(size_t) 255;
+  blob.resize(off + v.size() * sizeof(T));
+  memcpy(blob.data() + off, v.data(), v.size() * sizeof(T));
+  return off;
+}
+
+static int upload_model(mx_context *c) {
+  HostModel &M = c->hm;
+  std::vector<char> blob;
+  size_t o_sh = put(blob, M.shells), o_opt = put(blob, M.optc), o_fh = put(blob, M.fold_hdr),
+         o_fe = put(blob, M.fold_ealpha), o_ft = put(blob, M.fold_theta), o_gr = put(blob, M.gratings),
+         o_ge = put(blob, M.geff_energy), o_gc = put(blob, M.geff_cum), o_ok = put(blob, M.order_k),
+         o_se = put(blob, M.sectors), o_ch = put(blob, M.chips);
+  cudaError_t e = c->tables.ensure(blob.size());
+  if (e != cudaSuccess) return cuda_fail(c, e, "allocating device tables");
+  e = cudaMemcpy(c->tables.ptr, blob.data(), blob.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(c, e, "uploading device tables");
+  char *b = (char *) c->tables.ptr;
+  c->T = M.T;
+  c->T.shells = (const MxShellDev *) (b + o_sh);
+  c->T.optc = (const float *) (b + o_opt);
+  c->T.fold_hdr = (const double *) (b + o_fh);
+  c->T.fold_ealpha = (const double *) (b + o_fe);
+  c->T.fold_theta = (const float *) (b + o_ft);
+  c->T.gratings = (const MxGratingDev *) (b + o_gr);
+  c->T.geff_energy = (const float *) (b + o_ge);
+  c->T.geff_cum = (const float *) (b + o_gc);
+  c->T.order_k = (const double *) (b + o_ok);
+  c->T.sectors = (const double *) (b + o_se);
+  c->T.chips = (const MxChipDev *) (b + o_ch);
+  c->shared_bytes = trace_shared_bytes(c->T);
+  if (c->shared_bytes > 200 * 1024) return fail(c, MX_ERANGE, "tables exceed the shared-memory budget");
+  return MX_OK;
+}
+
+static int configure(mx_context *c, const mx_config *cfg) {
+  std::string err;
+  if (!build_model(c->pack, *cfg, c->hm, err)) return fail(c, MX_EINVAL, err);
+  c->cfg = *cfg;
+  int r = upload_model(c);
+  if (r) return r;
+  for (int s = 0; s < 2; s++) {
+    cudaError_t e = trace_occupancy(s == 1, (int) c->shared_bytes, &c->trace_blocks[s]);
+    if (e != cudaSuccess) return cuda_fail(c, e, "querying occupancy");
+    if (c->trace_blocks[s] < 1) return fail(c, MX_ERANGE, "trace kernel cannot be resident");
+  }
+  return MX_OK;
+}
+
+// ------------------------------------------------------------------ ABI --
+extern "C" {
+
+void mx_config_default(mx_config *c) {
+  memset(c, 0, sizeof(*c));
+  static const double xo[4] = {-3.277664, -0.257891, 0.733315, -0.541755};
+  static const double bp[4] = {0.303427, 0.0951899, 0.178899, 0.151085};
+  static const double bh[4] = {0.0051428, 0.0713614, 0.0101367, 0.0239287};
+  static const double sp[4] = {2.8420331, 1.7305226, 1.0077613, 2.1199425};
+  static const double sh[4] = {3.2451338, 2.4618956, 2.9027099, 2.0209803};
+  static const double th[4] = {4.755, 4.755, -5.205, -5.205};
+  static const double pe[4] = {0.400195, 0.400195, 0.200081, 0.200081};
+  static const double dpp[4] = {162e-6, 162e-6, 146e-6, 146e-6};
+  c->hrma_cap_x = 10079.771554;
+  for (int i = 0; i < 4; i++) {
+    c->shell_xoffset[i] = xo[i]; c->blur_p[i] = bp[i]; c->blur_h[i] = bh[i];
+    c->scat_p[i] = sp[i]; c->scat_h[i] = sh[i]; c->shutters[i] = 0xF;
+    c->hetg_theta[i] = th[i]; c->hetg_dtheta[i] = 1.5; c->hetg_period[i] = pe[i];
+    c->hetg_dpp[i] = dpp[i]; c->hetg_vig[i] = 1.0;
+  }
+  c->hrma_vig = 1.0;
+  c->use_blur = c->use_wfold = c->use_struts = c->use_scale_factors = 1;
+  c->grating = MX_GRATING_HETG; c->use_sector_files = 1;
+  c->meg_rowland = c->heg_rowland = 8632.48;
+  c->dither = MX_DITHER_INTERNAL;
+  c->dither_amp[0] = 16.0; c->dither_amp[1] = 16.0; c->dither_amp[2] = 0.0;
+  c->dither_period[0] = 1414.2; c->dither_period[1] = 2000.0; c->dither_period[2] = 1e5;
+  c->roll_nom = 237.36968458476;
+  c->aspect_blur = 0.07;
+  c->detector = MX_DETECTOR_ACIS_S;
+  c->acis_exposure_time = 3.2; c->acis_frame_transfer_time = 0.041;
+  c->focal_length = 10065.5;
+}
+
+mx_context *mx_create(const char *pack_path, const mx_config *cfg) {
+  if (!pack_path || !cfg) { g_create_err = "mx_create: null argument"; return nullptr; }
+  mx_context *c = new mx_context();
+  std::string err;
+  if (!c->pack.load(pack_path, err)) { g_create_err = err; delete c; return nullptr; }
+  cudaError_t e = cudaGetDevice(&c->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc((void **) &c->d_overrun, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(c->d_overrun, 0, sizeof(unsigned long long));
+  if (e != cudaSuccess) { g_create_err = std::string("CUDA: ") + cudaGetErrorString(e); mx_destroy(c); return nullptr; }
+  if (configure(c, cfg) != MX_OK) { g_create_err = c->err; mx_destroy(c); return nullptr; }
+  return c;
+}
+
+int mx_configure(mx_context *c, const mx_config *cfg) {
+  if (!c || !cfg) return fail(c, MX_EINVAL, "mx_configure: null argument");
+  cudaStreamSynchronize(c->stream);
+  return configure(c, cfg);
+}
+
+int mx_validate_config(const char *pack_path, const mx_config *cfg) {
+  if (!pack_path || !cfg) { g_create_err = "mx_validate_config: null argument"; return MX_EINVAL; }
+  Pack pk;
+  HostModel hm;
+  std::string err;
+  if (!pk.load(pack_path, err)) { g_create_err = err; return MX_EPACK; }
+  if (!build_model(pk, *cfg, hm, err)) { g_create_err = err; return MX_EINVAL; }
+  return MX_OK;
+}
+
+void mx_destroy(mx_context *c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  c->tables.release();
+  for (auto &b : c->io) b.release();
+  c->scan.release();
+  if (c->d_overrun) cudaFree(c->d_overrun);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char *mx_last_error(const mx_context *c) { return c ? c->err.c_str() : g_create_err.c_str(); }
+
+void *mx_stream(mx_context *c) { return c ? (void *) c->stream : nullptr; }
+
+int mx_table_bytes(const mx_context *c, size_t *shared_bytes, size_t *global_bytes) {
+  if (!c) return MX_EINVAL;
+  if (shared_bytes) *shared_bytes = c->shared_bytes;
+  if (global_bytes) *global_bytes = c->tables.bytes;
+  return MX_OK;
+}
+
+uint64_t mx_launch_count(const mx_context *c) { return c ? c->launches : 0; }
+
+static int trace_device(mx_context *c, const mx_photons *ph, uint32_t stages, const double *U, const double *N,
+                        uint64_t seed, cudaStream_t st, bool fresh) {
+  if (!ph || !ph->energy || !ph->p) return fail(c, MX_EINVAL, "mx_trace: energy and p are required");
+  if ((U == nullptr) != (N == nullptr)) return fail(c, MX_EINVAL, "mx_trace: give both U and N or neither");
+  if ((stages & MX_STAGE_DETECT) && c->T.nchips && (!ph->x)) return fail(c, MX_EINVAL, "mx_trace: x is required");
+  if (ph->n == 0) return MX_OK;
+  TraceIO io;
+  io.energy = ph->energy; io.x = ph->x; io.p = ph->p; io.t = ph->arrival_time; io.flags = ph->flags;
+  io.tag = ph->tag; io.shell = ph->mirror_shell; io.order = ph->order; io.ccd = ph->ccd_num;
+  io.ypix = ph->y_pixel; io.zpix = ph->z_pixel; io.dith = ph->dither_state;
+  io.U = U; io.N = N; io.n = ph->n; io.seed = seed; io.stages = stages; io.fresh = fresh ? 1 : 0;
+  io.overrun = c->d_overrun;
+  int slots = U != nullptr;
+  int grid = c->num_sms * c->trace_blocks[slots ? 0 : 1];
+  cudaError_t e = launch_trace(c->T, io, grid, (int) c->shared_bytes, slots != 0, st);
+  c->launches++;
+  if (e != cudaSuccess) return cuda_fail(c, e, "launching the trace kernel");
+  return MX_OK;
+}
+
+int mx_trace(mx_context *c, const mx_photons *ph, uint32_t stages, const mx_variates *var, uint64_t seed,
+             void *stream) {
+  if (!c) return MX_EINVAL;
+  return trace_device(c, ph, stages, var ? var->U : nullptr, var ? var->N : nullptr, seed,
+                      (cudaStream_t) stream, false);
+}
+
+int mx_trace_host(mx_context *c, const mx_photons *h, uint32_t stages, const mx_variates *hv, uint64_t seed) {
+  if (!c) return MX_EINVAL;
+  if (!h || !h->energy || !h->p) return fail(c, MX_EINVAL, "mx_trace_host: energy and p are required");
+  size_t n = h->n;
+  if (n == 0) return MX_OK;
+  struct Col { const void *host; size_t elem; int comps; bool in, out; };
+  const Col cols[12] = {
+      {h->energy, 8, 1, true, false},     {h->x, 8, 3, false, true},         {h->p, 8, 3, true, true},
+      {h->arrival_time, 8, 1, true, false}, {h->flags, 4, 1, true, true},   {h->tag, 4, 1, true, false},
+      {h->mirror_shell, 1, 1, false, true}, {h->order, 1, 1, false, true},   {h->ccd_num, 1, 1, false, true},
+      {h->y_pixel, 4, 1, false, true},    {h->z_pixel, 4, 1, false, true},   {h->dither_state, 4, 3, false, true}};
+  void *dev[12];
+  cudaStream_t st = c->stream;
+  cudaError_t e;
+  for (int k = 0; k < 12; k++) {
+    dev[k] = nullptr;
+    if (!cols[k].host) continue;
+    size_t bytes = n * cols[k].elem * cols[k].comps;
+    if ((e = c->io[k].ensure(bytes)) != cudaSuccess) return cuda_fail(c, e, "allocating staging buffers");
+    dev[k] = c->io[k].ptr;
+    if (cols[k].in && (e = cudaMemcpyAsync(dev[k], cols[k].host, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+      return cuda_fail(c, e, "copying photons to the device");
+  }
+  const double *dU = nullptr, *dN = nullptr;
+  if (hv && hv->U && hv->N) {
+    if ((e = c->io[12].ensure(n * MX_NUM_U * 8)) != cudaSuccess || (e = c->io[13].ensure(n * MX_NUM_N * 8)) != cudaSuccess)
+      return cuda_fail(c, e, "allocating variate buffers");
+    cudaMemcpyAsync(c->io[12].ptr, hv->U, n * MX_NUM_U * 8, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(c->io[13].ptr, hv->N, n * MX_NUM_N * 8, cudaMemcpyHostToDevice, st);
+    dU = (const double *) c->io[12].ptr; dN = (const double *) c->io[13].ptr;
+  }
+  mx_photons d;
+  memset(&d, 0, sizeof(d));
+  d.n = h->n;
+  d.energy = (double *) dev[0]; d.x = (double *) dev[1]; d.p = (double *) dev[2];
+  d.arrival_time = (double *) dev[3]; d.flags = (uint32_t *) dev[4]; d.tag = (uint32_t *) dev[5];
+  d.mirror_shell = (int8_t *) dev[6]; d.order = (int8_t *) dev[7]; d.ccd_num = (int8_t *) dev[8];
+  d.y_pixel = (float *) dev[9]; d.z_pixel = (float *) dev[10]; d.dither_state = (float *) dev[11];
+  int r = trace_device(c, &d, stages, dU, dN, seed, st, true);
+  if (r) return r;
+  for (int k = 0; k < 12; k++) {
+    if (!cols[k].host || !cols[k].out) continue;
+    size_t bytes = n * cols[k].elem * cols[k].comps;
+    if ((e = cudaMemcpyAsync((void *) cols[k].host, dev[k], bytes, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+      return cuda_fail(c, e, "copying photons to the host");
+  }
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(c, e, "trace");
+  return MX_OK;
+}
+
+int mx_compact(mx_context *c, const uint32_t *flags, uint32_t n, uint32_t *idx_out, uint32_t *count_out,
+               void *stream) {
+  if (!c || !flags || !idx_out || !count_out) return fail(c, MX_EINVAL, "mx_compact: null argument");
+  if (n == 0) { *count_out = 0; return MX_OK; }
+  uint32_t nblk = (n + MX_COMPACT_TILE - 1) / MX_COMPACT_TILE;
+  cudaError_t e = c->scan.ensure((size_t) (nblk + 1) * sizeof(uint32_t));
+  if (e != cudaSuccess) return cuda_fail(c, e, "allocating compaction scratch");
+  cudaStream_t st = (cudaStream_t) stream;
+  e = launch_compact(flags, n, idx_out, (uint32_t *) c->scan.ptr, nblk, st);
+  c->launches += 3;
+  if (e != cudaSuccess) return cuda_fail(c, e, "launching compaction");
+  e = cudaMemcpyAsync(count_out, (uint32_t *) c->scan.ptr + nblk, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(c, e, "compaction");
+  return MX_OK;
+}
+
+int mx_overrun_count(mx_context *c, unsigned long long *count, int reset) {
+  if (!c || !count) return MX_EINVAL;
+  cudaError_t e = cudaMemcpy(count, c->d_overrun, sizeof(*count), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && reset) e = cudaMemset(c->d_overrun, 0, sizeof(unsigned long long));
+  if (e != cudaSuccess) return cuda_fail(c, e, "reading the overrun counter");
+  return MX_OK;
+}
+
+int mx_probe_fp64(double *tflops, double *ms) {
+  return probe_fp64(tflops, ms) == cudaSuccess ? MX_OK : MX_ECUDA;
+}
+
+}  // extern "C"

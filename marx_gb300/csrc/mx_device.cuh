@@ -1,0 +1,620 @@
+// Per-photon trace stages for the GB300 kernels.
+//
+// Each stage follows the reference function it replaces (paths inside MARX
+// 5.5.3, cited per function) in FP64 for geometry and FP32 where the
+// reference keeps float tables.  Unlike the oracle it is written for the
+// GPU's scarce FP64 pipe: one reciprocal square root instead of a scaled
+// hypot plus three divisions per normalisation, sincos pairs, precomputed
+// per-shell sines and cosines, and |a/b|^2 = |a|^2/|b|^2 in the Fresnel
+// reflectivity.  These change results only at the last-bit level; every
+// comparison that decides a photon's fate (shell, reflectivity, order,
+// chip) uses the same quantities and order as the reference.
+#pragma once
+#include <stdint.h>
+#include "mx_model.h"
+
+#ifdef __CUDACC__
+#define MXD __host__ __device__ __forceinline__
+#else
+#define MXD inline
+#include <cmath>
+#endif
+
+namespace mx {
+
+constexpr double PI = 3.14159265358979323846264338327950288;
+
+struct D3 { double x, y, z; };
+MXD D3 mk(double x, double y, double z) { D3 r; r.x = x; r.y = y; r.z = z; return r; }
+MXD D3 operator+(D3 a, D3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+MXD D3 operator-(D3 a, D3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+MXD D3 operator*(double s, D3 a) { return mk(s * a.x, s * a.y, s * a.z); }
+MXD double dot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+MXD D3 cross(D3 a, D3 b) { return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+
+MXD double mx_rsqrt(double x) {
+#ifdef __CUDA_ARCH__
+  return rsqrt(x);
+#else
+  return 1.0 / std::sqrt(x);
+#endif
+}
+MXD void mx_sincos(double x, double *s, double *c) {
+#ifdef __CUDA_ARCH__
+  sincos(x, s, c);
+#else
+  *s = std::sin(x); *c = std::cos(x);
+#endif
+}
+// JDMv_normalize (vector.c:99): a / |a|, a unchanged when |a| = 0.
+MXD D3 normalized(D3 a) {
+  double d = dot(a, a);
+  if (d == 0.0) return a;
+  return mx_rsqrt(d) * a;
+}
+// JDMv_rotate_unit_vector1 (vector.c:198): Rodrigues rotation of p about
+// unit n by (c, s), renormalised.
+MXD D3 rotate_unit(D3 p, D3 n, double c, double s) {
+  double pn = dot(p, n);
+  D3 u = c * p + (pn * (1.0 - c)) * n + s * cross(n, p);
+  return normalized(u);
+}
+MXD D3 rotate_unit_angle(D3 p, D3 n, double theta) {
+  double s, c;
+  mx_sincos(theta, &s, &c);
+  return rotate_unit(p, n, c, s);
+}
+MXD D3 mat_mul(const double *m, D3 v) {  // JDM3m_vector_mul (rotate.c:121), row-major 3x3
+  return mk(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[3] * v.x + m[4] * v.y + m[5] * v.z,
+            m[6] * v.x + m[7] * v.y + m[8] * v.z);
+}
+
+#ifdef __CUDA_ARCH__
+#define MX_LDG(p) __ldg(p)
+#define MX_DMUL(a, b) __dmul_rn(a, b)
+#define MX_DADD(a, b) __dadd_rn(a, b)
+#define MX_DDIV(a, b) __ddiv_rn(a, b)
+#else
+#define MX_LDG(p) (*(p))
+#define MX_DMUL(a, b) ((a) * (b))
+#define MX_DADD(a, b) ((a) + (b))
+#define MX_DDIV(a, b) ((a) / (b))
+#endif
+
+// JDMbinary_search_f (finterpo.c:37): first index with xp >= x (an equal
+// element returns its index), n if all are smaller.
+MXD unsigned bsearch_f(float x, const float *xp, unsigned n) {
+  unsigned n0 = 0, n1 = n;
+  while (n1 > n0 + 1) {
+    unsigned n2 = (n0 + n1) >> 1;
+    float v = xp[n2];
+    if (v >= x) { if (v == x) return n2; n1 = n2; }
+    else n0 = n2;
+  }
+  return (x >= xp[n0]) ? n1 : n0;
+}
+MXD unsigned bsearch_d(double x, const double *xp, unsigned n) {  // JDMbinary_search_d (dinterpo.c:30)
+  unsigned n0 = 0, n1 = n;
+  while (n1 > n0 + 1) {
+    unsigned n2 = (n0 + n1) >> 1;
+    double v = MX_LDG(xp + n2);
+    if (v >= x) { if (v == x) return n2; n1 = n2; }
+    else n0 = n2;
+  }
+  return (x >= MX_LDG(xp + n0)) ? n1 : n0;
+}
+// JDMinterpolate_f (finterpo.c:59-86).  The result is rounded to float, so
+// the double expression is evaluated without contraction exactly as the
+// reference writes it.
+MXD float interp_f(float x, const float *xp, const float *yp, unsigned n) {
+  if (n == 1) return yp[0];
+  unsigned n1 = bsearch_f(x, xp, n), n0 = n1 - 1;
+  if (n1 < n && x == xp[n1]) return yp[n1];
+  if (n1 == n) { n1--; n0--; }
+  if (n1 == 0) n0 = 1;
+  double x0 = xp[n0], x1 = xp[n1];
+  if (x1 == x0) return yp[n1];
+  double dy = (double) (yp[n1] - yp[n0]);
+  double q = MX_DDIV(dy, MX_DADD(x1, -x0));
+  return (float) MX_DADD((double) yp[n0], MX_DMUL(q, MX_DADD((double) x, -x0)));
+}
+
+// ----------------------------------------------------------- variates --
+// Philox4x32-10 (Salmon et al., SC'11).  Uniform slot k of photon `tag`
+// carries 53 random bits; normals use single-precision Box-Muller.
+MXD void philox(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+#ifdef __CUDA_ARCH__
+    uint32_t hi0 = __umulhi(0xD2511F53u, c[0]), lo0 = 0xD2511F53u * c[0];
+    uint32_t hi1 = __umulhi(0xCD9E8D57u, c[2]), lo1 = 0xCD9E8D57u * c[2];
+#else
+    uint64_t p0 = (uint64_t) 0xD2511F53u * c[0], p1 = (uint64_t) 0xCD9E8D57u * c[2];
+    uint32_t hi0 = (uint32_t) (p0 >> 32), lo0 = (uint32_t) p0, hi1 = (uint32_t) (p1 >> 32), lo1 = (uint32_t) p1;
+#endif
+    uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+  }
+}
+MXD double philox_uniform(uint64_t seed, uint32_t tag, uint32_t k) {
+  uint32_t c[4] = {tag, k, 0x5A5A0001u, 0u};
+  philox(c, (uint32_t) seed, (uint32_t) (seed >> 32));
+  uint64_t b = ((uint64_t) c[0] << 32) | c[1];
+  return (double) (b >> 11) * (1.0 / 9007199254740992.0);
+}
+MXD double philox_normal(uint64_t seed, uint32_t tag, uint32_t k) {
+  uint32_t c[4] = {tag, k, 0x5A5A0002u, 0u};
+  philox(c, (uint32_t) seed, (uint32_t) (seed >> 32));
+  float u1 = (float) ((c[0] >> 8) + 1u) * (1.0f / 16777216.0f);
+  float u2 = (float) (c[1] >> 8) * (1.0f / 16777216.0f);
+#ifdef __CUDA_ARCH__
+  float r = sqrtf(-2.0f * logf(u1));
+  return (double) (r * cosf(6.28318530717958647692f * u2));
+#else
+  float r = std::sqrt(-2.0f * std::log(u1));
+  return (double) (r * std::cos(6.28318530717958647692f * u2));
+#endif
+}
+
+// Variate source for one photon: fixed per-stage slot windows.
+struct Rng {
+  const double *U, *N;   // slot-major pre-drawn arrays, or null for Philox
+  uint64_t seed;
+  uint32_t n, i, tag;
+  int upos, uend, npos, nend;
+  bool overrun;
+  MXD void window(int ub, int uc, int nb, int nc) { upos = ub; uend = ub + uc; npos = nb; nend = nb + nc; }
+  MXD double uniform() {
+    if (upos >= uend) { overrun = true; return 0.5; }
+    int k = upos++;
+    return U ? MX_LDG(U + (size_t) k * n + i) : philox_uniform(seed, tag, (uint32_t) k);
+  }
+  MXD double normal() {
+    if (npos >= nend) { overrun = true; return 0.0; }
+    int k = npos++;
+    return N ? MX_LDG(N + (size_t) k * n + i) : philox_normal(seed, tag, (uint32_t) k);
+  }
+};
+
+// Photon state held in registers through the fused trace.
+struct Ph {
+  double e, t;
+  D3 x, p;
+  uint32_t flags;
+  int shell, order, ccd;
+  float ypix, zpix, dith[3];
+};
+
+// ------------------------------------------------------------- mirror --
+// JDMquadratic_root (qroot.c:36-70), same cancellation-free form.
+MXD int quadratic_root(double a, double b, double c, double &rp, double &rm) {
+  if (a == 0.0) return -1;
+  double bsqr = b * b, ac4 = a * c * 4, nb2a = -b / (2.0 * a);
+  if (bsqr > ac4) {
+    double factor = 1.0 + sqrt(1.0 - ac4 / bsqr);
+    rp = -2.0 * c / (b * factor);
+    rm = nb2a * factor;
+    return 1;
+  }
+  if (bsqr == ac4) { rp = rm = nb2a; return 1; }
+  return 0;
+}
+
+// compute_conic_intersection (hrma.c:411-478) for x^2+y^2+z^2 = a x^2+b x+c.
+MXD int conic_intersection(const MxShellDev &h, int o, D3 &x0, D3 p, D3 &normal) {
+  double a = h.a[o], b = h.b[o];
+  double t_plus = -x0.x / p.x, t_minus;
+  double x_y = x0.y + t_plus * p.y, x_z = x0.z + t_plus * p.z;
+  double alpha = a * p.x * p.x - 1.0;
+  double beta = b * p.x - 2.0 * (p.y * x_y + p.z * x_z);
+  double gamma = h.c[o] - x_z * x_z - x_y * x_y;
+  if (alpha == 0.0) {
+    if (beta == 0.0) return -1;
+    t_plus = t_minus = -gamma / beta;
+  } else if (0 >= quadratic_root(alpha, beta, gamma, t_plus, t_minus)) return -1;
+  double x_plus = p.x * t_plus, x_minus = p.x * t_minus;
+  double xmin = h.xmin[o], xmax = h.xmax[o], t;
+  bool okp = (x_plus >= xmin) && (x_plus < xmax), okm = (x_minus >= xmin) && (x_minus < xmax);
+  if (okp) t = (okm && x_minus > x_plus) ? t_minus : t_plus;
+  else if (okm) t = t_minus;
+  else return -1;
+  x0 = mk(p.x * t, x_y + p.y * t, x_z + p.z * t);
+  normal = normalized(mk((a - 1) * x0.x + 0.5 * b, -x0.y, -x0.z));
+  return 0;
+}
+
+// blur_normal (hrma.c:1054-1093): rotate n by a normal-distributed angle
+// about a random axis perpendicular to it.
+MXD void blur_normal(D3 &n, double blur_rad, Rng &rng) {
+  double inv = mx_rsqrt(n.y * n.y + n.z * n.z);
+  D3 perp = mk(0.0, n.z * inv, -n.y * inv);
+  double phi = (2.0 * PI) * rng.uniform();
+  perp = rotate_unit_angle(perp, n, phi);
+  double ang = blur_rad * rng.normal();
+  n = rotate_unit_angle(n, perp, ang);
+}
+
+// marx_reflectivity (reflect.c:39-77): polarisation-averaged Fresnel
+// |r|^2 for n = 1 - delta + i beta (Jackson 7.39, 7.41), with
+// |num/den|^2 = |num|^2 / |den|^2.
+MXD double reflectivity(double cos_t, double beta, double delta) {
+  double nr = 1.0 - delta, ni = beta;
+  double sin2 = 1.0 - cos_t * cos_t;                     // sin_theta^2
+  double sr = nr * nr - ni * ni, si = 2.0 * nr * ni;     // n^2
+  double wr = sr - sin2, wi = si;                        // n^2 - sin^2
+  // principal square root, branches as JDMc_sqrt (complex.c:201)
+  double rr, ri;
+  double r = sqrt(wr * wr + wi * wi);
+  if (r == 0.0) { rr = wr; ri = wi; }
+  else if (wr >= 0.0) { rr = sqrt(0.5 * (r + wr)); ri = 0.5 * wi / rr; }
+  else {
+    double q = sqrt(0.5 * (r - wr));
+    rr = 0.5 * wi / q; ri = q;
+    if (rr < 0.0) { rr = -rr; ri = -ri; }
+  }
+  // e_perp = (cos - root) / (cos + root)
+  double a1 = (cos_t - rr) * (cos_t - rr) + ri * ri, b1 = (cos_t + rr) * (cos_t + rr) + ri * ri;
+  // e_par = (cos n^2 - root) / (cos n^2 + root)
+  double pr = cos_t * sr, pi_ = cos_t * si;
+  double a2 = (pr - rr) * (pr - rr) + (pi_ - ri) * (pi_ - ri);
+  double b2 = (pr + rr) * (pr + rr) + (pi_ + ri) * (pi_ + ri);
+  return 0.5 * (a1 * b2 + a2 * b1) / (b1 * b2);
+}
+
+// interpolate_theta (wfold.c:304-332) on one fold array.
+MXD double fold_theta(const MxTables &T, int table, unsigned a, double p) {
+  const double *hd = T.fold_hdr + ((size_t) table * MX_FOLD_MAX + a) * 8;
+  double p_min = MX_LDG(hd + 1), p_max = MX_LDG(hd + 3);
+  if (p < p_min) return 0.0;
+#ifdef __CUDA_ARCH__
+  if (p > p_max) return pow(MX_LDG(hd + 4) * (1.0 - p), MX_LDG(hd + 5));
+#else
+  if (p > p_max) return std::pow(MX_LDG(hd + 4) * (1.0 - p), MX_LDG(hd + 5));
+#endif
+  double di = (p - p_min) / MX_LDG(hd + 2);
+  unsigned i = (unsigned) di;
+  unsigned num = (unsigned) MX_LDG(hd + 6);
+  const float *t = T.fold_theta + ((size_t) table * MX_FOLD_MAX + a) * MX_FOLD_THETA;
+  if (i + 1 >= num) return (double) MX_LDG(t + num - 1);
+  di -= (double) i;
+  return (1.0 - di) * (double) MX_LDG(t + i) + di * (double) MX_LDG(t + i + 1);
+}
+// marx_wfold_table_interp (wfold.c:334-363).
+MXD double wfold_interp(const MxTables &T, int table, double energy, double sin_alpha, double r) {
+  unsigned num = T.fold_num[table];
+  if (num == 1) return fold_theta(T, table, 0, r);
+  double ea = energy * sin_alpha;
+  const double *eas = T.fold_ealpha + (size_t) table * MX_FOLD_MAX;
+  unsigned i = bsearch_d(ea, eas, num);
+  if (i == num) i--;
+  if (i == 0) i++;
+  double t0 = fold_theta(T, table, i - 1, r), t1 = fold_theta(T, table, i, r);
+  double e0 = MX_LDG(eas + i - 1), e1 = MX_LDG(eas + i);
+  return t0 + (t1 - t0) * (ea - e0) / (e1 - e0);
+}
+
+// reflect_from_conic (hrma.c:488-545): -2 missed, -1 absorbed, 0 reflected.
+MXD int reflect_from_conic(const MxTables &T, const MxShellDev &h, int o, int table, D3 &x, D3 &p,
+                           double energy, double beta, double delta, double corr, Rng &rng) {
+  D3 n;
+  if (-1 == conic_intersection(h, o, x, p, n)) return -2;
+  if (T.use_blur) blur_normal(n, h.blur[o], rng);
+  double pdn = dot(p, n);
+  if (!T.ideal) {
+    double r = rng.uniform();
+    double rfl = reflectivity(fabs(pdn), beta, delta);
+    if (r >= rfl * corr) return -1;
+  }
+  p = p + (-2.0 * pdn) * n;
+  if (!T.use_wfold) return 0;
+  double r = rng.uniform();
+  double dg = wfold_interp(T, table, energy, -pdn, r) * h.scat[o];
+  if (dg > PI / 4) return -1;
+  if (rng.uniform() < 0.5) dg = -dg;
+  p = rotate_unit_angle(p, cross(p, n), dg);
+  return 0;
+}
+
+// intersects_struts (hrma.c:928-968): three bars rotated by 60 degrees.
+MXD bool struts_block(const MxTables &T, int set, D3 x, D3 p) {
+  for (int k = 0; k < 2; k++) {
+    double hw = T.strut_half_width[set][k];
+    double t = (T.strut_xpos[set][k] + T.cap - x.x) / p.x;
+    double y = x.y + p.y * t, z = x.z + p.z * t;
+    for (int i = 0; i < 3; i++) {
+      if (i != 0) { double tmp = T.cos30 * y - T.sin30 * z; z = T.sin30 * y + T.cos30 * z; y = tmp; }
+      if (((-hw < y) && (y < hw)) || ((-hw < z) && (z < hw))) return true;
+    }
+  }
+  return false;
+}
+
+// _marx_hrma_mirror_reflect per photon (hrma.c:1183-1339) with
+// project_photon_to_hrma (hrma.c:984-1050).
+MXD void mirror_stage(const MxTables &T, const MxShellDev *shells, const float *optc, Ph &ph, Rng &rng) {
+  rng.window(MX_U_MIRROR, 12, MX_N_MIRROR, 2);
+  if (!T.ideal) {
+    if (rng.uniform() > T.hrma_vig) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
+    if (ph.flags & MX_BAD_PHOTON_MASK) return;
+  }
+  D3 x = ph.x, p = ph.p;
+  // aperture sampling
+  int si = -1;
+  for (int guard = 0; guard < 64 && si < 0; guard++) {
+    double r = rng.uniform();
+    if (rng.overrun) return;
+    for (int i = 0; i < 4; i++)
+      if (r < shells[i].area_fraction) { si = i; break; }
+  }
+  if (si < 0) { rng.overrun = true; return; }
+  const MxShellDev &h = shells[si];
+  ph.shell = si;
+  double radius;
+  if (T.area_uniform) {
+    double r0 = h.min_radius, r1 = h.max_radius;
+    radius = sqrt(r0 * r0 + (r1 * r1 - r0 * r0) * rng.uniform());
+  } else
+    radius = h.min_radius + (h.max_radius - h.min_radius) * rng.uniform();
+  double theta;
+  for (int guard = 0;; guard++) {
+    theta = rng.uniform();
+    unsigned quad = (unsigned) (4.0 * theta);
+    if (rng.overrun || guard >= 64) { rng.overrun = true; return; }
+    if (h.shutter & (1u << quad)) break;
+  }
+  theta = (2.0 * PI) * (theta - 1.0 / 8.0);
+  double st, ct;
+  mx_sincos(theta, &st, &ct);
+  x = mk(h.front_position, radius * st - h.to_osac[0][1], radius * ct - h.to_osac[0][2]);
+  if (T.source_distance > 0.0) p = normalized(x + T.source_distance * p);
+  if (T.use_struts && struts_block(T, 0, x, p)) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
+
+  x = x + mk(h.to_osac[0][0], h.to_osac[0][1], h.to_osac[0][2]);
+  x = mat_mul(h.fwd[0], x);
+  p = mat_mul(h.fwd[0], p);
+  double beta = 0.0, delta = 1.0, corr = 1.0;
+  if (T.opt_n) {
+    float fe = (float) ph.e;
+    beta = (double) interp_f(fe, optc, optc + T.opt_n, T.opt_n);
+    delta = (double) interp_f(fe, optc, optc + 2 * T.opt_n, T.opt_n);
+    if (T.use_scale) {
+      const float *ce = optc + 3 * T.opt_n + h.corr_off;
+      corr = sqrt((double) interp_f(fe, ce, ce + h.corr_n, h.corr_n));
+    }
+  }
+  int st1 = reflect_from_conic(T, h, 0, 2 * si, x, p, ph.e, beta, delta, corr, rng);
+  if (st1 != 0) { ph.flags |= MX_PHOTON_UNREFLECTED; ph.x = x; ph.p = p; return; }
+  p = mat_mul(h.bwd[0], p);
+  x = mat_mul(h.bwd[0], x);
+  x = x - mk(h.to_osac[0][0], h.to_osac[0][1], h.to_osac[0][2]);
+  if (T.use_struts && struts_block(T, 1, x, p)) { ph.flags |= MX_PHOTON_MIRROR_VBLOCKED; ph.x = x; ph.p = p; return; }
+  x = x + mk(h.to_osac[1][0], h.to_osac[1][1], h.to_osac[1][2]);
+  p = mat_mul(h.fwd[1], p);
+  x = mat_mul(h.fwd[1], x);
+  if (0 != reflect_from_conic(T, h, 1, 2 * si + 1, x, p, ph.e, beta, delta, corr, rng)) {
+    ph.flags |= MX_PHOTON_UNREFLECTED; ph.x = x; ph.p = p; return;
+  }
+  p = mat_mul(h.bwd[1], p);
+  x = mat_mul(h.bwd[1], x);
+  x = x - mk(h.to_osac[1][0], h.to_osac[1][1], h.to_osac[1][2]);
+  if (T.use_struts && struts_block(T, 2, x, p)) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
+  ph.x = x; ph.p = p;
+}
+
+// ------------------------------------------------------------- dither --
+// get_internal_dither + dither_ray + apply_dither (dither.c:167-182,
+// 551-581, 609-628).  The dither angles pass through float as they do in
+// Marx_Dither_Type.
+MXD void dither_stage(const MxTables &T, Ph &ph, Rng &rng) {
+  rng.window(0, 0, MX_N_DITHER, 2);
+  double t = (2.0 * PI) * (T.start_time + ph.t);
+  float fra = (float) (T.dith_amp[0] * sin(t / T.dith_period[0] + T.dith_phase[0]));
+  float fdec = (float) (T.dith_amp[1] * sin(t / T.dith_period[1] + T.dith_phase[1]));
+  float froll = (float) (T.nominal_roll + T.dith_amp[2] * sin(t / T.dith_period[2] + T.dith_phase[2]));
+  ph.dith[0] = fra; ph.dith[1] = fdec; ph.dith[2] = froll;
+  double ra = (double) fra + T.aspect_blur * rng.normal();
+  double dec = (double) fdec + T.aspect_blur * rng.normal();
+  D3 p = rotate_unit_angle(ph.p, mk(1, 0, 0), -(double) froll);
+  double sr, cr, sd, cd;
+  mx_sincos(ra, &sr, &cr);
+  mx_sincos(dec, &sd, &cd);
+  double cos_theta = cd * cr;
+  D3 n = mk(0, sd, -cd * sr);
+  double s2 = n.y * n.y + n.z * n.z;
+  if (!(s2 > 1e-40)) { ph.p = p; return; }
+  double inv = mx_rsqrt(s2);
+  ph.p = rotate_unit(p, inv * n, cos_theta, s2 * inv);
+}
+
+// ------------------------------------------------------------ grating --
+MXD D3 rot_x(D3 a, double c, double s) { return mk(a.x, c * a.y - s * a.z, s * a.y + c * a.z); }
+
+// intersect + newtons_quartic (diffract.c:622-687): Rowland torus.
+MXD int rowland_intersect(D3 &x0, D3 p, double rowland) {
+  double t = -x0.x / p.x;
+  x0 = mk(0.0, x0.y + p.y * t, x0.z + p.z * t);
+  double pxpz = p.x * p.x + p.z * p.z;
+  double x2 = x0.z * x0.z + x0.y * x0.y;
+  double r2 = rowland * rowland;
+  double pdotx = p.y * x0.y + p.z * x0.z;
+  double a = 4.0 * pdotx;
+  double b = 2.0 * x2 + a * pdotx - r2 * pxpz;
+  double c = a * x2 - 2.0 * r2 * p.z * x0.z;
+  double d = x2 * x2 - r2 * x0.z * x0.z;
+  double t0 = -rowland * sqrt(pxpz);
+  double a2 = 2.0 * a, a3 = 3.0 * a, b2 = 2.0 * b;
+  for (int it = 0; it < 10; it++) {
+    double tt = t0 * t0;
+    double num = tt * (3.0 * tt + a2 * t0 + b) - d;
+    double den = tt * (4.0 * t0 + a3) + b2 * t0 + c;
+    t = num / den;
+    if (fabs(t - t0) < 1.0e-4) { x0 = x0 + t * p; return 0; }
+    t0 = t;
+  }
+  return -1;
+}
+
+// diffract_photon (diffract.c:706-823), HETG (theta = 0) with facet sectors.
+MXD int diffract_photon(const MxTables &T, const MxGratingDev &g, int order_idx, double energy,
+                        D3 x, D3 &P, Rng &rng) {
+  double nlod = MX_LDG(T.order_k + g.order_off + order_idx) / energy;
+  D3 n = -1.0 * normalized(x);
+  D3 l = normalized(mk(n.z, 0.0, -n.x));
+  D3 d = cross(n, l);
+  double dtheta, dpp;
+  if (g.nsec > 0) {
+    double sector = atan2(x.y, x.z);
+    if (sector < 0) sector = 2 * PI + sector;
+    const double *smin = T.sectors + g.sec_off;          // [6][nsec]: min max dth dthb dpp dppb
+    unsigned sn = bsearch_d(sector, smin, (unsigned) g.nsec);
+    if (sn == 0) return -1;
+    sn -= 1;
+    if ((MX_LDG(smin + g.nsec + sn) <= sector) || (MX_LDG(smin + sn) > sector)) return -1;
+    dtheta = MX_LDG(smin + 2 * g.nsec + sn) + MX_LDG(smin + 3 * g.nsec + sn) * rng.normal();
+    dpp = MX_LDG(smin + 4 * g.nsec + sn) + MX_LDG(smin + 5 * g.nsec + sn) * rng.normal();
+  } else {
+    dtheta = g.theta_blur * rng.normal();
+    dpp = g.dp_over_p * rng.normal();
+  }
+  double theta = 0.0 - dtheta;
+  if (theta != 0.0) {
+    double s, c;
+    mx_sincos(theta, &s, &c);
+    D3 lt = l, dt = d;
+    l = c * lt + s * dt;
+    d = (-s) * lt + c * dt;
+  }
+  D3 p = P;
+  double p_d = nlod + dot(p, d), p_l = dot(p, l);
+  double p_n = 1.0 - p_l * p_l - p_d * p_d;
+  if (p_n < 0.0) return -1;
+  p_n = sqrt(p_n);
+  P = p_d * d + p_n * n + p_l * l;
+  if (dpp == 0) return 0;
+  double f = nlod * dpp;
+  P = normalized(P + (-f) * d + (f * (p_d / p_n)) * n);
+  return 0;
+}
+
+// diffract (diffract.c:974-1130) for one photon: vignetting, rotation into
+// the grating frame, Rowland torus, cumulative order efficiencies at this
+// energy (JDMinterpolate_n_fvector, finterpo.c:134-190), order choice
+// (diffract_photon_from_grating, diffract.c:828-849) and rotation back.
+MXD void grating_stage(const MxTables &T, const MxGratingDev *grs, Ph &ph, Rng &rng) {
+  rng.window(MX_U_GRATING, 2, MX_N_GRATING, 2);
+  const MxGratingDev &g = grs[ph.shell];
+  if (rng.uniform() > g.vig) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
+  if (ph.flags & MX_BAD_PHOTON_MASK) return;
+  D3 x = rot_x(ph.x, g.cos_m, g.sin_m), p = rot_x(ph.p, g.cos_m, g.sin_m);
+  if (-1 == rowland_intersect(x, p, g.rowland)) ph.flags |= MX_PHOTON_UNDIFFRACTED;
+  // bracket the energy: first index >= 1 with E <= energies[idx], capped at n-1
+  float fe = (float) ph.e;
+  const float *ge = T.geff_energy + g.geff_off;
+  unsigned n = (unsigned) g.nenergy;
+  unsigned lo = 1, hi = n - 1;
+  while (lo < hi) {
+    unsigned mid = (lo + hi) >> 1;
+    if ((double) fe > (double) MX_LDG(ge + mid)) lo = mid + 1; else hi = mid;
+  }
+  unsigned idx = lo;
+  double x0 = MX_LDG(ge + idx - 1), x1 = MX_LDG(ge + idx), dx = MX_DADD(x1, -x0);
+  double w = MX_DADD((double) fe, -x0);
+  const float *c0 = T.geff_cum + g.cum_off + (size_t) (idx - 1) * g.norders;   // [energy][order]
+  double r = rng.uniform();
+  int chosen = -1;
+  for (int k = 0; k < g.norders; k++) {
+    float ck;
+    if (dx == 0.0) ck = MX_LDG(c0 + k);
+    else {
+      double y0 = MX_LDG(c0 + k), y1 = MX_LDG(c0 + g.norders + k);
+      ck = (float) MX_DADD(y0, MX_DDIV(MX_DMUL(MX_DADD(y1, -y0), w), dx));
+    }
+    if (r <= (double) ck) { chosen = k; break; }
+  }
+  if (chosen < 0) ph.flags |= MX_PHOTON_UNDIFFRACTED;
+  else {
+    ph.order = chosen - g.max_order;
+    if (-1 == diffract_photon(T, g, chosen, ph.e, x, p, rng)) ph.flags |= MX_PHOTON_UNDIFFRACTED;
+  }
+  ph.x = rot_x(x, g.cos_p, g.sin_p);
+  ph.p = rot_x(p, g.cos_p, g.sin_p);
+}
+
+// ----------------------------------------------------------- detector --
+// intersect_with_detector_plane (detector.c:56-109).
+MXD int chip_plane(const MxChipDev &g, D3 x0, D3 p, D3 &x, double &dx, double &dy, bool must_hit) {
+  D3 nrm = mk(g.normal[0], g.normal[1], g.normal[2]), ll = mk(g.x_ll[0], g.x_ll[1], g.x_ll[2]);
+  double pdn = dot(p, nrm);
+  if (pdn == 0) return -1;
+  D3 r = x0 - ll;
+  r = r + (-1.0 * dot(r, nrm) / pdn) * p;
+  int hit = 1;
+  double rx = r.x * g.xhat[0] + r.y * g.xhat[1] + r.z * g.xhat[2];
+  if ((rx < 0.0) || (rx >= g.xlen)) { if (must_hit) return 0; hit = 0; }
+  double ry = r.x * g.yhat[0] + r.y * g.yhat[1] + r.z * g.yhat[2];
+  if ((ry < 0.0) || (ry >= g.ylen)) { if (must_hit) return 0; hit = 0; }
+  x = r + ll; dx = rx; dy = ry;
+  return hit;
+}
+
+// _marx_acis_i_detect / _marx_acis_s_detect per photon (acis-i.c:124-157,
+// acis-s.c:203-239), _marx_intersect_with_detector (detector.c:112-168),
+// _marx_acis_apply_streak (acis-i.c:60-93).  QE and pulse height are not
+// modelled (DetIdeal); the detector frame is the identity rotation plus the
+// DetOffset translation (INTERNAL dither has no detector motion).
+MXD void detect_stage(const MxTables &T, const MxChipDev *chips, Ph &ph, Rng &rng) {
+  rng.window(MX_U_DETECT, 2, MX_N_DETECT, 2);
+  D3 off = mk(T.det_offset[0], T.det_offset[1], T.det_offset[2]);
+  D3 x = ph.x - off, p = ph.p;
+  int hit = -1;
+  D3 xh = x;
+  double dx = 0, dy = 0;
+  for (int k = 0; k < T.nchips; k++)
+    if (1 == chip_plane(chips[k], x, p, xh, dx, dy, true)) { hit = k; break; }
+  if (hit < 0 && T.det_extend) {
+    double best = -1;
+    for (int k = 0; k < T.nchips; k++) {
+      D3 xx; double ddx, ddy;
+      if (-1 == chip_plane(chips[k], x, p, xx, ddx, ddy, false)) continue;
+      double ex = ddx - 0.5 * chips[k].xlen, ey = ddy - 0.5 * chips[k].ylen, r2 = ex * ex + ey * ey;
+      if (r2 < best || hit < 0) { hit = k; xh = xx; dx = ddx; dy = ddy; best = r2; }
+    }
+  }
+  if (hit < 0) {
+    ph.flags |= MX_PHOTON_MISSED_DETECTOR;
+    ph.ccd = -1;
+  } else {
+    const MxChipDev &d = chips[hit];
+    x = xh;
+    ph.ccd = d.id;
+    ph.ypix = (float) (dx / d.xpix);
+    ph.zpix = (float) (dy / d.ypix);
+    if (T.frame_transfer > 0.0) {
+      double t = fmod(T.start_time + ph.t, T.frame_time);
+      if (t > T.exposure) {
+        ph.zpix = (float) (1.0 + 1022.0 * rng.uniform());
+        double xp = ((double) ph.ypix - d.xoff) * d.xpix, yp = ((double) ph.zpix - d.yoff) * d.ypix;
+        x = mk(d.x_ll[0] + (xp * d.xhat[0] + yp * d.yhat[0]), d.x_ll[1] + (xp * d.xhat[1] + yp * d.yhat[1]),
+               d.x_ll[2] + (xp * d.xhat[2] + yp * d.yhat[2]));
+        p = normalized(x - mk(T.focal_length, 0, 0));
+        ph.flags |= MX_PHOTON_ACIS_STREAKED;
+      }
+    }
+  }
+  ph.x = x + off;
+  ph.p = p;
+}
+
+// The fused per-photon trace: dither at creation (source.c:357), then the
+// stages of process_photons (marx.c:240-273); a photon with a bad flag is
+// skipped by later stages as marx_prune_photons drops it.
+MXD void trace_photon(const MxTables &T, const MxShellDev *shells, const float *optc, const MxGratingDev *grs,
+                      const MxChipDev *chips, uint32_t stages, Ph &ph, Rng &rng) {
+  if ((stages & MX_STAGE_DITHER) && T.dither) dither_stage(T, ph, rng);
+  if ((stages & MX_STAGE_MIRROR) && !(ph.flags & MX_BAD_PHOTON_MASK)) mirror_stage(T, shells, optc, ph, rng);
+  if ((stages & MX_STAGE_GRATING) && T.grating && !(ph.flags & MX_BAD_PHOTON_MASK)) grating_stage(T, grs, ph, rng);
+  if ((stages & MX_STAGE_DETECT) && T.nchips && !(ph.flags & MX_BAD_PHOTON_MASK)) detect_stage(T, chips, ph, rng);
+}
+
+}  // namespace mx

@@ -1,0 +1,34 @@
+// Host-side types shared by the model builder and the C ABI.
+#pragma once
+#include <map>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "mx_model.h"
+
+namespace mx {
+
+struct Pack {
+  struct Section { int dtype; size_t count; std::vector<char> data; };
+  std::map<std::string, Section> sections;
+  bool load(const char *path, std::string &err);
+  template <class T> const T *get(const std::string &name, size_t *count, std::string &err) const;
+};
+
+// Host copies of every device table, plus the scalar launch parameters.
+struct HostModel {
+  MxTables T;
+  std::vector<MxShellDev> shells;
+  std::vector<float> optc;
+  std::vector<double> fold_hdr, fold_ealpha;
+  std::vector<float> fold_theta;
+  std::vector<MxGratingDev> gratings;
+  std::vector<float> geff_energy, geff_cum;
+  std::vector<double> order_k, sectors;
+  std::vector<MxChipDev> chips;
+};
+
+bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string &err);
+
+}  // namespace mx

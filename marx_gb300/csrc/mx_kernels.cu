@@ -1,0 +1,221 @@
+// Trace, compaction and probe kernels.
+#include <cuda_runtime.h>
+
+#include "mx_device.cuh"
+#include "mx_kernels.cuh"
+
+using namespace mx;
+
+__host__ __device__ static inline size_t align16(size_t x) { return (x + 15) & ~(size_t) 15; }
+
+// Shared-memory staging per block: shell geometry, gratings, chips, then
+// the optical-constant and correction-factor tables (the per-photon binary
+// searches run on these).
+size_t trace_shared_bytes(const MxTables &T) {
+  return align16(4 * sizeof(MxShellDev)) + align16(4 * sizeof(MxGratingDev)) +
+         align16(MX_MAX_CHIPS * sizeof(MxChipDev)) + align16((size_t) T.optc_len * sizeof(float));
+}
+
+__device__ __forceinline__ void copy_words(uint32_t *dst, const uint32_t *src, size_t words) {
+  for (size_t k = threadIdx.x; k < words; k += blockDim.x) dst[k] = __ldg(src + k);
+}
+
+// Fused dither -> mirror -> grating -> detector trace, one photon per
+// thread, grid-stride over the photon list with a resident grid.
+__global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_trace_kernel(MxTables T, TraceIO io) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  size_t o_gr = align16(4 * sizeof(MxShellDev));
+  size_t o_ch = o_gr + align16(4 * sizeof(MxGratingDev));
+  size_t o_op = o_ch + align16(MX_MAX_CHIPS * sizeof(MxChipDev));
+  MxShellDev *sh = (MxShellDev *) smem;
+  MxGratingDev *gr = (MxGratingDev *) (smem + o_gr);
+  MxChipDev *ch = (MxChipDev *) (smem + o_ch);
+  float *optc = (float *) (smem + o_op);
+  copy_words((uint32_t *) sh, (const uint32_t *) T.shells, 4 * sizeof(MxShellDev) / 4);
+  copy_words((uint32_t *) gr, (const uint32_t *) T.gratings, 4 * sizeof(MxGratingDev) / 4);
+  copy_words((uint32_t *) ch, (const uint32_t *) T.chips, (size_t) (T.nchips > 0 ? T.nchips : 1) * sizeof(MxChipDev) / 4);
+  copy_words((uint32_t *) optc, (const uint32_t *) T.optc, (size_t) T.optc_len);
+  __syncthreads();
+
+  const size_t n = io.n;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < io.n; i += stride) {
+    Ph q;
+    q.e = io.energy[i];
+    q.t = io.t ? io.t[i] : 0.0;
+    q.p = mk(io.p[i], io.p[n + i], io.p[2 * n + i]);
+    q.flags = io.flags ? io.flags[i] : 0u;
+    if (io.fresh) {
+      q.x = mk(0.0, 0.0, 0.0);
+      q.shell = 0; q.order = 0; q.ccd = -1; q.ypix = 0.f; q.zpix = 0.f;
+      q.dith[0] = q.dith[1] = q.dith[2] = 0.f;
+    } else {
+      q.x = io.x ? mk(io.x[i], io.x[n + i], io.x[2 * n + i]) : mk(0.0, 0.0, 0.0);
+      q.shell = io.shell ? io.shell[i] : 0;
+      q.order = io.order ? io.order[i] : 0;
+      q.ccd = io.ccd ? io.ccd[i] : -1;
+      q.ypix = io.ypix ? io.ypix[i] : 0.f;
+      q.zpix = io.zpix ? io.zpix[i] : 0.f;
+      for (int k = 0; k < 3; k++) q.dith[k] = io.dith ? io.dith[k * n + i] : 0.f;
+    }
+    Rng r;
+    r.U = io.U; r.N = io.N; r.seed = io.seed; r.n = io.n; r.i = i;
+    r.tag = io.tag ? io.tag[i] : i;
+    r.upos = r.uend = r.npos = r.nend = 0;
+    r.overrun = false;
+    trace_photon(T, sh, optc, gr, ch, io.stages, q, r);
+    if (r.overrun) {
+      q.flags |= MX_PHOTON_VARIATE_OVERRUN;
+      atomicAdd(io.overrun, 1ull);
+    }
+    if (io.x) { io.x[i] = q.x.x; io.x[n + i] = q.x.y; io.x[2 * n + i] = q.x.z; }
+    io.p[i] = q.p.x; io.p[n + i] = q.p.y; io.p[2 * n + i] = q.p.z;
+    if (io.flags) io.flags[i] = q.flags;
+    if (io.shell) io.shell[i] = (int8_t) q.shell;
+    if (io.order) io.order[i] = (int8_t) q.order;
+    if (io.ccd) io.ccd[i] = (int8_t) q.ccd;
+    if (io.ypix) io.ypix[i] = q.ypix;
+    if (io.zpix) io.zpix[i] = q.zpix;
+    if (io.dith) for (int k = 0; k < 3; k++) io.dith[k * n + i] = q.dith[k];
+  }
+}
+
+cudaError_t trace_occupancy(bool philox, int shared_bytes, int *blocks_per_sm) {
+  (void) philox;
+  cudaError_t e = cudaFuncSetAttribute(mx_trace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, shared_bytes);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, mx_trace_kernel, MX_TRACE_BLOCK, shared_bytes);
+}
+
+cudaError_t launch_trace(const MxTables &T, const TraceIO &io, int grid, int shared_bytes, bool slots,
+                         cudaStream_t st) {
+  (void) slots;
+  uint32_t need = (io.n + MX_TRACE_BLOCK - 1) / MX_TRACE_BLOCK;
+  if ((uint32_t) grid > need) grid = (int) need;
+  if (grid < 1) grid = 1;
+  mx_trace_kernel<<<grid, MX_TRACE_BLOCK, shared_bytes, st>>>(T, io);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ compaction --
+// marx_prune_photons (photon.c:40) as a three-pass stream compaction:
+// per-tile survivor counts, an exclusive scan of the counts, then a
+// warp-ballot / block-prefix scatter that keeps ascending index order.
+__global__ void __launch_bounds__(MX_COMPACT_THREADS) mx_compact_count(const uint32_t *flags, uint32_t n,
+                                                                       uint32_t *counts) {
+  __shared__ uint32_t warp_tot[MX_COMPACT_THREADS / 32];
+  uint32_t base = blockIdx.x * MX_COMPACT_TILE, c = 0;
+  for (int j = 0; j < MX_COMPACT_ITEMS; j++) {
+    uint32_t e = base + j * MX_COMPACT_THREADS + threadIdx.x;
+    c += (e < n && (flags[e] & MX_BAD_PHOTON_MASK) == 0) ? 1u : 0u;
+  }
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0) warp_tot[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t s = 0;
+    for (int w = 0; w < MX_COMPACT_THREADS / 32; w++) s += warp_tot[w];
+    counts[blockIdx.x] = s;
+  }
+}
+
+__global__ void __launch_bounds__(1024) mx_compact_scan(uint32_t *counts, uint32_t nblk) {
+  __shared__ uint32_t part[1024];
+  __shared__ uint32_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (uint32_t base = 0; base < nblk; base += 1024) {
+    uint32_t k = base + threadIdx.x;
+    uint32_t v = k < nblk ? counts[k] : 0;
+    part[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {   // inclusive Hillis-Steele scan
+      uint32_t t = threadIdx.x >= (unsigned) o ? part[threadIdx.x - o] : 0;
+      __syncthreads();
+      part[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (k < nblk) counts[k] = carry + part[threadIdx.x] - v;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry += part[1023];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) counts[nblk] = carry;
+}
+
+__global__ void __launch_bounds__(MX_COMPACT_THREADS) mx_compact_scatter(const uint32_t *flags, uint32_t n,
+                                                                         const uint32_t *offsets, uint32_t *idx) {
+  __shared__ uint32_t warp_tot[MX_COMPACT_THREADS / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t run = offsets[blockIdx.x];
+  uint32_t base = blockIdx.x * MX_COMPACT_TILE;
+  for (int j = 0; j < MX_COMPACT_ITEMS; j++) {
+    uint32_t e = base + j * MX_COMPACT_THREADS + threadIdx.x;
+    bool good = e < n && (flags[e] & MX_BAD_PHOTON_MASK) == 0;
+    uint32_t ball = __ballot_sync(0xffffffffu, good);
+    if (lane == 0) warp_tot[warp] = __popc(ball);
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+    for (int w = 0; w < MX_COMPACT_THREADS / 32; w++) {
+      uint32_t t = warp_tot[w];
+      before += (w < warp) ? t : 0;
+      total += t;
+    }
+    if (good) idx[run + before + __popc(ball & ((1u << lane) - 1u))] = e;
+    run += total;
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_compact(const uint32_t *flags, uint32_t n, uint32_t *idx_out, uint32_t *scan, uint32_t nblk,
+                           cudaStream_t st) {
+  mx_compact_count<<<nblk, MX_COMPACT_THREADS, 0, st>>>(flags, n, scan);
+  mx_compact_scan<<<1, 1024, 0, st>>>(scan, nblk);
+  mx_compact_scatter<<<nblk, MX_COMPACT_THREADS, 0, st>>>(flags, n, scan, idx_out);
+  return cudaGetLastError();
+}
+
+// ----------------------------------------------------------- FP64 probe --
+// Dependent-free DFMA chains: 8 accumulators per thread, so the FP64 pipe
+// rather than latency bounds the rate.
+__global__ void __launch_bounds__(256) mx_fp64_probe(double *out, int iters, double a, double b) {
+  double acc[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) acc[k] = threadIdx.x * 1e-3 + k;
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int k = 0; k < 8; k++) acc[k] = fma(acc[k], a, b);
+  }
+  double s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) s += acc[k];
+  if (s == 1234.5) out[0] = s;   // keeps the chains live
+}
+
+cudaError_t probe_fp64(double *tflops, double *ms_out) {
+  int dev, sms;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  double *out;
+  if ((e = cudaMalloc(&out, sizeof(double))) != cudaSuccess) return e;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  const int blocks = sms * 8, iters = 1 << 14;
+  mx_fp64_probe<<<blocks, 256>>>(out, 256, 0.999999, 1e-9);   // warm-up
+  cudaEventRecord(a);
+  mx_fp64_probe<<<blocks, 256>>>(out, iters, 0.999999, 1e-9);
+  cudaEventRecord(b);
+  e = cudaEventSynchronize(b);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(out);
+  if (e != cudaSuccess) return e;
+  double flops = 2.0 * 8.0 * iters * (double) blocks * 256.0;
+  *tflops = flops / (ms * 1e-3) / 1e12;
+  if (ms_out) *ms_out = ms;
+  return cudaGetLastError();
+}

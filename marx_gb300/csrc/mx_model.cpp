@@ -1,0 +1,361 @@
+// Host-side model derivation: table pack + mx_config -> the flat device
+// tables of mx_model.h.  Pure C++ (no CUDA), so it is also exercised by the
+// CPU test suite.
+//
+// The derived quantities follow the reference's init code: get_shell_geometry
+// (hrma.c:551-602), init_hrma_shells (hrma.c:671-745), init_yaw_pitch
+// (hrma.c:842-897) with JDM3m_rot_z_matrix / JDM3m_rot_matrix / JDM3m_mul
+// (rotate.c:60-119), the WFold reader's delta_p adjustment (wfold.c:191-197),
+// sum_file_efficiencies (diffract.c:1254-1300), read_sector_info
+// (diffract.c:1897-1948), the CALDB chip patching and basis
+// (caldb.c:256-491, detector.c:383-402, acis_geom.c:54-67) and the dither
+// parameter scaling (dither.c:508-547).  Host libm evaluates the init-time
+// sines and cosines, as it does in the reference.
+#include "mx_host.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+namespace mx {
+
+static const double PI_ = 3.14159265358979323846264338327950288;
+static const double HBAR_C = 1.973269631e-4;   // marx.h:477, keV um
+
+bool Pack::load(const char *path, std::string &err) {
+  FILE *f = fopen(path, "rb");
+  if (!f) { err = std::string("cannot open table pack ") + (path ? path : "(null)"); return false; }
+  fseek(f, 0, SEEK_END);
+  long sz = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  std::vector<char> b((size_t) (sz > 0 ? sz : 0));
+  size_t got = sz > 0 ? fread(b.data(), 1, (size_t) sz, f) : 0;
+  fclose(f);
+  if ((long) got != sz || sz < 16 || memcmp(b.data(), "MXPACK01", 8) != 0) { err = "not a table pack"; return false; }
+  uint32_t n;
+  memcpy(&n, b.data() + 8, 4);
+  if (16 + 104ull * n > (unsigned long long) sz) { err = "table pack header truncated"; return false; }
+  for (uint32_t i = 0; i < n; i++) {
+    const char *e = b.data() + 16 + 104 * i;
+    char name[49] = {0};
+    memcpy(name, e, 48);
+    Section s;
+    uint32_t dt, nd;
+    uint64_t dims[4], off, nb;
+    memcpy(&dt, e + 48, 4); memcpy(&nd, e + 52, 4); memcpy(dims, e + 56, 32);
+    memcpy(&off, e + 88, 8); memcpy(&nb, e + 96, 8);
+    if (off + nb > (uint64_t) sz || dt > 2) { err = std::string("bad pack section ") + name; return false; }
+    s.dtype = (int) dt;
+    s.count = nb / (dt == 1 ? 8 : 4);
+    s.data.assign(b.data() + off, b.data() + off + nb);
+    sections[name] = std::move(s);
+  }
+  return true;
+}
+
+template <class T> const T *Pack::get(const std::string &name, size_t *count, std::string &err) const {
+  auto it = sections.find(name);
+  if (it == sections.end()) { err = "table pack lacks " + name; return nullptr; }
+  int want = sizeof(T) == 8 ? 1 : (std::is_same<T, float>::value ? 0 : 2);
+  if (it->second.dtype != want) { err = "table pack section " + name + " has the wrong type"; return nullptr; }
+  if (count) *count = it->second.count;
+  return reinterpret_cast<const T *>(it->second.data.data());
+}
+template const double *Pack::get<double>(const std::string &, size_t *, std::string &) const;
+template const float *Pack::get<float>(const std::string &, size_t *, std::string &) const;
+
+// ---------------------------------------------------------------- matrices --
+static void rot_z(double m[9], double theta) {
+  double c = cos(theta), s = sin(theta);
+  s = -s;
+  double r[9] = {c, s, 0.0, -s, c, 0.0, 0.0, 0.0, 1.0};
+  memcpy(m, r, sizeof(r));
+}
+static void rot_axis(double m[9], const double n[3], double theta) {
+  double c = cos(theta), s = sin(theta), c1 = 1 - c;
+  double n0 = n[0], n1 = n[1], n2 = n[2];
+  double n01 = n0 * n1 * c1, n02 = n0 * n2 * c1, n12 = n1 * n2 * c1;
+  m[0] = n0 * n0 * c1 + c; m[1] = n01 - s * n2; m[2] = n02 + s * n1;
+  m[3] = n01 + s * n2; m[4] = n1 * n1 * c1 + c; m[5] = n12 - s * n0;
+  m[6] = n02 - s * n1; m[7] = n12 + s * n0; m[8] = n2 * n2 * c1 + c;
+}
+static void mat3_mul(double c[9], const double a[9], const double b[9]) {
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) c[3 * i + j] = a[3 * i] * b[j] + a[3 * i + 1] * b[3 + j] + a[3 * i + 2] * b[6 + j];
+}
+static double vlen(const double a[3]) {  // JDMv_length (vector.c:77)
+  double x = fabs(a[0]), y = fabs(a[1]), z = fabs(a[2]), t;
+  if (z < x) { t = z; z = x; x = t; }
+  if (z < y) { t = z; z = y; y = t; }
+  if (z == 0.0) return 0.0;
+  x = x / z; y = y / z;
+  return z * sqrt(1.0 + x * x + y * y);
+}
+static void vnorm(double a[3]) {
+  double l = vlen(a);
+  if (l != 0.0) { a[0] = a[0] / l; a[1] = a[1] / l; a[2] = a[2] / l; }
+}
+
+bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string &err) {
+  M = HostModel();
+  MxTables &T = M.T;
+  memset(&T, 0, sizeof(T));
+  static const int ids[4] = {1, 3, 4, 6};
+  T.ideal = cfg.hrma_ideal != 0;
+  T.use_blur = !T.ideal && cfg.use_blur;
+  T.use_wfold = !T.ideal && cfg.use_wfold;
+  T.use_struts = cfg.use_struts != 0;
+  T.use_scale = cfg.use_scale_factors != 0;
+  T.area_uniform = cfg.aperture_area_uniform != 0;
+  T.hrma_vig = cfg.hrma_vig;
+  T.source_distance = cfg.source_distance;
+  T.cap = cfg.hrma_cap_x;
+  double th30 = 30.0 * (PI_ / 180.0);
+  T.cos30 = cos(th30); T.sin30 = sin(th30);
+  const double sx[3][2] = {{1492.060, 942.266}, {0.5 * 1.965 * 25.4, -0.5 * 1.965 * 25.4}, {-1050.353, -1271.333}};
+  const double sw[3][2] = {{0.5 * 0.5 * 25.4, 0.5 * 0.5 * 25.4}, {0.5 * 0.75 * 25.4, 0.5 * 0.75 * 25.4},
+                           {0.5 * 0.5 * 25.4, 0.5 * 0.5 * 25.4}};
+  memcpy(T.strut_xpos, sx, sizeof(sx));
+  memcpy(T.strut_half_width, sw, sizeof(sw));
+
+  if (cfg.hrma_vig < 0 || cfg.hrma_vig > 1) { err = "HRMAVig must lie in [0,1]"; return false; }
+  for (int i = 0; i < 4; i++)
+    if (!(cfg.hetg_period[i] > 0) && cfg.grating == MX_GRATING_HETG) { err = "HETG period must be > 0"; return false; }
+
+  // ---- HRMA shells
+  size_t cnt;
+  const double *rdb = pk.get<double>("hrma/rdb", &cnt, err);
+  if (!rdb) return false;
+  if (cnt != 72) { err = "hrma/rdb must hold 8 x 9 values"; return false; }
+  const float *opt = pk.get<float>("hrma/optconst", &cnt, err);
+  if (!opt) return false;
+  unsigned optn = (unsigned) (cnt / 3);
+  T.opt_n = T.ideal ? 0 : (int32_t) optn;
+  M.optc.assign(opt, opt + 3 * optn);
+  double total_area = 0.0;
+  M.shells.resize(4);
+  for (int i = 0; i < 4; i++) {
+    MxShellDev &h = M.shells[i];
+    memset(&h, 0, sizeof(h));
+    double cap_pos = cfg.hrma_cap_x + cfg.shell_xoffset[i];
+    double len[2];
+    for (int o = 0; o < 2; o++) {
+      const double *q = rdb + (4 * o + i) * 9;   // x0 y0 z0 p k rho0 az el l
+      len[o] = q[8];
+      h.c[o] = q[5] * q[5]; h.b[o] = -2.0 * q[4]; h.a[o] = 1.0 - q[3];
+      h.xmin[o] = -0.5 * q[8]; h.xmax[o] = 0.5 * q[8];
+      h.to_osac[o][0] = -(-q[2]) - cap_pos;
+      h.to_osac[o][1] = (-q[0]);
+      h.to_osac[o][2] = -(-q[1]);
+      double el = -q[7] * (PI_ / 180.0), az = -q[6] * (PI_ / 180);
+      double rz[9], ry[9], ny[3];
+      rot_z(rz, -az);
+      ny[0] = rz[1]; ny[1] = rz[4]; ny[2] = rz[7];   // rz * (0,1,0)
+      ny[0] = rz[0] * 0 + rz[1] * 1 + rz[2] * 0;
+      ny[1] = rz[3] * 0 + rz[4] * 1 + rz[5] * 0;
+      ny[2] = rz[6] * 0 + rz[7] * 1 + rz[8] * 0;
+      rot_axis(ry, ny, -el);
+      mat3_mul(h.fwd[o], ry, rz);
+      rot_axis(ry, ny, el);
+      rot_z(rz, az);
+      mat3_mul(h.bwd[o], rz, ry);
+    }
+    const double *qp = rdb + i * 9;
+    h.front_position = cap_pos - qp[2] + h.xmax[0];
+    auto radius = [](double a, double b, double c, double x) { return sqrt(c + x * (b + x * (a - 1))); };
+    h.min_radius = radius(h.a[0], h.b[0], h.c[0], h.xmin[0]);
+    h.max_radius = radius(h.a[0], h.b[0], h.c[0], h.xmax[0]);
+    h.min_radius -= len[0] * tan(0.67 * PI_ / 180);
+    h.shutter = cfg.shutters[i] & 0xF;
+    unsigned nopen = (unsigned) __builtin_popcount(h.shutter);
+    if (nopen) total_area += (nopen / 4.0) * (h.max_radius - h.min_radius) * (h.max_radius + h.min_radius);
+    h.area_fraction = total_area;
+    h.blur[0] = cfg.blur_p[i] * (1.0 / 3600.0 * PI_ / 180.0);
+    h.blur[1] = cfg.blur_h[i] * (1.0 / 3600.0 * PI_ / 180.0);
+    h.scat[0] = cfg.scat_p[i]; h.scat[1] = cfg.scat_h[i];
+    const float *corr = pk.get<float>("hrma/corr" + std::to_string(ids[i]), &cnt, err);
+    if (!corr) return false;
+    h.corr_off = (int32_t) (M.optc.size() - 3 * optn);
+    h.corr_n = (int32_t) (cnt / 2);
+    M.optc.insert(M.optc.end(), corr, corr + cnt);
+  }
+  if (total_area <= 0.0) { err = "The mirror geometric area is 0.  Check shutters."; return false; }
+  for (auto &h : M.shells) h.area_fraction = h.area_fraction / total_area;
+  T.optc_len = (int32_t) M.optc.size();
+
+  // ---- WFold tables: index 2*shell + optic
+  M.fold_hdr.assign((size_t) 8 * MX_FOLD_MAX * 8, 0.0);
+  M.fold_ealpha.assign((size_t) 8 * MX_FOLD_MAX, 0.0);
+  M.fold_theta.assign((size_t) 8 * MX_FOLD_MAX * MX_FOLD_THETA, 0.0f);
+  for (int i = 0; i < 4; i++)
+    for (int o = 0; o < 2; o++) {
+      std::string base = std::string("wfold/") + (o ? "h" : "p") + std::to_string(ids[i]);
+      size_t nh, nt;
+      const double *hd = pk.get<double>(base + "/hdr", &nh, err);
+      const float *th = pk.get<float>(base + "/theta", &nt, err);
+      if (!hd || !th) return false;
+      size_t narr = nh / 7, nmax = narr ? nt / narr : 0;
+      if (narr == 0 || narr > MX_FOLD_MAX || nmax > MX_FOLD_THETA) { err = base + ": table too large"; return false; }
+      int t = 2 * i + o;
+      T.fold_num[t] = (uint32_t) narr;
+      for (size_t a = 0; a < narr; a++) {
+        double *dst = &M.fold_hdr[((size_t) t * MX_FOLD_MAX + a) * 8];
+        memcpy(dst, hd + 7 * a, 7 * sizeof(double));
+        if (hd[7 * a + 6] > (double) nmax || hd[7 * a + 6] < 1) { err = base + ": bad angle count"; return false; }
+        M.fold_ealpha[(size_t) t * MX_FOLD_MAX + a] = hd[7 * a];
+        memcpy(&M.fold_theta[((size_t) t * MX_FOLD_MAX + a) * MX_FOLD_THETA], th + a * nmax, nmax * sizeof(float));
+      }
+    }
+
+  // ---- HETG
+  T.grating = cfg.grating == MX_GRATING_HETG;
+  M.gratings.assign(4, MxGratingDev());
+  if (T.grating) {
+    for (int i = 0; i < 4; i++) {
+      MxGratingDev &g = M.gratings[i];
+      memset(&g, 0, sizeof(g));
+      size_t ne, neff;
+      const float *e = pk.get<float>("hetg/geff" + std::to_string(i) + "/energy", &ne, err);
+      const float *eff = pk.get<float>("hetg/geff" + std::to_string(i) + "/eff", &neff, err);
+      if (!e || !eff) return false;
+      unsigned no = (unsigned) (neff / ne);
+      if (ne < 2 || no < 3 || (no % 2) != 1) { err = "grating efficiency table malformed"; return false; }
+      int max_order = (int) (no / 2);
+      std::vector<float> cum(eff, eff + neff);   // [order][energy]
+      if (cfg.max_order > 0) {
+        for (unsigned j = 0; j < ne; j++) {
+          double tot = 0.0, kept = 0.0;
+          for (unsigned k = 0; k < no; k++) {
+            tot += (double) cum[k * ne + j];
+            if (abs((int) k - max_order) <= cfg.max_order) kept += (double) cum[k * ne + j];
+          }
+          for (unsigned k = 0; k < no; k++)
+            cum[k * ne + j] = (abs((int) k - max_order) <= cfg.max_order && kept > 0.0)
+                                  ? (float) ((double) cum[k * ne + j] * (tot / kept)) : 0.0f;
+        }
+      }
+      for (unsigned j = 0; j < ne; j++) {   // sum_file_efficiencies with scale 1
+        double sum = 0.0;
+        for (unsigned k = 0; k < no; k++) { sum += 1.0 * (double) cum[k * ne + j]; cum[k * ne + j] = (float) sum; }
+        if (sum > 1.0)
+          for (unsigned k = 0; k < no; k++) cum[k * ne + j] = (float) (cum[k * ne + j] / sum);
+      }
+      g.geff_off = (int32_t) M.geff_energy.size();
+      M.geff_energy.insert(M.geff_energy.end(), e, e + ne);
+      g.cum_off = (int32_t) M.geff_cum.size();
+      for (unsigned j = 0; j < ne; j++)
+        for (unsigned k = 0; k < no; k++) M.geff_cum.push_back(cum[k * ne + j]);   // [energy][order]
+      g.nenergy = (int32_t) ne; g.norders = (int32_t) no; g.max_order = max_order;
+      g.order_off = (int32_t) M.order_k.size();
+      for (unsigned k = 0; k < no; k++) {
+        int order = (int) k - max_order;
+        M.order_k.push_back(order * (2.0 * PI_ * HBAR_C) / cfg.hetg_period[i]);
+      }
+      double disp = (cfg.hetg_theta[i] * (PI_ / 180.0));
+      double th = -1 * disp;
+      g.cos_m = cos(th); g.sin_m = sin(th);
+      th = 1 * disp;
+      g.cos_p = cos(th); g.sin_p = sin(th);
+      g.theta_blur = (cfg.hetg_dtheta[i] * (PI_ / 180.0) / 60.0);
+      g.dp_over_p = cfg.hetg_dpp[i];
+      g.vig = cfg.hetg_vig[i];
+      g.rowland = i < 2 ? cfg.meg_rowland : cfg.heg_rowland;
+      g.nsec = 0;
+      if (cfg.use_sector_files) {
+        size_t ns;
+        const double *s = pk.get<double>("hetg/sector" + std::to_string(ids[i]), &ns, err);
+        if (!s) return false;
+        ns /= 6;
+        if (ns == 0 || ns > MX_MAX_SECTORS) { err = "sector table size"; return false; }
+        g.sec_off = (int32_t) M.sectors.size();
+        g.nsec = (int32_t) ns;
+        std::vector<double> cols(6 * ns);
+        for (size_t k = 0; k < ns; k++) {
+          cols[0 * ns + k] = s[6 * k] * (PI_ / 180.0);
+          cols[1 * ns + k] = s[6 * k + 1] * (PI_ / 180.0);
+          cols[2 * ns + k] = s[6 * k + 2] * (PI_ / (180.0 * 60.0));
+          cols[3 * ns + k] = s[6 * k + 3] * (PI_ / (180.0 * 60.0));
+          cols[4 * ns + k] = s[6 * k + 4];
+          cols[5 * ns + k] = s[6 * k + 5];
+        }
+        M.sectors.insert(M.sectors.end(), cols.begin(), cols.end());
+      }
+    }
+  }
+  if (M.geff_energy.empty()) M.geff_energy.push_back(0.f);
+  if (M.geff_cum.empty()) M.geff_cum.push_back(0.f);
+  if (M.order_k.empty()) M.order_k.push_back(0.0);
+  if (M.sectors.empty()) M.sectors.push_back(0.0);
+
+  // ---- detector chips
+  T.nchips = 0;
+  if (cfg.detector == MX_DETECTOR_ACIS_I || cfg.detector == MX_DETECTOR_ACIS_S) {
+    size_t ng;
+    const double *geom = pk.get<double>("acis/geom", &ng, err);
+    const double *orig = pk.get<double>("acis/origin", nullptr, err);
+    const double *aim = pk.get<double>(cfg.detector == MX_DETECTOR_ACIS_I ? "acis/aimpt_i" : "acis/aimpt_s", nullptr, err);
+    if (!geom || !orig || !aim) return false;
+    ng /= 13;
+    int lo = cfg.detector == MX_DETECTOR_ACIS_I ? 0 : 4, hi = cfg.detector == MX_DETECTOR_ACIS_I ? 3 : 9;
+    double ofs[3] = {aim[0] + orig[0], aim[1] + orig[1], aim[2] + orig[2]};
+    for (int id = lo; id <= hi; id++) {
+      double ll[3] = {0, 0, 0}, lr[3] = {0, 0, 0}, ul[3] = {0, 0, 0};
+      bool found = false;
+      for (size_t r = 0; r < ng; r++)
+        if ((int) geom[13 * r] == id) {
+          const double *q = geom + 13 * r;
+          for (int k = 0; k < 3; k++) { ll[k] = q[1 + k]; lr[k] = q[4 + k]; ul[k] = q[7 + k]; }
+          found = true;
+        }
+      if (!found) { err = "chip missing from the geometry table"; return false; }
+      MxChipDev c;
+      memset(&c, 0, sizeof(c));
+      c.id = id;
+      double xh[3], yh[3];
+      for (int k = 0; k < 3; k++) {
+        lr[k] = lr[k] + ofs[k]; ll[k] = ll[k] + ofs[k]; ul[k] = ul[k] + ofs[k];
+        xh[k] = lr[k] - ll[k]; yh[k] = ul[k] - ll[k];
+      }
+      c.xlen = vlen(xh); c.ylen = vlen(yh);
+      vnorm(xh); vnorm(yh);
+      for (int k = 0; k < 3; k++) { c.x_ll[k] = ll[k]; c.xhat[k] = xh[k]; c.yhat[k] = yh[k]; }
+      c.normal[2] = xh[0] * yh[1] - xh[1] * yh[0];
+      c.normal[0] = xh[1] * yh[2] - xh[2] * yh[1];
+      c.normal[1] = xh[2] * yh[0] - xh[0] * yh[2];
+      c.xpix = c.xlen / 1024.0; c.ypix = c.ylen / 1024.0;
+      M.chips.push_back(c);
+    }
+    if (cfg.acis_exposure_time <= 0) { err = "ACIS_Exposure_Time must be greater than 0"; return false; }
+    T.nchips = (int32_t) M.chips.size();
+    T.det_extend = cfg.det_extend != 0;
+    for (int k = 0; k < 3; k++) T.det_offset[k] = cfg.det_offset[k];
+    T.frame_transfer = cfg.acis_frame_transfer_time < 0.0 ? 0.0 : cfg.acis_frame_transfer_time;
+    T.exposure = cfg.acis_exposure_time;
+    T.frame_time = T.frame_transfer + T.exposure;
+    T.focal_length = cfg.focal_length;
+  } else if (cfg.detector != MX_DETECTOR_NONE) {
+    err = "unsupported detector"; return false;
+  }
+  if (M.chips.empty()) M.chips.push_back(MxChipDev());
+
+  // ---- dither
+  T.dither = cfg.dither == MX_DITHER_INTERNAL;
+  T.aspect_blur = cfg.aspect_blur * (PI_ / (180.0 * 3600.0));
+  if (T.aspect_blur < 0) T.aspect_blur = 0.0;
+  for (int k = 0; k < 3; k++) {
+    T.dith_amp[k] = cfg.dither_amp[k] * (PI_ / (180.0 * 3600));
+    T.dith_period[k] = cfg.dither_period[k];
+    T.dith_phase[k] = cfg.dither_phase[k];
+    if (T.dither && !(cfg.dither_period[k] > 0)) { err = "dither periods must be > 0"; return false; }
+  }
+  double roll = cfg.roll_nom * (PI_ / 180.0);
+  double xr = fmod(roll, 2 * PI_);
+  if (xr >= PI_) xr -= (2 * PI_);
+  if (xr < -PI_) xr += (2 * PI_);
+  T.nominal_roll = xr;
+  T.start_time = cfg.start_time;
+  return true;
+}
+
+}  // namespace mx

@@ -1,0 +1,66 @@
+// Device-side model tables, derived on the host from the table pack and an
+// mx_config (see mx_host.cpp) and read by the trace kernels.
+#pragma once
+#include <stdint.h>
+#include "../../include/marx_gb300.h"
+
+#define MX_FOLD_MAX 256      // WFold arrays per table (the HRMA tables hold 200)
+#define MX_FOLD_THETA 208    // angles per WFold array (the HRMA tables hold 201)
+#define MX_MAX_CHIPS 10
+#define MX_MAX_SECTORS 64
+
+// One HRMA shell: both optics (index 0 = paraboloid P, 1 = hyperboloid H).
+struct MxShellDev {
+  double a[2], b[2], c[2], xmin[2], xmax[2];   // conic x^2+r^2 = a x^2 + b x + c, x-limits (hrma.c:555-575)
+  double to_osac[2][3];                        // MARX -> OSAC translation (hrma.c:590-599)
+  double fwd[2][9], bwd[2][9];                 // pitch/yaw matrices (hrma.c:842-897)
+  double front_position, area_fraction, min_radius, max_radius;
+  double blur[2];                              // normal blur sigma (rad)
+  double scat[2];                              // WFold scattering factor
+  int32_t corr_off, corr_n;                    // correction-factor table (floats after the optical constants)
+  uint32_t shutter;                            // open-quadrant bitmap
+  int32_t pad;
+};
+
+// One HETG grating (per mirror shell, diffract.c:51-77).
+struct MxGratingDev {
+  double vig, rowland, theta_blur, dp_over_p;
+  double cos_m, sin_m, cos_p, sin_p;           // rotation by -/+ dispersion angle
+  int32_t geff_off, cum_off, nenergy, norders; // cumulative efficiencies [energy][order]
+  int32_t max_order, order_off, sec_off, nsec; // order_k offset; sectors [6][nsec]
+};
+
+struct MxChipDev {
+  double x_ll[3], xhat[3], yhat[3], normal[3];
+  double xlen, ylen, xpix, ypix, xoff, yoff;
+  int32_t id, pad;
+};
+
+// Everything the kernels read, passed by value as a launch parameter.
+struct MxTables {
+  // device pointers
+  const MxShellDev *shells;
+  const float *optc;            // [beta-table energies | beta | delta | corr(E,f) per shell]
+  int32_t optc_len;             // floats in optc
+  int32_t opt_n;                // rows of the optical-constant table (0: perfect reflector)
+  const double *fold_hdr;       // [8][MX_FOLD_MAX][8]: e_alpha p_min delta_p p_max norm expon num -
+  const double *fold_ealpha;    // [8][MX_FOLD_MAX]
+  const float *fold_theta;      // [8][MX_FOLD_MAX][MX_FOLD_THETA]
+  uint32_t fold_num[8];         // table index = 2 * shell + optic
+  const MxGratingDev *gratings;
+  const float *geff_energy;
+  const float *geff_cum;
+  const double *order_k;        // order * (2 pi hbar c) / period, per grating and order
+  const double *sectors;
+  const MxChipDev *chips;
+  // mirror
+  int32_t ideal, use_blur, use_wfold, use_struts, use_scale, area_uniform;
+  double hrma_vig, source_distance, cap, cos30, sin30;
+  double strut_xpos[3][2], strut_half_width[3][2];
+  // dither
+  int32_t dither, grating;
+  double dith_amp[3], dith_period[3], dith_phase[3], nominal_roll, aspect_blur, start_time;
+  // detector
+  int32_t nchips, det_extend;
+  double det_offset[3], frame_transfer, frame_time, exposure, focal_length;
+};

@@ -139,13 +139,13 @@ static bool setup(mxo_model *o, const mx_config *cfg) {
       mmul(h.bwd[o2], rz, ry);
     }
     // correction factors and WFold tables
-    size_t cnt;
+    size_t cnt = 0;
     const float *corr = sec<float>(o, "hrma/corr" + std::to_string(ids[i]), &cnt);
     if (!corr) return false;
     h.corr_n = (unsigned) (cnt / 2); h.corr_e = corr; h.corr_f = corr + h.corr_n;
     for (int o2 = 0; o2 < 2; o2++) {
       std::string base = std::string("wfold/") + (o2 ? "h" : "p") + std::to_string(ids[i]);
-      size_t nh, nt;
+      size_t nh = 0, nt = 0;
       const double *hdr = sec<double>(o, base + "/hdr", &nh);
       const float *th = sec<float>(o, base + "/theta", &nt);
       if (!hdr || !th) return false;
@@ -161,7 +161,7 @@ static bool setup(mxo_model *o, const mx_config *cfg) {
   }
   if (total_area <= 0.0) { g_err = "mirror geometric area is 0"; return false; }
   for (int i = 0; i < 4; i++) M.sh[i].area_fraction = M.sh[i].area_fraction / total_area;
-  size_t cnt;
+  size_t cnt = 0;
   const float *opt = sec<float>(o, "hrma/optconst", &cnt);
   if (!opt) return false;
   if (M.ideal) M.opt_n = 0;
@@ -171,7 +171,7 @@ static bool setup(mxo_model *o, const mx_config *cfg) {
   if (cfg->grating == MX_GRATING_HETG) {
     for (int i = 0; i < 4; i++) {
       Grating &g = M.gr[i];
-      size_t ne, neff;
+      size_t ne = 0, neff = 0;
       const float *e = sec<float>(o, "hetg/geff" + std::to_string(i) + "/energy", &ne);
       const float *eff = sec<float>(o, "hetg/geff" + std::to_string(i) + "/eff", &neff);
       if (!e || !eff) return false;
@@ -212,7 +212,7 @@ static bool setup(mxo_model *o, const mx_config *cfg) {
       g.rowland = (i < 2) ? cfg->meg_rowland : cfg->heg_rowland;
       g.have_sectors = cfg->use_sector_files != 0;
       if (g.have_sectors) {
-        size_t ns;
+        size_t ns = 0;
         const double *s = sec<double>(o, "hetg/sector" + std::to_string(ids[i]), &ns);
         if (!s) return false;
         ns /= 6;
@@ -233,7 +233,7 @@ static bool setup(mxo_model *o, const mx_config *cfg) {
   // detector chips
   M.chips.clear();
   if (cfg->detector != MX_DETECTOR_NONE) {
-    size_t ng;
+    size_t ng = 0;
     const double *geom = sec<double>(o, "acis/geom", &ng);
     const double *orig = sec<double>(o, "acis/origin");
     const double *aim = sec<double>(o, cfg->detector == MX_DETECTOR_ACIS_I ? "acis/aimpt_i" : "acis/aimpt_s");

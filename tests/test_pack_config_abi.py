@@ -1,0 +1,102 @@
+"""Host-side pieces that need no GPU: the table pack, parameter handling,
+configuration validation, and the C ABI library's exports."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from marx_gb300 import config as cfgmod
+from marx_gb300.caldb.pack import DEFAULT_PACK, read_pack, write_pack
+from marx_gb300 import workloads as W
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_pack_holds_every_table():
+    S = read_pack(DEFAULT_PACK)
+    assert S["hrma/rdb"].shape == (8, 9)
+    assert S["hrma/optconst"].shape[0] == 3
+    for s in (1, 3, 4, 6):
+        assert S[f"hrma/corr{s}"].shape[0] == 2
+        for k in "ph":
+            h = S[f"wfold/{k}{s}/hdr"]
+            assert np.all(np.diff(h[:, 0]) > 0)           # sorted by E sin(alpha), no duplicates
+            assert S[f"wfold/{k}{s}/theta"].shape[0] == h.shape[0]
+    for i in range(4):
+        e = S[f"hetg/geff{i}/energy"]
+        assert np.all(np.diff(e) >= 0)
+        assert S[f"hetg/geff{i}/eff"].shape == (23, e.size)
+    assert S["acis/geom"].shape == (10, 13)
+
+
+def test_pack_round_trip(tmp_path):
+    S = {"a": np.arange(5, dtype=np.float64), "b/c": np.ones((2, 3), np.float32), "d": np.array([7], np.int32)}
+    p = tmp_path / "t.mxpack"
+    write_pack(str(p), S)
+    T = read_pack(str(p))
+    for k in S:
+        assert T[k].dtype == S[k].dtype and np.array_equal(T[k], S[k])
+
+
+def test_par_round_trip(tmp_path):
+    c = W.plain_scatter().cfg
+    par = cfgmod.to_par(c)
+    lines = [f'{k},s,h,"{v}",,,""' for k, v in par.items()]
+    p = tmp_path / "x.par"
+    p.write_text("\n".join(lines) + "\n")
+    d = cfgmod.from_par(str(p))
+    assert bytes(d) == bytes(c)
+
+
+def _native():
+    from marx_gb300.build import build
+    build()
+    from marx_gb300 import _native
+    return _native
+
+
+def declared_functions():
+    txt = open(os.path.join(ROOT, "include", "marx_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(mx_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_function():
+    L = _native().load_library()
+    names = declared_functions()
+    assert len(names) >= 14
+    for n in names:
+        assert hasattr(L, n), n
+
+
+def test_validate_config_rejects_bad_values():
+    nat = _native()
+    c = cfgmod.default_config()
+    assert nat.validate_config(c) is None
+    bad = cfgmod.copy_config(c); bad.hrma_vig = 1.5
+    assert "HRMAVig" in nat.validate_config(bad)
+    bad = cfgmod.copy_config(c); bad.shutters[:] = [0, 0, 0, 0]
+    assert "area is 0" in nat.validate_config(bad)
+    bad = cfgmod.copy_config(c); bad.acis_exposure_time = 0
+    assert "Exposure" in nat.validate_config(bad)
+    bad = cfgmod.copy_config(c); bad.detector = 7
+    assert nat.validate_config(bad) is not None
+    assert nat.validate_config(c, pack="/nonexistent.mxpack") is not None
+
+
+def test_engine_fails_loudly_without_a_device():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    nat = _native()
+    with pytest.raises(RuntimeError):
+        nat.Engine(cfgmod.default_config())
+
+
+def test_default_config_matches_c_defaults():
+    L = _native().load_library()
+    c = cfgmod.MxConfig()
+    L.mx_config_default(C.byref(c))
+    assert bytes(c) == bytes(cfgmod.default_config())

@@ -1,0 +1,151 @@
+"""GPU trace against the reference's outputs and the CPU oracle.
+
+Tolerances (the parity contract): positions within 1e-9 mm, directions
+within 1e-12, and flags, mirror shell, grating order, chip, pixel and
+dither state exact.
+"""
+import numpy as np
+import pytest
+
+from marx_gb300 import workloads as W
+from marx_gb300.photons import PhotonList, predraw_variates, BAD_PHOTON_MASK
+
+from helpers import load_trace_fixture, assert_parity, compare
+
+pytestmark = pytest.mark.gpu
+NAMES = list(W.PLAIN)
+
+
+def engine(cfg):
+    from marx_gb300._native import Engine
+    return Engine(cfg)
+
+
+def device_trace(eng, ph, U=None, N=None, seed=0, stages=15):
+    import torch
+    from marx_gb300._native import DevicePhotons
+    d = DevicePhotons.from_host(ph)
+    Ud = torch.from_numpy(U).cuda() if U is not None else None
+    Nd = torch.from_numpy(N).cuda() if N is not None else None
+    eng.trace(d, stages=stages, U=Ud, N=Nd, seed=seed)
+    torch.cuda.synchronize()
+    return d.to_host()
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_gpu_matches_reference_fixture(cuda, name):
+    w, ph, U, N, z = load_trace_fixture(name)
+    eng = engine(w.cfg)
+    q = device_trace(eng, ph, U, N)
+    assert_parity(q, z, f"{name} device buffers")
+    assert eng.overrun_count() == 0
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_gpu_host_entry_matches_reference_fixture(cuda, name):
+    w, ph, U, N, z = load_trace_fixture(name)
+    eng = engine(w.cfg)
+    q = ph.copy()
+    eng.trace_host(q, U=U, N=N)
+    assert_parity(q, z, f"{name} host buffers")
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_gpu_matches_oracle_philox(cuda, name):
+    from oracle.bindings import Oracle
+    w = W.PLAIN[name]()
+    ph = w.photons(200_000, seed=4242)
+    a = ph.copy()
+    Oracle(w.cfg).trace(a, seed=31337)
+    q = device_trace(engine(w.cfg), ph, seed=31337)
+    assert_parity(q, a, f"{name} philox")
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_split_stages_equal_fused(cuda, name):
+    w, ph, U, N, z = load_trace_fixture(name)
+    eng = engine(w.cfg)
+    fused = device_trace(eng, ph, U, N)
+    import torch
+    from marx_gb300._native import DevicePhotons
+    d = DevicePhotons.from_host(ph)
+    Ud, Nd = torch.from_numpy(U).cuda(), torch.from_numpy(N).cuda()
+    for st in (1, 2, 4, 8):
+        eng.trace(d, stages=st, U=Ud, N=Nd)
+    torch.cuda.synchronize()
+    r = compare(d.to_host(), fused)
+    assert r["dx"] == 0 and r["dp"] == 0 and all(v == 0 for k, v in r.items() if k not in ("dx", "dp")), r
+
+
+def test_empty_single_and_ragged_lists(cuda):
+    from oracle.bindings import Oracle
+    w = W.plain_hetg()
+    eng = engine(w.cfg)
+    o = Oracle(w.cfg)
+    for n in (0, 1, 31, 257, 4099):
+        ph = w.photons(n, seed=n + 1)
+        a = ph.copy()
+        o.trace(a, seed=5)
+        q = device_trace(eng, ph, seed=5)
+        if n:
+            assert_parity(q, a, f"n={n}")
+        q2 = ph.copy()
+        eng.trace_host(q2, seed=5)
+        if n:
+            assert_parity(q2, a, f"host n={n}")
+
+
+def test_bad_photons_are_left_untouched(cuda):
+    w = W.plain_scatter()
+    ph = w.photons(10_000, seed=8)
+    ph.flags[::3] = 0x08       # already missed: every stage skips them
+    q = device_trace(engine(w.cfg), ph, seed=1, stages=14)
+    pre = (ph.flags & BAD_PHOTON_MASK) != 0
+    assert np.array_equal(q.p[:, pre], ph.p[:, pre])
+    assert np.array_equal(q.x[:, pre], ph.x[:, pre])
+    assert np.array_equal(q.flags[pre], ph.flags[pre])
+
+
+def test_out_of_table_energies_match_oracle(cuda):
+    from oracle.bindings import Oracle
+    w = W.plain_hetg()
+    ph = w.photons(5000, seed=2)
+    ph.energy[:] = np.linspace(0.05, 12.0, ph.n)   # beyond both ends of every table
+    a = ph.copy()
+    Oracle(w.cfg).trace(a, seed=11)
+    q = device_trace(engine(w.cfg), ph, seed=11)
+    assert_parity(q, a, "edge energies")
+
+
+def test_variate_overrun_matches_oracle(cuda):
+    from oracle.bindings import Oracle
+    w = W.plain_onaxis(parity=True)
+    for i in range(4):
+        w.cfg.shutters[i] = 0x1
+    ph = w.photons(4000)
+    U, N = predraw_variates(4000, seed=3)
+    a = ph.copy()
+    nbad = Oracle(w.cfg).trace(a, U=U, N=N)
+    eng = engine(w.cfg)
+    q = device_trace(eng, ph, U, N)
+    assert nbad > 0 and eng.overrun_count() == nbad
+    assert np.array_equal(q.flags, a.flags)
+
+
+def test_compaction_matches_prune(cuda):
+    import torch
+    w = W.plain_scatter()
+    eng = engine(w.cfg)
+    for n in (1, 1000, 4096, 4097, 300_001):
+        flags = np.random.default_rng(n).integers(0, 4, n).astype(np.uint32) * 0x04
+        t = torch.from_numpy(flags.view(np.int32)).cuda()
+        idx = eng.compact(t).cpu().numpy()
+        assert np.array_equal(idx, np.nonzero((flags & BAD_PHOTON_MASK) == 0)[0])
+
+
+def test_launch_count_tracks_kernels(cuda):
+    w = W.plain_onaxis()
+    eng = engine(w.cfg)
+    before = eng.launch_count()
+    device_trace(eng, w.photons(1000))
+    assert eng.launch_count() == before + 1

@@ -1,0 +1,62 @@
+"""Seeded GPU runs (Philox variates) against seeded runs of the reference
+with its own generator (fixtures in tests/golden/stats_*.npz): survivor
+fractions within binomial error, PSF encircled-energy radii under a
+two-sample KS test, order and chip histograms under chi-square."""
+import os
+
+import numpy as np
+import pytest
+from scipy import stats
+
+from marx_gb300 import workloads as W
+
+from helpers import GOLDEN
+
+pytestmark = pytest.mark.gpu
+N = 200_000
+
+
+def run_gpu(name, n=N, seed=99):
+    import torch
+    from marx_gb300._native import Engine, DevicePhotons
+    w = W.PLAIN[name](parity=True)
+    eng = Engine(w.cfg)
+    d = DevicePhotons.from_host(w.photons(n, seed=w.seed + 10))
+    eng.trace(d, seed=seed)
+    torch.cuda.synchronize()
+    return w, d.to_host()
+
+
+def chi2_p(a, b):
+    keep = (a + b) > 0
+    a, b = a[keep].astype(float), b[keep].astype(float)
+    ka, kb = np.sqrt(b.sum() / a.sum()), np.sqrt(a.sum() / b.sum())
+    chi2 = np.sum((ka * a - kb * b) ** 2 / (a + b))
+    return stats.chi2.sf(chi2, keep.sum() - 1)
+
+
+@pytest.mark.parametrize("name", list(W.PLAIN))
+def test_survivor_fraction_and_histograms(cuda, name):
+    ref = np.load(os.path.join(GOLDEN, f"stats_{name}.npz"))
+    w, q = run_gpu(name)
+    good = (q.flags & 0xFF) == 0
+    f_ref, f_gpu = float(ref["good_fraction"]), good.mean()
+    sigma = np.sqrt(f_ref * (1 - f_ref) * (1 / N + 1 / int(ref["n"])))
+    assert abs(f_gpu - f_ref) < 5 * sigma, (f_gpu, f_ref)
+    ccd = np.bincount(q.ccd_num[good].astype(int) + 1, minlength=11)
+    assert chi2_p(ccd, ref["ccd_hist"]) > 1e-4
+    if "order_hist" in ref:
+        orders = np.bincount(q.order[good].astype(int) + 11, minlength=23)
+        assert chi2_p(orders, ref["order_hist"]) > 1e-4
+
+
+@pytest.mark.parametrize("name", ["plain_onaxis", "plain_scatter"])
+def test_psf_encircled_energy(cuda, name):
+    ref = np.load(os.path.join(GOLDEN, f"stats_{name}.npz"))
+    w, q = run_gpu(name)
+    good = (q.flags & 0xFF) == 0
+    y, z = q.x[1][good], q.x[2][good]
+    r = np.hypot(y - np.median(y), z - np.median(z))
+    ee = np.array([(r <= a).mean() for a in ref["ee_radii"]])
+    assert np.max(np.abs(ee - ref["ee"])) < 0.01, (ee, ref["ee"])
+    assert stats.ks_2samp(np.sort(r)[:: max(1, len(r) // 5000)], ref["radius_sample"]).pvalue > 1e-3
