@@ -177,6 +177,19 @@ const char *mx_last_error(const mx_context *ctx);  /* ctx may be NULL */
 int mx_trace(mx_context *ctx, const mx_photons *ph, uint32_t stages,
              const mx_variates *var, uint64_t seed, void *stream);
 
+/* Kernel organisation for mx_trace / mx_trace_host.  FUSED runs every stage
+ * of a photon in one kernel; WAVEFRONT splits the mirror at its two conic
+ * intersections into three kernels with survivor queues between them (the
+ * photons lost on the way then stop occupying SIMT lanes) and needs
+ * 2 x 128 bytes of device scratch per photon; AUTO picks the wavefront from
+ * MX_WAVEFRONT_MIN_PHOTONS photons up.  Both give the same per-photon
+ * results. */
+#define MX_MODE_AUTO 0
+#define MX_MODE_FUSED 1
+#define MX_MODE_WAVEFRONT 2
+#define MX_WAVEFRONT_MIN_PHOTONS 65536
+int mx_set_trace_mode(mx_context *ctx, int mode);
+
 /* Same trace on HOST buffers: copies inputs to the device, traces and
  * copies results back; blocks until done. */
 int mx_trace_host(mx_context *ctx, const mx_photons *host, uint32_t stages,

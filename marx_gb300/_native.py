@@ -19,8 +19,9 @@ LIB_PATH = os.path.join(HERE, "_build", "libmarx_gb300.so")
 SYMBOLS = [
     "mx_config_default", "mx_create", "mx_configure", "mx_destroy", "mx_last_error", "mx_trace",
     "mx_trace_host", "mx_compact", "mx_table_bytes", "mx_launch_count", "mx_validate_config",
-    "mx_stream", "mx_overrun_count", "mx_probe_fp64",
+    "mx_stream", "mx_overrun_count", "mx_probe_fp64", "mx_set_trace_mode",
 ]
+MODE_AUTO, MODE_FUSED, MODE_WAVEFRONT = 0, 1, 2
 
 _lib = None
 
@@ -50,6 +51,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.mx_stream.argtypes = [C.c_void_p]
     L.mx_overrun_count.argtypes = [C.c_void_p, C.POINTER(C.c_ulonglong), C.c_int]
     L.mx_probe_fp64.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.mx_set_trace_mode.argtypes = [C.c_void_p, C.c_int]
     _lib = L
     return L
 
@@ -120,6 +122,10 @@ class Engine:
     def _check(self, r):
         if r != 0:
             raise RuntimeError(f"marx_gb300 error {r}: " + self.lib.mx_last_error(self.h).decode())
+
+    def set_mode(self, mode: int):
+        """MODE_AUTO, MODE_FUSED or MODE_WAVEFRONT (include/marx_gb300.h)."""
+        self._check(self.lib.mx_set_trace_mode(self.h, mode))
 
     def configure(self, cfg: MxConfig):
         self._check(self.lib.mx_configure(self.h, C.byref(cfg)))

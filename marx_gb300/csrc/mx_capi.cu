@@ -43,6 +43,9 @@ struct mx_context {
   cudaStream_t stream = nullptr;
   DevBuf io[14];           // staging for mx_trace_host
   DevBuf scan;             // compaction block counts
+  DevBuf wave;             // wavefront record queues
+  int wave_blocks = 0;     // resident blocks per SM for the wavefront kernels
+  int mode = MX_MODE_AUTO;
   unsigned long long *d_overrun = nullptr;
   unsigned long long launches = 0;
 };
@@ -103,6 +106,9 @@ static int configure(mx_context *c, const mx_config *cfg) {
     if (e != cudaSuccess) return cuda_fail(c, e, "querying occupancy");
     if (c->trace_blocks[s] < 1) return fail(c, MX_ERANGE, "trace kernel cannot be resident");
   }
+  cudaError_t e = wave_occupancy((int) c->shared_bytes, &c->wave_blocks);
+  if (e != cudaSuccess) return cuda_fail(c, e, "querying occupancy");
+  if (c->wave_blocks < 1) return fail(c, MX_ERANGE, "wavefront kernels cannot be resident");
   return MX_OK;
 }
 
@@ -177,6 +183,7 @@ void mx_destroy(mx_context *c) {
   c->tables.release();
   for (auto &b : c->io) b.release();
   c->scan.release();
+  c->wave.release();
   if (c->d_overrun) cudaFree(c->d_overrun);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -195,6 +202,12 @@ int mx_table_bytes(const mx_context *c, size_t *shared_bytes, size_t *global_byt
 
 uint64_t mx_launch_count(const mx_context *c) { return c ? c->launches : 0; }
 
+int mx_set_trace_mode(mx_context *c, int mode) {
+  if (!c || mode < MX_MODE_AUTO || mode > MX_MODE_WAVEFRONT) return fail(c, MX_EINVAL, "mx_set_trace_mode: bad mode");
+  c->mode = mode;
+  return MX_OK;
+}
+
 static int trace_device(mx_context *c, const mx_photons *ph, uint32_t stages, const double *U, const double *N,
                         uint64_t seed, cudaStream_t st, bool fresh) {
   if (!ph || !ph->energy || !ph->p) return fail(c, MX_EINVAL, "mx_trace: energy and p are required");
@@ -208,10 +221,24 @@ static int trace_device(mx_context *c, const mx_photons *ph, uint32_t stages, co
   io.U = U; io.N = N; io.n = ph->n; io.seed = seed; io.stages = stages; io.fresh = fresh ? 1 : 0;
   io.overrun = c->d_overrun;
   int slots = U != nullptr;
-  int grid = c->num_sms * c->trace_blocks[slots ? 0 : 1];
-  cudaError_t e = launch_trace(c->T, io, grid, (int) c->shared_bytes, slots != 0, st);
-  c->launches++;
-  if (e != cudaSuccess) return cuda_fail(c, e, "launching the trace kernel");
+  bool wave = (stages & MX_STAGE_MIRROR) &&
+              (c->mode == MX_MODE_WAVEFRONT || (c->mode == MX_MODE_AUTO && ph->n >= MX_WAVEFRONT_MIN_PHOTONS));
+  cudaError_t e;
+  if (wave) {
+    size_t qbytes = (size_t) ph->n * sizeof(MxRec);
+    e = c->wave.ensure(2 * qbytes + 256);
+    if (e != cudaSuccess) return cuda_fail(c, e, "allocating wavefront queues");
+    WaveBufs w;
+    w.q1 = (MxRec *) c->wave.ptr;
+    w.q2 = (MxRec *) ((char *) c->wave.ptr + qbytes);
+    w.counts = (unsigned int *) ((char *) c->wave.ptr + 2 * qbytes);
+    e = launch_wavefront(c->T, io, w, c->num_sms * c->wave_blocks, (int) c->shared_bytes, st);
+    c->launches += 3;
+  } else {
+    e = launch_trace(c->T, io, c->num_sms * c->trace_blocks[slots ? 0 : 1], (int) c->shared_bytes, slots != 0, st);
+    c->launches++;
+  }
+  if (e != cudaSuccess) return cuda_fail(c, e, "launching the trace kernels");
   return MX_OK;
 }
 

@@ -13,11 +13,12 @@
 #include <stdint.h>
 #include "mx_model.h"
 
+#include <cmath>
+#include <cstring>
 #ifdef __CUDACC__
 #define MXD __host__ __device__ __forceinline__
 #else
 #define MXD inline
-#include <cmath>
 #endif
 
 namespace mx {
@@ -59,9 +60,26 @@ MXD D3 rotate_unit(D3 p, D3 n, double c, double s) {
   D3 u = c * p + (pn * (1.0 - c)) * n + s * cross(n, p);
   return normalized(u);
 }
+// sin and cos of an angle that is usually tiny (mirror blur, aspect blur,
+// dither offsets, facet misalignment, scattering): below 1e-3 rad the Taylor
+// series to x^7 / x^6 is exact to the last bit (the next terms are below
+// 1e-24 relative); larger angles take the library sincos.
+MXD void sincos_small(double x, double *s, double *c) {
+  if (fabs(x) < 1e-3) {
+    double x2 = x * x;
+    *s = x + x * x2 * (-1.0 / 6.0 + x2 * (1.0 / 120.0 + x2 * (-1.0 / 5040.0)));
+    *c = 1.0 + x2 * (-0.5 + x2 * (1.0 / 24.0 + x2 * (-1.0 / 720.0)));
+  } else
+    mx_sincos(x, s, c);
+}
 MXD D3 rotate_unit_angle(D3 p, D3 n, double theta) {
   double s, c;
   mx_sincos(theta, &s, &c);
+  return rotate_unit(p, n, c, s);
+}
+MXD D3 rotate_unit_small(D3 p, D3 n, double theta) {
+  double s, c;
+  sincos_small(theta, &s, &c);
   return rotate_unit(p, n, c, s);
 }
 MXD D3 mat_mul(const double *m, D3 v) {  // JDM3m_vector_mul (rotate.c:121), row-major 3x3
@@ -143,18 +161,59 @@ MXD double philox_uniform(uint64_t seed, uint32_t tag, uint32_t k) {
   uint64_t b = ((uint64_t) c[0] << 32) | c[1];
   return (double) (b >> 11) * (1.0 / 9007199254740992.0);
 }
+// Single-precision natural log and cos(2 pi u) for the normal variates,
+// from their series (ln m = 2 atanh((m-1)/(m+1)); Taylor series of sin and
+// cos on [0, pi/2)) with every operation explicitly rounded, so the CPU
+// oracle reproduces each normal bit for bit.
+#ifdef __CUDA_ARCH__
+#define FADD(a, b) __fadd_rn(a, b)
+#define FSUB(a, b) __fsub_rn(a, b)
+#define FMUL(a, b) __fmul_rn(a, b)
+#define FDIV(a, b) __fdiv_rn(a, b)
+#define FSQRT(a) __fsqrt_rn(a)
+MXD uint32_t f2u(float f) { return __float_as_uint(f); }
+MXD float u2f(uint32_t u) { return __uint_as_float(u); }
+#else
+#define FADD(a, b) ((a) + (b))
+#define FSUB(a, b) ((a) - (b))
+#define FMUL(a, b) ((a) * (b))
+#define FDIV(a, b) ((a) / (b))
+#define FSQRT(a) std::sqrt(a)
+inline uint32_t f2u(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
+inline float u2f(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
+#endif
+MXD float series_logf(float u) {   // u in (0, 1], normal (u >= 2^-24)
+  uint32_t b = f2u(u);
+  int e = (int) ((b >> 23) & 0xffu) - 127;
+  float m = u2f((b & 0x7fffffu) | 0x3f800000u);
+  if (m > 1.41421356f) { m = FMUL(m, 0.5f); e += 1; }
+  float s = FDIV(FSUB(m, 1.0f), FADD(m, 1.0f));
+  float s2 = FMUL(s, s);
+  float poly = FMUL(s2, FADD(0.333333333f, FMUL(s2, FADD(0.2f, FMUL(s2, FADD(0.142857143f,
+               FMUL(s2, FADD(0.111111111f, FMUL(s2, 0.0909090909f)))))))));
+  float lnm = FMUL(FMUL(2.0f, s), FADD(1.0f, poly));
+  float fe = (float) e;
+  return FADD(FMUL(fe, 0.693145752f), FADD(FMUL(fe, 1.42860677e-06f), lnm));
+}
+MXD float series_cos2pi(float u) {   // cos(2 pi u), u in [0, 1)
+  float x4 = FMUL(u, 4.0f);
+  int q = (int) x4;
+  float f = FSUB(x4, (float) q);
+  float t = FMUL(f, 1.57079632679f), t2 = FMUL(t, t);
+  float c = FADD(1.0f, FMUL(t2, FADD(-0.5f, FMUL(t2, FADD(4.16666667e-02f, FMUL(t2, FADD(-1.38888889e-03f,
+            FMUL(t2, FADD(2.48015873e-05f, FMUL(t2, FADD(-2.75573192e-07f, FMUL(t2, 2.08767570e-09f))))))))))));
+  float s = FMUL(t, FADD(1.0f, FMUL(t2, FADD(-1.66666667e-01f, FMUL(t2, FADD(8.33333333e-03f, FMUL(t2,
+            FADD(-1.98412698e-04f, FMUL(t2, FADD(2.75573192e-06f, FMUL(t2, FADD(-2.50521084e-08f,
+            FMUL(t2, 1.60590438e-10f)))))))))))));
+  return q == 0 ? c : (q == 1 ? -s : (q == 2 ? -c : s));
+}
 MXD double philox_normal(uint64_t seed, uint32_t tag, uint32_t k) {
   uint32_t c[4] = {tag, k, 0x5A5A0002u, 0u};
   philox(c, (uint32_t) seed, (uint32_t) (seed >> 32));
   float u1 = (float) ((c[0] >> 8) + 1u) * (1.0f / 16777216.0f);
   float u2 = (float) (c[1] >> 8) * (1.0f / 16777216.0f);
-#ifdef __CUDA_ARCH__
-  float r = sqrtf(-2.0f * logf(u1));
-  return (double) (r * cosf(6.28318530717958647692f * u2));
-#else
-  float r = std::sqrt(-2.0f * std::log(u1));
-  return (double) (r * std::cos(6.28318530717958647692f * u2));
-#endif
+  float r = FSQRT(FMUL(-2.0f, series_logf(u1)));
+  return (double) FMUL(r, series_cos2pi(u2));
 }
 
 // Variate source for one photon: fixed per-stage slot windows.
@@ -232,7 +291,7 @@ MXD void blur_normal(D3 &n, double blur_rad, Rng &rng) {
   double phi = (2.0 * PI) * rng.uniform();
   perp = rotate_unit_angle(perp, n, phi);
   double ang = blur_rad * rng.normal();
-  n = rotate_unit_angle(n, perp, ang);
+  n = rotate_unit_small(n, perp, ang);
 }
 
 // marx_reflectivity (reflect.c:39-77): polarisation-averaged Fresnel
@@ -294,11 +353,12 @@ MXD double wfold_interp(const MxTables &T, int table, double energy, double sin_
   return t0 + (t1 - t0) * (ea - e0) / (e1 - e0);
 }
 
-// reflect_from_conic (hrma.c:488-545): -2 missed, -1 absorbed, 0 reflected.
-MXD int reflect_from_conic(const MxTables &T, const MxShellDev &h, int o, int table, D3 &x, D3 &p,
-                           double energy, double beta, double delta, double corr, Rng &rng) {
-  D3 n;
-  if (-1 == conic_intersection(h, o, x, p, n)) return -2;
+// reflect_from_conic (hrma.c:488-545) after the intersection: normal blur,
+// reflectivity test, specular reflection and WFold scattering at the
+// intersection point.  Returns -1 if the photon is absorbed (p then holds
+// what the reference leaves in it), 0 if it is reflected.
+MXD int reflect_at(const MxTables &T, const MxShellDev &h, int o, int table, D3 &p, D3 n, double energy,
+                   double beta, double delta, double corr, Rng &rng) {
   if (T.use_blur) blur_normal(n, h.blur[o], rng);
   double pdn = dot(p, n);
   if (!T.ideal) {
@@ -312,7 +372,7 @@ MXD int reflect_from_conic(const MxTables &T, const MxShellDev &h, int o, int ta
   double dg = wfold_interp(T, table, energy, -pdn, r) * h.scat[o];
   if (dg > PI / 4) return -1;
   if (rng.uniform() < 0.5) dg = -dg;
-  p = rotate_unit_angle(p, cross(p, n), dg);
+  p = rotate_unit_small(p, cross(p, n), dg);
   return 0;
 }
 
@@ -330,24 +390,35 @@ MXD bool struts_block(const MxTables &T, int set, D3 x, D3 p) {
   return false;
 }
 
-// _marx_hrma_mirror_reflect per photon (hrma.c:1183-1339) with
-// project_photon_to_hrma (hrma.c:984-1050).
-MXD void mirror_stage(const MxTables &T, const MxShellDev *shells, const float *optc, Ph &ph, Rng &rng) {
+// Mirror state carried between the three parts of the HRMA trace: the
+// photon at a conic intersection (OSAC frame of that optic), the inward
+// normal there, and the optical constants at the photon's energy.
+struct MirrorState {
+  D3 x, p, n;
+  double corr;
+  float beta, delta;
+};
+
+// _marx_hrma_mirror_reflect per photon (hrma.c:1183-1339), part 1:
+// vignetting, project_photon_to_hrma (hrma.c:984-1050), transform into the
+// paraboloid's frame, optical constants, paraboloid intersection.  Returns
+// true if the photon reached the paraboloid.
+MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *optc, Ph &ph, Rng &rng,
+                      MirrorState &m) {
   rng.window(MX_U_MIRROR, 12, MX_N_MIRROR, 2);
   if (!T.ideal) {
     if (rng.uniform() > T.hrma_vig) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
-    if (ph.flags & MX_BAD_PHOTON_MASK) return;
+    if (ph.flags & MX_BAD_PHOTON_MASK) return false;
   }
   D3 x = ph.x, p = ph.p;
-  // aperture sampling
   int si = -1;
   for (int guard = 0; guard < 64 && si < 0; guard++) {
     double r = rng.uniform();
-    if (rng.overrun) return;
+    if (rng.overrun) return false;
     for (int i = 0; i < 4; i++)
       if (r < shells[i].area_fraction) { si = i; break; }
   }
-  if (si < 0) { rng.overrun = true; return; }
+  if (si < 0) { rng.overrun = true; return false; }
   const MxShellDev &h = shells[si];
   ph.shell = si;
   double radius;
@@ -360,7 +431,7 @@ MXD void mirror_stage(const MxTables &T, const MxShellDev *shells, const float *
   for (int guard = 0;; guard++) {
     theta = rng.uniform();
     unsigned quad = (unsigned) (4.0 * theta);
-    if (rng.overrun || guard >= 64) { rng.overrun = true; return; }
+    if (rng.overrun || guard >= 64) { rng.overrun = true; return false; }
     if (h.shutter & (1u << quad)) break;
   }
   theta = (2.0 * PI) * (theta - 1.0 / 8.0);
@@ -373,26 +444,49 @@ MXD void mirror_stage(const MxTables &T, const MxShellDev *shells, const float *
   x = x + mk(h.to_osac[0][0], h.to_osac[0][1], h.to_osac[0][2]);
   x = mat_mul(h.fwd[0], x);
   p = mat_mul(h.fwd[0], p);
-  double beta = 0.0, delta = 1.0, corr = 1.0;
+  m.beta = 0.0f; m.delta = 1.0f; m.corr = 1.0;
   if (T.opt_n) {
     float fe = (float) ph.e;
-    beta = (double) interp_f(fe, optc, optc + T.opt_n, T.opt_n);
-    delta = (double) interp_f(fe, optc, optc + 2 * T.opt_n, T.opt_n);
+    m.beta = interp_f(fe, optc, optc + T.opt_n, T.opt_n);
+    m.delta = interp_f(fe, optc, optc + 2 * T.opt_n, T.opt_n);
     if (T.use_scale) {
       const float *ce = optc + 3 * T.opt_n + h.corr_off;
-      corr = sqrt((double) interp_f(fe, ce, ce + h.corr_n, h.corr_n));
+      m.corr = sqrt((double) interp_f(fe, ce, ce + h.corr_n, h.corr_n));
     }
   }
-  int st1 = reflect_from_conic(T, h, 0, 2 * si, x, p, ph.e, beta, delta, corr, rng);
-  if (st1 != 0) { ph.flags |= MX_PHOTON_UNREFLECTED; ph.x = x; ph.p = p; return; }
+  D3 n;
+  if (-1 == conic_intersection(h, 0, x, p, n)) { ph.flags |= MX_PHOTON_UNREFLECTED; ph.x = x; ph.p = p; return false; }
+  m.x = x; m.p = p; m.n = n;
+  return true;
+}
+
+// Part 2: reflection from the paraboloid, back to the MARX frame, cap
+// struts, into the hyperboloid's frame and its intersection.
+MXD bool mirror_middle(const MxTables &T, const MxShellDev *shells, Ph &ph, Rng &rng, MirrorState &m) {
+  const MxShellDev &h = shells[ph.shell];
+  D3 x = m.x, p = m.p;
+  if (0 != reflect_at(T, h, 0, 2 * ph.shell, p, m.n, ph.e, m.beta, m.delta, m.corr, rng)) {
+    ph.flags |= MX_PHOTON_UNREFLECTED; ph.x = x; ph.p = p; return false;
+  }
   p = mat_mul(h.bwd[0], p);
   x = mat_mul(h.bwd[0], x);
   x = x - mk(h.to_osac[0][0], h.to_osac[0][1], h.to_osac[0][2]);
-  if (T.use_struts && struts_block(T, 1, x, p)) { ph.flags |= MX_PHOTON_MIRROR_VBLOCKED; ph.x = x; ph.p = p; return; }
+  if (T.use_struts && struts_block(T, 1, x, p)) { ph.flags |= MX_PHOTON_MIRROR_VBLOCKED; ph.x = x; ph.p = p; return false; }
   x = x + mk(h.to_osac[1][0], h.to_osac[1][1], h.to_osac[1][2]);
   p = mat_mul(h.fwd[1], p);
   x = mat_mul(h.fwd[1], x);
-  if (0 != reflect_from_conic(T, h, 1, 2 * si + 1, x, p, ph.e, beta, delta, corr, rng)) {
+  D3 n;
+  if (-1 == conic_intersection(h, 1, x, p, n)) { ph.flags |= MX_PHOTON_UNREFLECTED; ph.x = x; ph.p = p; return false; }
+  m.x = x; m.p = p; m.n = n;
+  return true;
+}
+
+// Part 3: reflection from the hyperboloid, back to the MARX frame,
+// post-collimator struts.  Leaves the photon in ph.
+MXD void mirror_back(const MxTables &T, const MxShellDev *shells, Ph &ph, Rng &rng, MirrorState &m) {
+  const MxShellDev &h = shells[ph.shell];
+  D3 x = m.x, p = m.p;
+  if (0 != reflect_at(T, h, 1, 2 * ph.shell + 1, p, m.n, ph.e, m.beta, m.delta, m.corr, rng)) {
     ph.flags |= MX_PHOTON_UNREFLECTED; ph.x = x; ph.p = p; return;
   }
   p = mat_mul(h.bwd[1], p);
@@ -400,6 +494,12 @@ MXD void mirror_stage(const MxTables &T, const MxShellDev *shells, const float *
   x = x - mk(h.to_osac[1][0], h.to_osac[1][1], h.to_osac[1][2]);
   if (T.use_struts && struts_block(T, 2, x, p)) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
   ph.x = x; ph.p = p;
+}
+
+MXD void mirror_stage(const MxTables &T, const MxShellDev *shells, const float *optc, Ph &ph, Rng &rng) {
+  MirrorState m;
+  if (mirror_front(T, shells, optc, ph, rng, m) && mirror_middle(T, shells, ph, rng, m))
+    mirror_back(T, shells, ph, rng, m);
 }
 
 // ------------------------------------------------------------- dither --
@@ -415,10 +515,10 @@ MXD void dither_stage(const MxTables &T, Ph &ph, Rng &rng) {
   ph.dith[0] = fra; ph.dith[1] = fdec; ph.dith[2] = froll;
   double ra = (double) fra + T.aspect_blur * rng.normal();
   double dec = (double) fdec + T.aspect_blur * rng.normal();
-  D3 p = rotate_unit_angle(ph.p, mk(1, 0, 0), -(double) froll);
+  D3 p = rotate_unit_small(ph.p, mk(1, 0, 0), -(double) froll);
   double sr, cr, sd, cd;
-  mx_sincos(ra, &sr, &cr);
-  mx_sincos(dec, &sd, &cd);
+  sincos_small(ra, &sr, &cr);
+  sincos_small(dec, &sd, &cd);
   double cos_theta = cd * cr;
   D3 n = mk(0, sd, -cd * sr);
   double s2 = n.y * n.y + n.z * n.z;
@@ -480,7 +580,7 @@ MXD int diffract_photon(const MxTables &T, const MxGratingDev &g, int order_idx,
   double theta = 0.0 - dtheta;
   if (theta != 0.0) {
     double s, c;
-    mx_sincos(theta, &s, &c);
+    sincos_small(theta, &s, &c);
     D3 lt = l, dt = d;
     l = c * lt + s * dt;
     d = (-s) * lt + c * dt;
@@ -608,12 +708,15 @@ MXD void detect_stage(const MxTables &T, const MxChipDev *chips, Ph &ph, Rng &rn
 
 // The fused per-photon trace: dither at creation (source.c:357), then the
 // stages of process_photons (marx.c:240-273); a photon with a bad flag is
-// skipped by later stages as marx_prune_photons drops it.
+// skipped by later stages as marx_prune_photons drops it, and a photon
+// whose stage ran out of pre-drawn variates is not traced further.
 MXD void trace_photon(const MxTables &T, const MxShellDev *shells, const float *optc, const MxGratingDev *grs,
                       const MxChipDev *chips, uint32_t stages, Ph &ph, Rng &rng) {
   if ((stages & MX_STAGE_DITHER) && T.dither) dither_stage(T, ph, rng);
   if ((stages & MX_STAGE_MIRROR) && !(ph.flags & MX_BAD_PHOTON_MASK)) mirror_stage(T, shells, optc, ph, rng);
+  if (rng.overrun) return;
   if ((stages & MX_STAGE_GRATING) && T.grating && !(ph.flags & MX_BAD_PHOTON_MASK)) grating_stage(T, grs, ph, rng);
+  if (rng.overrun) return;
   if ((stages & MX_STAGE_DETECT) && T.nchips && !(ph.flags & MX_BAD_PHOTON_MASK)) detect_stage(T, chips, ph, rng);
 }
 

@@ -80,6 +80,199 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_trace_kernel(MxTables T, Tr
   }
 }
 
+// ------------------------------------------------------------ wavefront --
+// The same trace as mx_trace_kernel split at the two conic intersections,
+// so that photons lost on the way (between the shells, absorbed by the
+// paraboloid) stop occupying SIMT lanes: phase A runs every photon up to
+// the paraboloid intersection and appends survivors to queue 1; phase B
+// reflects them, intersects the hyperboloid and appends to queue 2; phase
+// C reflects from the hyperboloid and runs the grating and the detector.
+// Appends are warp-aggregated (one atomic per warp); the order of records
+// in a queue does not affect any photon's result.
+
+__device__ __forceinline__ void stage_tables(const MxTables &T, MxShellDev *&sh, MxGratingDev *&gr, MxChipDev *&ch,
+                                             float *&optc) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  size_t o_gr = align16(4 * sizeof(MxShellDev));
+  size_t o_ch = o_gr + align16(4 * sizeof(MxGratingDev));
+  size_t o_op = o_ch + align16(MX_MAX_CHIPS * sizeof(MxChipDev));
+  sh = (MxShellDev *) smem;
+  gr = (MxGratingDev *) (smem + o_gr);
+  ch = (MxChipDev *) (smem + o_ch);
+  optc = (float *) (smem + o_op);
+  copy_words((uint32_t *) sh, (const uint32_t *) T.shells, 4 * sizeof(MxShellDev) / 4);
+  copy_words((uint32_t *) gr, (const uint32_t *) T.gratings, 4 * sizeof(MxGratingDev) / 4);
+  copy_words((uint32_t *) ch, (const uint32_t *) T.chips, (size_t) (T.nchips > 0 ? T.nchips : 1) * sizeof(MxChipDev) / 4);
+  copy_words((uint32_t *) optc, (const uint32_t *) T.optc, (size_t) T.optc_len);
+  __syncthreads();
+}
+
+__device__ __forceinline__ void append(bool keep, const MxRec &r, MxRec *q, unsigned int *cnt) {
+  const unsigned lane = threadIdx.x & 31;
+  unsigned mask = __ballot_sync(0xffffffffu, keep);
+  if (mask == 0) return;
+  int leader = __ffs(mask) - 1;
+  unsigned base = 0;
+  if ((int) lane == leader) base = atomicAdd(cnt, (unsigned) __popc(mask));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (keep) q[base + __popc(mask & ((1u << lane) - 1u))] = r;
+}
+
+__device__ __forceinline__ void to_rec(MxRec &r, const Ph &q, const MirrorState &m, const Rng &rng, uint32_t i) {
+  r.x[0] = m.x.x; r.x[1] = m.x.y; r.x[2] = m.x.z;
+  r.p[0] = m.p.x; r.p[1] = m.p.y; r.p[2] = m.p.z;
+  r.n[0] = m.n.x; r.n[1] = m.n.y; r.n[2] = m.n.z;
+  r.e = q.e; r.t = q.t; r.corr = m.corr; r.beta = m.beta; r.delta = m.delta;
+  r.i = i; r.tag = rng.tag; r.flags = q.flags;
+  r.shell = (uint8_t) q.shell; r.upos = (uint8_t) rng.upos; r.npos = (uint8_t) rng.npos; r.pad0 = 0;
+}
+
+__device__ __forceinline__ void from_rec(const MxRec &r, Ph &q, MirrorState &m, Rng &rng, const TraceIO &io) {
+  m.x = mk(r.x[0], r.x[1], r.x[2]); m.p = mk(r.p[0], r.p[1], r.p[2]); m.n = mk(r.n[0], r.n[1], r.n[2]);
+  m.corr = r.corr; m.beta = r.beta; m.delta = r.delta;
+  q.e = r.e; q.t = r.t; q.flags = r.flags; q.shell = r.shell;
+  q.x = m.x; q.p = m.p;
+  rng.U = io.U; rng.N = io.N; rng.seed = io.seed; rng.n = io.n; rng.i = r.i; rng.tag = r.tag;
+  rng.upos = r.upos; rng.uend = MX_U_MIRROR + 12; rng.npos = r.npos; rng.nend = MX_N_MIRROR + 2;
+  rng.overrun = false;
+}
+
+// x, p, flags and shell of a photon whose trace ends in this phase.
+__device__ __forceinline__ void store_core(const TraceIO &io, uint32_t i, const Ph &q, bool overrun) {
+  const size_t n = io.n;
+  uint32_t f = q.flags;
+  if (overrun) { f |= MX_PHOTON_VARIATE_OVERRUN; atomicAdd(io.overrun, 1ull); }
+  if (io.x) { io.x[i] = q.x.x; io.x[n + i] = q.x.y; io.x[2 * n + i] = q.x.z; }
+  io.p[i] = q.p.x; io.p[n + i] = q.p.y; io.p[2 * n + i] = q.p.z;
+  if (io.flags) io.flags[i] = f;
+  if (io.shell) io.shell[i] = (int8_t) q.shell;
+}
+
+__global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_wave_a(MxTables T, TraceIO io, WaveBufs w) {
+  MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc;
+  stage_tables(T, sh, gr, ch, optc);
+  const size_t n = io.n;
+  const uint32_t lane = threadIdx.x & 31, warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t base = warp * 32; base < io.n; base += nwarps * 32) {
+    const uint32_t i = base + lane;
+    bool keep = false;
+    MxRec rec;
+    if (i < io.n) {
+      Ph q;
+      q.e = io.energy[i];
+      q.t = io.t ? io.t[i] : 0.0;
+      q.p = mk(io.p[i], io.p[n + i], io.p[2 * n + i]);
+      q.flags = io.flags ? io.flags[i] : 0u;
+      if (io.fresh) {
+        q.x = mk(0.0, 0.0, 0.0); q.shell = 0;
+        q.dith[0] = q.dith[1] = q.dith[2] = 0.f;
+        if (io.order) io.order[i] = 0;
+        if (io.ccd) io.ccd[i] = -1;
+        if (io.ypix) io.ypix[i] = 0.f;
+        if (io.zpix) io.zpix[i] = 0.f;
+      } else {
+        q.x = io.x ? mk(io.x[i], io.x[n + i], io.x[2 * n + i]) : mk(0.0, 0.0, 0.0);
+        q.shell = io.shell ? io.shell[i] : 0;
+        for (int k = 0; k < 3; k++) q.dith[k] = io.dith ? io.dith[k * n + i] : 0.f;
+      }
+      Rng r;
+      r.U = io.U; r.N = io.N; r.seed = io.seed; r.n = io.n; r.i = i;
+      r.tag = io.tag ? io.tag[i] : i;
+      r.upos = r.uend = r.npos = r.nend = 0;
+      r.overrun = false;
+      if ((io.stages & MX_STAGE_DITHER) && T.dither) dither_stage(T, q, r);
+      if (io.dith) for (int k = 0; k < 3; k++) io.dith[k * n + i] = q.dith[k];
+      MirrorState m;
+      if (!(q.flags & MX_BAD_PHOTON_MASK) && mirror_front(T, sh, optc, q, r, m)) {
+        keep = true;
+        to_rec(rec, q, m, r, i);
+      } else
+        store_core(io, i, q, r.overrun);
+    }
+    append(keep, rec, w.q1, &w.counts[0]);
+  }
+}
+
+__global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_wave_b(MxTables T, TraceIO io, WaveBufs w) {
+  MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc;
+  stage_tables(T, sh, gr, ch, optc);
+  const uint32_t count = *(volatile unsigned int *) &w.counts[0];
+  const uint32_t lane = threadIdx.x & 31, warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t base = warp * 32; base < count; base += nwarps * 32) {
+    const uint32_t k = base + lane;
+    bool keep = false;
+    MxRec rec;
+    if (k < count) {
+      rec = w.q1[k];
+      Ph q; MirrorState m; Rng r;
+      from_rec(rec, q, m, r, io);
+      if (mirror_middle(T, sh, q, r, m)) {
+        keep = true;
+        to_rec(rec, q, m, r, rec.i);
+      } else
+        store_core(io, rec.i, q, r.overrun);
+    }
+    append(keep, rec, w.q2, &w.counts[1]);
+  }
+}
+
+__global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_wave_c(MxTables T, TraceIO io, WaveBufs w) {
+  MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc;
+  stage_tables(T, sh, gr, ch, optc);
+  const uint32_t count = *(volatile unsigned int *) &w.counts[1];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += stride) {
+    const MxRec rec = w.q2[k];
+    const uint32_t i = rec.i;
+    Ph q; MirrorState m; Rng r;
+    from_rec(rec, q, m, r, io);
+    const int unset = 0x7fff;
+    q.order = unset; q.ccd = unset;
+    mirror_back(T, sh, q, r, m);
+    if (!r.overrun && (io.stages & MX_STAGE_GRATING) && T.grating && !(q.flags & MX_BAD_PHOTON_MASK))
+      grating_stage(T, gr, q, r);
+    if (!r.overrun && (io.stages & MX_STAGE_DETECT) && T.nchips && !(q.flags & MX_BAD_PHOTON_MASK))
+      detect_stage(T, ch, q, r);
+    store_core(io, i, q, r.overrun);
+    if (q.order != unset && io.order) io.order[i] = (int8_t) q.order;
+    if (q.ccd != unset) {
+      if (io.ccd) io.ccd[i] = (int8_t) q.ccd;
+      if (q.ccd >= 0) {
+        if (io.ypix) io.ypix[i] = q.ypix;
+        if (io.zpix) io.zpix[i] = q.zpix;
+      }
+    }
+  }
+}
+
+cudaError_t wave_occupancy(int shared_bytes, int *blocks_per_sm) {
+  int b[3];
+  const void *f[3] = {(const void *) mx_wave_a, (const void *) mx_wave_b, (const void *) mx_wave_c};
+  for (int k = 0; k < 3; k++) {
+    cudaError_t e = cudaFuncSetAttribute(f[k], cudaFuncAttributeMaxDynamicSharedMemorySize, shared_bytes);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[k], f[k], MX_TRACE_BLOCK, shared_bytes);
+    if (e != cudaSuccess) return e;
+  }
+  *blocks_per_sm = b[0] < b[1] ? (b[0] < b[2] ? b[0] : b[2]) : (b[1] < b[2] ? b[1] : b[2]);
+  return cudaSuccess;
+}
+
+cudaError_t launch_wavefront(const MxTables &T, const TraceIO &io, const WaveBufs &w, int grid, int shared_bytes,
+                             cudaStream_t st) {
+  uint32_t need = (io.n + MX_TRACE_BLOCK - 1) / MX_TRACE_BLOCK;
+  int ga = (uint32_t) grid > need ? (int) need : grid;
+  if (ga < 1) ga = 1;
+  cudaError_t e = cudaMemsetAsync(w.counts, 0, 2 * sizeof(unsigned int), st);
+  if (e != cudaSuccess) return e;
+  mx_wave_a<<<ga, MX_TRACE_BLOCK, shared_bytes, st>>>(T, io, w);
+  mx_wave_b<<<ga, MX_TRACE_BLOCK, shared_bytes, st>>>(T, io, w);
+  mx_wave_c<<<ga, MX_TRACE_BLOCK, shared_bytes, st>>>(T, io, w);
+  return cudaGetLastError();
+}
+
 cudaError_t trace_occupancy(bool philox, int shared_bytes, int *blocks_per_sm) {
   (void) philox;
   cudaError_t e = cudaFuncSetAttribute(mx_trace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, shared_bytes);

@@ -23,7 +23,26 @@ struct TraceIO {
   unsigned long long *overrun;  // count of photons that ran out of variate slots
 };
 
+// One photon between wavefront phases (128 bytes, written and read whole).
+struct __align__(16) MxRec {
+  double x[3], p[3], n[3];      // state at the last conic intersection, and its normal
+  double e, t, corr;
+  float beta, delta;
+  uint32_t i, tag, flags;       // photon index in the list, generator counter, flags
+  uint8_t shell, upos, npos, pad0;
+  uint32_t pad[2];
+};
+
+// Wavefront scratch: two record queues of n entries and their fill counts.
+struct WaveBufs {
+  MxRec *q1, *q2;
+  unsigned int *counts;         // [0]: q1 entries, [1]: q2 entries
+};
+
 size_t trace_shared_bytes(const MxTables &T);
+cudaError_t wave_occupancy(int shared_bytes, int *blocks_per_sm);
+cudaError_t launch_wavefront(const MxTables &T, const TraceIO &io, const WaveBufs &w, int grid, int shared_bytes,
+                             cudaStream_t st);
 cudaError_t trace_occupancy(bool philox, int shared_bytes, int *blocks_per_sm);
 cudaError_t launch_trace(const MxTables &T, const TraceIO &io, int grid, int shared_bytes, bool slots,
                          cudaStream_t st);

@@ -73,14 +73,40 @@ inline double philox_uniform(uint64_t seed, uint32_t tag, uint32_t k) {
   uint64_t b = ((uint64_t) c[0] << 32) | c[1];
   return (double) (b >> 11) * (1.0 / 9007199254740992.0);
 }
-// Normal slot k: Box-Muller in single precision on 24-bit uniforms.
+// Normal slot k: Box-Muller in single precision on 24-bit uniforms, with
+// ln u = e ln 2 + 2 atanh((m-1)/(m+1)) and cos(2 pi u) from Taylor series on
+// [0, pi/2), every operation rounded separately (no fused multiply-add).
+inline float series_logf(float u) {
+  uint32_t b; std::memcpy(&b, &u, 4);
+  int e = (int) ((b >> 23) & 0xffu) - 127;
+  uint32_t mb = (b & 0x7fffffu) | 0x3f800000u;
+  float m; std::memcpy(&m, &mb, 4);
+  if (m > 1.41421356f) { m = m * 0.5f; e += 1; }
+  float s = (m - 1.0f) / (m + 1.0f);
+  float s2 = s * s;
+  float poly = s2 * (0.333333333f + s2 * (0.2f + s2 * (0.142857143f + s2 * (0.111111111f + s2 * 0.0909090909f))));
+  float lnm = (2.0f * s) * (1.0f + poly);
+  float fe = (float) e;
+  return fe * 0.693145752f + (fe * 1.42860677e-06f + lnm);
+}
+inline float series_cos2pi(float u) {
+  float x4 = u * 4.0f;
+  int q = (int) x4;
+  float f = x4 - (float) q;
+  float t = f * 1.57079632679f, t2 = t * t;
+  float c = 1.0f + t2 * (-0.5f + t2 * (4.16666667e-02f + t2 * (-1.38888889e-03f + t2 * (2.48015873e-05f +
+            t2 * (-2.75573192e-07f + t2 * 2.08767570e-09f)))));
+  float s = t * (1.0f + t2 * (-1.66666667e-01f + t2 * (8.33333333e-03f + t2 * (-1.98412698e-04f +
+            t2 * (2.75573192e-06f + t2 * (-2.50521084e-08f + t2 * 1.60590438e-10f))))));
+  return q == 0 ? c : (q == 1 ? -s : (q == 2 ? -c : s));
+}
 inline double philox_normal(uint64_t seed, uint32_t tag, uint32_t k) {
   uint32_t c[4] = {tag, k, 0x5A5A0002u, 0u};
   philox4x32_10(c, (uint32_t) seed, (uint32_t) (seed >> 32));
   float u1 = (float) ((c[0] >> 8) + 1u) * (1.0f / 16777216.0f);
   float u2 = (float) (c[1] >> 8) * (1.0f / 16777216.0f);
-  float r = std::sqrt(-2.0f * std::log(u1));
-  return (double) (r * std::cos(6.28318530717958647692f * u2));
+  float r = std::sqrt(-2.0f * series_logf(u1));
+  return (double) (r * series_cos2pi(u2));
 }
 
 struct Variates {
@@ -762,11 +788,15 @@ template <class R> inline void detect_photon(const Model &M, Photon &ph, Variate
 // (marx.c:240-273) preceded by the dither applied at photon creation
 // (source.c:357).  Photons with a bad flag skip later stages, as
 // marx_prune_photons drops them from sorted_index.
+// A photon whose stage ran out of pre-drawn variates is not traced further
+// (an engine rule; the reference draws from an unbounded stream).
 template <class R> inline bool trace_photon(const Model &M, Photon &ph, uint32_t stages, Variates &v) {
   if ((stages & MX_STAGE_DITHER) && M.cfg.dither == MX_DITHER_INTERNAL) dither_photon<R>(M, ph, v);
   if ((stages & MX_STAGE_MIRROR) && !(ph.flags & MX_BAD_PHOTON_MASK)) mirror_photon<R>(M, ph, v);
+  if (v.overrun) return true;
   if ((stages & MX_STAGE_GRATING) && M.cfg.grating == MX_GRATING_HETG && !(ph.flags & MX_BAD_PHOTON_MASK))
     grating_photon<R>(M, ph, v);
+  if (v.overrun) return true;
   if ((stages & MX_STAGE_DETECT) && M.cfg.detector != MX_DETECTOR_NONE && !(ph.flags & MX_BAD_PHOTON_MASK))
     detect_photon<R>(M, ph, v);
   return v.overrun;

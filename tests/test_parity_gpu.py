@@ -16,9 +16,13 @@ pytestmark = pytest.mark.gpu
 NAMES = list(W.PLAIN)
 
 
-def engine(cfg):
+def engine(cfg, mode=0):
     from marx_gb300._native import Engine
-    return Engine(cfg)
+    e = Engine(cfg)
+    e.set_mode(mode)
+    return e
+
+MODES = {"fused": 1, "wavefront": 2}
 
 
 def device_trace(eng, ph, U=None, N=None, seed=0, stages=15):
@@ -32,19 +36,21 @@ def device_trace(eng, ph, U=None, N=None, seed=0, stages=15):
     return d.to_host()
 
 
+@pytest.mark.parametrize("mode", list(MODES))
 @pytest.mark.parametrize("name", NAMES)
-def test_gpu_matches_reference_fixture(cuda, name):
+def test_gpu_matches_reference_fixture(cuda, name, mode):
     w, ph, U, N, z = load_trace_fixture(name)
-    eng = engine(w.cfg)
+    eng = engine(w.cfg, MODES[mode])
     q = device_trace(eng, ph, U, N)
-    assert_parity(q, z, f"{name} device buffers")
+    assert_parity(q, z, f"{name} device buffers {mode}")
     assert eng.overrun_count() == 0
 
 
+@pytest.mark.parametrize("mode", list(MODES))
 @pytest.mark.parametrize("name", NAMES)
-def test_gpu_host_entry_matches_reference_fixture(cuda, name):
+def test_gpu_host_entry_matches_reference_fixture(cuda, name, mode):
     w, ph, U, N, z = load_trace_fixture(name)
-    eng = engine(w.cfg)
+    eng = engine(w.cfg, MODES[mode])
     q = ph.copy()
     eng.trace_host(q, U=U, N=N)
     assert_parity(q, z, f"{name} host buffers")
@@ -62,9 +68,18 @@ def test_gpu_matches_oracle_philox(cuda, name):
 
 
 @pytest.mark.parametrize("name", NAMES)
+def test_wavefront_equals_fused(cuda, name):
+    w = W.PLAIN[name]()
+    ph = w.photons(100_000, seed=77)
+    a = device_trace(engine(w.cfg, MODES["fused"]), ph, seed=3)
+    b = device_trace(engine(w.cfg, MODES["wavefront"]), ph, seed=3)
+    assert_parity(b, a, f"{name} wavefront vs fused")
+
+
+@pytest.mark.parametrize("name", NAMES)
 def test_split_stages_equal_fused(cuda, name):
     w, ph, U, N, z = load_trace_fixture(name)
-    eng = engine(w.cfg)
+    eng = engine(w.cfg, MODES["fused"])
     fused = device_trace(eng, ph, U, N)
     import torch
     from marx_gb300._native import DevicePhotons
@@ -77,10 +92,11 @@ def test_split_stages_equal_fused(cuda, name):
     assert r["dx"] == 0 and r["dp"] == 0 and all(v == 0 for k, v in r.items() if k not in ("dx", "dp")), r
 
 
-def test_empty_single_and_ragged_lists(cuda):
+@pytest.mark.parametrize("mode", list(MODES))
+def test_empty_single_and_ragged_lists(cuda, mode):
     from oracle.bindings import Oracle
     w = W.plain_hetg()
-    eng = engine(w.cfg)
+    eng = engine(w.cfg, MODES[mode])
     o = Oracle(w.cfg)
     for n in (0, 1, 31, 257, 4099):
         ph = w.photons(n, seed=n + 1)
@@ -95,11 +111,12 @@ def test_empty_single_and_ragged_lists(cuda):
             assert_parity(q2, a, f"host n={n}")
 
 
-def test_bad_photons_are_left_untouched(cuda):
+@pytest.mark.parametrize("mode", list(MODES))
+def test_bad_photons_are_left_untouched(cuda, mode):
     w = W.plain_scatter()
     ph = w.photons(10_000, seed=8)
     ph.flags[::3] = 0x08       # already missed: every stage skips them
-    q = device_trace(engine(w.cfg), ph, seed=1, stages=14)
+    q = device_trace(engine(w.cfg, MODES[mode]), ph, seed=1, stages=14)
     pre = (ph.flags & BAD_PHOTON_MASK) != 0
     assert np.array_equal(q.p[:, pre], ph.p[:, pre])
     assert np.array_equal(q.x[:, pre], ph.x[:, pre])
@@ -117,7 +134,8 @@ def test_out_of_table_energies_match_oracle(cuda):
     assert_parity(q, a, "edge energies")
 
 
-def test_variate_overrun_matches_oracle(cuda):
+@pytest.mark.parametrize("mode", list(MODES))
+def test_variate_overrun_matches_oracle(cuda, mode):
     from oracle.bindings import Oracle
     w = W.plain_onaxis(parity=True)
     for i in range(4):
@@ -126,10 +144,10 @@ def test_variate_overrun_matches_oracle(cuda):
     U, N = predraw_variates(4000, seed=3)
     a = ph.copy()
     nbad = Oracle(w.cfg).trace(a, U=U, N=N)
-    eng = engine(w.cfg)
+    eng = engine(w.cfg, MODES[mode])
     q = device_trace(eng, ph, U, N)
     assert nbad > 0 and eng.overrun_count() == nbad
-    assert np.array_equal(q.flags, a.flags)
+    assert_parity(q, a, f"overrun {mode}")
 
 
 def test_compaction_matches_prune(cuda):
@@ -145,7 +163,10 @@ def test_compaction_matches_prune(cuda):
 
 def test_launch_count_tracks_kernels(cuda):
     w = W.plain_onaxis()
-    eng = engine(w.cfg)
+    eng = engine(w.cfg, MODES["fused"])
     before = eng.launch_count()
     device_trace(eng, w.photons(1000))
     assert eng.launch_count() == before + 1
+    eng.set_mode(MODES["wavefront"])
+    device_trace(eng, w.photons(1000))
+    assert eng.launch_count() == before + 4
