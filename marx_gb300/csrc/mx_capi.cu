@@ -210,7 +210,9 @@ int mx_set_trace_mode(mx_context *c, int mode) {
 
 static int trace_device(mx_context *c, const mx_photons *ph, uint32_t stages, const double *U, const double *N,
                         uint64_t seed, cudaStream_t st, bool fresh) {
-  if (!ph || !ph->energy || !ph->p) return fail(c, MX_EINVAL, "mx_trace: energy and p are required");
+  if (!ph) return fail(c, MX_EINVAL, "mx_trace: null photon list");
+  if (ph->n == 0) return MX_OK;
+  if (!ph->energy || !ph->p) return fail(c, MX_EINVAL, "mx_trace: energy and p are required");
   if ((U == nullptr) != (N == nullptr)) return fail(c, MX_EINVAL, "mx_trace: give both U and N or neither");
   if ((stages & MX_STAGE_DETECT) && c->T.nchips && (!ph->x)) return fail(c, MX_EINVAL, "mx_trace: x is required");
   if (ph->n == 0) return MX_OK;
@@ -251,9 +253,10 @@ int mx_trace(mx_context *c, const mx_photons *ph, uint32_t stages, const mx_vari
 
 int mx_trace_host(mx_context *c, const mx_photons *h, uint32_t stages, const mx_variates *hv, uint64_t seed) {
   if (!c) return MX_EINVAL;
-  if (!h || !h->energy || !h->p) return fail(c, MX_EINVAL, "mx_trace_host: energy and p are required");
+  if (!h) return fail(c, MX_EINVAL, "mx_trace_host: null photon list");
   size_t n = h->n;
   if (n == 0) return MX_OK;
+  if (!h->energy || !h->p) return fail(c, MX_EINVAL, "mx_trace_host: energy and p are required");
   struct Col { const void *host; size_t elem; int comps; bool in, out; };
   const Col cols[12] = {
       {h->energy, 8, 1, true, false},     {h->x, 8, 3, false, true},         {h->p, 8, 3, true, true},
