@@ -71,6 +71,7 @@ static int upload_model(mx_context *c) {
   std::vector<char> blob;
   size_t o_sh = put(blob, M.shells), o_opt = put(blob, M.optc), o_fh = put(blob, M.fold_hdr),
          o_fe = put(blob, M.fold_ealpha), o_ft = put(blob, M.fold_theta), o_gr = put(blob, M.gratings),
+         o_sl = put(blob, M.optc_slope), o_fi = put(blob, M.fold_inv_de),
          o_ge = put(blob, M.geff_energy), o_gc = put(blob, M.geff_cum), o_ok = put(blob, M.order_k),
          o_se = put(blob, M.sectors), o_ch = put(blob, M.chips);
   cudaError_t e = c->tables.ensure(blob.size());
@@ -84,6 +85,8 @@ static int upload_model(mx_context *c) {
   c->T.fold_hdr = (const double *) (b + o_fh);
   c->T.fold_ealpha = (const double *) (b + o_fe);
   c->T.fold_theta = (const float *) (b + o_ft);
+  c->T.optc_slope = (const double *) (b + o_sl);
+  c->T.fold_inv_de = (const double *) (b + o_fi);
   c->T.gratings = (const MxGratingDev *) (b + o_gr);
   c->T.geff_energy = (const float *) (b + o_ge);
   c->T.geff_cum = (const float *) (b + o_gc);

@@ -72,6 +72,14 @@ MXD void sincos_small(double x, double *s, double *c) {
   } else
     mx_sincos(x, s, c);
 }
+// sin(pi y), cos(pi y): the argument needs no reduction by pi.
+MXD void mx_sincospi(double y, double *s, double *c) {
+#ifdef __CUDA_ARCH__
+  sincospi(y, s, c);
+#else
+  *s = std::sin(PI * y); *c = std::cos(PI * y);
+#endif
+}
 MXD D3 rotate_unit_angle(D3 p, D3 n, double theta) {
   double s, c;
   mx_sincos(theta, &s, &c);
@@ -124,7 +132,10 @@ MXD unsigned bsearch_d(double x, const double *xp, unsigned n) {  // JDMbinary_s
 // JDMinterpolate_f (finterpo.c:59-86).  The result is rounded to float, so
 // the double expression is evaluated without contraction exactly as the
 // reference writes it.
-MXD float interp_f(float x, const float *xp, const float *yp, unsigned n) {
+// The interval slopes (float dy over double dx, as the reference divides)
+// are precomputed on the host, so the kernel only multiplies; the slope of
+// the interval between n0 and n1 is slope[min(n0, n1)] in either order.
+MXD float interp_f(float x, const float *xp, const float *yp, const double *slope, unsigned n) {
   if (n == 1) return yp[0];
   unsigned n1 = bsearch_f(x, xp, n), n0 = n1 - 1;
   if (n1 < n && x == xp[n1]) return yp[n1];
@@ -132,8 +143,7 @@ MXD float interp_f(float x, const float *xp, const float *yp, unsigned n) {
   if (n1 == 0) n0 = 1;
   double x0 = xp[n0], x1 = xp[n1];
   if (x1 == x0) return yp[n1];
-  double dy = (double) (yp[n1] - yp[n0]);
-  double q = MX_DDIV(dy, MX_DADD(x1, -x0));
+  double q = slope[n0 < n1 ? n0 : n1];
   return (float) MX_DADD((double) yp[n0], MX_DMUL(q, MX_DADD((double) x, -x0)));
 }
 
@@ -249,14 +259,16 @@ struct Ph {
 // JDMquadratic_root (qroot.c:36-70), same cancellation-free form.
 MXD int quadratic_root(double a, double b, double c, double &rp, double &rm) {
   if (a == 0.0) return -1;
-  double bsqr = b * b, ac4 = a * c * 4, nb2a = -b / (2.0 * a);
+  double bsqr = b * b, ac4 = a * c * 4;
   if (bsqr > ac4) {
+    // rp = -2c / (b f), rm = -b f / (2a) from one reciprocal of a b f
     double factor = 1.0 + sqrt(1.0 - ac4 / bsqr);
-    rp = -2.0 * c / (b * factor);
-    rm = nb2a * factor;
+    double bf = b * factor, inv = 1.0 / (a * bf);
+    rp = -2.0 * c * a * inv;
+    rm = -0.5 * bf * bf * inv;
     return 1;
   }
-  if (bsqr == ac4) { rp = rm = nb2a; return 1; }
+  if (bsqr == ac4) { rp = rm = -b / (2.0 * a); return 1; }
   return 0;
 }
 
@@ -288,8 +300,9 @@ MXD int conic_intersection(const MxShellDev &h, int o, D3 &x0, D3 p, D3 &normal)
 MXD void blur_normal(D3 &n, double blur_rad, Rng &rng) {
   double inv = mx_rsqrt(n.y * n.y + n.z * n.z);
   D3 perp = mk(0.0, n.z * inv, -n.y * inv);
-  double phi = (2.0 * PI) * rng.uniform();
-  perp = rotate_unit_angle(perp, n, phi);
+  double s, c;
+  mx_sincospi(2.0 * rng.uniform(), &s, &c);   // phi = 2 pi u
+  perp = rotate_unit(perp, n, c, s);
   double ang = blur_rad * rng.normal();
   n = rotate_unit_small(n, perp, ang);
 }
@@ -306,10 +319,12 @@ MXD double reflectivity(double cos_t, double beta, double delta) {
   double rr, ri;
   double r = sqrt(wr * wr + wi * wi);
   if (r == 0.0) { rr = wr; ri = wi; }
-  else if (wr >= 0.0) { rr = sqrt(0.5 * (r + wr)); ri = 0.5 * wi / rr; }
-  else {
-    double q = sqrt(0.5 * (r - wr));
-    rr = 0.5 * wi / q; ri = q;
+  else if (wr >= 0.0) {
+    double h = 0.5 * (r + wr), inv = mx_rsqrt(h);
+    rr = h * inv; ri = 0.5 * wi * inv;
+  } else {
+    double h = 0.5 * (r - wr), inv = mx_rsqrt(h);
+    rr = 0.5 * wi * inv; ri = h * inv;
     if (rr < 0.0) { rr = -rr; ri = -ri; }
   }
   // e_perp = (cos - root) / (cos + root)
@@ -331,7 +346,7 @@ MXD double fold_theta(const MxTables &T, int table, unsigned a, double p) {
 #else
   if (p > p_max) return std::pow(MX_LDG(hd + 4) * (1.0 - p), MX_LDG(hd + 5));
 #endif
-  double di = (p - p_min) / MX_LDG(hd + 2);
+  double di = (p - p_min) * MX_LDG(hd + 7);
   unsigned i = (unsigned) di;
   unsigned num = (unsigned) MX_LDG(hd + 6);
   const float *t = T.fold_theta + ((size_t) table * MX_FOLD_MAX + a) * MX_FOLD_THETA;
@@ -349,8 +364,8 @@ MXD double wfold_interp(const MxTables &T, int table, double energy, double sin_
   if (i == num) i--;
   if (i == 0) i++;
   double t0 = fold_theta(T, table, i - 1, r), t1 = fold_theta(T, table, i, r);
-  double e0 = MX_LDG(eas + i - 1), e1 = MX_LDG(eas + i);
-  return t0 + (t1 - t0) * (ea - e0) / (e1 - e0);
+  double e0 = MX_LDG(eas + i - 1);
+  return t0 + (t1 - t0) * (ea - e0) * MX_LDG(T.fold_inv_de + (size_t) table * MX_FOLD_MAX + i - 1);
 }
 
 // reflect_from_conic (hrma.c:488-545) after the intersection: normal blur,
@@ -378,9 +393,10 @@ MXD int reflect_at(const MxTables &T, const MxShellDev &h, int o, int table, D3 
 
 // intersects_struts (hrma.c:928-968): three bars rotated by 60 degrees.
 MXD bool struts_block(const MxTables &T, int set, D3 x, D3 p) {
+  double inv_px = 1.0 / p.x;
   for (int k = 0; k < 2; k++) {
     double hw = T.strut_half_width[set][k];
-    double t = (T.strut_xpos[set][k] + T.cap - x.x) / p.x;
+    double t = (T.strut_xpos[set][k] + T.cap - x.x) * inv_px;
     double y = x.y + p.y * t, z = x.z + p.z * t;
     for (int i = 0; i < 3; i++) {
       if (i != 0) { double tmp = T.cos30 * y - T.sin30 * z; z = T.sin30 * y + T.cos30 * z; y = tmp; }
@@ -403,8 +419,8 @@ struct MirrorState {
 // vignetting, project_photon_to_hrma (hrma.c:984-1050), transform into the
 // paraboloid's frame, optical constants, paraboloid intersection.  Returns
 // true if the photon reached the paraboloid.
-MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *optc, Ph &ph, Rng &rng,
-                      MirrorState &m) {
+MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *optc, const double *slope, Ph &ph,
+                      Rng &rng, MirrorState &m) {
   rng.window(MX_U_MIRROR, 12, MX_N_MIRROR, 2);
   if (!T.ideal) {
     if (rng.uniform() > T.hrma_vig) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
@@ -434,9 +450,8 @@ MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *
     if (rng.overrun || guard >= 64) { rng.overrun = true; return false; }
     if (h.shutter & (1u << quad)) break;
   }
-  theta = (2.0 * PI) * (theta - 1.0 / 8.0);
   double st, ct;
-  mx_sincos(theta, &st, &ct);
+  mx_sincospi(2.0 * (theta - 1.0 / 8.0), &st, &ct);   // angle 2 pi (u - 1/8)
   x = mk(h.front_position, radius * st - h.to_osac[0][1], radius * ct - h.to_osac[0][2]);
   if (T.source_distance > 0.0) p = normalized(x + T.source_distance * p);
   if (T.use_struts && struts_block(T, 0, x, p)) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
@@ -447,11 +462,11 @@ MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *
   m.beta = 0.0f; m.delta = 1.0f; m.corr = 1.0;
   if (T.opt_n) {
     float fe = (float) ph.e;
-    m.beta = interp_f(fe, optc, optc + T.opt_n, T.opt_n);
-    m.delta = interp_f(fe, optc, optc + 2 * T.opt_n, T.opt_n);
+    m.beta = interp_f(fe, optc, optc + T.opt_n, slope, T.opt_n);
+    m.delta = interp_f(fe, optc, optc + 2 * T.opt_n, slope + (T.opt_n - 1), T.opt_n);
     if (T.use_scale) {
       const float *ce = optc + 3 * T.opt_n + h.corr_off;
-      m.corr = sqrt((double) interp_f(fe, ce, ce + h.corr_n, h.corr_n));
+      m.corr = sqrt((double) interp_f(fe, ce, ce + h.corr_n, slope + h.corr_slope_off, h.corr_n));
     }
   }
   D3 n;
@@ -496,9 +511,10 @@ MXD void mirror_back(const MxTables &T, const MxShellDev *shells, Ph &ph, Rng &r
   ph.x = x; ph.p = p;
 }
 
-MXD void mirror_stage(const MxTables &T, const MxShellDev *shells, const float *optc, Ph &ph, Rng &rng) {
+MXD void mirror_stage(const MxTables &T, const MxShellDev *shells, const float *optc, const double *slope, Ph &ph,
+                      Rng &rng) {
   MirrorState m;
-  if (mirror_front(T, shells, optc, ph, rng, m) && mirror_middle(T, shells, ph, rng, m))
+  if (mirror_front(T, shells, optc, slope, ph, rng, m) && mirror_middle(T, shells, ph, rng, m))
     mirror_back(T, shells, ph, rng, m);
 }
 
@@ -509,9 +525,13 @@ MXD void mirror_stage(const MxTables &T, const MxShellDev *shells, const float *
 MXD void dither_stage(const MxTables &T, Ph &ph, Rng &rng) {
   rng.window(0, 0, MX_N_DITHER, 2);
   double t = (2.0 * PI) * (T.start_time + ph.t);
-  float fra = (float) (T.dith_amp[0] * sin(t / T.dith_period[0] + T.dith_phase[0]));
-  float fdec = (float) (T.dith_amp[1] * sin(t / T.dith_period[1] + T.dith_phase[1]));
-  float froll = (float) (T.nominal_roll + T.dith_amp[2] * sin(t / T.dith_period[2] + T.dith_phase[2]));
+  // A zero amplitude makes amp * sin(...) zero whatever the sine; skip it.
+  double v[3];
+  for (int k = 0; k < 3; k++)
+    v[k] = T.dith_amp[k] != 0.0 ? T.dith_amp[k] * sin(t / T.dith_period[k] + T.dith_phase[k]) : 0.0;
+  float fra = (float) v[0];
+  float fdec = (float) v[1];
+  float froll = (float) (T.nominal_roll + v[2]);
   ph.dith[0] = fra; ph.dith[1] = fdec; ph.dith[2] = froll;
   double ra = (double) fra + T.aspect_blur * rng.normal();
   double dec = (double) fdec + T.aspect_blur * rng.normal();
@@ -710,10 +730,10 @@ MXD void detect_stage(const MxTables &T, const MxChipDev *chips, Ph &ph, Rng &rn
 // stages of process_photons (marx.c:240-273); a photon with a bad flag is
 // skipped by later stages as marx_prune_photons drops it, and a photon
 // whose stage ran out of pre-drawn variates is not traced further.
-MXD void trace_photon(const MxTables &T, const MxShellDev *shells, const float *optc, const MxGratingDev *grs,
-                      const MxChipDev *chips, uint32_t stages, Ph &ph, Rng &rng) {
+MXD void trace_photon(const MxTables &T, const MxShellDev *shells, const float *optc, const double *slope,
+                      const MxGratingDev *grs, const MxChipDev *chips, uint32_t stages, Ph &ph, Rng &rng) {
   if ((stages & MX_STAGE_DITHER) && T.dither) dither_stage(T, ph, rng);
-  if ((stages & MX_STAGE_MIRROR) && !(ph.flags & MX_BAD_PHOTON_MASK)) mirror_stage(T, shells, optc, ph, rng);
+  if ((stages & MX_STAGE_MIRROR) && !(ph.flags & MX_BAD_PHOTON_MASK)) mirror_stage(T, shells, optc, slope, ph, rng);
   if (rng.overrun) return;
   if ((stages & MX_STAGE_GRATING) && T.grating && !(ph.flags & MX_BAD_PHOTON_MASK)) grating_stage(T, grs, ph, rng);
   if (rng.overrun) return;

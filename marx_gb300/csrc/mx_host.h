@@ -21,7 +21,8 @@ struct HostModel {
   MxTables T;
   std::vector<MxShellDev> shells;
   std::vector<float> optc;
-  std::vector<double> fold_hdr, fold_ealpha;
+  std::vector<double> optc_slope;
+  std::vector<double> fold_hdr, fold_ealpha, fold_inv_de;
   std::vector<float> fold_theta;
   std::vector<MxGratingDev> gratings;
   std::vector<float> geff_energy, geff_cum;

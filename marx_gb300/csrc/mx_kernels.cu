@@ -13,7 +13,8 @@ __host__ __device__ static inline size_t align16(size_t x) { return (x + 15) & ~
 // searches run on these).
 size_t trace_shared_bytes(const MxTables &T) {
   return align16(4 * sizeof(MxShellDev)) + align16(4 * sizeof(MxGratingDev)) +
-         align16(MX_MAX_CHIPS * sizeof(MxChipDev)) + align16((size_t) T.optc_len * sizeof(float));
+         align16(MX_MAX_CHIPS * sizeof(MxChipDev)) + align16((size_t) T.optc_len * sizeof(float)) +
+         align16((size_t) T.slope_len * sizeof(double));
 }
 
 __device__ __forceinline__ void copy_words(uint32_t *dst, const uint32_t *src, size_t words) {
@@ -22,20 +23,12 @@ __device__ __forceinline__ void copy_words(uint32_t *dst, const uint32_t *src, s
 
 // Fused dither -> mirror -> grating -> detector trace, one photon per
 // thread, grid-stride over the photon list with a resident grid.
+__device__ __forceinline__ void stage_tables(const MxTables &T, MxShellDev *&sh, MxGratingDev *&gr, MxChipDev *&ch,
+                                             float *&optc, double *&slope);
+
 __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_trace_kernel(MxTables T, TraceIO io) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  size_t o_gr = align16(4 * sizeof(MxShellDev));
-  size_t o_ch = o_gr + align16(4 * sizeof(MxGratingDev));
-  size_t o_op = o_ch + align16(MX_MAX_CHIPS * sizeof(MxChipDev));
-  MxShellDev *sh = (MxShellDev *) smem;
-  MxGratingDev *gr = (MxGratingDev *) (smem + o_gr);
-  MxChipDev *ch = (MxChipDev *) (smem + o_ch);
-  float *optc = (float *) (smem + o_op);
-  copy_words((uint32_t *) sh, (const uint32_t *) T.shells, 4 * sizeof(MxShellDev) / 4);
-  copy_words((uint32_t *) gr, (const uint32_t *) T.gratings, 4 * sizeof(MxGratingDev) / 4);
-  copy_words((uint32_t *) ch, (const uint32_t *) T.chips, (size_t) (T.nchips > 0 ? T.nchips : 1) * sizeof(MxChipDev) / 4);
-  copy_words((uint32_t *) optc, (const uint32_t *) T.optc, (size_t) T.optc_len);
-  __syncthreads();
+  MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
+  stage_tables(T, sh, gr, ch, optc, slope);
 
   const size_t n = io.n;
   const uint32_t stride = gridDim.x * blockDim.x;
@@ -63,7 +56,7 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_trace_kernel(MxTables T, Tr
     r.tag = io.tag ? io.tag[i] : i;
     r.upos = r.uend = r.npos = r.nend = 0;
     r.overrun = false;
-    trace_photon(T, sh, optc, gr, ch, io.stages, q, r);
+    trace_photon(T, sh, optc, slope, gr, ch, io.stages, q, r);
     if (r.overrun) {
       q.flags |= MX_PHOTON_VARIATE_OVERRUN;
       atomicAdd(io.overrun, 1ull);
@@ -90,16 +83,21 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_trace_kernel(MxTables T, Tr
 // Appends are warp-aggregated (one atomic per warp); the order of records
 // in a queue does not affect any photon's result.
 
+// Shared-memory layout: shells | gratings | chips | optical-constant and
+// correction tables (float) | their interval slopes (double).
 __device__ __forceinline__ void stage_tables(const MxTables &T, MxShellDev *&sh, MxGratingDev *&gr, MxChipDev *&ch,
-                                             float *&optc) {
+                                             float *&optc, double *&slope) {
   extern __shared__ __align__(16) unsigned char smem[];
   size_t o_gr = align16(4 * sizeof(MxShellDev));
   size_t o_ch = o_gr + align16(4 * sizeof(MxGratingDev));
   size_t o_op = o_ch + align16(MX_MAX_CHIPS * sizeof(MxChipDev));
+  size_t o_sl = o_op + align16((size_t) T.optc_len * sizeof(float));
   sh = (MxShellDev *) smem;
   gr = (MxGratingDev *) (smem + o_gr);
   ch = (MxChipDev *) (smem + o_ch);
   optc = (float *) (smem + o_op);
+  slope = (double *) (smem + o_sl);
+  copy_words((uint32_t *) slope, (const uint32_t *) T.optc_slope, (size_t) T.slope_len * 2);
   copy_words((uint32_t *) sh, (const uint32_t *) T.shells, 4 * sizeof(MxShellDev) / 4);
   copy_words((uint32_t *) gr, (const uint32_t *) T.gratings, 4 * sizeof(MxGratingDev) / 4);
   copy_words((uint32_t *) ch, (const uint32_t *) T.chips, (size_t) (T.nchips > 0 ? T.nchips : 1) * sizeof(MxChipDev) / 4);
@@ -149,8 +147,8 @@ __device__ __forceinline__ void store_core(const TraceIO &io, uint32_t i, const 
 }
 
 __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_wave_a(MxTables T, TraceIO io, WaveBufs w) {
-  MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc;
-  stage_tables(T, sh, gr, ch, optc);
+  MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
+  stage_tables(T, sh, gr, ch, optc, slope);
   const size_t n = io.n;
   const uint32_t lane = threadIdx.x & 31, warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -184,7 +182,7 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_wave_a(MxTables T, TraceIO 
       if ((io.stages & MX_STAGE_DITHER) && T.dither) dither_stage(T, q, r);
       if (io.dith) for (int k = 0; k < 3; k++) io.dith[k * n + i] = q.dith[k];
       MirrorState m;
-      if (!(q.flags & MX_BAD_PHOTON_MASK) && mirror_front(T, sh, optc, q, r, m)) {
+      if (!(q.flags & MX_BAD_PHOTON_MASK) && mirror_front(T, sh, optc, slope, q, r, m)) {
         keep = true;
         to_rec(rec, q, m, r, i);
       } else
@@ -195,8 +193,8 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_wave_a(MxTables T, TraceIO 
 }
 
 __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_wave_b(MxTables T, TraceIO io, WaveBufs w) {
-  MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc;
-  stage_tables(T, sh, gr, ch, optc);
+  MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
+  stage_tables(T, sh, gr, ch, optc, slope);
   const uint32_t count = *(volatile unsigned int *) &w.counts[0];
   const uint32_t lane = threadIdx.x & 31, warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -219,8 +217,8 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_wave_b(MxTables T, TraceIO 
 }
 
 __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_wave_c(MxTables T, TraceIO io, WaveBufs w) {
-  MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc;
-  stage_tables(T, sh, gr, ch, optc);
+  MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
+  stage_tables(T, sh, gr, ch, optc, slope);
   const uint32_t count = *(volatile unsigned int *) &w.counts[1];
   const uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += stride) {

@@ -97,6 +97,17 @@ static void vnorm(double a[3]) {
   if (l != 0.0) { a[0] = a[0] / l; a[1] = a[1] / l; a[2] = a[2] / l; }
 }
 
+// Slope of each interval of a float table exactly as JDMinterpolate_f
+// (finterpo.c:83) forms it: float difference of the ordinates over the
+// double difference of the abscissae.  The kernels then only multiply.
+static void append_slopes(std::vector<double> &out, const float *x, const float *y, unsigned n) {
+  for (unsigned k = 0; k + 1 < n; k++) {
+    double x0 = x[k], x1 = x[k + 1];
+    float dy = y[k + 1] - y[k];
+    out.push_back(x1 == x0 ? 0.0 : (double) dy / (x1 - x0));
+  }
+}
+
 bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string &err) {
   M = HostModel();
   MxTables &T = M.T;
@@ -133,6 +144,8 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
   unsigned optn = (unsigned) (cnt / 3);
   T.opt_n = T.ideal ? 0 : (int32_t) optn;
   M.optc.assign(opt, opt + 3 * optn);
+  append_slopes(M.optc_slope, opt, opt + optn, optn);          // beta
+  append_slopes(M.optc_slope, opt, opt + 2 * optn, optn);      // delta
   double total_area = 0.0;
   M.shells.resize(4);
   for (int i = 0; i < 4; i++) {
@@ -179,14 +192,19 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
     h.corr_off = (int32_t) (M.optc.size() - 3 * optn);
     h.corr_n = (int32_t) (cnt / 2);
     M.optc.insert(M.optc.end(), corr, corr + cnt);
+    h.corr_slope_off = (int32_t) M.optc_slope.size();
+    append_slopes(M.optc_slope, corr, corr + h.corr_n, (unsigned) h.corr_n);
   }
   if (total_area <= 0.0) { err = "The mirror geometric area is 0.  Check shutters."; return false; }
   for (auto &h : M.shells) h.area_fraction = h.area_fraction / total_area;
   T.optc_len = (int32_t) M.optc.size();
+  if (M.optc_slope.empty()) M.optc_slope.push_back(0.0);
+  T.slope_len = (int32_t) M.optc_slope.size();
 
   // ---- WFold tables: index 2*shell + optic
   M.fold_hdr.assign((size_t) 8 * MX_FOLD_MAX * 8, 0.0);
   M.fold_ealpha.assign((size_t) 8 * MX_FOLD_MAX, 0.0);
+  M.fold_inv_de.assign((size_t) 8 * MX_FOLD_MAX, 0.0);
   M.fold_theta.assign((size_t) 8 * MX_FOLD_MAX * MX_FOLD_THETA, 0.0f);
   for (int i = 0; i < 4; i++)
     for (int o = 0; o < 2; o++) {
@@ -204,6 +222,8 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
         memcpy(dst, hd + 7 * a, 7 * sizeof(double));
         if (hd[7 * a + 6] > (double) nmax || hd[7 * a + 6] < 1) { err = base + ": bad angle count"; return false; }
         M.fold_ealpha[(size_t) t * MX_FOLD_MAX + a] = hd[7 * a];
+        dst[7] = 1.0 / hd[7 * a + 2];
+        if (a + 1 < narr) M.fold_inv_de[(size_t) t * MX_FOLD_MAX + a] = 1.0 / (hd[7 * (a + 1)] - hd[7 * a]);
         memcpy(&M.fold_theta[((size_t) t * MX_FOLD_MAX + a) * MX_FOLD_THETA], th + a * nmax, nmax * sizeof(float));
       }
     }

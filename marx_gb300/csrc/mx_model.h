@@ -19,7 +19,7 @@ struct MxShellDev {
   double scat[2];                              // WFold scattering factor
   int32_t corr_off, corr_n;                    // correction-factor table (floats after the optical constants)
   uint32_t shutter;                            // open-quadrant bitmap
-  int32_t pad;
+  int32_t corr_slope_off;                      // its interval slopes in optc_slope
 };
 
 // One HETG grating (per mirror shell, diffract.c:51-77).
@@ -43,7 +43,11 @@ struct MxTables {
   const float *optc;            // [beta-table energies | beta | delta | corr(E,f) per shell]
   int32_t optc_len;             // floats in optc
   int32_t opt_n;                // rows of the optical-constant table (0: perfect reflector)
-  const double *fold_hdr;       // [8][MX_FOLD_MAX][8]: e_alpha p_min delta_p p_max norm expon num -
+  const double *optc_slope;     // per-interval slopes of beta, delta and each correction table
+  int32_t slope_len;            // doubles in optc_slope
+  int32_t pad_slope;
+  const double *fold_hdr;       // [8][MX_FOLD_MAX][8]: e_alpha p_min delta_p p_max norm expon num 1/delta_p
+  const double *fold_inv_de;    // [8][MX_FOLD_MAX]: 1 / (e_alpha[k+1] - e_alpha[k])
   const double *fold_ealpha;    // [8][MX_FOLD_MAX]
   const float *fold_theta;      // [8][MX_FOLD_MAX][MX_FOLD_THETA]
   uint32_t fold_num[8];         // table index = 2 * shell + optic
