@@ -683,18 +683,18 @@ MXD int chip_plane(const MxChipDev &g, D3 x0, D3 p, D3 &x, double &dx, double &d
 // _marx_acis_apply_streak (acis-i.c:60-93).  QE and pulse height are not
 // modelled (DetIdeal); the detector frame is the identity rotation plus the
 // DetOffset translation (INTERNAL dither has no detector motion).
-MXD void detect_stage(const MxTables &T, const MxChipDev *chips, Ph &ph, Rng &rng) {
+MXD void detect_stage(const MxTables &T, const MxChipDev *chips, int nchips, Ph &ph, Rng &rng) {
   rng.window(MX_U_DETECT, 2, MX_N_DETECT, 2);
   D3 off = mk(T.det_offset[0], T.det_offset[1], T.det_offset[2]);
   D3 x = ph.x - off, p = ph.p;
   int hit = -1;
   D3 xh = x;
   double dx = 0, dy = 0;
-  for (int k = 0; k < T.nchips; k++)
+  for (int k = 0; k < nchips; k++)
     if (1 == chip_plane(chips[k], x, p, xh, dx, dy, true)) { hit = k; break; }
   if (hit < 0 && T.det_extend) {
     double best = -1;
-    for (int k = 0; k < T.nchips; k++) {
+    for (int k = 0; k < nchips; k++) {
       D3 xx; double ddx, ddy;
       if (-1 == chip_plane(chips[k], x, p, xx, ddx, ddy, false)) continue;
       double ex = ddx - 0.5 * chips[k].xlen, ey = ddy - 0.5 * chips[k].ylen, r2 = ex * ex + ey * ey;
@@ -737,7 +737,8 @@ MXD void trace_photon(const MxTables &T, const MxShellDev *shells, const float *
   if (rng.overrun) return;
   if ((stages & MX_STAGE_GRATING) && T.grating && !(ph.flags & MX_BAD_PHOTON_MASK)) grating_stage(T, grs, ph, rng);
   if (rng.overrun) return;
-  if ((stages & MX_STAGE_DETECT) && T.nchips && !(ph.flags & MX_BAD_PHOTON_MASK)) detect_stage(T, chips, ph, rng);
+  if ((stages & MX_STAGE_DETECT) && T.nchips && !(ph.flags & MX_BAD_PHOTON_MASK))
+    detect_stage(T, chips + T.chip_off, T.nchips, ph, rng);
 }
 
 }  // namespace mx

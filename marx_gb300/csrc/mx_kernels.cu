@@ -100,7 +100,7 @@ __device__ __forceinline__ void stage_tables(const MxTables &T, MxShellDev *&sh,
   copy_words((uint32_t *) slope, (const uint32_t *) T.optc_slope, (size_t) T.slope_len * 2);
   copy_words((uint32_t *) sh, (const uint32_t *) T.shells, 4 * sizeof(MxShellDev) / 4);
   copy_words((uint32_t *) gr, (const uint32_t *) T.gratings, 4 * sizeof(MxGratingDev) / 4);
-  copy_words((uint32_t *) ch, (const uint32_t *) T.chips, (size_t) (T.nchips > 0 ? T.nchips : 1) * sizeof(MxChipDev) / 4);
+  copy_words((uint32_t *) ch, (const uint32_t *) T.chips, MX_MAX_CHIPS * sizeof(MxChipDev) / 4);
   copy_words((uint32_t *) optc, (const uint32_t *) T.optc, (size_t) T.optc_len);
   __syncthreads();
 }
@@ -146,7 +146,7 @@ __device__ __forceinline__ void store_core(const TraceIO &io, uint32_t i, const 
   if (io.shell) io.shell[i] = (int8_t) q.shell;
 }
 
-__global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_wave_a(MxTables T, TraceIO io, WaveBufs w) {
+__global__ void __launch_bounds__(MX_TRACE_BLOCK, 3) mx_wave_a(MxTables T, TraceIO io, WaveBufs w) {
   MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
   stage_tables(T, sh, gr, ch, optc, slope);
   const size_t n = io.n;
@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_wave_a(MxTables T, TraceIO 
   }
 }
 
-__global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_wave_b(MxTables T, TraceIO io, WaveBufs w) {
+__global__ void __launch_bounds__(MX_TRACE_BLOCK, 3) mx_wave_b(MxTables T, TraceIO io, WaveBufs w) {
   MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
   stage_tables(T, sh, gr, ch, optc, slope);
   const uint32_t count = *(volatile unsigned int *) &w.counts[0];
@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_wave_c(MxTables T, TraceIO 
     if (!r.overrun && (io.stages & MX_STAGE_GRATING) && T.grating && !(q.flags & MX_BAD_PHOTON_MASK))
       grating_stage(T, gr, q, r);
     if (!r.overrun && (io.stages & MX_STAGE_DETECT) && T.nchips && !(q.flags & MX_BAD_PHOTON_MASK))
-      detect_stage(T, ch, q, r);
+      detect_stage(T, ch + T.chip_off, T.nchips, q, r);
     store_core(io, i, q, r.overrun);
     if (q.order != unset && io.order) io.order[i] = (int8_t) q.order;
     if (q.ccd != unset) {

@@ -229,9 +229,12 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
     }
 
   // ---- HETG
+  // The HETG tables are built whatever the configured grating, so that a
+  // batch of sources can choose per source.
   T.grating = cfg.grating == MX_GRATING_HETG;
+  if (cfg.grating != MX_GRATING_NONE && cfg.grating != MX_GRATING_HETG) { err = "unsupported grating"; return false; }
   M.gratings.assign(4, MxGratingDev());
-  if (T.grating) {
+  {
     for (int i = 0; i < 4; i++) {
       MxGratingDev &g = M.gratings[i];
       memset(&g, 0, sizeof(g));
@@ -308,18 +311,23 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
   if (M.order_k.empty()) M.order_k.push_back(0.0);
   if (M.sectors.empty()) M.sectors.push_back(0.0);
 
-  // ---- detector chips
-  T.nchips = 0;
-  if (cfg.detector == MX_DETECTOR_ACIS_I || cfg.detector == MX_DETECTOR_ACIS_S) {
-    size_t ng;
+  // ---- detector chips: ACIS-I (ids 0-3, aimpoint AI2) then ACIS-S (ids
+  // 4-9, aimpoint AS1), each set as the reference builds it for that
+  // detector; a chip's index in the table is its id.
+  if (cfg.detector != MX_DETECTOR_NONE && cfg.detector != MX_DETECTOR_ACIS_I && cfg.detector != MX_DETECTOR_ACIS_S) {
+    err = "unsupported detector"; return false;
+  }
+  {
+    size_t ng = 0;
     const double *geom = pk.get<double>("acis/geom", &ng, err);
     const double *orig = pk.get<double>("acis/origin", nullptr, err);
-    const double *aim = pk.get<double>(cfg.detector == MX_DETECTOR_ACIS_I ? "acis/aimpt_i" : "acis/aimpt_s", nullptr, err);
-    if (!geom || !orig || !aim) return false;
+    const double *aim_i = pk.get<double>("acis/aimpt_i", nullptr, err);
+    const double *aim_s = pk.get<double>("acis/aimpt_s", nullptr, err);
+    if (!geom || !orig || !aim_i || !aim_s) return false;
     ng /= 13;
-    int lo = cfg.detector == MX_DETECTOR_ACIS_I ? 0 : 4, hi = cfg.detector == MX_DETECTOR_ACIS_I ? 3 : 9;
-    double ofs[3] = {aim[0] + orig[0], aim[1] + orig[1], aim[2] + orig[2]};
-    for (int id = lo; id <= hi; id++) {
+    for (int id = 0; id <= 9; id++) {
+      const double *aim = id < 4 ? aim_i : aim_s;
+      double ofs[3] = {aim[0] + orig[0], aim[1] + orig[1], aim[2] + orig[2]};
       double ll[3] = {0, 0, 0}, lr[3] = {0, 0, 0}, ul[3] = {0, 0, 0};
       bool found = false;
       for (size_t r = 0; r < ng; r++)
@@ -346,18 +354,18 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
       c.xpix = c.xlen / 1024.0; c.ypix = c.ylen / 1024.0;
       M.chips.push_back(c);
     }
-    if (cfg.acis_exposure_time <= 0) { err = "ACIS_Exposure_Time must be greater than 0"; return false; }
-    T.nchips = (int32_t) M.chips.size();
+    if (cfg.detector != MX_DETECTOR_NONE && cfg.acis_exposure_time <= 0) {
+      err = "ACIS_Exposure_Time must be greater than 0"; return false;
+    }
+    T.chip_off = cfg.detector == MX_DETECTOR_ACIS_S ? 4 : 0;
+    T.nchips = cfg.detector == MX_DETECTOR_NONE ? 0 : (cfg.detector == MX_DETECTOR_ACIS_I ? 4 : 6);
     T.det_extend = cfg.det_extend != 0;
     for (int k = 0; k < 3; k++) T.det_offset[k] = cfg.det_offset[k];
     T.frame_transfer = cfg.acis_frame_transfer_time < 0.0 ? 0.0 : cfg.acis_frame_transfer_time;
     T.exposure = cfg.acis_exposure_time;
     T.frame_time = T.frame_transfer + T.exposure;
     T.focal_length = cfg.focal_length;
-  } else if (cfg.detector != MX_DETECTOR_NONE) {
-    err = "unsupported detector"; return false;
   }
-  if (M.chips.empty()) M.chips.push_back(MxChipDev());
 
   // ---- dither
   T.dither = cfg.dither == MX_DITHER_INTERNAL;

@@ -65,6 +65,7 @@ struct MxTables {
   int32_t dither, grating;
   double dith_amp[3], dith_period[3], dith_phase[3], nominal_roll, aspect_blur, start_time;
   // detector
-  int32_t nchips, det_extend;
+  int32_t nchips, det_extend;   // configured detector's chips: chips[chip_off .. chip_off + nchips)
+  int32_t chip_off, pad_chip;
   double det_offset[3], frame_transfer, frame_time, exposure, focal_length;
 };
