@@ -124,11 +124,13 @@ typedef struct mx_config {
 } mx_config;
 
 /* Structure-of-arrays photon list.  3-vectors are component-major:
- * x[0*n + i], x[1*n + i], x[2*n + i].  Which pointers must be set depends
+ * x[0*s + i], x[1*s + i], x[2*s + i] with s = stride (n when 0).  Which pointers must be set depends
  * on the stages run; unused outputs may be NULL. */
 typedef struct mx_photons {
   uint32_t n;
-  uint32_t reserved;
+  uint32_t stride;         /* distance between the components of x, p and
+                              dither_state (0: n); a larger stride views a
+                              slice of a longer list in place */
   double   *energy;        /* keV */
   double   *x;             /* 3n, mm (output of the mirror) */
   double   *p;             /* 3n, unit direction (input and output) */
@@ -194,6 +196,60 @@ int mx_set_trace_mode(mx_context *ctx, int mode);
  * copies results back; blocks until done. */
 int mx_trace_host(mx_context *ctx, const mx_photons *host, uint32_t stages,
                   const mx_variates *host_var, uint64_t seed);
+
+/* ------------------------------------------------------ point sources --
+ * A point source at infinity with a flat spectrum: the input producer of
+ * the trace (point_create_photons, marx/libsrc/s-point.c:59, with
+ * flat_energy, spectrum.c:138).  Photon k gets tag first_tag + k, energy
+ * emin + (emax - emin) u with u the Philox draw of that tag in the
+ * source domain, direction p, arrival time 0 and flags 0. */
+typedef struct mx_source {
+  double p[3];              /* unit direction of travel (toward the mirror) */
+  double energy_min, energy_max;   /* keV */
+  uint32_t num_photons;
+  int32_t grating;          /* MX_GRATING_NONE or MX_GRATING_HETG */
+  int32_t detector;         /* MX_DETECTOR_ACIS_I or MX_DETECTOR_ACIS_S */
+  uint32_t reserved;
+} mx_source;
+
+/* Fill energy, p, arrival_time, flags and tag of dev (device pointers,
+ * dev->n = src->num_photons) with the source's photons. */
+int mx_generate_source(mx_context *ctx, const mx_source *src, uint32_t first_tag, uint64_t seed,
+                       const mx_photons *dev, void *stream);
+
+/* ------------------------------------------------------------ batches --
+ * Many sources of uneven size traced in ONE persistent cooperative kernel
+ * launch (generation, dither, mirror, per-source grating and detector),
+ * replayed from a captured CUDA graph.  Source s owns photons
+ * [start[s], start[s+1]) of the batch's output list, tagged by their
+ * index in it.  The kernel's block size, work-tile size and resident
+ * blocks per SM are chosen by mx_batch_tune (timed trials, remembered per
+ * source-table and configuration hash for the life of the process). */
+typedef struct mx_batch mx_batch;
+typedef struct mx_batch_params {
+  int32_t block;            /* threads per block: 128 or 256 */
+  int32_t tile;             /* photons a warp claims per visit of the work counter (multiple of 32) */
+  int32_t blocks_per_sm;    /* resident blocks per SM (<= the occupancy limit) */
+  int32_t reserved;
+} mx_batch_params;
+
+mx_batch *mx_batch_create(mx_context *ctx, const mx_source *sources, int nsrc);
+int  mx_batch_set_params(mx_batch *b, const mx_batch_params *params);
+int  mx_batch_get_params(const mx_batch *b, mx_batch_params *params);
+/* Time candidate parameter sets (each run `trials` times) and keep the
+ * fastest; *best receives it.  A second call for an identical batch and
+ * configuration returns the remembered choice without timing. */
+int  mx_batch_tune(mx_batch *b, int trials, mx_batch_params *best);
+/* One graph launch: the whole batch, generation to detection. */
+int  mx_batch_run(mx_batch *b, uint64_t seed, void *stream);
+/* The same photons traced source by source with the plain entry points
+ * (mx_generate_source + mx_trace per source): the comparison baseline. */
+int  mx_batch_run_sequential(mx_batch *b, uint64_t seed, void *stream);
+/* Device views of the batch's photon list and the host array of nsrc + 1
+ * source offsets. */
+int  mx_batch_photons(mx_batch *b, mx_photons *dev_view, const uint32_t **source_start);
+uint64_t mx_batch_total_photons(const mx_batch *b);
+void mx_batch_destroy(mx_batch *b);
 
 /* Survivor compaction (marx_prune_photons, photon.c:40): writes the indices
  * of photons without MX_BAD_PHOTON_MASK bits to idx_out (device, n entries)

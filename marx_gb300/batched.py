@@ -1,0 +1,169 @@
+"""Batched form: many point sources in one persistent launch (mx_batch_* in
+include/marx_gb300.h), and the 256-source workload.
+
+    eng = Engine(batched_config())
+    b = Batch(eng, batched_sources())
+    b.tune()                      # autotuner, remembered per batch hash
+    b.run(seed)                   # one CUDA-graph launch
+    ph = b.photons()              # device columns (torch views)
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from .config import MxConfig, default_config, DETECTOR, GRATING, DITHER
+from .photons import COLUMNS, MxPhotons
+
+ARCMIN = math.pi / (180.0 * 60.0)
+
+
+class MxSource(C.Structure):
+    _fields_ = [("p", C.c_double * 3), ("energy_min", C.c_double), ("energy_max", C.c_double),
+                ("num_photons", C.c_uint32), ("grating", C.c_int32), ("detector", C.c_int32),
+                ("reserved", C.c_uint32)]
+
+
+class MxBatchParams(C.Structure):
+    _fields_ = [("block", C.c_int32), ("tile", C.c_int32), ("blocks_per_sm", C.c_int32), ("reserved", C.c_int32)]
+
+    def as_dict(self):
+        return {"block": self.block, "tile": self.tile, "blocks_per_sm": self.blocks_per_sm}
+
+
+def batched_config() -> MxConfig:
+    """Mirror with blur, WFold scattering and struts; no dither (each
+    source's direction is given); per-source grating and detector."""
+    c = default_config()
+    c.dither = DITHER["NONE"]
+    c.roll_nom = 0.0
+    c.grating = GRATING["NONE"]
+    c.detector = DETECTOR["ACIS-I"]
+    return c
+
+
+def batched_sources(nsrc: int = 256, seed: int = 404, nmin: float = 1e3, nmax: float = 1e6,
+                    emin: float = 0.3, emax: float = 10.0, max_offaxis_arcmin: float = 10.0):
+    """256 point sources: photon counts log-uniform in [nmin, nmax], off-axis
+    angle uniform in [0, 10'] at uniform azimuth, energies uniform in
+    [0.3, 10] keV, grating NONE or HETG and detector ACIS-I or ACIS-S drawn
+    independently per source."""
+    r = np.random.default_rng(seed)
+    counts = np.exp(r.uniform(np.log(nmin), np.log(nmax), nsrc)).astype(np.int64)
+    theta = r.uniform(0.0, max_offaxis_arcmin * ARCMIN, nsrc)
+    phi = r.uniform(0.0, 2 * np.pi, nsrc)
+    grat = r.integers(0, 2, nsrc)
+    det = r.integers(0, 2, nsrc)
+    arr = (MxSource * nsrc)()
+    for s in range(nsrc):
+        st = math.sin(theta[s])
+        arr[s].p[:] = [-math.cos(theta[s]), st * math.cos(phi[s]), st * math.sin(phi[s])]
+        arr[s].energy_min, arr[s].energy_max = emin, emax
+        arr[s].num_photons = int(counts[s])
+        arr[s].grating = GRATING["HETG"] if grat[s] else GRATING["NONE"]
+        arr[s].detector = DETECTOR["ACIS-S"] if det[s] else DETECTOR["ACIS-I"]
+    return arr
+
+
+class _DevArray:
+    """__cuda_array_interface__ view of a device pointer (no copy)."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {"data": (int(ptr), False), "shape": tuple(shape),
+                                         "typestr": typestr, "version": 3}
+
+
+def bind(L):
+    L.mx_batch_create.restype = C.c_void_p
+    L.mx_batch_create.argtypes = [C.c_void_p, C.POINTER(MxSource), C.c_int]
+    L.mx_batch_destroy.argtypes = [C.c_void_p]
+    L.mx_batch_set_params.argtypes = [C.c_void_p, C.POINTER(MxBatchParams)]
+    L.mx_batch_get_params.argtypes = [C.c_void_p, C.POINTER(MxBatchParams)]
+    L.mx_batch_tune.argtypes = [C.c_void_p, C.c_int, C.POINTER(MxBatchParams)]
+    L.mx_batch_run.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p]
+    L.mx_batch_run_sequential.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p]
+    L.mx_batch_photons.argtypes = [C.c_void_p, C.POINTER(MxPhotons), C.POINTER(C.POINTER(C.c_uint32))]
+    L.mx_batch_total_photons.restype = C.c_uint64
+    L.mx_batch_total_photons.argtypes = [C.c_void_p]
+    L.mx_generate_source.argtypes = [C.c_void_p, C.POINTER(MxSource), C.c_uint32, C.c_uint64,
+                                     C.POINTER(MxPhotons), C.c_void_p]
+
+
+class Batch:
+    def __init__(self, engine, sources):
+        self.eng = engine
+        self.L = engine.lib
+        bind(self.L)
+        self.sources = sources
+        self.h = self.L.mx_batch_create(engine.h, sources, len(sources))
+        if not self.h:
+            raise RuntimeError("mx_batch_create: " + self.L.mx_last_error(None).decode())
+        self.n = int(self.L.mx_batch_total_photons(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.mx_batch_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def tune(self, trials: int = 2) -> dict:
+        p = MxBatchParams()
+        self.eng._check(self.L.mx_batch_tune(self.h, trials, C.byref(p)))
+        return p.as_dict()
+
+    def params(self) -> dict:
+        p = MxBatchParams()
+        self.L.mx_batch_get_params(self.h, C.byref(p))
+        return p.as_dict()
+
+    def set_params(self, block, tile, blocks_per_sm):
+        p = MxBatchParams(block, tile, blocks_per_sm, 0)
+        self.eng._check(self.L.mx_batch_set_params(self.h, C.byref(p)))
+
+    def run(self, seed: int = 0, stream=None):
+        st = stream.cuda_stream if stream is not None else self.eng.current_stream()
+        self.eng._check(self.L.mx_batch_run(self.h, seed, C.c_void_p(st)))
+
+    def run_sequential(self, seed: int = 0, stream=None):
+        st = stream.cuda_stream if stream is not None else self.eng.current_stream()
+        self.eng._check(self.L.mx_batch_run_sequential(self.h, seed, C.c_void_p(st)))
+
+    def source_start(self) -> np.ndarray:
+        s = MxPhotons()
+        st = C.POINTER(C.c_uint32)()
+        self.L.mx_batch_photons(self.h, C.byref(s), C.byref(st))
+        return np.ctypeslib.as_array(st, shape=(len(self.sources) + 1,)).copy()
+
+    def photons(self):
+        """Torch views of the batch's device columns (valid while the batch lives)."""
+        import torch
+        s = MxPhotons()
+        st = C.POINTER(C.c_uint32)()
+        self.L.mx_batch_photons(self.h, C.byref(s), C.byref(st))
+        out = {}
+        code = {np.float64: "<f8", np.float32: "<f4", np.uint32: "<i4", np.int8: "|i1"}
+        for k, (dt, m) in COLUMNS.items():
+            shape = (m, self.n) if m > 1 else (self.n,)
+            out[k] = torch.as_tensor(_DevArray(getattr(s, k), shape, code[dt]), device="cuda")
+        return out
+
+    def to_host(self):
+        from .photons import PhotonList
+        q = PhotonList.__new__(PhotonList)
+        q.n = self.n
+        for k, t in self.photons().items():
+            a = t.cpu().numpy()
+            dt = COLUMNS[k][0]
+            setattr(q, k, a.view(dt) if a.dtype != dt else a.copy())
+        return q
+
+
+def generate_source(engine, src: MxSource, first_tag: int, seed: int, dev_photons, stream=None):
+    """Fill a DevicePhotons with one source's photons (mx_generate_source)."""
+    bind(engine.lib)
+    s = dev_photons.struct()
+    st = stream.cuda_stream if stream is not None else engine.current_stream()
+    engine._check(engine.lib.mx_generate_source(engine.h, C.byref(src), first_tag, seed, C.byref(s), C.c_void_p(st)))

@@ -10,53 +10,21 @@
 #include "mx_device.cuh"
 #include "mx_host.h"
 #include "mx_kernels.cuh"
+#include "mx_context.h"
 
 using namespace mx;
 
-static thread_local std::string g_create_err;
+thread_local std::string g_create_err;
 
-struct DevBuf {
-  void *ptr = nullptr;
-  size_t bytes = 0;
-  cudaError_t ensure(size_t need) {
-    if (need <= bytes) return cudaSuccess;
-    if (ptr) cudaFree(ptr);
-    ptr = nullptr; bytes = 0;
-    cudaError_t e = cudaMalloc(&ptr, need);
-    if (e == cudaSuccess) bytes = need;
-    return e;
-  }
-  void release() { if (ptr) cudaFree(ptr); ptr = nullptr; bytes = 0; }
-};
-
-struct mx_context {
-  int device = 0;
-  int num_sms = 0;
-  std::string err;
-  mx_config cfg;
-  Pack pack;
-  HostModel hm;
-  MxTables T;              // launch copy with device pointers
-  DevBuf tables;           // every table in one allocation
-  size_t shared_bytes = 0;
-  int trace_blocks[2] = {0, 0};   // resident blocks per SM for the slot / Philox kernels
-  cudaStream_t stream = nullptr;
-  DevBuf io[14];           // staging for mx_trace_host
-  DevBuf scan;             // compaction block counts
-  DevBuf wave;             // wavefront record queues
-  int wave_blocks = 0;     // resident blocks per SM for the wavefront kernels
-  int mode = MX_MODE_AUTO;
-  unsigned long long *d_overrun = nullptr;
-  unsigned long long launches = 0;
-};
-
-static int fail(mx_context *c, int code, const std::string &msg) {
+int mx_fail(mx_context *c, int code, const std::string &msg) {
   if (c) c->err = msg; else g_create_err = msg;
   return code;
 }
-static int cuda_fail(mx_context *c, cudaError_t e, const char *what) {
-  return fail(c, MX_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+int mx_cuda_fail(mx_context *c, cudaError_t e, const char *what) {
+  return mx_fail(c, MX_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
+static int fail(mx_context *c, int code, const std::string &msg) { return mx_fail(c, code, msg); }
+static int cuda_fail(mx_context *c, cudaError_t e, const char *what) { return mx_cuda_fail(c, e, what); }
 
 // ------------------------------------------------------------ uploading --
 template <class T> static size_t put(std::vector<char> &blob, const std::vector<T> &v) {
@@ -211,19 +179,21 @@ int mx_set_trace_mode(mx_context *c, int mode) {
   return MX_OK;
 }
 
-static int trace_device(mx_context *c, const mx_photons *ph, uint32_t stages, const double *U, const double *N,
-                        uint64_t seed, cudaStream_t st, bool fresh) {
+int mx_trace_tables(mx_context *c, const MxTables &T, const mx_photons *ph, uint32_t stages, const double *U,
+                    const double *N, uint64_t seed, cudaStream_t st, bool fresh) {
   if (!ph) return fail(c, MX_EINVAL, "mx_trace: null photon list");
   if (ph->n == 0) return MX_OK;
   if (!ph->energy || !ph->p) return fail(c, MX_EINVAL, "mx_trace: energy and p are required");
   if ((U == nullptr) != (N == nullptr)) return fail(c, MX_EINVAL, "mx_trace: give both U and N or neither");
-  if ((stages & MX_STAGE_DETECT) && c->T.nchips && (!ph->x)) return fail(c, MX_EINVAL, "mx_trace: x is required");
+  if ((stages & MX_STAGE_DETECT) && T.nchips && (!ph->x)) return fail(c, MX_EINVAL, "mx_trace: x is required");
   if (ph->n == 0) return MX_OK;
   TraceIO io;
   io.energy = ph->energy; io.x = ph->x; io.p = ph->p; io.t = ph->arrival_time; io.flags = ph->flags;
   io.tag = ph->tag; io.shell = ph->mirror_shell; io.order = ph->order; io.ccd = ph->ccd_num;
   io.ypix = ph->y_pixel; io.zpix = ph->z_pixel; io.dith = ph->dither_state;
   io.U = U; io.N = N; io.n = ph->n; io.seed = seed; io.stages = stages; io.fresh = fresh ? 1 : 0;
+  io.stride = ph->stride ? ph->stride : ph->n;
+  if (io.stride < io.n) return fail(c, MX_EINVAL, "mx_trace: stride below n");
   io.overrun = c->d_overrun;
   int slots = U != nullptr;
   bool wave = (stages & MX_STAGE_MIRROR) &&
@@ -237,10 +207,10 @@ static int trace_device(mx_context *c, const mx_photons *ph, uint32_t stages, co
     w.q1 = (MxRec *) c->wave.ptr;
     w.q2 = (MxRec *) ((char *) c->wave.ptr + qbytes);
     w.counts = (unsigned int *) ((char *) c->wave.ptr + 2 * qbytes);
-    e = launch_wavefront(c->T, io, w, c->num_sms * c->wave_blocks, (int) c->shared_bytes, st);
+    e = launch_wavefront(T, io, w, c->num_sms * c->wave_blocks, (int) c->shared_bytes, st);
     c->launches += 3;
   } else {
-    e = launch_trace(c->T, io, c->num_sms * c->trace_blocks[slots ? 0 : 1], (int) c->shared_bytes, slots != 0, st);
+    e = launch_trace(T, io, c->num_sms * c->trace_blocks[slots ? 0 : 1], (int) c->shared_bytes, slots != 0, st);
     c->launches++;
   }
   if (e != cudaSuccess) return cuda_fail(c, e, "launching the trace kernels");
@@ -250,8 +220,8 @@ static int trace_device(mx_context *c, const mx_photons *ph, uint32_t stages, co
 int mx_trace(mx_context *c, const mx_photons *ph, uint32_t stages, const mx_variates *var, uint64_t seed,
              void *stream) {
   if (!c) return MX_EINVAL;
-  return trace_device(c, ph, stages, var ? var->U : nullptr, var ? var->N : nullptr, seed,
-                      (cudaStream_t) stream, false);
+  return mx_trace_tables(c, c->T, ph, stages, var ? var->U : nullptr, var ? var->N : nullptr, seed,
+                         (cudaStream_t) stream, false);
 }
 
 int mx_trace_host(mx_context *c, const mx_photons *h, uint32_t stages, const mx_variates *hv, uint64_t seed) {
@@ -260,6 +230,7 @@ int mx_trace_host(mx_context *c, const mx_photons *h, uint32_t stages, const mx_
   size_t n = h->n;
   if (n == 0) return MX_OK;
   if (!h->energy || !h->p) return fail(c, MX_EINVAL, "mx_trace_host: energy and p are required");
+  if (h->stride && h->stride != h->n) return fail(c, MX_EINVAL, "mx_trace_host: host lists must be contiguous (stride 0 or n)");
   struct Col { const void *host; size_t elem; int comps; bool in, out; };
   const Col cols[12] = {
       {h->energy, 8, 1, true, false},     {h->x, 8, 3, false, true},         {h->p, 8, 3, true, true},
@@ -293,7 +264,7 @@ int mx_trace_host(mx_context *c, const mx_photons *h, uint32_t stages, const mx_
   d.arrival_time = (double *) dev[3]; d.flags = (uint32_t *) dev[4]; d.tag = (uint32_t *) dev[5];
   d.mirror_shell = (int8_t *) dev[6]; d.order = (int8_t *) dev[7]; d.ccd_num = (int8_t *) dev[8];
   d.y_pixel = (float *) dev[9]; d.z_pixel = (float *) dev[10]; d.dither_state = (float *) dev[11];
-  int r = trace_device(c, &d, stages, dU, dN, seed, st, true);
+  int r = mx_trace_tables(c, c->T, &d, stages, dU, dN, seed, st, true);
   if (r) return r;
   for (int k = 0; k < 12; k++) {
     if (!cols[k].host || !cols[k].out) continue;

@@ -1,0 +1,56 @@
+// The context object behind the C ABI's opaque mx_context, shared by the
+// translation units that implement the ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "mx_host.h"
+#include "mx_kernels.cuh"
+
+struct DevBuf {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t need) {
+    if (need <= bytes) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr; bytes = 0;
+    cudaError_t e = cudaMalloc(&ptr, need);
+    if (e == cudaSuccess) bytes = need;
+    return e;
+  }
+  void release() { if (ptr) cudaFree(ptr); ptr = nullptr; bytes = 0; }
+};
+
+struct mx_context {
+  int device = 0;
+  int num_sms = 0;
+  std::string err;
+  mx_config cfg;
+  mx::Pack pack;
+  mx::HostModel hm;
+  MxTables T;              // launch copy with device pointers
+  DevBuf tables;           // every table in one allocation
+  size_t shared_bytes = 0;
+  int trace_blocks[2] = {0, 0};   // resident blocks per SM for the slot / Philox kernels
+  cudaStream_t stream = nullptr;
+  DevBuf io[14];           // staging for mx_trace_host
+  DevBuf scan;             // compaction block counts
+  DevBuf wave;             // wavefront record queues
+  int wave_blocks = 0;     // resident blocks per SM for the wavefront kernels
+  int mode = MX_MODE_AUTO;
+  unsigned long long *d_overrun = nullptr;
+  unsigned long long launches = 0;
+};
+
+// Record an error on the context (or as the creation error when c is null)
+// and return code.
+int mx_fail(mx_context *c, int code, const std::string &msg);
+int mx_cuda_fail(mx_context *c, cudaError_t e, const char *what);
+extern thread_local std::string g_create_err;
+
+// mx_trace with an explicit copy of the launch tables (a batch traces each
+// source with its own grating and detector choice).  fresh: the output
+// columns start from their defaults instead of being read.
+extern "C" __attribute__((visibility("hidden"))) int mx_trace_tables(mx_context *c, const MxTables &T, const mx_photons *ph, uint32_t stages,
+                               const double *U, const double *N, uint64_t seed, cudaStream_t st, bool fresh);

@@ -226,6 +226,15 @@ MXD double philox_normal(uint64_t seed, uint32_t tag, uint32_t k) {
   return (double) FMUL(r, series_cos2pi(u2));
 }
 
+// Source-level draws (photon generation) use their own Philox domain, so
+// they never coincide with a stage's slots: draw k of photon `tag`.
+MXD double source_uniform(uint64_t seed, uint32_t tag, uint32_t k) {
+  uint32_t c[4] = {tag, k, 0x5A5A0003u, 0u};
+  philox(c, (uint32_t) seed, (uint32_t) (seed >> 32));
+  uint64_t b = ((uint64_t) c[0] << 32) | c[1];
+  return (double) (b >> 11) * (1.0 / 9007199254740992.0);
+}
+
 // Variate source for one photon: fixed per-stage slot windows.
 struct Rng {
   const double *U, *N;   // slot-major pre-drawn arrays, or null for Philox

@@ -3,34 +3,22 @@
 
 #include "mx_device.cuh"
 #include "mx_kernels.cuh"
+#include "mx_wave.cuh"
 
 using namespace mx;
-
-__host__ __device__ static inline size_t align16(size_t x) { return (x + 15) & ~(size_t) 15; }
 
 // Shared-memory staging per block: shell geometry, gratings, chips, then
 // the optical-constant and correction-factor tables (the per-photon binary
 // searches run on these).
-size_t trace_shared_bytes(const MxTables &T) {
-  return align16(4 * sizeof(MxShellDev)) + align16(4 * sizeof(MxGratingDev)) +
-         align16(MX_MAX_CHIPS * sizeof(MxChipDev)) + align16((size_t) T.optc_len * sizeof(float)) +
-         align16((size_t) T.slope_len * sizeof(double));
-}
-
-__device__ __forceinline__ void copy_words(uint32_t *dst, const uint32_t *src, size_t words) {
-  for (size_t k = threadIdx.x; k < words; k += blockDim.x) dst[k] = __ldg(src + k);
-}
+size_t trace_shared_bytes(const MxTables &T) { return tables_shared_bytes(T); }
 
 // Fused dither -> mirror -> grating -> detector trace, one photon per
 // thread, grid-stride over the photon list with a resident grid.
-__device__ __forceinline__ void stage_tables(const MxTables &T, MxShellDev *&sh, MxGratingDev *&gr, MxChipDev *&ch,
-                                             float *&optc, double *&slope);
-
 __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_trace_kernel(MxTables T, TraceIO io) {
   MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
   stage_tables(T, sh, gr, ch, optc, slope);
 
-  const size_t n = io.n;
+  const size_t n = io.stride;   // component stride of the 3-vector columns
   const uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < io.n; i += stride) {
     Ph q;
@@ -83,73 +71,10 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_trace_kernel(MxTables T, Tr
 // Appends are warp-aggregated (one atomic per warp); the order of records
 // in a queue does not affect any photon's result.
 
-// Shared-memory layout: shells | gratings | chips | optical-constant and
-// correction tables (float) | their interval slopes (double).
-__device__ __forceinline__ void stage_tables(const MxTables &T, MxShellDev *&sh, MxGratingDev *&gr, MxChipDev *&ch,
-                                             float *&optc, double *&slope) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  size_t o_gr = align16(4 * sizeof(MxShellDev));
-  size_t o_ch = o_gr + align16(4 * sizeof(MxGratingDev));
-  size_t o_op = o_ch + align16(MX_MAX_CHIPS * sizeof(MxChipDev));
-  size_t o_sl = o_op + align16((size_t) T.optc_len * sizeof(float));
-  sh = (MxShellDev *) smem;
-  gr = (MxGratingDev *) (smem + o_gr);
-  ch = (MxChipDev *) (smem + o_ch);
-  optc = (float *) (smem + o_op);
-  slope = (double *) (smem + o_sl);
-  copy_words((uint32_t *) slope, (const uint32_t *) T.optc_slope, (size_t) T.slope_len * 2);
-  copy_words((uint32_t *) sh, (const uint32_t *) T.shells, 4 * sizeof(MxShellDev) / 4);
-  copy_words((uint32_t *) gr, (const uint32_t *) T.gratings, 4 * sizeof(MxGratingDev) / 4);
-  copy_words((uint32_t *) ch, (const uint32_t *) T.chips, MX_MAX_CHIPS * sizeof(MxChipDev) / 4);
-  copy_words((uint32_t *) optc, (const uint32_t *) T.optc, (size_t) T.optc_len);
-  __syncthreads();
-}
-
-__device__ __forceinline__ void append(bool keep, const MxRec &r, MxRec *q, unsigned int *cnt) {
-  const unsigned lane = threadIdx.x & 31;
-  unsigned mask = __ballot_sync(0xffffffffu, keep);
-  if (mask == 0) return;
-  int leader = __ffs(mask) - 1;
-  unsigned base = 0;
-  if ((int) lane == leader) base = atomicAdd(cnt, (unsigned) __popc(mask));
-  base = __shfl_sync(0xffffffffu, base, leader);
-  if (keep) q[base + __popc(mask & ((1u << lane) - 1u))] = r;
-}
-
-__device__ __forceinline__ void to_rec(MxRec &r, const Ph &q, const MirrorState &m, const Rng &rng, uint32_t i) {
-  r.x[0] = m.x.x; r.x[1] = m.x.y; r.x[2] = m.x.z;
-  r.p[0] = m.p.x; r.p[1] = m.p.y; r.p[2] = m.p.z;
-  r.n[0] = m.n.x; r.n[1] = m.n.y; r.n[2] = m.n.z;
-  r.e = q.e; r.t = q.t; r.corr = m.corr; r.beta = m.beta; r.delta = m.delta;
-  r.i = i; r.tag = rng.tag; r.flags = q.flags;
-  r.shell = (uint8_t) q.shell; r.upos = (uint8_t) rng.upos; r.npos = (uint8_t) rng.npos; r.pad0 = 0;
-}
-
-__device__ __forceinline__ void from_rec(const MxRec &r, Ph &q, MirrorState &m, Rng &rng, const TraceIO &io) {
-  m.x = mk(r.x[0], r.x[1], r.x[2]); m.p = mk(r.p[0], r.p[1], r.p[2]); m.n = mk(r.n[0], r.n[1], r.n[2]);
-  m.corr = r.corr; m.beta = r.beta; m.delta = r.delta;
-  q.e = r.e; q.t = r.t; q.flags = r.flags; q.shell = r.shell;
-  q.x = m.x; q.p = m.p;
-  rng.U = io.U; rng.N = io.N; rng.seed = io.seed; rng.n = io.n; rng.i = r.i; rng.tag = r.tag;
-  rng.upos = r.upos; rng.uend = MX_U_MIRROR + 12; rng.npos = r.npos; rng.nend = MX_N_MIRROR + 2;
-  rng.overrun = false;
-}
-
-// x, p, flags and shell of a photon whose trace ends in this phase.
-__device__ __forceinline__ void store_core(const TraceIO &io, uint32_t i, const Ph &q, bool overrun) {
-  const size_t n = io.n;
-  uint32_t f = q.flags;
-  if (overrun) { f |= MX_PHOTON_VARIATE_OVERRUN; atomicAdd(io.overrun, 1ull); }
-  if (io.x) { io.x[i] = q.x.x; io.x[n + i] = q.x.y; io.x[2 * n + i] = q.x.z; }
-  io.p[i] = q.p.x; io.p[n + i] = q.p.y; io.p[2 * n + i] = q.p.z;
-  if (io.flags) io.flags[i] = f;
-  if (io.shell) io.shell[i] = (int8_t) q.shell;
-}
-
 __global__ void __launch_bounds__(MX_TRACE_BLOCK, 3) mx_wave_a(MxTables T, TraceIO io, WaveBufs w) {
   MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
   stage_tables(T, sh, gr, ch, optc, slope);
-  const size_t n = io.n;
+  const size_t n = io.stride;   // component stride of the 3-vector columns
   const uint32_t lane = threadIdx.x & 31, warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t base = warp * 32; base < io.n; base += nwarps * 32) {

@@ -29,7 +29,7 @@ NUM_U, NUM_N = 16, 8
 
 class MxPhotons(C.Structure):
     _fields_ = [
-        ("n", C.c_uint32), ("reserved", C.c_uint32),
+        ("n", C.c_uint32), ("stride", C.c_uint32),
         ("energy", C.c_void_p), ("x", C.c_void_p), ("p", C.c_void_p),
         ("arrival_time", C.c_void_p), ("flags", C.c_void_p), ("tag", C.c_void_p),
         ("mirror_shell", C.c_void_p), ("order", C.c_void_p), ("ccd_num", C.c_void_p),

@@ -57,6 +57,8 @@ class Oracle:
         L.mxo_philox_uniform.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32]
         L.mxo_philox_normal.restype = C.c_double
         L.mxo_philox_normal.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32]
+        L.mxo_source_uniform.restype = C.c_double
+        L.mxo_source_uniform.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32]
         if pack is None:
             from marx_gb300.caldb.pack import DEFAULT_PACK
             pack = DEFAULT_PACK
@@ -93,6 +95,9 @@ class Oracle:
 
     def philox_normal(self, seed, tag, slot):
         return self.lib.mxo_philox_normal(seed, tag, slot)
+
+    def source_uniform(self, seed, tag, k=0):
+        return self.lib.mxo_source_uniform(seed, tag, k)
 
 
 class Reference:

@@ -292,7 +292,7 @@ void mxo_destroy(mxo_model *m) { delete m; }
 const char *mxo_last_error(void) { return g_err.c_str(); }
 
 static void load_photon(const mx_photons *ph, uint32_t i, Photon &q) {
-  uint32_t n = ph->n;
+  uint32_t n = ph->stride ? ph->stride : ph->n;
   q.energy = ph->energy[i];
   q.t = ph->arrival_time ? ph->arrival_time[i] : 0.0;
   q.x = ph->x ? V3<double>{ph->x[i], ph->x[n + i], ph->x[2 * n + i]} : V3<double>{0, 0, 0};
@@ -306,7 +306,7 @@ static void load_photon(const mx_photons *ph, uint32_t i, Photon &q) {
   for (int k = 0; k < 3; k++) q.dith[k] = ph->dither_state ? ph->dither_state[k * n + i] : 0.f;
 }
 static void store_photon(const mx_photons *ph, uint32_t i, const Photon &q) {
-  uint32_t n = ph->n;
+  uint32_t n = ph->stride ? ph->stride : ph->n;
   if (ph->x) { ph->x[i] = q.x.x; ph->x[n + i] = q.x.y; ph->x[2 * n + i] = q.x.z; }
   ph->p[i] = q.p.x; ph->p[n + i] = q.p.y; ph->p[2 * n + i] = q.p.z;
   if (ph->flags) ph->flags[i] = q.flags;
@@ -382,5 +382,6 @@ int mxo_detector_geometry(const mxo_model *m, double *out, int max_chips) {
 
 double mxo_philox_uniform(uint64_t seed, uint32_t tag, uint32_t slot) { return philox_uniform(seed, tag, slot); }
 double mxo_philox_normal(uint64_t seed, uint32_t tag, uint32_t slot) { return philox_normal(seed, tag, slot); }
+double mxo_source_uniform(uint64_t seed, uint32_t tag, uint32_t k) { return source_uniform(seed, tag, k); }
 
 }  // extern "C"

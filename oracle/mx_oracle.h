@@ -43,6 +43,8 @@ int mxo_detector_geometry(const mxo_model *m, double *out, int max_chips);
 /* Philox variates as the engine defines them, for tests. */
 double mxo_philox_uniform(uint64_t seed, uint32_t tag, uint32_t slot);
 double mxo_philox_normal(uint64_t seed, uint32_t tag, uint32_t slot);
+/* Photon-generation draw k of photon `tag` (energies of point sources). */
+double mxo_source_uniform(uint64_t seed, uint32_t tag, uint32_t k);
 
 #ifdef __cplusplus
 }

@@ -109,6 +109,14 @@ inline double philox_normal(uint64_t seed, uint32_t tag, uint32_t k) {
   return (double) (r * series_cos2pi(u2));
 }
 
+// Source-level draw k of photon `tag` (photon generation), its own domain.
+inline double source_uniform(uint64_t seed, uint32_t tag, uint32_t k) {
+  uint32_t c[4] = {tag, k, 0x5A5A0003u, 0u};
+  philox4x32_10(c, (uint32_t) seed, (uint32_t) (seed >> 32));
+  uint64_t b = ((uint64_t) c[0] << 32) | c[1];
+  return (double) (b >> 11) * (1.0 / 9007199254740992.0);
+}
+
 struct Variates {
   // pre-drawn slot arrays (slot-major) or Philox
   const double *U = nullptr, *N = nullptr;
