@@ -43,7 +43,7 @@ struct BatchIO {
 // point_create_photons (s-point.c:59) with flat_energy (spectrum.c:138)
 // for one photon of a source.
 __device__ __forceinline__ void generate_photon(const MxSourceDev &S, uint64_t seed, uint32_t tag, Ph &q) {
-  q.e = S.emin + S.de * source_uniform(seed, tag, 0);
+  q.e = MX_DADD(S.emin, MX_DMUL(S.de, source_uniform(seed, tag, 0)));   // rounded as written, no contraction
   q.t = 0.0;
   q.p = mk(S.p[0], S.p[1], S.p[2]);
   q.x = mk(0.0, 0.0, 0.0);
