@@ -5,6 +5,7 @@
 
 #include <string>
 
+#include "../../include/marx_gb300.h"
 #include "mx_host.h"
 #include "mx_kernels.cuh"
 
