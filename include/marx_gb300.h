@@ -192,6 +192,26 @@ int mx_trace(mx_context *ctx, const mx_photons *ph, uint32_t stages,
 #define MX_WAVEFRONT_MIN_PHOTONS 65536
 int mx_set_trace_mode(mx_context *ctx, int mode);
 
+/* The wavefront trace of mx_trace with its survivor queues in a device
+ * array built into the library instead of memory the context allocates, so
+ * the call allocates nothing: for callers that cannot allocate device
+ * memory while they trace, such as a host whose GPU memory is all reserved
+ * by another allocator, or a latency-critical loop that must stay out of
+ * the CUDA allocator (cudaMalloc and cudaFree may synchronise the device).
+ * No counterpart in the reference (MARX allocates its photon arrays on the
+ * host per batch).
+ *   - at most MX_STATIC_MAX_PHOTONS photons per call (MX_ERANGE beyond);
+ *     the array (2 x 128 bytes per photon, 32 MiB) is held by every GPU
+ *     that loads the library until the process exits;
+ *   - stages must include MX_STAGE_MIRROR; pointers as for mx_trace;
+ *   - the first call on a device looks up the array's address there, with
+ *     that device current; make that first call before any stream capture;
+ *   - every call shares the one array: calls that overlap on the GPU (other
+ *     streams or threads) race on it, so serialise them. */
+#define MX_STATIC_MAX_PHOTONS 131072
+int mx_trace_static(mx_context *ctx, const mx_photons *ph, uint32_t stages, const mx_variates *var,
+                    uint64_t seed, void *stream);
+
 /* Same trace on HOST buffers: copies inputs to the device, traces and
  * copies results back; blocks until done. */
 int mx_trace_host(mx_context *ctx, const mx_photons *host, uint32_t stages,
