@@ -271,6 +271,79 @@ int  mx_batch_photons(mx_batch *b, mx_photons *dev_view, const uint32_t **source
 uint64_t mx_batch_total_photons(const mx_batch *b);
 void mx_batch_destroy(mx_batch *b);
 
+/* ----------------------------------------------- differentiable form --
+ * Weighted rays: each ray takes the aperture point the mirror stage would
+ * give a photon of the same tag (project_photon_to_hrma, hrma.c:984-1050)
+ * and the HRMA geometry of the trace, without normal blur or scattering,
+ * to the focal plane x = 0.  Instead of random absorption it carries a
+ * weight: HRMAVig times, at each reflection, the Fresnel reflectivity
+ * (reflect.c:39-77) times the shell's effective-area correction (1 with
+ * HRMA_Ideal).  The image is the weighted rays splatted with a normalised
+ * Gaussian of sigma pixels, truncated at 5 pixels, divided by n_rays.
+ * No counterpart in the reference; its parameters are the ones the
+ * reference reads from HRMA_Geometry_File (read_hrma_geometry_file,
+ * hrma.c:319-391) and the source direction.
+ *
+ * theta[MX_DIFF_NPARAM] perturbs the configured model:
+ *   theta[4 s + 0]  shell s az_mis   (arcsec, added to P and H rows)
+ *   theta[4 s + 1]  shell s el_mis   (arcsec, added to P and H rows)
+ *   theta[4 s + 2]  shell s x0       (micrometres, added to P and H rows)
+ *   theta[4 s + 3]  shell s y0       (micrometres, added to P and H rows)
+ *   theta[16], theta[17]  source offset in y and z (arcsec)
+ * with shells s = 0..3 in the order 1, 3, 4, 6.  The source direction is
+ * unit(-1, -tan(ay), -tan(az)), ay = src_y + theta[16] and
+ * az = src_z + theta[17] in arcsec.
+ *
+ * Which root each conic gives, whether the ray hits both optics and
+ * whether a strut blocks it are discrete.  MX_DIFF_RECORD decides them
+ * afresh and keeps them per ray; MX_DIFF_REPLAY follows the kept decisions
+ * (without the x-limit and strut tests), so the image is smooth in theta;
+ * MX_DIFF_FRESH decides afresh without keeping them.  The adjoint
+ * differentiates the replayed function at theta and needs a recorded set. */
+#define MX_DIFF_NPARAM 18
+#define MX_DIFF_RECORD 0
+#define MX_DIFF_REPLAY 1
+#define MX_DIFF_FRESH  2
+#define MX_DIFF_MAX_RAYS 4294967295ull
+
+typedef struct mx_diff_config {
+  uint64_t n_rays;          /* rays per evaluation, tags 0 .. n_rays-1 */
+  uint64_t seed;            /* Philox key of the aperture points */
+  double energy;            /* keV, every ray */
+  double src_y, src_z;      /* source direction before theta[16..17], arcsec */
+  double center_y, center_z;/* focal-plane position of the image centre, mm */
+  double pitch;             /* pixel size, mm */
+  double sigma;             /* splat width in pixels, 0.5 .. 1 */
+  uint32_t nx, ny;          /* image columns (focal-plane y) and rows (z), 16 .. 4096 */
+} mx_diff_config;
+
+typedef struct mx_diff mx_diff;
+
+/* Weighted rays over the context's mirror model (its MirrorType must be
+ * HRMA with a source at infinity).  NULL on error (mx_last_error(ctx)). */
+mx_diff *mx_diff_create(mx_context *ctx, const mx_diff_config *cfg);
+/* The image at theta into image (device, ny x nx doubles, row-major,
+ * row = z).  moments (host, may be NULL) receives sum w, sum w y,
+ * sum w z and the number of rays reaching the focal plane; with moments
+ * the call waits for the stream. */
+int mx_diff_forward(mx_diff *d, const double *theta, int mode, double *image, double *moments, void *stream);
+/* Per-ray focal-plane y, z (mm) and weight w into yzw (device, 3 x n_rays,
+ * column-major: y[0..n), z[0..n), w[0..n)); lost rays get w = 0. */
+int mx_diff_rays(mx_diff *d, const double *theta, int mode, double *yzw, void *stream);
+/* Mean squared difference of two images (device) into *loss (device) and,
+ * when dl_dimage is not NULL, its gradient 2 (image - target) / (nx ny). */
+int mx_diff_mse(mx_diff *d, const double *image, const double *target, double *dl_dimage, double *loss,
+                void *stream);
+/* The adjoint: grad (host, MX_DIFF_NPARAM) = sum over pixels of
+ * dl_dimage (device) times d image / d theta at theta, through the
+ * decisions of the last MX_DIFF_RECORD call.  Waits for the stream. */
+int mx_diff_adjoint(mx_diff *d, const double *theta, const double *dl_dimage, double *grad, void *stream);
+/* Device-side form of mx_diff_adjoint: grad_dev is a device array of
+ * MX_DIFF_NPARAM doubles; does not wait. */
+int mx_diff_adjoint_async(mx_diff *d, const double *theta, const double *dl_dimage, double *grad_dev,
+                          void *stream);
+void mx_diff_destroy(mx_diff *d);
+
 /* Survivor compaction (marx_prune_photons, photon.c:40): writes the indices
  * of photons without MX_BAD_PHOTON_MASK bits to idx_out (device, n entries)
  * in ascending order and their count to *count_out (host). */

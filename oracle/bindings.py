@@ -59,6 +59,10 @@ class Oracle:
         L.mxo_philox_normal.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32]
         L.mxo_source_uniform.restype = C.c_double
         L.mxo_source_uniform.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32]
+        from marx_gb300.diff import MxDiffConfig
+        L.mxo_splat_exp.restype = C.c_float
+        L.mxo_splat_exp.argtypes = [C.c_float]
+        L.mxo_weighted.argtypes = [C.c_void_p, C.POINTER(MxDiffConfig), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         if pack is None:
             from marx_gb300.caldb.pack import DEFAULT_PACK
             pack = DEFAULT_PACK
@@ -99,12 +103,26 @@ class Oracle:
     def source_uniform(self, seed, tag, k=0):
         return self.lib.mxo_source_uniform(seed, tag, k)
 
+    def splat_exp(self, x: float) -> float:
+        return self.lib.mxo_splat_exp(x)
+
+    def weighted(self, dcfg, theta, rays: bool = True, image: bool = True, threads: int = 0):
+        """Weighted rays of the differentiable form at theta (decisions made
+        afresh): (yzw (3, n) or None, image (ny, nx) or None)."""
+        th = np.ascontiguousarray(theta, dtype=np.float64)
+        yzw = np.zeros((3, dcfg.n_rays)) if rays else None
+        img = np.zeros((dcfg.ny, dcfg.nx)) if image else None
+        r = self.lib.mxo_weighted(self.h, C.byref(dcfg), _p(th), _p(yzw), _p(img), threads)
+        if r != 0:
+            raise RuntimeError(f"oracle weighted rays failed: {r}")
+        return yzw, img
+
 
 class Reference:
     """The reference MARX library compiled from its own sources (only in a
     checkout that has them).  ``native=True`` keeps its own generator."""
 
-    def __init__(self, cfg: MxConfig, native: bool = False, seed: int = 1):
+    def __init__(self, cfg: MxConfig, native: bool = False, seed: int = 1, datadir: str | None = None):
         so = REF_NATIVE_SO if native else REF_SLOTS_SO
         if not os.path.exists(so):
             if not build_reference():
@@ -118,7 +136,7 @@ class Reference:
         names = (C.c_char_p * len(par))(*[k.encode() for k in par])
         vals = (C.c_char_p * len(par))(*[v.encode() for v in par.values()])
         parfile = os.path.join(REF_ROOT, "marx", "par", "marx.par").encode()
-        datadir = os.path.join(REF_ROOT, "marx", "data").encode()
+        datadir = (datadir or os.path.join(REF_ROOT, "marx", "data")).encode()
         if native:
             L.mxref_seed(C.c_ulong(seed))
         r = L.mxref_setup(parfile, datadir, len(par), names, vals)

@@ -84,6 +84,27 @@ static void mmul(M3<double> &c, const M3<double> &a, const M3<double> &b) {  // 
     for (int j = 0; j < 3; j++) c.m[i][j] = a.m[i][0] * b.m[0][j] + a.m[i][1] * b.m[1][j] + a.m[i][2] * b.m[2][j];
 }
 
+// The shell's MARX -> optic translations (get_shell_geometry) and its
+// pitch/yaw rotations (init_yaw_pitch) from its geometry-file rows.
+static void shell_frames(Shell &h, double cap_pos) {
+  for (int o2 = 0; o2 < 2; o2++) {
+    double x0 = h.osac[o2][0], y0 = h.osac[o2][1], z0 = h.osac[o2][2];
+    h.to_osac[o2].x = -(-z0); h.to_osac[o2].y = (-x0); h.to_osac[o2].z = -(-y0);
+    h.to_osac[o2].x -= cap_pos;
+  }
+  for (int o2 = 0; o2 < 2; o2++) {
+    double el = -h.osac[o2][7] * (PI / 180.0), az = -h.osac[o2][6] * (PI / 180);
+    M3<double> rz, ry;
+    rot_z_matrix(rz, -az);
+    V3<double> ny = mvmul(rz, V3<double>{0, 1, 0});
+    rot_matrix(ry, ny, -el);
+    mmul(h.fwd[o2], ry, rz);
+    rot_matrix(ry, ny, el);
+    rot_z_matrix(rz, az);
+    mmul(h.bwd[o2], rz, ry);
+  }
+}
+
 static bool setup(mxo_model *o, const mx_config *cfg) {
   Model &M = o->M;
   M.cfg = *cfg;
@@ -108,13 +129,12 @@ static bool setup(mxo_model *o, const mx_config *cfg) {
     // get_shell_geometry
     double cap_pos = M.cap + h.xoffset;
     for (int o2 = 0; o2 < 2; o2++) {
-      double x0 = h.osac[o2][0], y0 = h.osac[o2][1], z0 = h.osac[o2][2], pp = h.osac[o2][3], kk = h.osac[o2][4];
+      double pp = h.osac[o2][3], kk = h.osac[o2][4];
       double r = h.osac[o2][5], len = h.osac[o2][8];
       h.c[o2] = r * r; h.b[o2] = -2.0 * kk; h.a[o2] = 1.0 - pp;
       h.xmin[o2] = -0.5 * len; h.xmax[o2] = 0.5 * len;
-      h.to_osac[o2].x = -(-z0); h.to_osac[o2].y = (-x0); h.to_osac[o2].z = -(-y0);
-      h.to_osac[o2].x -= cap_pos;
     }
+    shell_frames(h, cap_pos);
     h.front_position = cap_pos - h.osac[0][2] + h.xmax[0];
     // init_hrma_shells
     auto radius = [](double a, double b, double c, double x) { return sqrt(c + x * (b + x * (a - 1))); };
@@ -126,18 +146,6 @@ static bool setup(mxo_model *o, const mx_config *cfg) {
     if (h.num_open)
       total_area += (h.num_open / 4.0) * (h.max_radius - h.min_radius) * (h.max_radius + h.min_radius);
     h.area_fraction = total_area;
-    // init_yaw_pitch
-    for (int o2 = 0; o2 < 2; o2++) {
-      double el = -h.osac[o2][7] * (PI / 180.0), az = -h.osac[o2][6] * (PI / 180);
-      M3<double> rz, ry;
-      rot_z_matrix(rz, -az);
-      V3<double> ny = mvmul(rz, V3<double>{0, 1, 0});
-      rot_matrix(ry, ny, -el);
-      mmul(h.fwd[o2], ry, rz);
-      rot_matrix(ry, ny, el);
-      rot_z_matrix(rz, az);
-      mmul(h.bwd[o2], rz, ry);
-    }
     // correction factors and WFold tables
     size_t cnt = 0;
     const float *corr = sec<float>(o, "hrma/corr" + std::to_string(ids[i]), &cnt);
@@ -385,3 +393,156 @@ double mxo_philox_normal(uint64_t seed, uint32_t tag, uint32_t slot) { return ph
 double mxo_source_uniform(uint64_t seed, uint32_t tag, uint32_t k) { return source_uniform(seed, tag, k); }
 
 }  // extern "C"
+
+// ------------------------------------------------- weighted rays (oracle) --
+// CPU restatement of the differentiable form's forward pass: the mirror
+// stage of mirror_photon above on the aperture point of each ray's tag,
+// with the shell geometry perturbed as the geometry file would carry it,
+// no normal blur or scattering, reflectivity times correction as a weight
+// instead of the random absorption test, then the focal plane x = 0 and
+// the engine's fixed-point Gaussian splat.
+
+// exp(-x), x >= 0: Cody-Waite reduction and the Taylor series of exp(-r)
+// to r^7, each operation rounded to single precision in the engine's order.
+static float exp_neg_f(float x) {
+  if (!(x < 80.0f)) return 0.0f;
+  const int n = (int) (x * 1.44269502f + 0.5f);
+  const float fn = (float) n;
+  const float r = (x - fn * 0.693145752f) - fn * 1.42860677e-06f;
+  const float s = -r;
+  float p = 1.0f + s * (1.0f / 7.0f);
+  p = 1.0f + (s * (1.0f / 6.0f)) * p;
+  p = 1.0f + (s * 0.2f) * p;
+  p = 1.0f + (s * 0.25f) * p;
+  p = 1.0f + (s * (1.0f / 3.0f)) * p;
+  p = 1.0f + (s * 0.5f) * p;
+  p = 1.0f + s * p;
+  uint32_t b = (uint32_t) (127 - n) << 23;
+  float scale;
+  memcpy(&scale, &b, 4);
+  return p * scale;
+}
+
+static bool weighted_ray(const Model &M, uint64_t seed, uint32_t tag, const V3<double> &p0, double energy,
+                         double &y, double &z, double &w) {
+  Variates v;
+  v.seed = seed; v.tag = tag;
+  v.window(MX_U_MIRROR, 12, MX_N_MIRROR, 2);
+  double wt = 1.0;
+  if (!M.ideal) { v.uniform(); wt = M.cfg.hrma_vig; }
+  Photon ph{};
+  V3<double> x{0.0, 0.0, 0.0}, p = p0;
+  project_photon_to_hrma<double>(M, ph, x, p, v);
+  if (v.overrun || (ph.flags & MX_PHOTON_MIRROR_VBLOCKED)) return false;
+  const Shell &h = M.sh[ph.shell];
+  double beta = 0.0, delta = 1.0, corr = 1.0;
+  if (M.opt_n) {
+    beta = (double) interpolate_f<double>((float) energy, M.opt_e, M.opt_beta, M.opt_n);
+    delta = (double) interpolate_f<double>((float) energy, M.opt_e, M.opt_delta, M.opt_n);
+    if (M.use_scale) corr = sqrt((double) interpolate_f<double>((float) energy, h.corr_e, h.corr_f, h.corr_n));
+  }
+  uint32_t flags = 0;
+  for (int o = 0; o < 2; o++) {
+    x = vsum(x, h.to_osac[o]);
+    x = mvmul(h.fwd[o], x);
+    p = mvmul(h.fwd[o], p);
+    V3<double> n;
+    if (-1 == conic_intersection(h.a[o], h.b[o], h.c[o], x, p, n, h.xmin[o], h.xmax[o])) return false;
+    double pdn = dot(p, n);
+    if (!M.ideal) wt *= reflectivity(fabs(pdn), beta, delta) * corr;
+    p = ax1_bx2(1.0, p, -2.0 * pdn, n);
+    p = mvmul(h.bwd[o], p);
+    x = mvmul(h.bwd[o], x);
+    x = vdiff(x, h.to_osac[o]);
+    if (M.use_struts && intersects_struts(M, x, p, flags, o == 0 ? CAP_STRUTS : POST_STRUTS)) return false;
+  }
+  double t = -x.x / p.x;
+  y = x.y + t * p.y;
+  z = x.z + t * p.z;
+  w = wt;
+  return true;
+}
+
+extern "C" float mxo_splat_exp(float x) { return exp_neg_f(x); }
+
+extern "C" int mxo_weighted(const mxo_model *m, const mx_diff_config *cfg, const double *theta, double *yzw,
+                            double *image, int nthreads) {
+  if (!m || !cfg || !theta || cfg->n_rays < 1 || cfg->n_rays > 0xffffffffull) return MX_EINVAL;
+  Model M = m->M;
+  for (int s = 0; s < 4; s++) {
+    Shell &h = M.sh[s];
+    for (int o = 0; o < 2; o++) {
+      h.osac[o][0] += theta[4 * s + 2] * 1e-3;
+      h.osac[o][1] += theta[4 * s + 3] * 1e-3;
+      h.osac[o][6] += theta[4 * s] / 3600.0;
+      h.osac[o][7] += theta[4 * s + 1] / 3600.0;
+    }
+    shell_frames(h, M.cap + h.xoffset);
+  }
+  const double arcsec = PI / (180.0 * 3600.0);
+  V3<double> p0{-1.0, -tan((cfg->src_y + theta[16]) * arcsec), -tan((cfg->src_z + theta[17]) * arcsec)};
+  normalize(p0);
+  const uint64_t n = cfg->n_rays;
+  const int nx = (int) cfg->nx, ny = (int) cfg->ny;
+  const float knorm = (float) (1.0 / (std::sqrt(2.0 * PI) * cfg->sigma));
+  const float half_inv_s2 = (float) (0.5 / (cfg->sigma * cfg->sigma));
+  const double kmax = knorm;
+  int shift = (int) std::ceil(std::log2((double) n * kmax * kmax / 4.0)) + 1;
+  if (shift < 0) shift = 0;
+  const double inv_pitch = 1.0 / cfg->pitch, cxp = 0.5 * nx - 0.5, czp = 0.5 * ny - 0.5;
+  unsigned nt = nthreads > 0 ? (unsigned) nthreads : std::max(1u, std::thread::hardware_concurrency());
+  nt = (unsigned) std::min<uint64_t>(nt, n / 1024 + 1);
+  std::vector<std::vector<uint64_t>> acc(image ? nt : 0);
+  auto work = [&](unsigned wk) {
+    std::vector<uint64_t> *A = image ? &acc[wk] : nullptr;
+    if (A) A->assign((size_t) nx * ny, 0);
+    for (uint64_t i = wk; i < n; i += nt) {
+      double y = 0, z = 0, w = 0;
+      bool hit = weighted_ray(M, cfg->seed, (uint32_t) i, p0, cfg->energy, y, z, w);
+      if (yzw) {
+        yzw[i] = hit ? y : NAN;
+        yzw[n + i] = hit ? z : NAN;
+        yzw[2 * n + i] = hit ? w : 0.0;
+      }
+      if (!A || !hit || !(w > 0.0)) continue;
+      const double u = (y - cfg->center_y) * inv_pitch + cxp, vv = (z - cfg->center_z) * inv_pitch + czp;
+      if (!(u > -6.0 && u < nx + 5.0 && vv > -6.0 && vv < ny + 5.0)) continue;
+      const double uc = std::floor(u + 0.5), vc = std::floor(vv + 0.5);
+      const int ic = (int) uc, jc = (int) vc;
+      const float fu = (float) (u - uc), fv = (float) (vv - vc);
+      const uint32_t wq = (uint32_t) std::nearbyint(std::fmin(w * 2147483648.0, 4294967295.0));
+      uint32_t a[11], b[11];
+      for (int k = 0; k < 11; k++) {
+        float d = (float) (k - 5) - fu;
+        uint32_t gy = (uint32_t) std::nearbyint((double) (knorm * exp_neg_f((d * d) * half_inv_s2) * 2147483648.0f));
+        a[k] = (uint32_t) (((uint64_t) wq * gy) >> 32);
+        float e = (float) (k - 5) - fv;
+        b[k] = (uint32_t) std::nearbyint((double) (knorm * exp_neg_f((e * e) * half_inv_s2) * 2147483648.0f));
+      }
+      for (int kz = 0; kz < 11; kz++) {
+        int row = jc - 5 + kz;
+        if (row < 0 || row >= ny) continue;
+        for (int ky = 0; ky < 11; ky++) {
+          int col = ic - 5 + ky;
+          if (col < 0 || col >= nx) continue;
+          (*A)[(size_t) row * nx + col] += ((uint64_t) a[ky] * b[kz]) >> shift;
+        }
+      }
+    }
+  };
+  if (nt == 1) work(0);
+  else {
+    std::vector<std::thread> th;
+    for (unsigned w = 0; w < nt; w++) th.emplace_back(work, w);
+    for (auto &t : th) t.join();
+  }
+  if (image) {
+    const double scale = std::ldexp(1.0, shift - 61) / (double) n;
+    for (size_t k = 0; k < (size_t) nx * ny; k++) {
+      uint64_t s = 0;
+      for (unsigned w = 0; w < nt; w++) s += acc[w][k];
+      image[k] = (double) s * scale;
+    }
+  }
+  return 0;
+}

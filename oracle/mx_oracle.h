@@ -46,6 +46,15 @@ double mxo_philox_normal(uint64_t seed, uint32_t tag, uint32_t slot);
 /* Photon-generation draw k of photon `tag` (energies of point sources). */
 double mxo_source_uniform(uint64_t seed, uint32_t tag, uint32_t k);
 
+/* Weighted rays of the differentiable form (mx_diff_config) at theta,
+ * decisions made afresh: per-ray focal-plane y, z and weight into yzw
+ * (3 x n_rays, lost rays NaN, NaN, 0; may be NULL) and the splatted image
+ * into image (ny x nx; may be NULL). */
+int mxo_weighted(const mxo_model *m, const mx_diff_config *cfg, const double *theta, double *yzw,
+                 double *image, int nthreads);
+/* The splat's single-precision exp(-x). */
+float mxo_splat_exp(float x);
+
 #ifdef __cplusplus
 }
 #endif

@@ -13,11 +13,18 @@ oracle/Makefile compiles them in place into oracle/_ref.  Writes:
   stats_<workload>.npz   seeded statistical fixtures from the reference's own
                          generator: encircled-energy curve, chip/pixel and
                          order histograms, survivor fractions.
+  diff_rays.npz          focal-plane positions of the differentiable form's
+                         rays traced by the reference's mirror stage, at
+                         theta = 0 and at the workload's perturbation written
+                         into a copy of the HRMA geometry file, for an ideal
+                         and a reflecting (no blur, no scattering) mirror.
 """
 from __future__ import annotations
 
 import os
+import shutil
 import sys
+import tempfile
 
 import numpy as np
 
@@ -26,7 +33,9 @@ sys.path.insert(0, ROOT)
 
 from marx_gb300 import workloads as W  # noqa: E402
 from marx_gb300.photons import predraw_variates  # noqa: E402
-from oracle.bindings import Reference  # noqa: E402
+from oracle.bindings import Reference, Oracle, REF_ROOT  # noqa: E402
+from marx_gb300.diff import diff_workload, diff_mirror_config, source_direction, NPARAM  # noqa: E402
+from marx_gb300.photons import PhotonList, NUM_U, NUM_N  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 N_TRACE = 1000
@@ -77,5 +86,83 @@ def main():
         print(name, "good fraction", float(s["good_fraction"]), f"reference {N_STATS / secs:.3g} photons/s")
 
 
+N_DIFF = 4000
+RDB = "EKCHDOS06.rdb"
+SHELL_OF = {"1": 0, "3": 1, "4": 2, "6": 3}
+
+
+def perturbed_datadir(theta, where: str) -> str:
+    """A MARX data directory whose HRMA geometry file has theta added to
+    az_mis, el_mis (arcsec -> degrees) and x0, y0 (um -> mm) of both rows of
+    every shell; every other file is a link to the reference's own."""
+    src = os.path.join(REF_ROOT, "marx", "data")
+    for e in os.listdir(src):
+        if e != "hrma":
+            os.symlink(os.path.join(src, e), os.path.join(where, e))
+    os.makedirs(os.path.join(where, "hrma"))
+    for e in os.listdir(os.path.join(src, "hrma")):
+        if e != RDB:
+            os.symlink(os.path.join(src, "hrma", e), os.path.join(where, "hrma", e))
+    lines = open(os.path.join(src, "hrma", RDB)).read().split("\n")
+    cols = None
+    out = []
+    for ln in lines:
+        f = ln.split("\t")
+        if cols is None and f and f[0] == "mirror":
+            cols = {c: k for k, c in enumerate(f)}
+        elif cols is not None and f and f[0][:1] in "ph" and f[0][1:] in SHELL_OF:
+            s = SHELL_OF[f[0][1:]]
+            add = {"az_mis": theta[4 * s] / 3600.0, "el_mis": theta[4 * s + 1] / 3600.0,
+                   "x0": theta[4 * s + 2] * 1e-3, "y0": theta[4 * s + 3] * 1e-3}
+            for c, d in add.items():
+                f[cols[c]] = repr(float(float(f[cols[c]]) + float(d)))
+            ln = "\t".join(f)
+        out.append(ln)
+    with open(os.path.join(where, "hrma", RDB), "w") as fh:
+        fh.write("\n".join(out))
+    return where
+
+
+def diff_rays():
+    """The reference's mirror stage on the weighted rays' aperture points:
+    each photon gets the Philox variates of its tag, so it picks the shell,
+    radius and azimuth the engine's ray of that tag picks."""
+    w = diff_workload(n_rays=N_DIFF)
+    oracle = Oracle(diff_mirror_config(ideal=True))
+    tags = np.arange(N_DIFF, dtype=np.uint32)
+    U = np.array([[oracle.philox_uniform(w.cfg.seed, int(i), k) for i in tags] for k in range(NUM_U)])
+    N = np.array([[oracle.philox_normal(w.cfg.seed, int(i), k) for i in tags] for k in range(NUM_N)])
+    out = {"seed": np.array(w.cfg.seed), "n": np.array(N_DIFF), "energy": np.array(w.cfg.energy),
+           "src": np.array([w.cfg.src_y, w.cfg.src_z])}
+    thetas = {"zero": np.zeros(NPARAM), "true": w.theta_true}
+    for mname, ideal in (("ideal", True), ("reflect", False)):
+        cfg = diff_mirror_config(ideal=ideal)
+        cfg.use_blur = 0
+        cfg.use_wfold = 0
+        for tname, theta in thetas.items():
+            tmp = tempfile.mkdtemp(prefix="mxdiff")
+            try:
+                ref = Reference(cfg, datadir=perturbed_datadir(theta, tmp))
+                p0 = source_direction(w.cfg.src_y + theta[16], w.cfg.src_z + theta[17])
+                ph = PhotonList.from_inputs(np.full(N_DIFF, w.cfg.energy), np.repeat(p0[:, None], N_DIFF, 1),
+                                            np.zeros(N_DIFF))
+                ph.tag[:] = tags
+                q, used, bad = ref.trace_slots(ph, U, N, stages=2)
+                assert bad == 0
+            finally:
+                shutil.rmtree(tmp)
+            hit = (q.flags & 0xFF) == 0
+            t = -q.x[0] / q.p[0]
+            out[f"{mname}_{tname}_y"] = np.where(hit, q.x[1] + t * q.p[1], np.nan)
+            out[f"{mname}_{tname}_z"] = np.where(hit, q.x[2] + t * q.p[2], np.nan)
+            out[f"{mname}_{tname}_theta"] = theta
+            print(mname, tname, "reflected", hit.mean())
+    np.savez_compressed(os.path.join(HERE, "diff_rays.npz"), **out)
+
+
 if __name__ == "__main__":
-    main()
+    if "--diff" in sys.argv:
+        diff_rays()
+    else:
+        main()
+        diff_rays()
