@@ -228,3 +228,34 @@ def diff_workload(n_rays: int = 4_000_000, seed: int = 5, perturb_seed: int = 55
     t[16] = r.normal(0.0, 0.5)
     t[17] = r.normal(0.0, 0.5)
     return DiffWorkload(c, t, seed + 1000)
+
+
+def main(argv=None):
+    """Gradient steps of the differentiable workload on the current GPU:
+    python -m marx_gb300.diff [--rays N] [--steps K]"""
+    import argparse
+    import torch
+    from ._native import Engine
+    ap = argparse.ArgumentParser(description=main.__doc__)
+    ap.add_argument("--rays", type=int, default=4_000_000)
+    ap.add_argument("--steps", type=int, default=2)
+    a = ap.parse_args(argv)
+    eng = Engine(diff_mirror_config())
+    w = diff_workload(n_rays=a.rays)
+    d = DiffImage.centred(eng, w.cfg)
+    tc = d.cfg.copy()
+    tc.seed = w.target_seed
+    target = DiffImage(eng, tc).forward(w.theta_true, FRESH).clone()
+    theta = np.zeros(NPARAM)
+    for _ in range(a.steps):
+        img = d.forward(theta, RECORD)
+        loss, dl = d.mse(img, target)
+        g = d.adjoint(theta, dl)
+    torch.cuda.synchronize()
+    print(f"loss {float(loss):.6e}")
+    for name, v in zip(PARAM_NAMES, g):
+        print(f"{name:>10s} {v: .6e}")
+
+
+if __name__ == "__main__":
+    main()

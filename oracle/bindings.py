@@ -60,6 +60,7 @@ class Oracle:
         L.mxo_source_uniform.restype = C.c_double
         L.mxo_source_uniform.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32]
         from marx_gb300.diff import MxDiffConfig
+        L.mxo_weighted_flops.argtypes = [C.c_void_p, C.POINTER(MxDiffConfig), C.c_void_p, C.c_void_p]
         L.mxo_splat_exp.restype = C.c_float
         L.mxo_splat_exp.argtypes = [C.c_float]
         L.mxo_weighted.argtypes = [C.c_void_p, C.POINTER(MxDiffConfig), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
@@ -102,6 +103,15 @@ class Oracle:
 
     def source_uniform(self, seed, tag, k=0):
         return self.lib.mxo_source_uniform(seed, tag, k)
+
+    def weighted_flops(self, dcfg, theta):
+        """(FP64 operations, rays, rays reaching the focal plane) of the
+        weighted rays at theta, from the counting arithmetic."""
+        th = np.ascontiguousarray(theta, dtype=np.float64)
+        out = np.zeros(3)
+        if self.lib.mxo_weighted_flops(self.h, C.byref(dcfg), _p(th), _p(out)) != 0:
+            raise RuntimeError("oracle weighted flop count failed")
+        return out
 
     def splat_exp(self, x: float) -> float:
         return self.lib.mxo_splat_exp(x)

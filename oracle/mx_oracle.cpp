@@ -423,52 +423,58 @@ static float exp_neg_f(float x) {
   return p * scale;
 }
 
-static bool weighted_ray(const Model &M, uint64_t seed, uint32_t tag, const V3<double> &p0, double energy,
+template <class R>
+static bool weighted_ray(const Model &M, uint64_t seed, uint32_t tag, const V3<double> &p0d, double energy,
                          double &y, double &z, double &w) {
   Variates v;
   v.seed = seed; v.tag = tag;
   v.window(MX_U_MIRROR, 12, MX_N_MIRROR, 2);
-  double wt = 1.0;
-  if (!M.ideal) { v.uniform(); wt = M.cfg.hrma_vig; }
+  R wt = R(1.0);
+  if (!M.ideal) { v.uniform(); wt = R(M.cfg.hrma_vig); }
   Photon ph{};
-  V3<double> x{0.0, 0.0, 0.0}, p = p0;
-  project_photon_to_hrma<double>(M, ph, x, p, v);
+  V3<R> x{R(0.0), R(0.0), R(0.0)}, p{R(p0d.x), R(p0d.y), R(p0d.z)};
+  project_photon_to_hrma<R>(M, ph, x, p, v);
   if (v.overrun || (ph.flags & MX_PHOTON_MIRROR_VBLOCKED)) return false;
   const Shell &h = M.sh[ph.shell];
-  double beta = 0.0, delta = 1.0, corr = 1.0;
+  R beta = R(0.0), delta = R(1.0), corr = R(1.0);
   if (M.opt_n) {
-    beta = (double) interpolate_f<double>((float) energy, M.opt_e, M.opt_beta, M.opt_n);
-    delta = (double) interpolate_f<double>((float) energy, M.opt_e, M.opt_delta, M.opt_n);
-    if (M.use_scale) corr = sqrt((double) interpolate_f<double>((float) energy, h.corr_e, h.corr_f, h.corr_n));
+    beta = (double) interpolate_f<R>((float) energy, M.opt_e, M.opt_beta, M.opt_n);
+    delta = (double) interpolate_f<R>((float) energy, M.opt_e, M.opt_delta, M.opt_n);
+    if (M.use_scale) corr = sqrt(R((double) interpolate_f<R>((float) energy, h.corr_e, h.corr_f, h.corr_n)));
   }
   uint32_t flags = 0;
   for (int o = 0; o < 2; o++) {
-    x = vsum(x, h.to_osac[o]);
-    x = mvmul(h.fwd[o], x);
-    p = mvmul(h.fwd[o], p);
-    V3<double> n;
-    if (-1 == conic_intersection(h.a[o], h.b[o], h.c[o], x, p, n, h.xmin[o], h.xmax[o])) return false;
-    double pdn = dot(p, n);
+    V3<R> to{R(h.to_osac[o].x), R(h.to_osac[o].y), R(h.to_osac[o].z)};
+    M3<R> fw, bw;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) { fw.m[i][j] = h.fwd[o].m[i][j]; bw.m[i][j] = h.bwd[o].m[i][j]; }
+    x = vsum(x, to);
+    x = mvmul(fw, x);
+    p = mvmul(fw, p);
+    V3<R> n;
+    if (-1 == conic_intersection(R(h.a[o]), R(h.b[o]), R(h.c[o]), x, p, n, R(h.xmin[o]), R(h.xmax[o]))) return false;
+    R pdn = dot(p, n);
     if (!M.ideal) wt *= reflectivity(fabs(pdn), beta, delta) * corr;
-    p = ax1_bx2(1.0, p, -2.0 * pdn, n);
-    p = mvmul(h.bwd[o], p);
-    x = mvmul(h.bwd[o], x);
-    x = vdiff(x, h.to_osac[o]);
+    p = ax1_bx2(R(1.0), p, R(-2.0) * pdn, n);
+    p = mvmul(bw, p);
+    x = mvmul(bw, x);
+    x = vdiff(x, to);
     if (M.use_struts && intersects_struts(M, x, p, flags, o == 0 ? CAP_STRUTS : POST_STRUTS)) return false;
   }
-  double t = -x.x / p.x;
-  y = x.y + t * p.y;
-  z = x.z + t * p.z;
-  w = wt;
+  R t = -x.x / p.x;
+  y = dv(x.y + t * p.y);
+  z = dv(x.z + t * p.z);
+  w = dv(wt);
   return true;
 }
 
 extern "C" float mxo_splat_exp(float x) { return exp_neg_f(x); }
 
-extern "C" int mxo_weighted(const mxo_model *m, const mx_diff_config *cfg, const double *theta, double *yzw,
-                            double *image, int nthreads) {
-  if (!m || !cfg || !theta || cfg->n_rays < 1 || cfg->n_rays > 0xffffffffull) return MX_EINVAL;
-  Model M = m->M;
+// The model with theta added to the geometry-file rows of every shell, as
+// the reference would read it from a perturbed HRMA_Geometry_File, and the
+// source direction at theta.
+static void perturbed(const mxo_model *m, const mx_diff_config *cfg, const double *theta, Model &M, V3<double> &p0) {
+  M = m->M;
   for (int s = 0; s < 4; s++) {
     Shell &h = M.sh[s];
     for (int o = 0; o < 2; o++) {
@@ -480,8 +486,33 @@ extern "C" int mxo_weighted(const mxo_model *m, const mx_diff_config *cfg, const
     shell_frames(h, M.cap + h.xoffset);
   }
   const double arcsec = PI / (180.0 * 3600.0);
-  V3<double> p0{-1.0, -tan((cfg->src_y + theta[16]) * arcsec), -tan((cfg->src_z + theta[17]) * arcsec)};
+  p0 = V3<double>{-1.0, -tan((cfg->src_y + theta[16]) * arcsec), -tan((cfg->src_z + theta[17]) * arcsec)};
   normalize(p0);
+}
+
+extern "C" int mxo_weighted_flops(const mxo_model *m, const mx_diff_config *cfg, const double *theta, double *counts) {
+  if (!m || !cfg || !theta || !counts) return MX_EINVAL;
+  Model M;
+  V3<double> p0;
+  perturbed(m, cfg, theta, M, p0);
+  Counted::ops = 0;
+  double hits = 0.0;
+  for (uint64_t i = 0; i < cfg->n_rays; i++) {
+    double y, z, w;
+    if (weighted_ray<Counted>(M, cfg->seed, (uint32_t) i, p0, cfg->energy, y, z, w)) hits += 1.0;
+  }
+  counts[0] = Counted::ops;
+  counts[1] = (double) cfg->n_rays;
+  counts[2] = hits;
+  return 0;
+}
+
+extern "C" int mxo_weighted(const mxo_model *m, const mx_diff_config *cfg, const double *theta, double *yzw,
+                            double *image, int nthreads) {
+  if (!m || !cfg || !theta || cfg->n_rays < 1 || cfg->n_rays > 0xffffffffull) return MX_EINVAL;
+  Model M;
+  V3<double> p0;
+  perturbed(m, cfg, theta, M, p0);
   const uint64_t n = cfg->n_rays;
   const int nx = (int) cfg->nx, ny = (int) cfg->ny;
   const float knorm = (float) (1.0 / (std::sqrt(2.0 * PI) * cfg->sigma));
@@ -498,7 +529,7 @@ extern "C" int mxo_weighted(const mxo_model *m, const mx_diff_config *cfg, const
     if (A) A->assign((size_t) nx * ny, 0);
     for (uint64_t i = wk; i < n; i += nt) {
       double y = 0, z = 0, w = 0;
-      bool hit = weighted_ray(M, cfg->seed, (uint32_t) i, p0, cfg->energy, y, z, w);
+      bool hit = weighted_ray<double>(M, cfg->seed, (uint32_t) i, p0, cfg->energy, y, z, w);
       if (yzw) {
         yzw[i] = hit ? y : NAN;
         yzw[n + i] = hit ? z : NAN;

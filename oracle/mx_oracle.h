@@ -52,6 +52,10 @@ double mxo_source_uniform(uint64_t seed, uint32_t tag, uint32_t k);
  * into image (ny x nx; may be NULL). */
 int mxo_weighted(const mxo_model *m, const mx_diff_config *cfg, const double *theta, double *yzw,
                  double *image, int nthreads);
+/* FP64 operations of the weighted rays (counting arithmetic, as
+ * mxo_count_flops): counts[0] operations, counts[1] rays, counts[2] rays
+ * that reached the focal plane. */
+int mxo_weighted_flops(const mxo_model *m, const mx_diff_config *cfg, const double *theta, double *counts);
 /* The splat's single-precision exp(-x). */
 float mxo_splat_exp(float x);
 
