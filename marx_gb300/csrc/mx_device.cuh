@@ -65,7 +65,12 @@ MXD D3 rotate_unit(D3 p, D3 n, double c, double s) {
 // series to x^7 / x^6 is exact to the last bit (the next terms are below
 // 1e-24 relative); larger angles take the library sincos.
 MXD void sincos_small(double x, double *s, double *c) {
-  if (fabs(x) < 1e-3) {
+  if (fabs(x) < 1e-4) {
+    // the x^5 and x^4 terms are below 1e-18 relative: under a tenth of an ulp
+    double x2 = x * x;
+    *s = x + x * x2 * (-1.0 / 6.0);
+    *c = 1.0 + x2 * -0.5;
+  } else if (fabs(x) < 1e-3) {
     double x2 = x * x;
     *s = x + x * x2 * (-1.0 / 6.0 + x2 * (1.0 / 120.0 + x2 * (-1.0 / 5040.0)));
     *c = 1.0 + x2 * (-0.5 + x2 * (1.0 / 24.0 + x2 * (-1.0 / 720.0)));
@@ -107,6 +112,79 @@ MXD D3 mat_mul(const double *m, D3 v) {  // JDM3m_vector_mul (rotate.c:121), row
 #define MX_DDIV(a, b) ((a) / (b))
 #endif
 
+// Conversions between float and double on the integer pipe.  On GB300 a
+// F2F conversion issues on the FP64 pipe, the one this trace is bound by.
+// f2d is exact (as the cast is); zeros, subnormals, infinities and NaN
+// take the cast.
+MXD double f2d(float f) {
+#ifdef __CUDA_ARCH__
+  const uint32_t u = __float_as_uint(f), a = u & 0x7fffffffu;
+  uint32_t hi, lo;
+  if (a >= 0x00800000u) {               // normal: rebias the exponent by 1023 - 127
+    hi = (a >> 3) + (896u << 20);
+    lo = a << 29;
+    if (a >= 0x7f800000u) hi = 0x7ff00000u | ((a & 0x7fffffu) >> 3);   // infinity, NaN
+  } else if (a != 0u) {                 // subnormal: a 2^-149 with a normalised
+    const uint32_t lz = (uint32_t) __clz((int) a);
+    const uint32_t m = (a << (lz - 8u)) & 0x7fffffu;
+    hi = ((905u - lz) << 20) | (m >> 3);
+    lo = m << 29;
+  } else
+    hi = lo = 0u;
+  return __hiloint2double((int) ((u & 0x80000000u) | hi), (int) lo);
+#else
+  return (double) f;
+#endif
+}
+// d truncated toward zero to float (relative error below 2^-23); magnitudes
+// below 2^-126 become zero, above float range infinity; NaN stays NaN.  For
+// single-precision screens only, never for a stored result.
+MXD float d2f_trunc(double d) {
+#ifdef __CUDA_ARCH__
+  const unsigned long long b = (unsigned long long) __double_as_longlong(d);
+  const uint32_t hi = (uint32_t) (b >> 32), lo = (uint32_t) b, e = (hi >> 20) & 0x7ffu;
+  uint32_t r = hi & 0x80000000u;
+  if (e - 897u < 254u) r |= ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+  else if (e >= 1151u) r |= 0x7f800000u | ((e == 2047u && ((hi & 0xfffffu) | lo)) ? 0x400000u : 0u);
+  return __uint_as_float(r);
+#else
+  return (float) d;
+#endif
+}
+// a / b from the correctly rounded reciprocal rb = 1/b by one Markstein
+// correction: q = a rb, r = a - q b (exact with a fused multiply-add),
+// q + r rb rounds to the correctly rounded quotient, as a division does,
+// for finite non-zero operands away from overflow and underflow.
+MXD double div_by(double a, double b, double rb) {
+#ifdef __CUDA_ARCH__
+  const double q = a * rb;
+  return fma(fma(-q, b, a), rb, q);
+#else
+  return a / b;
+#endif
+}
+// fmod(x, y) for x >= 0 and 0 < y from the correctly rounded ry = 1/y.
+// fmod's result is exact: with the integer quotient q right, x - q y is the
+// remainder itself and one fused multiply-add yields it exactly; a q off by
+// one (x ry rounded across an integer) shows as a remainder outside [0, y)
+// and is corrected.  Other operands take the library fmod.
+MXD double fmod_pos(double x, double y, double ry) {
+#ifdef __CUDA_ARCH__
+  const double qa = x * ry;
+  if (x >= 0.0 && qa < 4.0e15) {
+    double q = trunc(qa);
+    double r = fma(-q, y, x);
+    if (r < 0.0) r = fma(-(q - 1.0), y, x);
+    else if (r >= y) r = fma(-(q + 1.0), y, x);
+    return r;
+  }
+  return fmod(x, y);
+#else
+  (void) ry;
+  return std::fmod(x, y);
+#endif
+}
+
 // JDMbinary_search_f (finterpo.c:37): first index with xp >= x (an equal
 // element returns its index), n if all are smaller.
 MXD unsigned bsearch_f(float x, const float *xp, unsigned n) {
@@ -120,6 +198,23 @@ MXD unsigned bsearch_f(float x, const float *xp, unsigned n) {
   return (x >= xp[n0]) ? n1 : n0;
 }
 MXD unsigned bsearch_d(double x, const double *xp, unsigned n) {  // JDMbinary_search_d (dinterpo.c:30)
+#ifdef __CUDA_ARCH__
+  // Non-negative finite x against a non-negative table: IEEE doubles of
+  // one sign order as their bit patterns, so the search runs on the
+  // integer pipe.
+  const unsigned long long bx = (unsigned long long) __double_as_longlong(x);
+  if (bx < 0x7ff0000000000000ull) {
+    const unsigned long long *xb = (const unsigned long long *) xp;
+    unsigned n0 = 0, n1 = n;
+    while (n1 > n0 + 1) {
+      unsigned n2 = (n0 + n1) >> 1;
+      unsigned long long v = __ldg(xb + n2);
+      if (v >= bx) { if (v == bx) return n2; n1 = n2; }
+      else n0 = n2;
+    }
+    return (bx >= __ldg(xb + n0)) ? n1 : n0;
+  }
+#endif
   unsigned n0 = 0, n1 = n;
   while (n1 > n0 + 1) {
     unsigned n2 = (n0 + n1) >> 1;
@@ -141,10 +236,10 @@ MXD float interp_f(float x, const float *xp, const float *yp, const double *slop
   if (n1 < n && x == xp[n1]) return yp[n1];
   if (n1 == n) { n1--; n0--; }
   if (n1 == 0) n0 = 1;
-  double x0 = xp[n0], x1 = xp[n1];
-  if (x1 == x0) return yp[n1];
+  const float xf0 = xp[n0], xf1 = xp[n1];
+  if (xf1 == xf0) return yp[n1];   // the same test in float: the cast is exact
   double q = slope[n0 < n1 ? n0 : n1];
-  return (float) MX_DADD((double) yp[n0], MX_DMUL(q, MX_DADD((double) x, -x0)));
+  return (float) MX_DADD(f2d(yp[n0]), MX_DMUL(q, MX_DADD(f2d(x), -f2d(xf0))));
 }
 
 // ----------------------------------------------------------- variates --
@@ -223,7 +318,7 @@ MXD double philox_normal(uint64_t seed, uint32_t tag, uint32_t k) {
   float u1 = (float) ((c[0] >> 8) + 1u) * (1.0f / 16777216.0f);
   float u2 = (float) (c[1] >> 8) * (1.0f / 16777216.0f);
   float r = FSQRT(FMUL(-2.0f, series_logf(u1)));
-  return (double) FMUL(r, series_cos2pi(u2));
+  return f2d(FMUL(r, series_cos2pi(u2)));
 }
 
 // Source-level draws (photon generation) use their own Philox domain, so
@@ -270,9 +365,9 @@ MXD int quadratic_root(double a, double b, double c, double &rp, double &rm) {
   if (a == 0.0) return -1;
   double bsqr = b * b, ac4 = a * c * 4;
   if (bsqr > ac4) {
-    // rp = -2c / (b f), rm = -b f / (2a) from one reciprocal of a b f
-    double factor = 1.0 + sqrt(1.0 - ac4 / bsqr);
-    double bf = b * factor, inv = 1.0 / (a * bf);
+    // rp = -2c / (b f), rm = -b f / (2a) from one reciprocal of a b f,
+    // with b f = b (1 + sqrt(1 - 4ac/b^2)) = b + sign(b) sqrt(b^2 - 4ac)
+    double bf = b + copysign(sqrt(bsqr - ac4), b), inv = 1.0 / (a * bf);
     rp = -2.0 * c * a * inv;
     rm = -0.5 * bf * bf * inv;
     return 1;
@@ -306,14 +401,22 @@ MXD int conic_intersection(const MxShellDev &h, int o, D3 &x0, D3 p, D3 &normal)
 
 // blur_normal (hrma.c:1054-1093): rotate n by a normal-distributed angle
 // about a random axis perpendicular to it.
+// With e1 = (0, n.z, -n.y) / len the first perpendicular, e2 = n x e1 and
+// perp = cos(phi) e1 + sin(phi) e2 the rotated one, the rotation of unit n
+// about unit perp by ang is cos(ang) n + sin(ang) (perp x n), and
+// perp x n = sin(phi) e1 - cos(phi) e2, where
+// e2 = (-len, n.x n.y / len, n.x n.z / len): the two Rodrigues rotations
+// of the reference in closed form, one normalisation.
 MXD void blur_normal(D3 &n, double blur_rad, Rng &rng) {
-  double inv = mx_rsqrt(n.y * n.y + n.z * n.z);
-  D3 perp = mk(0.0, n.z * inv, -n.y * inv);
+  const double l2 = n.y * n.y + n.z * n.z, inv = mx_rsqrt(l2), len = l2 * inv;
   double s, c;
   mx_sincospi(2.0 * rng.uniform(), &s, &c);   // phi = 2 pi u
-  perp = rotate_unit(perp, n, c, s);
   double ang = blur_rad * rng.normal();
-  n = rotate_unit_small(n, perp, ang);
+  double sa, ca;
+  sincos_small(ang, &sa, &ca);
+  const double nxy = n.x * n.y, nxz = n.x * n.z;
+  const D3 w = mk(c * len, (s * n.z - c * nxy) * inv, (-s * n.y - c * nxz) * inv);   // perp x n
+  n = normalized(ca * n + sa * w);
 }
 
 // marx_reflectivity (reflect.c:39-77): polarisation-averaged Fresnel
@@ -396,12 +499,17 @@ MXD int reflect_at(const MxTables &T, const MxShellDev &h, int o, int table, D3 
   double dg = wfold_interp(T, table, energy, -pdn, r) * h.scat[o];
   if (dg > PI / 4) return -1;
   if (rng.uniform() < 0.5) dg = -dg;
-  p = rotate_unit_small(p, cross(p, n), dg);
+  // JDMv_rotate_unit_vector(p, p x n, dg): with a = p x n, p.a = 0 and
+  // a x p = n - (p.n) p for unit p, so p becomes cos(dg) p + sin(dg) (n - (p.n) p)
+  double sg, cg;
+  sincos_small(dg, &sg, &cg);
+  const double pn = dot(p, n);
+  p = normalized(cg * p + sg * (n + (-pn) * p));
   return 0;
 }
 
 // intersects_struts (hrma.c:928-968): three bars rotated by 60 degrees.
-MXD bool struts_block(const MxTables &T, int set, D3 x, D3 p) {
+MXD bool struts_block_exact(const MxTables &T, int set, D3 x, D3 p) {
   double inv_px = 1.0 / p.x;
   for (int k = 0; k < 2; k++) {
     double hw = T.strut_half_width[set][k];
@@ -413,6 +521,36 @@ MXD bool struts_block(const MxTables &T, int set, D3 x, D3 p) {
     }
   }
   return false;
+}
+
+// The same test screened in single precision: the bar coordinates of the
+// ray in float carry an absolute error far below MX_STRUT_MARGIN (under
+// 2e-3 mm for positions of 1e4 mm and directions within a few degrees of
+// the axis), so a coordinate more than the margin inside or outside every
+// bar edge decides the test as the double-precision one would.  Rays with
+// a coordinate within the margin of an edge, or not finite, take the
+// double-precision test.
+#define MX_STRUT_MARGIN 0.05f
+MXD bool struts_block(const MxTables &T, int set, D3 x, D3 p) {
+#ifdef __CUDA_ARCH__
+  const float xx = d2f_trunc(x.x), xy = d2f_trunc(x.y), xz = d2f_trunc(x.z);
+  const float px = d2f_trunc(p.x), py = d2f_trunc(p.y), pz = d2f_trunc(p.z);
+  const float inv = 1.0f / px;
+  bool unsure = false;
+  for (int k = 0; k < 2; k++) {
+    const float hw = T.strut_hwf[set][k];
+    const float t = (T.strut_xf[set][k] - xx) * inv;
+    float y = xy + py * t, z = xz + pz * t;
+    for (int i = 0; i < 3; i++) {
+      if (i != 0) { float tmp = T.cos30f * y - T.sin30f * z; z = T.sin30f * y + T.cos30f * z; y = tmp; }
+      const float dy = fabsf(y) - hw, dz = fabsf(z) - hw;
+      if (dy < -MX_STRUT_MARGIN || dz < -MX_STRUT_MARGIN) return true;
+      if (!(dy > MX_STRUT_MARGIN && dz > MX_STRUT_MARGIN)) unsure = true;
+    }
+  }
+  if (!unsure) return false;
+#endif
+  return struts_block_exact(T, set, x, p);
 }
 
 // Mirror state carried between the three parts of the HRMA trace: the
@@ -528,6 +666,11 @@ MXD void mirror_stage(const MxTables &T, const MxShellDev *shells, const float *
 }
 
 // ------------------------------------------------------------- dither --
+// rotate_unit about the x axis: n = (1, 0, 0), n x p = (0, -p.z, p.y).
+MXD D3 rotate_x(D3 p, double c, double s) {
+  return normalized(mk(c * p.x + p.x * (1.0 - c), c * p.y - s * p.z, c * p.z + s * p.y));
+}
+
 // get_internal_dither + dither_ray + apply_dither (dither.c:167-182,
 // 551-581, 609-628).  The dither angles pass through float as they do in
 // Marx_Dither_Type.
@@ -537,14 +680,23 @@ MXD void dither_stage(const MxTables &T, Ph &ph, Rng &rng) {
   // A zero amplitude makes amp * sin(...) zero whatever the sine; skip it.
   double v[3];
   for (int k = 0; k < 3; k++)
-    v[k] = T.dith_amp[k] != 0.0 ? T.dith_amp[k] * sin(t / T.dith_period[k] + T.dith_phase[k]) : 0.0;
+    v[k] = T.dith_amp[k] != 0.0 ? T.dith_amp[k] * sin(div_by(t, T.dith_period[k], T.dith_inv_period[k]) +
+                                                      T.dith_phase[k]) : 0.0;
   float fra = (float) v[0];
   float fdec = (float) v[1];
   float froll = (float) (T.nominal_roll + v[2]);
   ph.dith[0] = fra; ph.dith[1] = fdec; ph.dith[2] = froll;
-  double ra = (double) fra + T.aspect_blur * rng.normal();
-  double dec = (double) fdec + T.aspect_blur * rng.normal();
-  D3 p = rotate_unit_small(ph.p, mk(1, 0, 0), -(double) froll);
+  double ra = f2d(fra) + T.aspect_blur * rng.normal();
+  double dec = f2d(fdec) + T.aspect_blur * rng.normal();
+  // roll about the x axis (JDMv_rotate_unit_vector with n = x); a fixed
+  // roll of zero leaves p as it is
+  D3 p = ph.p;
+  if (!T.roll_fixed) {
+    double sr, cr;
+    sincos_small(-f2d(froll), &sr, &cr);
+    p = rotate_x(p, cr, sr);
+  } else if (!T.roll_zero)
+    p = rotate_x(p, T.roll_cos, T.roll_sin);
   double sr, cr, sd, cd;
   sincos_small(ra, &sr, &cr);
   sincos_small(dec, &sd, &cd);
@@ -552,8 +704,12 @@ MXD void dither_stage(const MxTables &T, Ph &ph, Rng &rng) {
   D3 n = mk(0, sd, -cd * sr);
   double s2 = n.y * n.y + n.z * n.z;
   if (!(s2 > 1e-40)) { ph.p = p; return; }
-  double inv = mx_rsqrt(s2);
-  ph.p = rotate_unit(p, inv * n, cos_theta, s2 * inv);
+  // rotate_unit(p, n / s, cos_theta, s) with s = |n| written without the
+  // unit axis: cos p + ((p.n)(1 - cos) / s^2) n + n x p, n.x = 0
+  const double pn = p.y * n.y + p.z * n.z;
+  const double k = pn * (1.0 - cos_theta) / s2;
+  ph.p = normalized(mk(cos_theta * p.x + (n.y * p.z - n.z * p.y), cos_theta * p.y + k * n.y + n.z * p.x,
+                       cos_theta * p.z + k * n.z - n.y * p.x));
 }
 
 // ------------------------------------------------------------ grating --
@@ -687,6 +843,26 @@ MXD int chip_plane(const MxChipDev &g, D3 x0, D3 p, D3 &x, double &dx, double &d
   return hit;
 }
 
+// Single-precision screen of chip_plane's must-hit test: 0 when the ray
+// certainly misses the chip (its chip coordinates lie more than
+// MX_CHIP_MARGIN outside an edge), 1 otherwise.  The float coordinates
+// carry an absolute error below 1e-2 mm for positions of up to 1e4 mm from
+// the chip, far inside the margin; a ray that is not certainly outside
+// takes the double-precision test, which alone decides a hit.
+#define MX_CHIP_MARGIN 0.1f
+MXD int chip_screen(const MxChipDev &g, float x0, float x1, float x2, float p0, float p1, float p2) {
+  const float r0 = x0 - g.f_ll[0], r1 = x1 - g.f_ll[1], r2 = x2 - g.f_ll[2];
+  const float pdn = p0 * g.f_normal[0] + p1 * g.f_normal[1] + p2 * g.f_normal[2];
+  const float s = -(r0 * g.f_normal[0] + r1 * g.f_normal[1] + r2 * g.f_normal[2]) / pdn;
+  const float q0 = r0 + s * p0, q1 = r1 + s * p1, q2 = r2 + s * p2;
+  const float rx = q0 * g.f_xhat[0] + q1 * g.f_xhat[1] + q2 * g.f_xhat[2];
+  const float ry = q0 * g.f_yhat[0] + q1 * g.f_yhat[1] + q2 * g.f_yhat[2];
+  if (rx < -MX_CHIP_MARGIN || rx > g.f_xlen + MX_CHIP_MARGIN || ry < -MX_CHIP_MARGIN ||
+      ry > g.f_ylen + MX_CHIP_MARGIN)
+    return 0;
+  return 1;
+}
+
 // _marx_acis_i_detect / _marx_acis_s_detect per photon (acis-i.c:124-157,
 // acis-s.c:203-239), _marx_intersect_with_detector (detector.c:112-168),
 // _marx_acis_apply_streak (acis-i.c:60-93).  QE and pulse height are not
@@ -699,8 +875,16 @@ MXD void detect_stage(const MxTables &T, const MxChipDev *chips, int nchips, Ph 
   int hit = -1;
   D3 xh = x;
   double dx = 0, dy = 0;
-  for (int k = 0; k < nchips; k++)
+#ifdef __CUDA_ARCH__
+  const float fx0 = d2f_trunc(x.x), fx1 = d2f_trunc(x.y), fx2 = d2f_trunc(x.z);
+  const float fp0 = d2f_trunc(p.x), fp1 = d2f_trunc(p.y), fp2 = d2f_trunc(p.z);
+#endif
+  for (int k = 0; k < nchips; k++) {
+#ifdef __CUDA_ARCH__
+    if (!chip_screen(chips[k], fx0, fx1, fx2, fp0, fp1, fp2)) continue;
+#endif
     if (1 == chip_plane(chips[k], x, p, xh, dx, dy, true)) { hit = k; break; }
+  }
   if (hit < 0 && T.det_extend) {
     double best = -1;
     for (int k = 0; k < nchips; k++) {
@@ -717,10 +901,10 @@ MXD void detect_stage(const MxTables &T, const MxChipDev *chips, int nchips, Ph 
     const MxChipDev &d = chips[hit];
     x = xh;
     ph.ccd = d.id;
-    ph.ypix = (float) (dx / d.xpix);
-    ph.zpix = (float) (dy / d.ypix);
+    ph.ypix = (float) div_by(dx, d.xpix, d.inv_xpix);
+    ph.zpix = (float) div_by(dy, d.ypix, d.inv_ypix);
     if (T.frame_transfer > 0.0) {
-      double t = fmod(T.start_time + ph.t, T.frame_time);
+      double t = fmod_pos(T.start_time + ph.t, T.frame_time, T.inv_frame_time);
       if (t > T.exposure) {
         ph.zpix = (float) (1.0 + 1022.0 * rng.uniform());
         double xp = ((double) ph.ypix - d.xoff) * d.xpix, yp = ((double) ph.zpix - d.yoff) * d.ypix;

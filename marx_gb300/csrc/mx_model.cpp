@@ -129,6 +129,12 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
                            {0.5 * 0.5 * 25.4, 0.5 * 0.5 * 25.4}};
   memcpy(T.strut_xpos, sx, sizeof(sx));
   memcpy(T.strut_half_width, sw, sizeof(sw));
+  for (int a = 0; a < 3; a++)
+    for (int k = 0; k < 2; k++) {
+      T.strut_xf[a][k] = (float) (sx[a][k] + T.cap);
+      T.strut_hwf[a][k] = (float) sw[a][k];
+    }
+  T.cos30f = (float) T.cos30; T.sin30f = (float) T.sin30;
 
   if (cfg.hrma_vig < 0 || cfg.hrma_vig > 1) { err = "HRMAVig must lie in [0,1]"; return false; }
   for (int i = 0; i < 4; i++)
@@ -352,6 +358,12 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
       c.normal[0] = xh[1] * yh[2] - xh[2] * yh[1];
       c.normal[1] = xh[2] * yh[0] - xh[0] * yh[2];
       c.xpix = c.xlen / 1024.0; c.ypix = c.ylen / 1024.0;
+      c.inv_xpix = 1.0 / c.xpix; c.inv_ypix = 1.0 / c.ypix;
+      for (int k = 0; k < 3; k++) {
+        c.f_ll[k] = (float) c.x_ll[k]; c.f_xhat[k] = (float) c.xhat[k];
+        c.f_yhat[k] = (float) c.yhat[k]; c.f_normal[k] = (float) c.normal[k];
+      }
+      c.f_xlen = (float) c.xlen; c.f_ylen = (float) c.ylen;
       M.chips.push_back(c);
     }
     if (cfg.detector != MX_DETECTOR_NONE && cfg.acis_exposure_time <= 0) {
@@ -364,6 +376,7 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
     T.frame_transfer = cfg.acis_frame_transfer_time < 0.0 ? 0.0 : cfg.acis_frame_transfer_time;
     T.exposure = cfg.acis_exposure_time;
     T.frame_time = T.frame_transfer + T.exposure;
+    T.inv_frame_time = 1.0 / T.frame_time;
     T.focal_length = cfg.focal_length;
   }
 
@@ -376,12 +389,28 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
     T.dith_period[k] = cfg.dither_period[k];
     T.dith_phase[k] = cfg.dither_phase[k];
     if (T.dither && !(cfg.dither_period[k] > 0)) { err = "dither periods must be > 0"; return false; }
+    T.dith_inv_period[k] = cfg.dither_period[k] > 0 ? 1.0 / cfg.dither_period[k] : 0.0;
   }
   double roll = cfg.roll_nom * (PI_ / 180.0);
   double xr = fmod(roll, 2 * PI_);
   if (xr >= PI_) xr -= (2 * PI_);
   if (xr < -PI_) xr += (2 * PI_);
   T.nominal_roll = xr;
+  // With no roll amplitude every photon is rolled by the same float angle
+  // (get_internal_dither, dither.c:175): its sine and cosine are taken once
+  // here as the per-photon code would take them (series below 1e-3 rad).
+  T.roll_fixed = T.dith_amp[2] == 0.0;
+  {
+    double a = -(double) (float) (T.nominal_roll + 0.0);
+    T.roll_zero = T.roll_fixed && a == 0.0;
+    if (fabs(a) < 1e-3) {
+      double a2 = a * a;
+      T.roll_sin = a + a * a2 * (-1.0 / 6.0 + a2 * (1.0 / 120.0 + a2 * (-1.0 / 5040.0)));
+      T.roll_cos = 1.0 + a2 * (-0.5 + a2 * (1.0 / 24.0 + a2 * (-1.0 / 720.0)));
+    } else {
+      T.roll_sin = sin(a); T.roll_cos = cos(a);
+    }
+  }
   T.start_time = cfg.start_time;
   return true;
 }

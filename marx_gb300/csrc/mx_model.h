@@ -33,6 +33,8 @@ struct MxGratingDev {
 struct MxChipDev {
   double x_ll[3], xhat[3], yhat[3], normal[3];
   double xlen, ylen, xpix, ypix, xoff, yoff;
+  double inv_xpix, inv_ypix;                   // correctly rounded 1/xpix, 1/ypix
+  float f_ll[3], f_xhat[3], f_yhat[3], f_normal[3], f_xlen, f_ylen;   // single-precision screen copies
   int32_t id, pad;
 };
 
@@ -61,11 +63,16 @@ struct MxTables {
   int32_t ideal, use_blur, use_wfold, use_struts, use_scale, area_uniform;
   double hrma_vig, source_distance, cap, cos30, sin30;
   double strut_xpos[3][2], strut_half_width[3][2];
+  float strut_xf[3][2], strut_hwf[3][2], cos30f, sin30f;   // cap + strut_xpos and half widths in float
   // dither
   int32_t dither, grating;
   double dith_amp[3], dith_period[3], dith_phase[3], nominal_roll, aspect_blur, start_time;
+  double dith_inv_period[3];    // correctly rounded 1 / dith_period
+  int32_t roll_fixed, roll_zero;// roll amplitude 0: the roll angle is the same for every photon (zero: no roll)
+  double roll_cos, roll_sin;    // cos and sin of -(float) nominal_roll, when roll_fixed
   // detector
   int32_t nchips, det_extend;   // configured detector's chips: chips[chip_off .. chip_off + nchips)
   int32_t chip_off, pad_chip;
   double det_offset[3], frame_transfer, frame_time, exposure, focal_length;
+  double inv_frame_time;
 };
