@@ -37,6 +37,7 @@ struct BatchIO {
   int32_t nsrc, tile;
   MxRec *q1, *q2;
   unsigned int *ctr;            // [0] q1 entries [1] q2 entries [2..4] work counters of phases A, B, C
+                                // [5] q1 entries of phase B (q1 reused) [6] work counter of phase T
   const uint64_t *seed;         // device scalar, written before each graph launch
 };
 
@@ -83,11 +84,11 @@ __device__ __forceinline__ int source_of(uint32_t i, const uint32_t *start, int 
   return lo;
 }
 
-// The whole batch in one persistent cooperative launch.  The three phases
+// The whole batch in one persistent cooperative launch.  The four phases
 // of the wavefront trace are separated by grid-wide barriers; inside a
 // phase warps claim tiles of work from a counter, so uneven sources and
-// uneven survivor counts spread over every SM.  Every thread reaches both
-// barriers: the claim loops end for a whole warp at once and nothing
+// uneven survivor counts spread over every SM.  Every thread reaches every
+// barrier: the claim loops end for a whole warp at once and nothing
 // returns early.
 __global__ void __launch_bounds__(256) mx_batch_kernel(MxTables T, BatchIO b) {
   MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
@@ -136,7 +137,6 @@ __global__ void __launch_bounds__(256) mx_batch_kernel(MxTables T, BatchIO b) {
         if (mirror_front(T, sh, optc, slope, q, r, m)) {
           keep = true;
           to_rec(rec, q, m, r, i);
-          rec.pad[0] = (uint32_t) s;
         } else
           store_core(io, i, q, r.overrun);
       }
@@ -145,8 +145,34 @@ __global__ void __launch_bounds__(256) mx_batch_kernel(MxTables T, BatchIO b) {
   }
   grid.sync();
 
-  // Phase B: paraboloid reflection, hyperboloid intersection.
-  const uint32_t nb = __ldcg(&b.ctr[0]);
+  // Phase T: the paraboloid's normal blur and reflectivity test.
+  const uint32_t nt = __ldcg(&b.ctr[0]);
+  for (;;) {
+    const uint32_t base = claim(&b.ctr[6], b.tile);
+    if (base >= nt) break;
+    const uint32_t end = min(base + (uint32_t) b.tile, nt);
+    for (uint32_t j = base; j < end; j += 32) {
+      const uint32_t k = j + lane;
+      bool keep = false;
+      MxRec rec;
+      if (k < end) {
+        rec = b.q1[k];
+        Ph q; MirrorState m; Rng r;
+        from_rec(rec, q, m, r, io);
+        if (mirror_ptest(T, sh, q, r, m)) {
+          keep = true;
+          to_rec(rec, q, m, r, rec.i);
+        } else
+          store_core(io, rec.i, q, r.overrun);
+      }
+      append(keep, rec, b.q2, &b.ctr[1]);
+    }
+  }
+  grid.sync();
+
+  // Phase B: the rest of the paraboloid reflection, hyperboloid
+  // intersection and reflectivity test (q1 is free again).
+  const uint32_t nb = __ldcg(&b.ctr[1]);
   for (;;) {
     const uint32_t base = claim(&b.ctr[3], b.tile);
     if (base >= nb) break;
@@ -156,31 +182,29 @@ __global__ void __launch_bounds__(256) mx_batch_kernel(MxTables T, BatchIO b) {
       bool keep = false;
       MxRec rec;
       if (k < end) {
-        rec = b.q1[k];
+        rec = b.q2[k];
         Ph q; MirrorState m; Rng r;
         from_rec(rec, q, m, r, io);
         if (mirror_middle(T, sh, q, r, m)) {
           keep = true;
-          uint32_t s = rec.pad[0];
           to_rec(rec, q, m, r, rec.i);
-          rec.pad[0] = s;
         } else
           store_core(io, rec.i, q, r.overrun);
       }
-      append(keep, rec, b.q2, &b.ctr[1]);
+      append(keep, rec, b.q1, &b.ctr[5]);
     }
   }
   grid.sync();
 
   // Phase C: hyperboloid reflection, the source's grating and detector.
-  const uint32_t nc = __ldcg(&b.ctr[1]);
+  const uint32_t nc = __ldcg(&b.ctr[5]);
   for (;;) {
     const uint32_t base = claim(&b.ctr[4], b.tile);
     if (base >= nc) break;
     const uint32_t end = min(base + (uint32_t) b.tile, nc);
     for (uint32_t k = base + lane; k < end; k += 32) {
-      const MxRec rec = b.q2[k];
-      const MxSourceDev &S = ssrc[rec.pad[0]];
+      const MxRec rec = b.q1[k];
+      const MxSourceDev &S = ssrc[source_of(rec.i, sstart, b.nsrc)];
       const uint32_t i = rec.i;
       Ph q; MirrorState m; Rng r;
       from_rec(rec, q, m, r, io);
@@ -212,7 +236,7 @@ struct mx_batch {
   DevBuf d_src;                 // sources then starts
   DevBuf cols[12];              // photon list columns
   DevBuf queues;                // two record queues
-  DevBuf ctr;                   // 5 counters + seed
+  DevBuf ctr;                   // 7 counters + seed
   uint64_t *h_seed = nullptr;   // pinned, copied into the graph's seed slot
   mx_batch_params params;
   bool have_params = false;
@@ -279,7 +303,7 @@ static int build_graph(mx_batch *b) {
   cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
   if (e != cudaSuccess) return mx_cuda_fail(c, e, "batch capture stream");
   e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
-  if (e == cudaSuccess) e = cudaMemsetAsync(b->ctr.ptr, 0, 5 * sizeof(unsigned int), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->ctr.ptr, 0, 7 * sizeof(unsigned int), st);
   if (e == cudaSuccess) e = cudaMemcpyAsync((char *) b->ctr.ptr + 64, b->h_seed, sizeof(uint64_t), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
     cudaLaunchConfig_t lc;

@@ -208,7 +208,7 @@ int mx_trace_tables(mx_context *c, const MxTables &T, const mx_photons *ph, uint
     w.q2 = (MxRec *) ((char *) c->wave.ptr + qbytes);
     w.counts = (unsigned int *) ((char *) c->wave.ptr + 2 * qbytes);
     e = launch_wavefront(T, io, w, c->num_sms * c->wave_blocks, (int) c->shared_bytes, st);
-    c->launches += 3;
+    c->launches += MX_WAVE_KERNELS;
   } else {
     e = launch_trace(T, io, c->num_sms * c->trace_blocks[slots ? 0 : 1], (int) c->shared_bytes, slots != 0, st);
     c->launches++;

@@ -480,19 +480,27 @@ MXD double wfold_interp(const MxTables &T, int table, double energy, double sin_
   return t0 + (t1 - t0) * (ea - e0) * MX_LDG(T.fold_inv_de + (size_t) table * MX_FOLD_MAX + i - 1);
 }
 
-// reflect_from_conic (hrma.c:488-545) after the intersection: normal blur,
-// reflectivity test, specular reflection and WFold scattering at the
-// intersection point.  Returns -1 if the photon is absorbed (p then holds
-// what the reference leaves in it), 0 if it is reflected.
-MXD int reflect_at(const MxTables &T, const MxShellDev &h, int o, int table, D3 &p, D3 n, double energy,
-                   double beta, double delta, double corr, Rng &rng) {
+// reflect_from_conic (hrma.c:488-545) after the intersection, in two
+// parts so that the wavefront can drop absorbed photons before the rest of
+// the reflection.  reflect_test: normal blur and the reflectivity test;
+// false if the photon is absorbed (p is left as the reference leaves it).
+// pdn receives p.n with the blurred normal n.
+MXD bool reflect_test(const MxTables &T, const MxShellDev &h, int o, D3 p, D3 &n, double &pdn, double beta,
+                      double delta, double corr, Rng &rng) {
   if (T.use_blur) blur_normal(n, h.blur[o], rng);
-  double pdn = dot(p, n);
+  pdn = dot(p, n);
   if (!T.ideal) {
     double r = rng.uniform();
     double rfl = reflectivity(fabs(pdn), beta, delta);
-    if (r >= rfl * corr) return -1;
+    if (r >= rfl * corr) return false;
   }
+  return true;
+}
+// reflect_finish: specular reflection and WFold scattering.  Returns -1 if
+// the scattering angle exceeds pi/4 (p then holds the specular direction,
+// as in the reference), 0 otherwise.
+MXD int reflect_finish(const MxTables &T, const MxShellDev &h, int o, int table, D3 &p, D3 n, double pdn,
+                       double energy, Rng &rng) {
   p = p + (-2.0 * pdn) * n;
   if (!T.use_wfold) return 0;
   double r = rng.uniform();
@@ -554,11 +562,12 @@ MXD bool struts_block(const MxTables &T, int set, D3 x, D3 p) {
 }
 
 // Mirror state carried between the three parts of the HRMA trace: the
-// photon at a conic intersection (OSAC frame of that optic), the inward
-// normal there, and the optical constants at the photon's energy.
+// photon at a conic intersection (OSAC frame of that optic) that passed
+// that optic's reflectivity test, its incoming direction, the blurred
+// normal there and p.n, and the optical constants at the photon's energy.
 struct MirrorState {
   D3 x, p, n;
-  double corr;
+  double corr, pdn;
   float beta, delta;
 };
 
@@ -613,7 +622,7 @@ MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *
     m.delta = interp_f(fe, optc, optc + 2 * T.opt_n, slope + (T.opt_n - 1), T.opt_n);
     if (T.use_scale) {
       const float *ce = optc + 3 * T.opt_n + h.corr_off;
-      m.corr = sqrt((double) interp_f(fe, ce, ce + h.corr_n, slope + h.corr_slope_off, h.corr_n));
+      m.corr = sqrt(f2d(interp_f(fe, ce, ce + h.corr_n, slope + h.corr_slope_off, h.corr_n)));
     }
   }
   D3 n;
@@ -622,12 +631,22 @@ MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *
   return true;
 }
 
-// Part 2: reflection from the paraboloid, back to the MARX frame, cap
-// struts, into the hyperboloid's frame and its intersection.
+// Part 2: normal blur and reflectivity test at the paraboloid.  Returns
+// false if the photon is absorbed there.
+MXD bool mirror_ptest(const MxTables &T, const MxShellDev *shells, Ph &ph, Rng &rng, MirrorState &m) {
+  if (!reflect_test(T, shells[ph.shell], 0, m.p, m.n, m.pdn, m.beta, m.delta, m.corr, rng)) {
+    ph.flags |= MX_PHOTON_UNREFLECTED; ph.x = m.x; ph.p = m.p; return false;
+  }
+  return true;
+}
+
+// Part 3: the rest of the reflection from the paraboloid, back to the MARX
+// frame, cap struts, into the hyperboloid's frame, its intersection, normal
+// blur and reflectivity test.
 MXD bool mirror_middle(const MxTables &T, const MxShellDev *shells, Ph &ph, Rng &rng, MirrorState &m) {
   const MxShellDev &h = shells[ph.shell];
   D3 x = m.x, p = m.p;
-  if (0 != reflect_at(T, h, 0, 2 * ph.shell, p, m.n, ph.e, m.beta, m.delta, m.corr, rng)) {
+  if (0 != reflect_finish(T, h, 0, 2 * ph.shell, p, m.n, m.pdn, ph.e, rng)) {
     ph.flags |= MX_PHOTON_UNREFLECTED; ph.x = x; ph.p = p; return false;
   }
   p = mat_mul(h.bwd[0], p);
@@ -639,16 +658,19 @@ MXD bool mirror_middle(const MxTables &T, const MxShellDev *shells, Ph &ph, Rng 
   x = mat_mul(h.fwd[1], x);
   D3 n;
   if (-1 == conic_intersection(h, 1, x, p, n)) { ph.flags |= MX_PHOTON_UNREFLECTED; ph.x = x; ph.p = p; return false; }
+  if (!reflect_test(T, h, 1, p, n, m.pdn, m.beta, m.delta, m.corr, rng)) {
+    ph.flags |= MX_PHOTON_UNREFLECTED; ph.x = x; ph.p = p; return false;
+  }
   m.x = x; m.p = p; m.n = n;
   return true;
 }
 
-// Part 3: reflection from the hyperboloid, back to the MARX frame,
-// post-collimator struts.  Leaves the photon in ph.
+// Part 4: the rest of the reflection from the hyperboloid, back to the
+// MARX frame, post-collimator struts.  Leaves the photon in ph.
 MXD void mirror_back(const MxTables &T, const MxShellDev *shells, Ph &ph, Rng &rng, MirrorState &m) {
   const MxShellDev &h = shells[ph.shell];
   D3 x = m.x, p = m.p;
-  if (0 != reflect_at(T, h, 1, 2 * ph.shell + 1, p, m.n, ph.e, m.beta, m.delta, m.corr, rng)) {
+  if (0 != reflect_finish(T, h, 1, 2 * ph.shell + 1, p, m.n, m.pdn, ph.e, rng)) {
     ph.flags |= MX_PHOTON_UNREFLECTED; ph.x = x; ph.p = p; return;
   }
   p = mat_mul(h.bwd[1], p);
@@ -661,7 +683,8 @@ MXD void mirror_back(const MxTables &T, const MxShellDev *shells, Ph &ph, Rng &r
 MXD void mirror_stage(const MxTables &T, const MxShellDev *shells, const float *optc, const double *slope, Ph &ph,
                       Rng &rng) {
   MirrorState m;
-  if (mirror_front(T, shells, optc, slope, ph, rng, m) && mirror_middle(T, shells, ph, rng, m))
+  if (mirror_front(T, shells, optc, slope, ph, rng, m) && mirror_ptest(T, shells, ph, rng, m) &&
+      mirror_middle(T, shells, ph, rng, m))
     mirror_back(T, shells, ph, rng, m);
 }
 

@@ -62,14 +62,16 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_trace_kernel(MxTables T, Tr
 }
 
 // ------------------------------------------------------------ wavefront --
-// The same trace as mx_trace_kernel split at the two conic intersections,
-// so that photons lost on the way (between the shells, absorbed by the
-// paraboloid) stop occupying SIMT lanes: phase A runs every photon up to
-// the paraboloid intersection and appends survivors to queue 1; phase B
-// reflects them, intersects the hyperboloid and appends to queue 2; phase
-// C reflects from the hyperboloid and runs the grating and the detector.
-// Appends are warp-aggregated (one atomic per warp); the order of records
-// in a queue does not affect any photon's result.
+// The same trace as mx_trace_kernel split where photons are lost, so that
+// lost photons stop occupying SIMT lanes: phase A runs every photon up to
+// the paraboloid intersection (the photons between the shells are lost
+// there) and appends the rest to queue 1; phase T draws the paraboloid's
+// normal blur and reflectivity test and moves the photons it reflects to
+// queue 2; phase B finishes that reflection, intersects the hyperboloid and
+// applies its reflectivity test, appending survivors to queue 1 again;
+// phase C finishes the hyperboloid reflection and runs the grating and the
+// detector.  Appends are warp-aggregated (one atomic per warp); the order
+// of records in a queue does not affect any photon's result.
 
 __global__ void __launch_bounds__(MX_TRACE_BLOCK, 3) mx_wave_a(MxTables T, TraceIO io, WaveBufs w) {
   MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
@@ -117,10 +119,12 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK, 3) mx_wave_a(MxTables T, Trace
   }
 }
 
-__global__ void __launch_bounds__(MX_TRACE_BLOCK, 3) mx_wave_b(MxTables T, TraceIO io, WaveBufs w) {
-  MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
-  stage_tables(T, sh, gr, ch, optc, slope);
-  const uint32_t count = *(volatile unsigned int *) &w.counts[0];
+// One queue-to-queue phase: records of `in` (count at *in_count) through
+// `step`; survivors are appended to `out`, the rest stored.
+template <typename Step>
+__device__ __forceinline__ void wave_pass(const TraceIO &io, const MxRec *in, const unsigned int *in_count, MxRec *out,
+                                          unsigned int *out_count, Step step) {
+  const uint32_t count = *(volatile const unsigned int *) in_count;
   const uint32_t lane = threadIdx.x & 31, warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t base = warp * 32; base < count; base += nwarps * 32) {
@@ -128,26 +132,40 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK, 3) mx_wave_b(MxTables T, Trace
     bool keep = false;
     MxRec rec;
     if (k < count) {
-      rec = w.q1[k];
+      rec = in[k];
       Ph q; MirrorState m; Rng r;
       from_rec(rec, q, m, r, io);
-      if (mirror_middle(T, sh, q, r, m)) {
+      if (step(q, r, m)) {
         keep = true;
         to_rec(rec, q, m, r, rec.i);
       } else
         store_core(io, rec.i, q, r.overrun);
     }
-    append(keep, rec, w.q2, &w.counts[1]);
+    append(keep, rec, out, out_count);
   }
+}
+
+__global__ void __launch_bounds__(MX_TRACE_BLOCK, 3) mx_wave_t(MxTables T, TraceIO io, WaveBufs w) {
+  MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
+  stage_tables(T, sh, gr, ch, optc, slope);
+  wave_pass(io, w.q1, &w.counts[0], w.q2, &w.counts[1],
+            [&](Ph &q, Rng &r, MirrorState &m) { return mirror_ptest(T, sh, q, r, m); });
+}
+
+__global__ void __launch_bounds__(MX_TRACE_BLOCK, 3) mx_wave_b(MxTables T, TraceIO io, WaveBufs w) {
+  MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
+  stage_tables(T, sh, gr, ch, optc, slope);
+  wave_pass(io, w.q2, &w.counts[1], w.q1, &w.counts[2],
+            [&](Ph &q, Rng &r, MirrorState &m) { return mirror_middle(T, sh, q, r, m); });
 }
 
 __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_wave_c(MxTables T, TraceIO io, WaveBufs w) {
   MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
   stage_tables(T, sh, gr, ch, optc, slope);
-  const uint32_t count = *(volatile unsigned int *) &w.counts[1];
+  const uint32_t count = *(volatile unsigned int *) &w.counts[2];
   const uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += stride) {
-    const MxRec rec = w.q2[k];
+    const MxRec rec = w.q1[k];
     const uint32_t i = rec.i;
     Ph q; MirrorState m; Rng r;
     from_rec(rec, q, m, r, io);
@@ -171,15 +189,18 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_wave_c(MxTables T, TraceIO 
 }
 
 cudaError_t wave_occupancy(int shared_bytes, int *blocks_per_sm) {
-  int b[3];
-  const void *f[3] = {(const void *) mx_wave_a, (const void *) mx_wave_b, (const void *) mx_wave_c};
-  for (int k = 0; k < 3; k++) {
+  const void *f[4] = {(const void *) mx_wave_a, (const void *) mx_wave_t, (const void *) mx_wave_b,
+                      (const void *) mx_wave_c};
+  int best = 1 << 30;
+  for (int k = 0; k < 4; k++) {
+    int b = 0;
     cudaError_t e = cudaFuncSetAttribute(f[k], cudaFuncAttributeMaxDynamicSharedMemorySize, shared_bytes);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[k], f[k], MX_TRACE_BLOCK, shared_bytes);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f[k], MX_TRACE_BLOCK, shared_bytes);
     if (e != cudaSuccess) return e;
+    if (b < best) best = b;
   }
-  *blocks_per_sm = b[0] < b[1] ? (b[0] < b[2] ? b[0] : b[2]) : (b[1] < b[2] ? b[1] : b[2]);
+  *blocks_per_sm = best;
   return cudaSuccess;
 }
 
@@ -188,9 +209,10 @@ cudaError_t launch_wavefront(const MxTables &T, const TraceIO &io, const WaveBuf
   uint32_t need = (io.n + MX_TRACE_BLOCK - 1) / MX_TRACE_BLOCK;
   int ga = (uint32_t) grid > need ? (int) need : grid;
   if (ga < 1) ga = 1;
-  cudaError_t e = cudaMemsetAsync(w.counts, 0, 2 * sizeof(unsigned int), st);
+  cudaError_t e = cudaMemsetAsync(w.counts, 0, 3 * sizeof(unsigned int), st);
   if (e != cudaSuccess) return e;
   mx_wave_a<<<ga, MX_TRACE_BLOCK, shared_bytes, st>>>(T, io, w);
+  mx_wave_t<<<ga, MX_TRACE_BLOCK, shared_bytes, st>>>(T, io, w);
   mx_wave_b<<<ga, MX_TRACE_BLOCK, shared_bytes, st>>>(T, io, w);
   mx_wave_c<<<ga, MX_TRACE_BLOCK, shared_bytes, st>>>(T, io, w);
   return cudaGetLastError();

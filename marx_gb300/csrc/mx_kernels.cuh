@@ -7,6 +7,7 @@
 #include "mx_model.h"
 
 #define MX_TRACE_BLOCK 256
+#define MX_WAVE_KERNELS 4        // kernels of one wavefront trace
 #define MX_COMPACT_THREADS 256
 #define MX_COMPACT_ITEMS 16
 #define MX_COMPACT_TILE (MX_COMPACT_THREADS * MX_COMPACT_ITEMS)
@@ -27,18 +28,20 @@ struct TraceIO {
 
 // One photon between wavefront phases (128 bytes, written and read whole).
 struct __align__(16) MxRec {
-  double x[3], p[3], n[3];      // state at the last conic intersection, and its normal
+  double x[3], p[3], n[3];      // state at the last conic intersection: incoming direction, blurred normal
   double e, t, corr;
   float beta, delta;
   uint32_t i, tag, flags;       // photon index in the list, generator counter, flags
-  uint8_t shell, upos, npos, pad0;
-  uint32_t pad[2];
+ uint8_t shell, upos, npos, overrun;   // overrun: a stage already ran past its variate slots
+  double pdn;                   // p.n with the blurred normal (reflectivity test passed)
 };
 
 // Wavefront scratch: two record queues of n entries and their fill counts.
+// Phase A appends to q1, the paraboloid test moves survivors to q2, phase B
+// appends to q1 again (its first use is over), phase C reads it.
 struct WaveBufs {
   MxRec *q1, *q2;
-  unsigned int *counts;         // [0]: q1 entries, [1]: q2 entries
+  unsigned int *counts;         // [0]: first q1 fill, [1]: q2 fill, [2]: second q1 fill
 };
 
 size_t trace_shared_bytes(const MxTables &T);

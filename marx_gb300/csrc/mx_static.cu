@@ -73,6 +73,6 @@ extern "C" int mx_trace_static(mx_context *c, const mx_photons *ph, uint32_t sta
   w.q2 = (MxRec *) ((char *) scratch + qbytes);
   w.counts = (unsigned int *) ((char *) scratch + 2 * qbytes);
   cudaError_t e = launch_wavefront(c->T, io, w, c->num_sms * c->wave_blocks, (int) c->shared_bytes, (cudaStream_t) stream);
-  c->launches += 3;
+  c->launches += MX_WAVE_KERNELS;
   return e == cudaSuccess ? MX_OK : mx_cuda_fail(c, e, "mx_trace_static: launching the trace kernels");
 }

@@ -61,17 +61,19 @@ __device__ __forceinline__ void to_rec(MxRec &r, const Ph &q, const MirrorState 
   r.n[0] = m.n.x; r.n[1] = m.n.y; r.n[2] = m.n.z;
   r.e = q.e; r.t = q.t; r.corr = m.corr; r.beta = m.beta; r.delta = m.delta;
   r.i = i; r.tag = rng.tag; r.flags = q.flags;
-  r.shell = (uint8_t) q.shell; r.upos = (uint8_t) rng.upos; r.npos = (uint8_t) rng.npos; r.pad0 = 0;
+  r.shell = (uint8_t) q.shell; r.upos = (uint8_t) rng.upos; r.npos = (uint8_t) rng.npos;
+  r.overrun = rng.overrun ? 1 : 0;
+  r.pdn = m.pdn;
 }
 
 __device__ __forceinline__ void from_rec(const MxRec &r, Ph &q, MirrorState &m, Rng &rng, const TraceIO &io) {
   m.x = mk(r.x[0], r.x[1], r.x[2]); m.p = mk(r.p[0], r.p[1], r.p[2]); m.n = mk(r.n[0], r.n[1], r.n[2]);
-  m.corr = r.corr; m.beta = r.beta; m.delta = r.delta;
+  m.corr = r.corr; m.beta = r.beta; m.delta = r.delta; m.pdn = r.pdn;
   q.e = r.e; q.t = r.t; q.flags = r.flags; q.shell = r.shell;
   q.x = m.x; q.p = m.p;
   rng.U = io.U; rng.N = io.N; rng.seed = io.seed; rng.n = io.n; rng.i = r.i; rng.tag = r.tag;
   rng.upos = r.upos; rng.uend = MX_U_MIRROR + 12; rng.npos = r.npos; rng.nend = MX_N_MIRROR + 2;
-  rng.overrun = false;
+  rng.overrun = r.overrun != 0;
 }
 
 // x, p, flags and shell of a photon whose trace ends in this phase.

@@ -169,4 +169,4 @@ def test_launch_count_tracks_kernels(cuda):
     assert eng.launch_count() == before + 1
     eng.set_mode(MODES["wavefront"])
     device_trace(eng, w.photons(1000))
-    assert eng.launch_count() == before + 4
+    assert eng.launch_count() == before + 1 + 4   # phases A, T, B and C
