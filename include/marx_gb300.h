@@ -1,5 +1,5 @@
 /* marx_gb300 — GB300-native photon trace for the MARX stage pipeline
- * (aspect dither -> HRMA mirror -> HETG grating -> ACIS detector).
+ * (aspect dither -> HRMA mirror -> HETG/LETG grating -> ACIS/HRC detector).
  *
  * C ABI: plain pointers, sizes and POD structs.  Every entry point returns
  * 0 on success and a negative MX_E* code on failure; mx_last_error() gives
@@ -60,22 +60,31 @@ extern "C" {
  *   mirror  U[0..11]: [vignetting] shell radius theta,
  *                     per optic P then H: [blur phi] [reflectivity] [wfold p, sign]
  *           N[2..3] : per optic [blur angle]
- *   grating U[12..13]: vignetting, order;  N[4..5]: dtheta, dP/P
- *   detect  U[14..15]: [QE] [streak row];  N[6..7]: reserved (pulse height)
+ *   HETG    U[12..13]: vignetting, order;  N[4..5]: dtheta, dP/P
+ *   ACIS    U[14..15]: [QE] [streak row];  N[6..7]: reserved (pulse height)
+ *   LETG    U[16..21]: vignetting, order, support orders (fine, coarse x3);
+ *           N[8..17] : dtheta, dP/P of the primary, then of each support
+ *   HRC     U[22..27]: MCP QE, UV/ion shield QE, blur component, radius,
+ *                      azimuth (one spare);  N[18..19]: pulse height (one spare)
  *   dither  N[0..1]  : aspect blur ra, dec
  * Slot arrays are slot-major: U[k * n + i] is uniform k of photon i. */
-#define MX_NUM_U 16
-#define MX_NUM_N 8
+#define MX_NUM_U 28
+#define MX_NUM_N 20
 #define MX_U_MIRROR   0
 #define MX_U_GRATING 12
 #define MX_U_DETECT  14
+#define MX_U_LETG    16
+#define MX_U_HRC     22
 #define MX_N_DITHER   0
 #define MX_N_MIRROR   2
 #define MX_N_GRATING  4
 #define MX_N_DETECT   6
+#define MX_N_LETG     8
+#define MX_N_HRC     18
 
-enum { MX_GRATING_NONE = 0, MX_GRATING_HETG = 1 };
-enum { MX_DETECTOR_NONE = 0, MX_DETECTOR_ACIS_I = 1, MX_DETECTOR_ACIS_S = 2 };
+enum { MX_GRATING_NONE = 0, MX_GRATING_HETG = 1, MX_GRATING_LETG = 2 };
+enum { MX_DETECTOR_NONE = 0, MX_DETECTOR_ACIS_I = 1, MX_DETECTOR_ACIS_S = 2, MX_DETECTOR_HRC_I = 3,
+       MX_DETECTOR_HRC_S = 4 };
 enum { MX_DITHER_NONE = 0, MX_DITHER_INTERNAL = 1 };
 
 /* Simulation parameters.  Names follow marx.par; units are marx.par's. */
@@ -121,6 +130,23 @@ typedef struct mx_config {
   double acis_frame_transfer_time; /* ACIS_Frame_Transfer_Time (s) */
   double focal_length;        /* Marx_Focal_Length (detpix.c:41) (mm) */
   double start_time;          /* Marx_Photon_Type.start_time (s) */
+  /* LETG (diffract.c:1727-1860; marx.par LETG_Shell*, leg*) */
+  double letg_theta[4];       /* LETG_Shell{1,3,4,6}_Theta (deg) */
+  double letg_dtheta[4];      /* LETG_Shell*_dTheta (arcmin, sigma) */
+  double letg_period[4];      /* LETG_Shell*_Period (um) */
+  double letg_dpp[4];         /* LETG_Shell*_dPoverP */
+  double letg_vig[4];         /* LETG_Shell*_Vig */
+  double leg_rowland;         /* LEGRowlandDiameter (mm) */
+  double letg_acis_dtheta;    /* LETG_ACIS_dTheta (deg), added with an ACIS detector */
+  int32_t leg_fine_orders;    /* legFineNumOrders (2n+1; 0: no fine support grating) */
+  int32_t leg_coarse_orders;  /* legCoarseNumOrders (2n+1; 0: no coarse support grating) */
+  double leg_fine_period, leg_fine_bar_height, leg_fine_bar_width;       /* legFine* (um) */
+  double leg_coarse_period, leg_coarse_bar_height, leg_coarse_bar_width; /* legCoarse* (um) */
+  /* HRC (hrc-i.c, hrc-s.c, hrcblur.c) */
+  int32_t det_ideal;          /* DetIdeal: no QE, no HRC position blur */
+  int32_t reserved2;
+  double hrc_i_blur[13];      /* HRC-I-Blur{G1FWHM,G1Xctr,G1Yctr,G1Amp,G2..,L1FWHM,L1Xctr,L1Yctr,L1Amp,L1Rmax} */
+  double hrc_s_blur[13];      /* the same for HRC-S (1/4 pixels) */
 } mx_config;
 
 /* Structure-of-arrays photon list.  3-vectors are component-major:
@@ -144,6 +170,11 @@ typedef struct mx_photons {
   float    *y_pixel;       /* chip x (0-based) */
   float    *z_pixel;       /* chip y (0-based) */
   float    *dither_state;  /* 3n: ra, dec, roll (rad), as Marx_Dither_Type */
+  int8_t   *support_orders;/* 4n: LETG fine and three coarse support orders */
+  int16_t  *pulse_height;  /* HRC pulse height */
+  float    *u_pixel;       /* HRC-S u, v pixel */
+  float    *v_pixel;
+  uint8_t  *detector_region; /* HRC-S UV/ion shield region */
 } mx_photons;
 
 /* Pre-drawn variates (device pointers for mx_trace).  When both are NULL

@@ -63,7 +63,7 @@ class DevicePhotons:
         import torch
         self.n = int(n)
         tmap = {np.float64: torch.float64, np.float32: torch.float32, np.uint32: torch.int32,
-                np.int8: torch.int8}
+                np.int8: torch.int8, np.int16: torch.int16, np.uint8: torch.uint8}
         for k, (dt, m) in COLUMNS.items():
             shape = (m, self.n) if m > 1 else (self.n,)
             setattr(self, k, torch.zeros(shape, dtype=tmap[dt], device=device))
@@ -93,7 +93,9 @@ class DevicePhotons:
         s = MxPhotons()
         s.n = self.n
         for k in COLUMNS:
-            t = getattr(self, k)
+            t = getattr(self, k, None)
+            if t is None:
+                continue
             assert t.is_contiguous()
             setattr(s, k, t.data_ptr())
         return s

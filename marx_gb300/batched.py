@@ -146,6 +146,8 @@ class Batch:
         out = {}
         code = {np.float64: "<f8", np.float32: "<f4", np.uint32: "<i4", np.int8: "|i1"}
         for k, (dt, m) in COLUMNS.items():
+            if not getattr(s, k):       # columns a batch does not carry (LETG, HRC outputs)
+                continue
             shape = (m, self.n) if m > 1 else (self.n,)
             out[k] = torch.as_tensor(_DevArray(getattr(s, k), shape, code[dt]), device="cuda")
         return out

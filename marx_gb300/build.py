@@ -30,7 +30,10 @@ def nvcc() -> str:
 
 
 def _flags(src: str, verbose: bool):
-    f = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-lineinfo", "--expt-relaxed-constexpr"]
+    # host code: no fused multiply-add contraction (gcc contracts by default on
+    # aarch64), so the init-time tables round as the reference's do
+    f = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-lineinfo",
+         "--expt-relaxed-constexpr"]
     if src.endswith(".cu"):
         f += ARCH
         if verbose:

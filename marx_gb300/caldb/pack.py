@@ -2,7 +2,9 @@
 
 The trace needs the HRMA shell geometry, the iridium optical constants, the
 per-shell effective-area correction factors, the WFold scattering tables, the
-HETG grating efficiencies and facet sector tables, and the ACIS chip corners.
+HETG and LETG grating efficiencies, the grating optical constants (for the
+LETG support gratings), the HETG facet sector tables, the ACIS chip corners
+and the HRC geometry and efficiency tables.
 MARX reads them at init from its data directory in four formats (RDB text,
 big-endian "bdat" float tables, the WFold binary format and FITS binary
 tables).  ``build_pack`` reads those files once and writes every table into a
@@ -242,6 +244,15 @@ def build_sections(data_dir: str) -> dict:
         c = byname[f"AXAF_GREFF{i + 1}"]
         S[f"hetg/geff{i}/energy"] = np.asarray(c["ENERGY"], dtype=np.float32)
         S[f"hetg/geff{i}/eff"] = np.ascontiguousarray(np.asarray(c["EFF"], dtype=np.float32).T)
+    geff = read_fits_bintables(os.path.join(data_dir, "caldb", "letgD1996-11-01greffpr001N0007.fits"))
+    byname = {h.get("HDUNAME", ""): c for h, c in geff}
+    for i in range(4):
+        c = byname[f"AXAF_GREFF{i + 1}"]
+        S[f"letg/geff{i}/energy"] = np.asarray(c["ENERGY"], dtype=np.float32)
+        S[f"letg/geff{i}/eff"] = np.ascontiguousarray(np.asarray(c["EFF"], dtype=np.float32).T)
+    # energy, beta, delta and the transmissions of gold, polyimide, chromium
+    # and nickel (read_grating_optical_consts, diffract.c:195-258)
+    S["grating/optconst"] = read_bdat(os.path.join(data_dir, "grating", "optical-constants.dat"))
     sector_files = {1: "hetgmp1D1996-11-01marxsectorN0002.tbl", 3: "hetgmp3D1996-11-01marxsectorN0002.tbl",
                     4: "hetgmp4D1996-11-01marxsectorN0003.tbl", 6: "hetgmp6D1996-11-01marxsectorN0003.tbl"}
     for s, fn in sector_files.items():

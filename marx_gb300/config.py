@@ -11,8 +11,11 @@ from __future__ import annotations
 import ctypes as C
 
 SHELLS = (1, 3, 4, 6)
-GRATING = {"NONE": 0, "HETG": 1}
-DETECTOR = {"NONE": 0, "ACIS-I": 1, "ACIS-S": 2}
+GRATING = {"NONE": 0, "HETG": 1, "LETG": 2}
+DETECTOR = {"NONE": 0, "ACIS-I": 1, "ACIS-S": 2, "HRC-I": 3, "HRC-S": 4}
+# HRC blur parameter suffixes, in the order of mx_config.hrc_*_blur
+HRC_BLUR = ("G1FWHM", "G1Xctr", "G1Yctr", "G1Amp", "G2FWHM", "G2Xctr", "G2Yctr", "G2Amp",
+            "L1FWHM", "L1Xctr", "L1Yctr", "L1Amp", "L1Rmax")
 DITHER = {"NONE": 0, "INTERNAL": 1}
 
 
@@ -42,6 +45,15 @@ class MxConfig(C.Structure):
         ("acis_exposure_time", C.c_double), ("acis_frame_transfer_time", C.c_double),
         ("focal_length", C.c_double),
         ("start_time", C.c_double),
+        ("letg_theta", C.c_double * 4), ("letg_dtheta", C.c_double * 4),
+        ("letg_period", C.c_double * 4), ("letg_dpp", C.c_double * 4), ("letg_vig", C.c_double * 4),
+        ("leg_rowland", C.c_double), ("letg_acis_dtheta", C.c_double),
+        ("leg_fine_orders", C.c_int32), ("leg_coarse_orders", C.c_int32),
+        ("leg_fine_period", C.c_double), ("leg_fine_bar_height", C.c_double), ("leg_fine_bar_width", C.c_double),
+        ("leg_coarse_period", C.c_double), ("leg_coarse_bar_height", C.c_double),
+        ("leg_coarse_bar_width", C.c_double),
+        ("det_ideal", C.c_int32), ("reserved2", C.c_int32),
+        ("hrc_i_blur", C.c_double * 13), ("hrc_s_blur", C.c_double * 13),
     ]
 
 
@@ -78,6 +90,21 @@ def default_config() -> MxConfig:
     c.acis_exposure_time, c.acis_frame_transfer_time = 3.2, 0.041
     c.focal_length = 10065.5
     c.start_time = 0.0
+    c.letg_theta[:] = [0.07] * 4
+    c.letg_dtheta[:] = [0.617] * 4
+    c.letg_period[:] = [0.991216] * 4
+    c.letg_dpp[:] = [78e-6] * 4
+    c.letg_vig[:] = [1.0] * 4
+    c.leg_rowland = 8637.0
+    c.letg_acis_dtheta = -0.0867
+    c.leg_fine_orders, c.leg_coarse_orders = 19, 121
+    c.leg_fine_period, c.leg_fine_bar_height, c.leg_fine_bar_width = 25.4, 2.5, 2.5
+    c.leg_coarse_period, c.leg_coarse_bar_height, c.leg_coarse_bar_width = 2000.0, 26.0, 68.0
+    c.det_ideal = 0
+    c.hrc_i_blur[:] = [13.8994, 64.1124, 64.5285, 15.7528, 4.25636, 61.35, 64.178, 0.0,
+                       10.8269, 73.3361, 63.9927, 0.0, 256.0]
+    c.hrc_s_blur[:] = [13.900, 64.110, 64.530, 15.750, 4.2560, 67.420, 64.110, 0.0,
+                       10.820, 53.030, 63.880, 0.0, 256.000]
     return c
 
 
@@ -117,7 +144,16 @@ def to_par(c: MxConfig) -> dict:
         "ACIS_Exposure_Time": repr(c.acis_exposure_time),
         "ACIS_Frame_Transfer_Time": repr(c.acis_frame_transfer_time),
         "Verbose": "0",
+        "LEGRowlandDiameter": repr(c.leg_rowland), "LETG_ACIS_dTheta": repr(c.letg_acis_dtheta),
+        "legFineNumOrders": str(c.leg_fine_orders), "legCoarseNumOrders": str(c.leg_coarse_orders),
+        "legFinePeriod": repr(c.leg_fine_period), "legFineBarHeight": repr(c.leg_fine_bar_height),
+        "legFineBarWidth": repr(c.leg_fine_bar_width), "legCoarsePeriod": repr(c.leg_coarse_period),
+        "legCoarseBarHeight": repr(c.leg_coarse_bar_height), "legCoarseBarWidth": repr(c.leg_coarse_bar_width),
+        "DetIdeal": _yn(c.det_ideal),
     }
+    for k, name in enumerate(HRC_BLUR):
+        P[f"HRC-I-Blur{name}"] = repr(c.hrc_i_blur[k])
+        P[f"HRC-S-Blur{name}"] = repr(c.hrc_s_blur[k])
     for i, s in enumerate(SHELLS):
         P[f"HRMA_P{s}H{s}_XOffset"] = repr(c.shell_xoffset[i])
         P[f"P{s}Blur"], P[f"H{s}Blur"] = repr(c.blur_p[i]), repr(c.blur_h[i])
@@ -128,6 +164,11 @@ def to_par(c: MxConfig) -> dict:
         P[f"HETG_Shell{s}_Period"] = repr(c.hetg_period[i])
         P[f"HETG_Shell{s}_dPoverP"] = repr(c.hetg_dpp[i])
         P[f"HETG_Shell{s}_Vig"] = repr(c.hetg_vig[i])
+        P[f"LETG_Shell{s}_Theta"] = repr(c.letg_theta[i])
+        P[f"LETG_Shell{s}_dTheta"] = repr(c.letg_dtheta[i])
+        P[f"LETG_Shell{s}_Period"] = repr(c.letg_period[i])
+        P[f"LETG_Shell{s}_dPoverP"] = repr(c.letg_dpp[i])
+        P[f"LETG_Shell{s}_Vig"] = repr(c.letg_vig[i])
     for k, ax in enumerate(("RA", "Dec", "Roll")):
         P[f"DitherAmp_{ax}"] = repr(c.dither_amp[k])
         P[f"DitherPeriod_{ax}"] = repr(c.dither_period[k])
@@ -167,6 +208,23 @@ def from_par(path: str, overrides: dict | None = None) -> MxConfig:
         c.hetg_period[i] = num(f"HETG_Shell{s}_Period", c.hetg_period[i])
         c.hetg_dpp[i] = num(f"HETG_Shell{s}_dPoverP", c.hetg_dpp[i])
         c.hetg_vig[i] = num(f"HETG_Shell{s}_Vig", c.hetg_vig[i])
+        c.letg_theta[i] = num(f"LETG_Shell{s}_Theta", c.letg_theta[i])
+        c.letg_dtheta[i] = num(f"LETG_Shell{s}_dTheta", c.letg_dtheta[i])
+        c.letg_period[i] = num(f"LETG_Shell{s}_Period", c.letg_period[i])
+        c.letg_dpp[i] = num(f"LETG_Shell{s}_dPoverP", c.letg_dpp[i])
+        c.letg_vig[i] = num(f"LETG_Shell{s}_Vig", c.letg_vig[i])
+    c.leg_rowland = num("LEGRowlandDiameter", c.leg_rowland)
+    c.letg_acis_dtheta = num("LETG_ACIS_dTheta", c.letg_acis_dtheta)
+    c.leg_fine_orders = int(num("legFineNumOrders", c.leg_fine_orders))
+    c.leg_coarse_orders = int(num("legCoarseNumOrders", c.leg_coarse_orders))
+    for k in ("period", "bar_height", "bar_width"):
+        name = "".join(w.capitalize() for w in k.split("_"))
+        setattr(c, f"leg_fine_{k}", num(f"legFine{name}", getattr(c, f"leg_fine_{k}")))
+        setattr(c, f"leg_coarse_{k}", num(f"legCoarse{name}", getattr(c, f"leg_coarse_{k}")))
+    c.det_ideal = yes("DetIdeal", c.det_ideal)
+    for k, name in enumerate(HRC_BLUR):
+        c.hrc_i_blur[k] = num(f"HRC-I-Blur{name}", c.hrc_i_blur[k])
+        c.hrc_s_blur[k] = num(f"HRC-S-Blur{name}", c.hrc_s_blur[k])
     if "GratingType" in vals:
         c.grating = GRATING[vals["GratingType"]]
     c.use_sector_files = yes("Use_HETG_Sector_Files", c.use_sector_files)

@@ -51,6 +51,8 @@ __device__ __forceinline__ void generate_photon(const MxSourceDev &S, uint64_t s
   q.flags = 0u;
   q.shell = 0; q.order = 0; q.ccd = -1; q.ypix = q.zpix = 0.f;
   q.dith[0] = q.dith[1] = q.dith[2] = 0.f;
+  q.set = 0;
+  for (int k = 0; k < 4; k++) q.sup[k] = 0;
 }
 
 __global__ void __launch_bounds__(256) mx_generate_kernel(MxSourceDev S, uint32_t first_tag, uint64_t seed,
@@ -120,6 +122,7 @@ __global__ void __launch_bounds__(256) mx_batch_kernel(MxTables T, BatchIO b) {
         const int s = source_of(i, sstart, b.nsrc);
         Ph q;
         generate_photon(ssrc[s], seed, i, q);
+        clear_extra(io, i);
         io.energy[i] = q.e;
         if (io.t) io.t[i] = 0.0;
         if (io.tag) io.tag[i] = i;
@@ -211,9 +214,10 @@ __global__ void __launch_bounds__(256) mx_batch_kernel(MxTables T, BatchIO b) {
       const int unset = 0x7fff;
       q.order = unset; q.ccd = unset;
       mirror_back(T, sh, q, r, m);
-      if (!r.overrun && S.grating && !(q.flags & MX_BAD_PHOTON_MASK)) grating_stage(T, gr, q, r);
+      if (!r.overrun && S.grating && !(q.flags & MX_BAD_PHOTON_MASK)) grating_stage(T, gr, S.grating, q, r);
       if (!r.overrun && S.nchips && !(q.flags & MX_BAD_PHOTON_MASK)) detect_stage(T, ch + S.chip_off, S.nchips, q, r);
       store_core(io, i, q, r.overrun);
+      store_extra(io, i, q);
       if (q.order != unset && io.order) io.order[i] = (int8_t) q.order;
       if (q.ccd != unset) {
         if (io.ccd) io.ccd[i] = (int8_t) q.ccd;
@@ -286,6 +290,8 @@ static int build_graph(mx_batch *b) {
   io.io.energy = d.energy; io.io.x = d.x; io.io.p = d.p; io.io.t = d.arrival_time; io.io.flags = d.flags;
   io.io.tag = d.tag; io.io.shell = d.mirror_shell; io.io.order = d.order; io.io.ccd = d.ccd_num;
   io.io.ypix = d.y_pixel; io.io.zpix = d.z_pixel; io.io.dith = d.dither_state;
+  io.io.support = d.support_orders; io.io.pha = d.pulse_height; io.io.upix = d.u_pixel; io.io.vpix = d.v_pixel;
+  io.io.region = d.detector_region;
   io.io.U = nullptr; io.io.N = nullptr; io.io.n = d.n; io.io.stride = d.n; io.io.stages = MX_STAGE_ALL; io.io.fresh = 1;
   io.io.overrun = c->d_overrun;
   io.src = (const MxSourceDev *) b->d_src.ptr;

@@ -42,6 +42,8 @@ static int upload_model(mx_context *c) {
          o_sl = put(blob, M.optc_slope), o_fi = put(blob, M.fold_inv_de),
          o_ge = put(blob, M.geff_energy), o_gc = put(blob, M.geff_cum), o_ok = put(blob, M.order_k),
          o_se = put(blob, M.sectors), o_ch = put(blob, M.chips);
+  if (M.support_energy.empty()) { M.support_energy.push_back(0.f); M.support_cum.push_back(0.f); M.support_k.push_back(0.0); }
+  size_t o_pe = put(blob, M.support_energy), o_pc = put(blob, M.support_cum), o_pk = put(blob, M.support_k);
   cudaError_t e = c->tables.ensure(blob.size());
   if (e != cudaSuccess) return cuda_fail(c, e, "allocating device tables");
   e = cudaMemcpy(c->tables.ptr, blob.data(), blob.size(), cudaMemcpyHostToDevice);
@@ -61,6 +63,9 @@ static int upload_model(mx_context *c) {
   c->T.order_k = (const double *) (b + o_ok);
   c->T.sectors = (const double *) (b + o_se);
   c->T.chips = (const MxChipDev *) (b + o_ch);
+  c->T.support_energy = (const float *) (b + o_pe);
+  c->T.support_cum = (const float *) (b + o_pc);
+  c->T.support_k = (const double *) (b + o_pk);
   c->shared_bytes = trace_shared_bytes(c->T);
   if (c->shared_bytes > 200 * 1024) return fail(c, MX_ERANGE, "tables exceed the shared-memory budget");
   return MX_OK;
@@ -115,6 +120,20 @@ void mx_config_default(mx_config *c) {
   c->detector = MX_DETECTOR_ACIS_S;
   c->acis_exposure_time = 3.2; c->acis_frame_transfer_time = 0.041;
   c->focal_length = 10065.5;
+  for (int i = 0; i < 4; i++) {
+    c->letg_theta[i] = 0.07; c->letg_dtheta[i] = 0.617; c->letg_period[i] = 0.991216;
+    c->letg_dpp[i] = 78e-6; c->letg_vig[i] = 1.0;
+  }
+  c->leg_rowland = 8637.0;
+  c->letg_acis_dtheta = -0.0867;
+  c->leg_fine_orders = 19; c->leg_coarse_orders = 121;
+  c->leg_fine_period = 25.4; c->leg_fine_bar_height = 2.5; c->leg_fine_bar_width = 2.5;
+  c->leg_coarse_period = 2000.0; c->leg_coarse_bar_height = 26.0; c->leg_coarse_bar_width = 68.0;
+  static const double bi[13] = {13.8994, 64.1124, 64.5285, 15.7528, 4.25636, 61.35, 64.178, 0.0,
+                                10.8269, 73.3361, 63.9927, 0.0, 256.0};
+  static const double bs[13] = {13.900, 64.110, 64.530, 15.750, 4.2560, 67.420, 64.110, 0.0,
+                                10.820, 53.030, 63.880, 0.0, 256.000};
+  for (int k = 0; k < 13; k++) { c->hrc_i_blur[k] = bi[k]; c->hrc_s_blur[k] = bs[k]; }
 }
 
 mx_context *mx_create(const char *pack_path, const mx_config *cfg) {
@@ -191,6 +210,8 @@ int mx_trace_tables(mx_context *c, const MxTables &T, const mx_photons *ph, uint
   io.energy = ph->energy; io.x = ph->x; io.p = ph->p; io.t = ph->arrival_time; io.flags = ph->flags;
   io.tag = ph->tag; io.shell = ph->mirror_shell; io.order = ph->order; io.ccd = ph->ccd_num;
   io.ypix = ph->y_pixel; io.zpix = ph->z_pixel; io.dith = ph->dither_state;
+  io.support = ph->support_orders; io.pha = ph->pulse_height; io.upix = ph->u_pixel; io.vpix = ph->v_pixel;
+  io.region = ph->detector_region;
   io.U = U; io.N = N; io.n = ph->n; io.seed = seed; io.stages = stages; io.fresh = fresh ? 1 : 0;
   io.stride = ph->stride ? ph->stride : ph->n;
   if (io.stride < io.n) return fail(c, MX_EINVAL, "mx_trace: stride below n");
@@ -232,15 +253,18 @@ int mx_trace_host(mx_context *c, const mx_photons *h, uint32_t stages, const mx_
   if (!h->energy || !h->p) return fail(c, MX_EINVAL, "mx_trace_host: energy and p are required");
   if (h->stride && h->stride != h->n) return fail(c, MX_EINVAL, "mx_trace_host: host lists must be contiguous (stride 0 or n)");
   struct Col { const void *host; size_t elem; int comps; bool in, out; };
-  const Col cols[12] = {
+  const int NC = 17;
+  const Col cols[NC] = {
       {h->energy, 8, 1, true, false},     {h->x, 8, 3, false, true},         {h->p, 8, 3, true, true},
       {h->arrival_time, 8, 1, true, false}, {h->flags, 4, 1, true, true},   {h->tag, 4, 1, true, false},
       {h->mirror_shell, 1, 1, false, true}, {h->order, 1, 1, false, true},   {h->ccd_num, 1, 1, false, true},
-      {h->y_pixel, 4, 1, false, true},    {h->z_pixel, 4, 1, false, true},   {h->dither_state, 4, 3, false, true}};
-  void *dev[12];
+      {h->y_pixel, 4, 1, false, true},    {h->z_pixel, 4, 1, false, true},   {h->dither_state, 4, 3, false, true},
+      {h->support_orders, 1, 4, false, true}, {h->pulse_height, 2, 1, false, true}, {h->u_pixel, 4, 1, false, true},
+      {h->v_pixel, 4, 1, false, true},    {h->detector_region, 1, 1, false, true}};
+  void *dev[NC];
   cudaStream_t st = c->stream;
   cudaError_t e;
-  for (int k = 0; k < 12; k++) {
+  for (int k = 0; k < NC; k++) {
     dev[k] = nullptr;
     if (!cols[k].host) continue;
     size_t bytes = n * cols[k].elem * cols[k].comps;
@@ -251,11 +275,11 @@ int mx_trace_host(mx_context *c, const mx_photons *h, uint32_t stages, const mx_
   }
   const double *dU = nullptr, *dN = nullptr;
   if (hv && hv->U && hv->N) {
-    if ((e = c->io[12].ensure(n * MX_NUM_U * 8)) != cudaSuccess || (e = c->io[13].ensure(n * MX_NUM_N * 8)) != cudaSuccess)
+    if ((e = c->io[NC].ensure(n * MX_NUM_U * 8)) != cudaSuccess || (e = c->io[NC + 1].ensure(n * MX_NUM_N * 8)) != cudaSuccess)
       return cuda_fail(c, e, "allocating variate buffers");
-    cudaMemcpyAsync(c->io[12].ptr, hv->U, n * MX_NUM_U * 8, cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(c->io[13].ptr, hv->N, n * MX_NUM_N * 8, cudaMemcpyHostToDevice, st);
-    dU = (const double *) c->io[12].ptr; dN = (const double *) c->io[13].ptr;
+    cudaMemcpyAsync(c->io[NC].ptr, hv->U, n * MX_NUM_U * 8, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(c->io[NC + 1].ptr, hv->N, n * MX_NUM_N * 8, cudaMemcpyHostToDevice, st);
+    dU = (const double *) c->io[NC].ptr; dN = (const double *) c->io[NC + 1].ptr;
   }
   mx_photons d;
   memset(&d, 0, sizeof(d));
@@ -264,9 +288,11 @@ int mx_trace_host(mx_context *c, const mx_photons *h, uint32_t stages, const mx_
   d.arrival_time = (double *) dev[3]; d.flags = (uint32_t *) dev[4]; d.tag = (uint32_t *) dev[5];
   d.mirror_shell = (int8_t *) dev[6]; d.order = (int8_t *) dev[7]; d.ccd_num = (int8_t *) dev[8];
   d.y_pixel = (float *) dev[9]; d.z_pixel = (float *) dev[10]; d.dither_state = (float *) dev[11];
+  d.support_orders = (int8_t *) dev[12]; d.pulse_height = (int16_t *) dev[13]; d.u_pixel = (float *) dev[14];
+  d.v_pixel = (float *) dev[15]; d.detector_region = (uint8_t *) dev[16];
   int r = mx_trace_tables(c, c->T, &d, stages, dU, dN, seed, st, true);
   if (r) return r;
-  for (int k = 0; k < 12; k++) {
+  for (int k = 0; k < NC; k++) {
     if (!cols[k].host || !cols[k].out) continue;
     size_t bytes = n * cols[k].elem * cols[k].comps;
     if ((e = cudaMemcpyAsync((void *) cols[k].host, dev[k], bytes, cudaMemcpyDeviceToHost, st)) != cudaSuccess)

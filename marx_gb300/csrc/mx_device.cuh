@@ -357,7 +357,16 @@ struct Ph {
   uint32_t flags;
   int shell, order, ccd;
   float ypix, zpix, dith[3];
+  // outputs of the LETG and HRC stages, valid where `set` says so
+  int8_t sup[4];               // LETG support orders (set bit 1)
+  int16_t pha;                 // HRC pulse height    (set bit 2)
+  uint8_t region;              // HRC-S shield region (set bit 2)
+  uint8_t set;
+  float upix, vpix;            // HRC-S u, v pixel    (set bit 4)
 };
+#define MX_SET_SUPPORT 1u
+#define MX_SET_HRC 2u
+#define MX_SET_UV 4u
 
 // ------------------------------------------------------------- mirror --
 // JDMquadratic_root (qroot.c:36-70), same cancellation-free form.
@@ -763,7 +772,8 @@ MXD int rowland_intersect(D3 &x0, D3 p, double rowland) {
   return -1;
 }
 
-// diffract_photon (diffract.c:706-823), HETG (theta = 0) with facet sectors.
+// diffract_photon (diffract.c:706-823) for a primary grating (theta = 0)
+// with facet sectors when the grating has them.
 MXD int diffract_photon(const MxTables &T, const MxGratingDev &g, int order_idx, double energy,
                         D3 x, D3 &P, Rng &rng) {
   double nlod = MX_LDG(T.order_k + g.order_off + order_idx) / energy;
@@ -805,21 +815,12 @@ MXD int diffract_photon(const MxTables &T, const MxGratingDev &g, int order_idx,
   return 0;
 }
 
-// diffract (diffract.c:974-1130) for one photon: vignetting, rotation into
-// the grating frame, Rowland torus, cumulative order efficiencies at this
-// energy (JDMinterpolate_n_fvector, finterpo.c:134-190), order choice
-// (diffract_photon_from_grating, diffract.c:828-849) and rotation back.
-MXD void grating_stage(const MxTables &T, const MxGratingDev *grs, Ph &ph, Rng &rng) {
-  rng.window(MX_U_GRATING, 2, MX_N_GRATING, 2);
-  const MxGratingDev &g = grs[ph.shell];
-  if (rng.uniform() > g.vig) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
-  if (ph.flags & MX_BAD_PHOTON_MASK) return;
-  D3 x = rot_x(ph.x, g.cos_m, g.sin_m), p = rot_x(ph.p, g.cos_m, g.sin_m);
-  if (-1 == rowland_intersect(x, p, g.rowland)) ph.flags |= MX_PHOTON_UNDIFFRACTED;
-  // bracket the energy: first index >= 1 with E <= energies[idx], capped at n-1
-  float fe = (float) ph.e;
-  const float *ge = T.geff_energy + g.geff_off;
-  unsigned n = (unsigned) g.nenergy;
+// Cumulative order efficiencies at energy fe (JDMinterpolate_n_fvector,
+// finterpo.c:134-190: first bracket index >= 1 with E <= energies[idx],
+// capped at n-1; each order's value rounded to float) and the order choice
+// of diffract_photon_from_grating (diffract.c:828-849): the first index
+// whose cumulative efficiency reaches r, or -1.  cum is [energy][order].
+MXD int choose_order(const float *ge, unsigned n, const float *cum, int norders, float fe, double r) {
   unsigned lo = 1, hi = n - 1;
   while (lo < hi) {
     unsigned mid = (lo + hi) >> 1;
@@ -828,22 +829,79 @@ MXD void grating_stage(const MxTables &T, const MxGratingDev *grs, Ph &ph, Rng &
   unsigned idx = lo;
   double x0 = MX_LDG(ge + idx - 1), x1 = MX_LDG(ge + idx), dx = MX_DADD(x1, -x0);
   double w = MX_DADD((double) fe, -x0);
-  const float *c0 = T.geff_cum + g.cum_off + (size_t) (idx - 1) * g.norders;   // [energy][order]
-  double r = rng.uniform();
-  int chosen = -1;
-  for (int k = 0; k < g.norders; k++) {
+  const float *c0 = cum + (size_t) (idx - 1) * norders;
+  for (int k = 0; k < norders; k++) {
     float ck;
     if (dx == 0.0) ck = MX_LDG(c0 + k);
     else {
-      double y0 = MX_LDG(c0 + k), y1 = MX_LDG(c0 + g.norders + k);
+      double y0 = MX_LDG(c0 + k), y1 = MX_LDG(c0 + norders + k);
       ck = (float) MX_DADD(y0, MX_DDIV(MX_DMUL(MX_DADD(y1, -y0), w), dx));
     }
-    if (r <= (double) ck) { chosen = k; break; }
+    if (r <= (double) ck) return k;
   }
+  return -1;
+}
+
+// diffract_photon for an LETG support grating (diffract_from_support_grating,
+// diffract.c:917-970): no facet sectors, no alignment blur and no dP/P
+// (both zero for the support gratings, though their normals are still
+// drawn), the facet basis rotated about n by the support's fixed angle.
+MXD int diffract_support(const MxTables &T, const MxSupportDev &g, int order_idx, double energy, D3 x, D3 &P,
+                         Rng &rng) {
+  double nlod = MX_LDG(T.support_k + g.order_off + order_idx) / energy;
+  D3 n = -1.0 * normalized(x);
+  D3 l = normalized(mk(n.z, 0.0, -n.x));
+  D3 d = cross(n, l);
+  (void) rng.normal();   // dtheta = 0 x N
+  (void) rng.normal();   // dP/P = 0 x N
+  if (g.rotate) {
+    D3 lt = l, dt = d;
+    l = g.cos_t * lt + g.sin_t * dt;
+    d = (-g.sin_t) * lt + g.cos_t * dt;
+  }
+  D3 p = P;
+  double p_d = nlod + dot(p, d), p_l = dot(p, l);
+  double p_n = 1.0 - p_l * p_l - p_d * p_d;
+  if (p_n < 0.0) return -1;
+  p_n = sqrt(p_n);
+  P = p_d * d + p_n * n + p_l * l;
+  return 0;
+}
+
+// diffract (diffract.c:974-1130) for one photon: vignetting, rotation into
+// the grating frame, Rowland torus, the primary grating's order and
+// diffraction, for the LETG the four support gratings (fine, then coarse
+// at 60, 120 and 0 degrees), and the rotation back.
+MXD void grating_stage(const MxTables &T, const MxGratingDev *grs, int kind, Ph &ph, Rng &rng) {
+  const bool letg = kind == MX_GRATING_LETG;
+  if (letg) rng.window(MX_U_LETG, 6, MX_N_LETG, 10);
+  else rng.window(MX_U_GRATING, 2, MX_N_GRATING, 2);
+  const MxGratingDev &g = grs[(letg ? 4 : 0) + ph.shell];
+  if (rng.uniform() > g.vig) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
+  if (ph.flags & MX_BAD_PHOTON_MASK) return;
+  D3 x = rot_x(ph.x, g.cos_m, g.sin_m), p = rot_x(ph.p, g.cos_m, g.sin_m);
+  if (-1 == rowland_intersect(x, p, g.rowland)) ph.flags |= MX_PHOTON_UNDIFFRACTED;
+  float fe = (float) ph.e;
+  int chosen = choose_order(T.geff_energy + g.geff_off, (unsigned) g.nenergy, T.geff_cum + g.cum_off, g.norders, fe,
+                            rng.uniform());
   if (chosen < 0) ph.flags |= MX_PHOTON_UNDIFFRACTED;
   else {
     ph.order = chosen - g.max_order;
     if (-1 == diffract_photon(T, g, chosen, ph.e, x, p, rng)) ph.flags |= MX_PHOTON_UNDIFFRACTED;
+  }
+  if (letg) {
+    for (int s = 0; s < 4; s++) {
+      const MxSupportDev &sg = T.supports[s];
+      if (!sg.norders) continue;
+      if (ph.flags & MX_BAD_PHOTON_MASK) continue;
+      int k = choose_order(T.support_energy, (unsigned) T.support_nenergy, T.support_cum + sg.cum_off, sg.norders, fe,
+                           rng.uniform());
+      if (k < 0) { ph.flags |= MX_PHOTON_UNDIFFRACTED; continue; }
+      // order list 0, +1, -1, +2, -2, ... (init_one_grating, diffract.c:392-405)
+      ph.sup[s] = (int8_t) ((k & 1) ? (k + 1) / 2 : -(k / 2));
+      ph.set |= MX_SET_SUPPORT;
+      if (-1 == diffract_support(T, sg, k, ph.e, x, p, rng)) ph.flags |= MX_PHOTON_UNDIFFRACTED;
+    }
   }
   ph.x = rot_x(x, g.cos_p, g.sin_p);
   ph.p = rot_x(p, g.cos_p, g.sin_p);
@@ -951,7 +1009,8 @@ MXD void trace_photon(const MxTables &T, const MxShellDev *shells, const float *
   if ((stages & MX_STAGE_DITHER) && T.dither) dither_stage(T, ph, rng);
   if ((stages & MX_STAGE_MIRROR) && !(ph.flags & MX_BAD_PHOTON_MASK)) mirror_stage(T, shells, optc, slope, ph, rng);
   if (rng.overrun) return;
-  if ((stages & MX_STAGE_GRATING) && T.grating && !(ph.flags & MX_BAD_PHOTON_MASK)) grating_stage(T, grs, ph, rng);
+  if ((stages & MX_STAGE_GRATING) && T.grating && !(ph.flags & MX_BAD_PHOTON_MASK))
+    grating_stage(T, grs, T.grating, ph, rng);
   if (rng.overrun) return;
   if ((stages & MX_STAGE_DETECT) && T.nchips && !(ph.flags & MX_BAD_PHOTON_MASK))
     detect_stage(T, chips + T.chip_off, T.nchips, ph, rng);

@@ -28,6 +28,8 @@ struct HostModel {
   std::vector<float> geff_energy, geff_cum;
   std::vector<double> order_k, sectors;
   std::vector<MxChipDev> chips;
+  std::vector<float> support_energy, support_cum;
+  std::vector<double> support_k;
 };
 
 bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string &err);

@@ -26,10 +26,13 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_trace_kernel(MxTables T, Tr
     q.t = io.t ? io.t[i] : 0.0;
     q.p = mk(io.p[i], io.p[n + i], io.p[2 * n + i]);
     q.flags = io.flags ? io.flags[i] : 0u;
+    q.set = 0;
+    for (int k = 0; k < 4; k++) q.sup[k] = (!io.fresh && io.support) ? io.support[k * n + i] : 0;
     if (io.fresh) {
       q.x = mk(0.0, 0.0, 0.0);
       q.shell = 0; q.order = 0; q.ccd = -1; q.ypix = 0.f; q.zpix = 0.f;
       q.dith[0] = q.dith[1] = q.dith[2] = 0.f;
+      clear_extra(io, i);
     } else {
       q.x = io.x ? mk(io.x[i], io.x[n + i], io.x[2 * n + i]) : mk(0.0, 0.0, 0.0);
       q.shell = io.shell ? io.shell[i] : 0;
@@ -58,6 +61,7 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_trace_kernel(MxTables T, Tr
     if (io.ypix) io.ypix[i] = q.ypix;
     if (io.zpix) io.zpix[i] = q.zpix;
     if (io.dith) for (int k = 0; k < 3; k++) io.dith[k * n + i] = q.dith[k];
+    store_extra(io, i, q);
   }
 }
 
@@ -89,9 +93,11 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK, 3) mx_wave_a(MxTables T, Trace
       q.t = io.t ? io.t[i] : 0.0;
       q.p = mk(io.p[i], io.p[n + i], io.p[2 * n + i]);
       q.flags = io.flags ? io.flags[i] : 0u;
+      q.set = 0;
       if (io.fresh) {
         q.x = mk(0.0, 0.0, 0.0); q.shell = 0;
         q.dith[0] = q.dith[1] = q.dith[2] = 0.f;
+        clear_extra(io, i);
         if (io.order) io.order[i] = 0;
         if (io.ccd) io.ccd[i] = -1;
         if (io.ypix) io.ypix[i] = 0.f;
@@ -171,12 +177,15 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_wave_c(MxTables T, TraceIO 
     from_rec(rec, q, m, r, io);
     const int unset = 0x7fff;
     q.order = unset; q.ccd = unset;
+    if (T.grating == MX_GRATING_LETG)   // supports skipped by this photon keep their values
+      for (int s = 0; s < 4; s++) q.sup[s] = io.support ? io.support[s * (size_t) io.stride + i] : 0;
     mirror_back(T, sh, q, r, m);
     if (!r.overrun && (io.stages & MX_STAGE_GRATING) && T.grating && !(q.flags & MX_BAD_PHOTON_MASK))
-      grating_stage(T, gr, q, r);
+      grating_stage(T, gr, T.grating, q, r);
     if (!r.overrun && (io.stages & MX_STAGE_DETECT) && T.nchips && !(q.flags & MX_BAD_PHOTON_MASK))
       detect_stage(T, ch + T.chip_off, T.nchips, q, r);
     store_core(io, i, q, r.overrun);
+    store_extra(io, i, q);
     if (q.order != unset && io.order) io.order[i] = (int8_t) q.order;
     if (q.ccd != unset) {
       if (io.ccd) io.ccd[i] = (int8_t) q.ccd;

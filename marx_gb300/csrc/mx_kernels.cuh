@@ -17,6 +17,10 @@ struct TraceIO {
   uint32_t *flags, *tag;
   int8_t *shell, *order, *ccd;
   float *ypix, *zpix, *dith;
+  int8_t *support;              // 4 components (stride): LETG support orders
+  int16_t *pha;                 // HRC pulse height
+  float *upix, *vpix;           // HRC-S u, v pixels
+  uint8_t *region;              // HRC-S shield region
   const double *U, *N;          // pre-drawn variates (slot-major) or null
   uint32_t n, stages;
   uint32_t stride;              // component stride of x, p and dither_state (>= n)

@@ -108,6 +108,209 @@ static void append_slopes(std::vector<double> &out, const float *x, const float 
   }
 }
 
+// JDMbinary_search_f (finterpo.c:37-57): the first index with xp >= x (an
+// equal element returns its index), n if every element is smaller.
+static unsigned jdm_bsearch_f(float x, const float *xp, unsigned n) {
+  unsigned n0 = 0, n1 = n;
+  while (n1 > n0 + 1) {
+    unsigned n2 = (n0 + n1) / 2;
+    if (xp[n2] >= x) {
+      if (xp[n2] == x) return n2;
+      n1 = n2;
+    } else
+      n0 = n2;
+  }
+  if (x >= xp[n0]) return n1;
+  return n0;
+}
+
+// JDMinterpolate_f (finterpo.c:59-86); the ordinate difference is a float
+// difference, the rest is double, as the reference writes it.
+static float jdm_interp_f(float x, const float *xp, const float *yp, unsigned n) {
+  if (n == 1) return yp[0];
+  unsigned n1 = jdm_bsearch_f(x, xp, n), n0 = n1 - 1;
+  if (n1 < n && x == xp[n1]) return yp[n1];
+  if (n1 == n) { n1--; n0--; }
+  if (n1 == 0) n0 = 1;
+  double x0 = xp[n0], x1 = xp[n1];
+  if (x1 == x0) return yp[n1];
+  return (float) (yp[n0] + (yp[n1] - yp[n0]) / (x1 - x0) * (x - x0));
+}
+
+// JDMinterpolate_n_fvector (finterpo.c:134-190) of ny columns at sorted x.
+static void jdm_interp_n(const float *x, unsigned n, const float *oldx, const float *const *oldy, unsigned oldn,
+                         unsigned ny, float *const *out) {
+  unsigned pos = 1;
+  for (unsigned j = 0; j < n; j++) {
+    double xv = x[j];
+    while (pos < oldn - 1 && xv > oldx[pos]) pos++;
+    double x0 = oldx[pos - 1], x1 = oldx[pos], dx = x1 - x0;
+    for (unsigned i = 0; i < ny; i++) {
+      if (dx == 0.0) out[i][j] = oldy[i][pos - 1];
+      else {
+        double y0 = oldy[i][pos - 1], y1 = oldy[i][pos];
+        out[i][j] = (float) (y0 + (y1 - y0) * (xv - x0) / dx);
+      }
+    }
+  }
+}
+
+// grating_efficiency (diffract.c:269-305) of a bar grating without material
+// layers (the LETG support gratings): the transmission factor is exp(0) = 1.
+static double bar_efficiency(int order, double energy, double beta, double delta, double period, double bar_height,
+                             double bar_width) {
+  double a = 1.0 - bar_width / period;
+  double k = energy / HBAR_C;
+  double kh = bar_height * k;
+  double khb = kh * beta;
+  double ekhb = exp(-khb);
+  double eff;
+  if (order != 0) {
+    double mpi = order * PI_;
+    a = sin(mpi * a) / mpi;
+    eff = a * a * (1 + ekhb * (ekhb - 2.0 * cos(kh * delta)));
+  } else {
+    double b = 1 - a;
+    eff = a * a + b * ekhb * (b * ekhb + 2 * a * cos(kh * delta));
+  }
+  return eff * 1.0;
+}
+
+// The LETG (_marx_letg_init, diffract.c:1727-1860): per-shell primary
+// efficiencies from the CALDB table (init_file_efficiencies with scale 1,
+// sum_file_efficiencies), the fine and coarse support gratings computed on
+// the grating energy grid (marx_create_grating_opt_const_tables,
+// diffract.c:1167-1188, read_grating_optical_consts :195-258,
+// init_one_grating :350-440), and the primary efficiencies divided by the
+// supports' total efficiencies (diffract.c:1790-1857).
+static bool build_letg(const Pack &pk, const mx_config &cfg, HostModel &M, std::string &err) {
+  MxTables &T = M.T;
+  const int nf = cfg.leg_fine_orders, nc = cfg.leg_coarse_orders;
+  if (nf < 0 || nc < 0 || nf > 127 || nc > 127 || (nf && nf % 2 == 0) || (nc && nc % 2 == 0)) {
+    err = "legFineNumOrders and legCoarseNumOrders must be odd and at most 127"; return false;
+  }
+  if (nf == 0 || nc == 0) { err = "the LETG needs both support gratings (legFineNumOrders, legCoarseNumOrders > 0)"; return false; }
+  // grating energy grid: 1024 points from 0.03 keV in steps of (10 - 0.03) / 1024
+  const unsigned NE = 1024;
+  std::vector<float> E(NE);
+  {
+    double d = (10.0 - 0.03) / NE, e = 0.03;
+    for (unsigned i = 0; i < NE; i++) { E[i] = (float) e; e += d; }
+  }
+  size_t cnt;
+  const float *oc = pk.get<float>("grating/optconst", &cnt, err);   // [7][rows]: E beta delta gold poly cr ni
+  if (!oc) return false;
+  unsigned rows = (unsigned) (cnt / 7);
+  if (rows < 2) { err = "grating optical constants malformed"; return false; }
+  std::vector<float> beta(NE), delta(NE);
+  {
+    const float *oy[2] = {oc + rows, oc + 2 * rows};
+    float *out[2] = {beta.data(), delta.data()};
+    jdm_interp_n(E.data(), NE, oc, oy, rows, 2, out);
+  }
+  // support gratings: cumulative efficiencies [order][energy] over the
+  // order list 0, +1, -1, +2, -2, ...
+  auto support = [&](int norders, double period, double bh, double bw, std::vector<float> &cum) {
+    cum.assign((size_t) norders * NE, 0.0f);
+    for (unsigned i = 0; i < NE; i++) {
+      double sum = 0.0;
+      for (int k = 0; k < norders; k++) {
+        int order = (k & 1) ? (k + 1) / 2 : -(k / 2);
+        sum += bar_efficiency(order, E[i], beta[i], delta[i], period, bh, bw);
+        cum[(size_t) k * NE + i] = (float) sum;
+      }
+    }
+  };
+  std::vector<float> fine, coarse;
+  support(nf, cfg.leg_fine_period, cfg.leg_fine_bar_height, cfg.leg_fine_bar_width, fine);
+  support(nc, cfg.leg_coarse_period, cfg.leg_coarse_bar_height, cfg.leg_coarse_bar_width, coarse);
+  const float *fine_tot = fine.data() + (size_t) (nf - 1) * NE, *coarse_tot = coarse.data() + (size_t) (nc - 1) * NE;
+
+  const bool acis = cfg.detector == MX_DETECTOR_ACIS_I || cfg.detector == MX_DETECTOR_ACIS_S;
+  for (int i = 0; i < 4; i++) {
+    MxGratingDev &g = M.gratings[4 + i];
+    memset(&g, 0, sizeof(g));
+    if (!(cfg.letg_period[i] > 0)) { err = "LETG period must be > 0"; return false; }
+    size_t ne, neff;
+    const float *e = pk.get<float>("letg/geff" + std::to_string(i) + "/energy", &ne, err);
+    const float *eff = pk.get<float>("letg/geff" + std::to_string(i) + "/eff", &neff, err);
+    if (!e || !eff) return false;
+    unsigned no = (unsigned) (neff / ne);
+    if (ne < 2 || no < 3 || (no % 2) != 1) { err = "grating efficiency table malformed"; return false; }
+    int max_order = (int) (no / 2);
+    std::vector<float> cum(eff, eff + neff);   // [order][energy]
+    for (unsigned j = 0; j < ne; j++) {         // sum_file_efficiencies with scale 1
+      double sum = 0.0;
+      for (unsigned k = 0; k < no; k++) { sum += 1.0 * (double) cum[k * ne + j]; cum[k * ne + j] = (float) sum; }
+      if (sum > 1.0)
+        for (unsigned k = 0; k < no; k++) cum[k * ne + j] = (float) (cum[k * ne + j] / sum);
+    }
+    for (unsigned j = 0; j < ne; j++) {         // divide out the fine support grating
+      float f = jdm_interp_f(e[j], E.data(), fine_tot, NE);
+      f = (float) (1.0 / f);
+      if (f <= 0) continue;
+      for (unsigned k = 0; k < no; k++) cum[k * ne + j] *= f;
+    }
+    for (unsigned j = 0; j < ne; j++) {         // and the coarse one, met three times
+      float f = jdm_interp_f(e[j], E.data(), coarse_tot, NE);
+      f = f * f * f;
+      if (f <= 0) continue;
+      f = (float) (1.0 / f);
+      for (unsigned k = 0; k < no; k++) cum[k * ne + j] *= f;
+    }
+    g.geff_off = (int32_t) M.geff_energy.size();
+    M.geff_energy.insert(M.geff_energy.end(), e, e + ne);
+    g.cum_off = (int32_t) M.geff_cum.size();
+    for (unsigned j = 0; j < ne; j++)
+      for (unsigned k = 0; k < no; k++) M.geff_cum.push_back(cum[k * ne + j]);   // [energy][order]
+    g.nenergy = (int32_t) ne; g.norders = (int32_t) no; g.max_order = max_order;
+    g.order_off = (int32_t) M.order_k.size();
+    for (unsigned k = 0; k < no; k++) {
+      int order = (int) k - max_order;
+      M.order_k.push_back(order * (2.0 * PI_ * HBAR_C) / cfg.letg_period[i]);
+    }
+    double disp = (cfg.letg_theta[i] * (PI_ / 180.0));
+    if (acis) disp += cfg.letg_acis_dtheta * (PI_ / 180.0);
+    double th = -1 * disp;
+    g.cos_m = cos(th); g.sin_m = sin(th);
+    th = 1 * disp;
+    g.cos_p = cos(th); g.sin_p = sin(th);
+    g.theta_blur = (cfg.letg_dtheta[i] * (PI_ / 180.0) / 60.0);
+    g.dp_over_p = cfg.letg_dpp[i];
+    g.vig = cfg.letg_vig[i];
+    g.rowland = cfg.leg_rowland;
+    g.nsec = 0;
+  }
+  // support tables on the device: the energy grid, [energy][order] per grating
+  M.support_energy = E;
+  M.support_cum.clear();
+  M.support_k.clear();
+  auto put = [&](const std::vector<float> &cum, int norders, double period) {
+    int32_t off = (int32_t) M.support_cum.size();
+    for (unsigned i = 0; i < NE; i++)
+      for (int k = 0; k < norders; k++) M.support_cum.push_back(cum[(size_t) k * NE + i]);
+    int32_t koff = (int32_t) M.support_k.size();
+    for (int k = 0; k < norders; k++) {
+      int order = (k & 1) ? (k + 1) / 2 : -(k / 2);
+      M.support_k.push_back(order * (2.0 * PI_ * HBAR_C) / period);
+    }
+    return std::make_pair(off, koff);
+  };
+  auto pf = put(fine, nf, cfg.leg_fine_period), pc = put(coarse, nc, cfg.leg_coarse_period);
+  const double angle[4] = {PI_ / 2.0, PI_ / 3.0, 2.0 * PI_ / 3.0, 0.0};
+  for (int s = 0; s < 4; s++) {
+    MxSupportDev &d = T.supports[s];
+    const bool isf = s == 0;
+    d.cum_off = isf ? pf.first : pc.first;
+    d.order_off = isf ? pf.second : pc.second;
+    d.norders = isf ? nf : nc;
+    d.rotate = angle[s] != 0.0;
+    d.cos_t = cos(angle[s]); d.sin_t = sin(angle[s]);
+  }
+  T.support_nenergy = (int32_t) NE;
+  return true;
+}
+
 bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string &err) {
   M = HostModel();
   MxTables &T = M.T;
@@ -237,9 +440,11 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
   // ---- HETG
   // The HETG tables are built whatever the configured grating, so that a
   // batch of sources can choose per source.
-  T.grating = cfg.grating == MX_GRATING_HETG;
-  if (cfg.grating != MX_GRATING_NONE && cfg.grating != MX_GRATING_HETG) { err = "unsupported grating"; return false; }
-  M.gratings.assign(4, MxGratingDev());
+  T.grating = cfg.grating;
+  if (cfg.grating != MX_GRATING_NONE && cfg.grating != MX_GRATING_HETG && cfg.grating != MX_GRATING_LETG) {
+    err = "unsupported grating"; return false;
+  }
+  M.gratings.assign(MX_MAX_GRATINGS, MxGratingDev());
   {
     for (int i = 0; i < 4; i++) {
       MxGratingDev &g = M.gratings[i];
@@ -312,6 +517,7 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
       }
     }
   }
+  if (cfg.grating == MX_GRATING_LETG && !build_letg(pk, cfg, M, err)) return false;
   if (M.geff_energy.empty()) M.geff_energy.push_back(0.f);
   if (M.geff_cum.empty()) M.geff_cum.push_back(0.f);
   if (M.order_k.empty()) M.order_k.push_back(0.0);

@@ -8,6 +8,7 @@
 #define MX_FOLD_THETA 208    // angles per WFold array (the HRMA tables hold 201)
 #define MX_MAX_CHIPS 10
 #define MX_MAX_SECTORS 64
+#define MX_MAX_GRATINGS 8     // HETG shells 1,3,4,6 then LETG shells 1,3,4,6
 
 // One HRMA shell: both optics (index 0 = paraboloid P, 1 = hyperboloid H).
 struct MxShellDev {
@@ -28,6 +29,14 @@ struct MxGratingDev {
   double cos_m, sin_m, cos_p, sin_p;           // rotation by -/+ dispersion angle
   int32_t geff_off, cum_off, nenergy, norders; // cumulative efficiencies [energy][order]
   int32_t max_order, order_off, sec_off, nsec; // order_k offset; sectors [6][nsec]
+};
+
+// One LETG support grating as the trace meets it (diffract.c:1097-1114):
+// the fine grating once at 90 degrees, the coarse grating at 60, 120 and 0.
+struct MxSupportDev {
+  int32_t cum_off, norders;    // cumulative efficiencies [energy][order] on the shared energy grid
+  int32_t order_off, rotate;   // order constants in support_k; rotate: the angle is not zero
+  double cos_t, sin_t;         // cos and sin of the angle
 };
 
 struct MxChipDev {
@@ -59,13 +68,19 @@ struct MxTables {
   const double *order_k;        // order * (2 pi hbar c) / period, per grating and order
   const double *sectors;
   const MxChipDev *chips;
+  // LETG support gratings
+  MxSupportDev supports[4];
+  const float *support_energy;  // the grating energy grid (marx_create_grating_opt_const_tables)
+  const float *support_cum;     // [energy][order] per support grating
+  const double *support_k;      // order * (2 pi hbar c) / period per support grating and order
+  int32_t support_nenergy, pad_support;
   // mirror
   int32_t ideal, use_blur, use_wfold, use_struts, use_scale, area_uniform;
   double hrma_vig, source_distance, cap, cos30, sin30;
   double strut_xpos[3][2], strut_half_width[3][2];
   float strut_xf[3][2], strut_hwf[3][2], cos30f, sin30f;   // cap + strut_xpos and half widths in float
   // dither
-  int32_t dither, grating;
+  int32_t dither, grating;      // grating: MX_GRATING_* of the configuration
   double dith_amp[3], dith_period[3], dith_phase[3], nominal_roll, aspect_blur, start_time;
   double dith_inv_period[3];    // correctly rounded 1 / dith_period
   int32_t roll_fixed, roll_zero;// roll amplitude 0: the roll angle is the same for every photon (zero: no roll)

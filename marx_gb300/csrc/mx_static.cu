@@ -60,6 +60,8 @@ extern "C" int mx_trace_static(mx_context *c, const mx_photons *ph, uint32_t sta
   io.energy = ph->energy; io.x = ph->x; io.p = ph->p; io.t = ph->arrival_time; io.flags = ph->flags;
   io.tag = ph->tag; io.shell = ph->mirror_shell; io.order = ph->order; io.ccd = ph->ccd_num;
   io.ypix = ph->y_pixel; io.zpix = ph->z_pixel; io.dith = ph->dither_state;
+  io.support = ph->support_orders; io.pha = ph->pulse_height; io.upix = ph->u_pixel; io.vpix = ph->v_pixel;
+  io.region = ph->detector_region;
   io.U = U; io.N = N; io.n = ph->n; io.seed = seed; io.stages = stages; io.fresh = 0;
   io.stride = ph->stride ? ph->stride : ph->n;
   if (io.stride < io.n) return mx_fail(c, MX_EINVAL, "mx_trace_static: stride below n");

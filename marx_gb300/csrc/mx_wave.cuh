@@ -13,7 +13,7 @@ __host__ __device__ static inline size_t align16(size_t x) { return (x + 15) & ~
 
 // Bytes of dynamic shared memory stage_tables fills.
 __host__ __device__ static inline size_t tables_shared_bytes(const MxTables &T) {
-  return align16(4 * sizeof(MxShellDev)) + align16(4 * sizeof(MxGratingDev)) +
+  return align16(4 * sizeof(MxShellDev)) + align16(MX_MAX_GRATINGS * sizeof(MxGratingDev)) +
          align16(MX_MAX_CHIPS * sizeof(MxChipDev)) + align16((size_t) T.optc_len * sizeof(float)) +
          align16((size_t) T.slope_len * sizeof(double));
 }
@@ -28,7 +28,7 @@ __device__ __forceinline__ void stage_tables(const MxTables &T, MxShellDev *&sh,
                                              float *&optc, double *&slope) {
   extern __shared__ __align__(16) unsigned char smem[];
   size_t o_gr = align16(4 * sizeof(MxShellDev));
-  size_t o_ch = o_gr + align16(4 * sizeof(MxGratingDev));
+  size_t o_ch = o_gr + align16(MX_MAX_GRATINGS * sizeof(MxGratingDev));
   size_t o_op = o_ch + align16(MX_MAX_CHIPS * sizeof(MxChipDev));
   size_t o_sl = o_op + align16((size_t) T.optc_len * sizeof(float));
   sh = (MxShellDev *) smem;
@@ -38,7 +38,7 @@ __device__ __forceinline__ void stage_tables(const MxTables &T, MxShellDev *&sh,
   slope = (double *) (smem + o_sl);
   copy_words((uint32_t *) slope, (const uint32_t *) T.optc_slope, (size_t) T.slope_len * 2);
   copy_words((uint32_t *) sh, (const uint32_t *) T.shells, 4 * sizeof(MxShellDev) / 4);
-  copy_words((uint32_t *) gr, (const uint32_t *) T.gratings, 4 * sizeof(MxGratingDev) / 4);
+  copy_words((uint32_t *) gr, (const uint32_t *) T.gratings, MX_MAX_GRATINGS * sizeof(MxGratingDev) / 4);
   copy_words((uint32_t *) ch, (const uint32_t *) T.chips, MX_MAX_CHIPS * sizeof(MxChipDev) / 4);
   copy_words((uint32_t *) optc, (const uint32_t *) T.optc, (size_t) T.optc_len);
   __syncthreads();
@@ -69,7 +69,7 @@ __device__ __forceinline__ void to_rec(MxRec &r, const Ph &q, const MirrorState 
 __device__ __forceinline__ void from_rec(const MxRec &r, Ph &q, MirrorState &m, Rng &rng, const TraceIO &io) {
   m.x = mk(r.x[0], r.x[1], r.x[2]); m.p = mk(r.p[0], r.p[1], r.p[2]); m.n = mk(r.n[0], r.n[1], r.n[2]);
   m.corr = r.corr; m.beta = r.beta; m.delta = r.delta; m.pdn = r.pdn;
-  q.e = r.e; q.t = r.t; q.flags = r.flags; q.shell = r.shell;
+  q.e = r.e; q.t = r.t; q.flags = r.flags; q.shell = r.shell; q.set = 0;
   q.x = m.x; q.p = m.p;
   rng.U = io.U; rng.N = io.N; rng.seed = io.seed; rng.n = io.n; rng.i = r.i; rng.tag = r.tag;
   rng.upos = r.upos; rng.uend = MX_U_MIRROR + 12; rng.npos = r.npos; rng.nend = MX_N_MIRROR + 2;
@@ -87,3 +87,29 @@ __device__ __forceinline__ void store_core(const TraceIO &io, uint32_t i, const 
   if (io.shell) io.shell[i] = (int8_t) q.shell;
 }
 
+
+// The LETG and HRC outputs of a photon whose trace ends in this phase: only
+// the columns its stages set (the reference leaves the others as they are).
+__device__ __forceinline__ void store_extra(const TraceIO &io, uint32_t i, const Ph &q) {
+  const size_t n = io.stride;
+  if ((q.set & MX_SET_SUPPORT) && io.support)
+    for (int k = 0; k < 4; k++) io.support[k * n + i] = q.sup[k];
+  if (q.set & MX_SET_HRC) {
+    if (io.pha) io.pha[i] = q.pha;
+    if (io.region) io.region[i] = q.region;
+  }
+  if (q.set & MX_SET_UV) {
+    if (io.upix) io.upix[i] = q.upix;
+    if (io.vpix) io.vpix[i] = q.vpix;
+  }
+}
+
+// Zero the LETG and HRC output columns of photon i (fresh lists).
+__device__ __forceinline__ void clear_extra(const TraceIO &io, uint32_t i) {
+  const size_t n = io.stride;
+  if (io.support) for (int k = 0; k < 4; k++) io.support[k * n + i] = 0;
+  if (io.pha) io.pha[i] = 0;
+  if (io.region) io.region[i] = 0;
+  if (io.upix) io.upix[i] = 0.f;
+  if (io.vpix) io.vpix[i] = 0.f;
+}

@@ -19,12 +19,14 @@ PHOTON_MISSED_DETECTOR = 0x08
 PHOTON_MIRROR_VBLOCKED = 0x10
 PHOTON_GRATING_VBLOCKED = 0x40
 BAD_PHOTON_MASK = 0xFF
+PHOTON_DRAKE_BLOCKED = 0x20
+PHOTON_DRAKE_REFLECTED = 0x100
 PHOTON_ACIS_STREAKED = 0x200
 PHOTON_VARIATE_OVERRUN = 0x10000
 
 STAGE_DITHER, STAGE_MIRROR, STAGE_GRATING, STAGE_DETECT = 1, 2, 4, 8
 STAGE_ALL = 15
-NUM_U, NUM_N = 16, 8
+NUM_U, NUM_N = 28, 20
 
 
 class MxPhotons(C.Structure):
@@ -35,6 +37,8 @@ class MxPhotons(C.Structure):
         ("mirror_shell", C.c_void_p), ("order", C.c_void_p), ("ccd_num", C.c_void_p),
         ("reserved8", C.c_void_p),
         ("y_pixel", C.c_void_p), ("z_pixel", C.c_void_p), ("dither_state", C.c_void_p),
+        ("support_orders", C.c_void_p), ("pulse_height", C.c_void_p), ("u_pixel", C.c_void_p),
+        ("v_pixel", C.c_void_p), ("detector_region", C.c_void_p),
     ]
 
 
@@ -48,6 +52,8 @@ COLUMNS = {
     "arrival_time": (np.float64, 1), "flags": (np.uint32, 1), "tag": (np.uint32, 1),
     "mirror_shell": (np.int8, 1), "order": (np.int8, 1), "ccd_num": (np.int8, 1),
     "y_pixel": (np.float32, 1), "z_pixel": (np.float32, 1), "dither_state": (np.float32, 3),
+    "support_orders": (np.int8, 4), "pulse_height": (np.int16, 1), "u_pixel": (np.float32, 1),
+    "v_pixel": (np.float32, 1), "detector_region": (np.uint8, 1),
 }
 
 
@@ -84,7 +90,9 @@ class PhotonList:
         s = MxPhotons()
         s.n = self.n
         for k in COLUMNS:
-            a = getattr(self, k)
+            a = getattr(self, k, None)
+            if a is None:
+                continue
             assert a.flags["C_CONTIGUOUS"]
             setattr(s, k, a.ctypes.data)
         return s

@@ -8,6 +8,8 @@ plain_scatter   1e7 photons, log-uniform 0.3-8 keV, off-axis angle uniform
                 blur and WFold scattering, ACIS-I.
 plain_hetg      2e7 photons, power law (photon index 1.7) on 0.4-8 keV
                 absorbed by NH = 1e21 cm^-2, HETG orders -3..+3, ACIS-S.
+plain_letg      4e6 photons of the same spectrum through the LETG and its
+                support gratings, ACIS-S.
 batched         256 sources (see marx_gb300.batched).
 differentiable  4e6 weighted rays (see marx_gb300.adjoint).
 
@@ -95,7 +97,7 @@ def _hetg(w, n, seed):
     return ph
 
 
-GENERATORS = {"plain_onaxis": _onaxis, "plain_scatter": _scatter, "plain_hetg": _hetg}
+GENERATORS = {"plain_onaxis": _onaxis, "plain_scatter": _scatter, "plain_hetg": _hetg, "plain_letg": _hetg}
 
 
 def plain_onaxis(parity: bool = False) -> Workload:
@@ -133,4 +135,17 @@ def plain_hetg(parity: bool = False) -> Workload:
     return Workload("plain_hetg", 20_000_000, c, seed=303, stages=15)
 
 
+def plain_letg(parity: bool = False) -> Workload:
+    """LETG with its fine and coarse support gratings, ACIS-S."""
+    c = default_config()
+    c.grating = GRATING["LETG"]
+    c.dither = DITHER["INTERNAL"]
+    c.detector = DETECTOR["ACIS-S"]
+    return Workload("plain_letg", 4_000_000, c, seed=404, stages=15)
+
+
 PLAIN = {"plain_onaxis": plain_onaxis, "plain_scatter": plain_scatter, "plain_hetg": plain_hetg}
+# Workloads of the stages the C++ restatement does not cover (LETG, HRC):
+# their parity is pinned to the reference's own outputs only.
+EXTRA = {"plain_letg": plain_letg}
+ALL = {**PLAIN, **EXTRA}

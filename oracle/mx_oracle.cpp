@@ -107,6 +107,10 @@ static void shell_frames(Shell &h, double cap_pos) {
 
 static bool setup(mxo_model *o, const mx_config *cfg) {
   Model &M = o->M;
+  if (cfg->grating == MX_GRATING_LETG || cfg->detector == MX_DETECTOR_HRC_I || cfg->detector == MX_DETECTOR_HRC_S) {
+    g_err = "the restatement covers the HETG and ACIS; LETG and HRC runs are checked against the reference's outputs";
+    return false;
+  }
   M.cfg = *cfg;
   M.cap = cfg->hrma_cap_x;
   M.ideal = cfg->hrma_ideal != 0;

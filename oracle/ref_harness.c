@@ -35,8 +35,8 @@
 #include "_marx.h"
 
 /* Variate slot layout, shared with the engine and the port. */
-#define MX_NU 16
-#define MX_NN 8
+#define MX_NU 28
+#define MX_NN 20
 #define MX_U_MIRROR 0
 #define MX_U_MIRROR_N 12
 #define MX_U_GRATING 12
@@ -51,6 +51,14 @@
 #define MX_N_GRATING_N 2
 #define MX_N_DETECT 6
 #define MX_N_DETECT_N 2
+#define MX_U_LETG 16
+#define MX_U_LETG_N 6
+#define MX_N_LETG 8
+#define MX_N_LETG_N 10
+#define MX_U_HRC 22
+#define MX_U_HRC_N 6
+#define MX_N_HRC 18
+#define MX_N_HRC_N 2
 
 static char Err[1024];
 static void set_err(const char *s) { strncpy(Err, s, sizeof(Err) - 1); }
@@ -95,6 +103,7 @@ double JDMfast_random(void) { Rng_Unexpected++; return 0.5; }
 /* ------------------------------------------------------------- set-up -- */
 static Param_File_Type *Pf;
 static int Have_Dither, Have_Grating, Det_Kind;   /* 0 none, 1 ACIS-I, 2 ACIS-S */
+static int Grating_Is_LETG;
 static Marx_Detector_Type *Det;
 
 int mxref_setup(const char *parfile, const char *datadir, int nover,
@@ -125,6 +134,7 @@ int mxref_setup(const char *parfile, const char *datadir, int nover,
    if (-1 == marx_grating_init(Pf)) { set_err("grating init failed"); return -1; }
    if (-1 == pf_get_string(Pf, "GratingType", buf, sizeof(buf))) return -1;
    Have_Grating = (0 != strcmp(buf, "NONE"));
+   Grating_Is_LETG = (0 == strcmp(buf, "LETG"));
 
    /* Detector: the part of marx_detector_init (detector.c:298-357) that does
     * not depend on the missing FEF file. */
@@ -232,6 +242,17 @@ static void fill_attr(Marx_Photon_Attr_Type *at, double e, const double *p, doub
    at->ccd_num = -1;
 }
 
+/* Outputs beyond the core columns, NULL when not wanted: LETG support
+ * orders (4 per photon), HRC pulse height, u/v pixel and detector region. */
+static signed char *X_Sup;
+static short *X_Pha;
+static float *X_U, *X_V;
+static unsigned char *X_Region;
+void mxref_set_extra_outputs(signed char *sup, short *pha, float *u, float *v, unsigned char *region)
+{
+   X_Sup = sup; X_Pha = pha; X_U = u; X_V = v; X_Region = region;
+}
+
 static void store_attr(const Marx_Photon_Attr_Type *at, int i, double *x, double *p,
                        unsigned int *flags, int *shell, int *order, int *ccd,
                        float *ypix, float *zpix, float *dith)
@@ -245,6 +266,15 @@ static void store_attr(const Marx_Photon_Attr_Type *at, int i, double *x, double
    ypix[i] = at->y_pixel; zpix[i] = at->z_pixel;
    dith[3*i] = at->dither_state.ra; dith[3*i+1] = at->dither_state.dec;
    dith[3*i+2] = at->dither_state.roll;
+   if (X_Sup != NULL)
+     {
+        int k;
+        for (k = 0; k < 4; k++) X_Sup[4*i+k] = at->support_orders[k];
+     }
+   if (X_Pha != NULL) X_Pha[i] = at->pulse_height;
+   if (X_U != NULL) X_U[i] = at->u_pixel;
+   if (X_V != NULL) X_V[i] = at->v_pixel;
+   if (X_Region != NULL) X_Region[i] = at->detector_region;
 }
 
 #define ST_DITHER 1
@@ -299,9 +329,13 @@ int mxref_trace_slots(int n, const double *energy, const double *p_in, const dou
           }
         if ((stages & ST_GRATING) && Have_Grating)
           {
-             rng_window(u, MX_U_GRATING, MX_U_GRATING_N, g, MX_N_GRATING, MX_N_GRATING_N);
+             if (Grating_Is_LETG)
+               rng_window(u, MX_U_LETG, MX_U_LETG_N, g, MX_N_LETG, MX_N_LETG_N);
+             else
+               rng_window(u, MX_U_GRATING, MX_U_GRATING_N, g, MX_N_GRATING, MX_N_GRATING_N);
              if (-1 == marx_grating_diffract(&pt, 0)) { set_err("grating"); return -1; }
-             us[4] = U_pos - MX_U_GRATING; us[5] = N_pos - MX_N_GRATING;
+             us[4] = U_pos - (Grating_Is_LETG ? MX_U_LETG : MX_U_GRATING);
+             us[5] = N_pos - (Grating_Is_LETG ? MX_N_LETG : MX_N_GRATING);
           }
         if ((stages & ST_DETECT) && Det_Kind)
           {

@@ -1,6 +1,6 @@
 """Generate the golden fixtures from the reference MARX library itself.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [workload ...]
 
 Needs the reference sources (MARX_REFERENCE_ROOT, default /root/reference);
 oracle/Makefile compiles them in place into oracle/_ref.  Writes:
@@ -57,13 +57,19 @@ def summarize(q, w):
             out["radius_sample"] = np.sort(r)[:: max(1, len(r) // 5000)]
         else:
             orders = q.order[good].astype(int)
-            out["order_hist"] = np.bincount(orders + 11, minlength=23)
+            if w.cfg.grating == 2:      # LETG: orders -25..25, and the fine support orders
+                out["order_hist"] = np.bincount(orders + 25, minlength=51)
+                out["fine_hist"] = np.bincount(q.support_orders[0][good].astype(int) + 9, minlength=19)
+            else:
+                out["order_hist"] = np.bincount(orders + 11, minlength=23)
         out["ccd_hist"] = np.bincount(q.ccd_num[good].astype(int) + 1, minlength=11)
     return out
 
 
-def main():
-    for name, make in W.PLAIN.items():
+def main(names=None):
+    for name, make in W.ALL.items():
+        if names and name not in names:
+            continue
         w = make(parity=True)
         # per-photon parity fixture
         ph = w.photons(N_TRACE, seed=w.seed + 1)
@@ -71,11 +77,18 @@ def main():
         ref = Reference(w.cfg)
         q, used, bad = ref.trace_slots(ph, U, N)
         assert bad == 0, "reference ran past its variate slots"
+        extra = {}
+        if w.cfg.grating == 2:
+            extra["support_orders"] = q.support_orders
+        if w.cfg.detector >= 3:
+            extra.update(pulse_height=q.pulse_height, detector_region=q.detector_region)
+            if w.cfg.detector == 4:
+                extra.update(u_pixel=q.u_pixel, v_pixel=q.v_pixel)
         np.savez_compressed(
             os.path.join(HERE, f"trace_{name}.npz"),
             energy=ph.energy, p_in=ph.p, arrival_time=ph.arrival_time, U=U, N=N,
             x=q.x, p=q.p, flags=q.flags, mirror_shell=q.mirror_shell, order=q.order, ccd_num=q.ccd_num,
-            y_pixel=q.y_pixel, z_pixel=q.z_pixel, dither_state=q.dither_state, used=used)
+            y_pixel=q.y_pixel, z_pixel=q.z_pixel, dither_state=q.dither_state, used=used, **extra)
         # statistical fixture with the reference's own generator
         ref_n = Reference(w.cfg, native=True, seed=w.seed)
         ph = w.photons(N_STATS, seed=w.seed + 3)
@@ -161,8 +174,11 @@ def diff_rays():
 
 
 if __name__ == "__main__":
+    names = [a for a in sys.argv[1:] if not a.startswith("-")]
     if "--diff" in sys.argv:
         diff_rays()
+    elif names:
+        main(names)
     else:
         main()
         diff_rays()

@@ -14,6 +14,7 @@ from helpers import load_trace_fixture, assert_parity, compare
 
 pytestmark = pytest.mark.gpu
 NAMES = list(W.PLAIN)
+ALL_NAMES = list(W.ALL)        # with the workloads pinned to reference fixtures only
 
 
 def engine(cfg, mode=0):
@@ -37,7 +38,7 @@ def device_trace(eng, ph, U=None, N=None, seed=0, stages=15):
 
 
 @pytest.mark.parametrize("mode", list(MODES))
-@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("name", ALL_NAMES)
 def test_gpu_matches_reference_fixture(cuda, name, mode):
     w, ph, U, N, z = load_trace_fixture(name)
     eng = engine(w.cfg, MODES[mode])
@@ -47,7 +48,7 @@ def test_gpu_matches_reference_fixture(cuda, name, mode):
 
 
 @pytest.mark.parametrize("mode", list(MODES))
-@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("name", ALL_NAMES)
 def test_gpu_host_entry_matches_reference_fixture(cuda, name, mode):
     w, ph, U, N, z = load_trace_fixture(name)
     eng = engine(w.cfg, MODES[mode])
@@ -67,16 +68,16 @@ def test_gpu_matches_oracle_philox(cuda, name):
     assert_parity(q, a, f"{name} philox")
 
 
-@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("name", ALL_NAMES)
 def test_wavefront_equals_fused(cuda, name):
-    w = W.PLAIN[name]()
+    w = W.ALL[name]()
     ph = w.photons(100_000, seed=77)
     a = device_trace(engine(w.cfg, MODES["fused"]), ph, seed=3)
     b = device_trace(engine(w.cfg, MODES["wavefront"]), ph, seed=3)
     assert_parity(b, a, f"{name} wavefront vs fused")
 
 
-@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("name", ALL_NAMES)
 def test_split_stages_equal_fused(cuda, name):
     w, ph, U, N, z = load_trace_fixture(name)
     eng = engine(w.cfg, MODES["fused"])

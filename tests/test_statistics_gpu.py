@@ -19,7 +19,7 @@ N = 200_000
 def run_gpu(name, n=N, seed=99):
     import torch
     from marx_gb300._native import Engine, DevicePhotons
-    w = W.PLAIN[name](parity=True)
+    w = W.ALL[name](parity=True)
     eng = Engine(w.cfg)
     d = DevicePhotons.from_host(w.photons(n, seed=w.seed + 10))
     eng.trace(d, seed=seed)
@@ -37,7 +37,7 @@ def chi2_p(a, b):
     return stats.chi2.sf(chi2, keep.sum() - 1)
 
 
-@pytest.mark.parametrize("name", list(W.PLAIN))
+@pytest.mark.parametrize("name", list(W.ALL))
 def test_survivor_fraction_and_histograms(cuda, name):
     ref = np.load(os.path.join(GOLDEN, f"stats_{name}.npz"))
     w, q = run_gpu(name)
@@ -48,8 +48,12 @@ def test_survivor_fraction_and_histograms(cuda, name):
     ccd = np.bincount(q.ccd_num[good].astype(int) + 1, minlength=11)
     assert chi2_p(ccd, ref["ccd_hist"]) > 1e-4
     if "order_hist" in ref:
-        orders = np.bincount(q.order[good].astype(int) + 11, minlength=23)
+        m = (len(ref["order_hist"]) - 1) // 2
+        orders = np.bincount(q.order[good].astype(int) + m, minlength=2 * m + 1)
         assert chi2_p(orders, ref["order_hist"]) > 1e-4
+    if "fine_hist" in ref:      # LETG fine support grating orders
+        fine = np.bincount(q.support_orders[0][good].astype(int) + 9, minlength=19)
+        assert chi2_p(fine, ref["fine_hist"]) > 1e-4
 
 
 @pytest.mark.parametrize("name", ["plain_onaxis", "plain_scatter"])
