@@ -147,6 +147,13 @@ typedef struct mx_config {
   int32_t reserved2;
   double hrc_i_blur[13];      /* HRC-I-Blur{G1FWHM,G1Xctr,G1Yctr,G1Amp,G2..,L1FWHM,L1Xctr,L1Yctr,L1Amp,L1Rmax} */
   double hrc_s_blur[13];      /* the same for HRC-S (1/4 pixels) */
+  /* HRC-S high-energy suppression filter, the Drake flat (drake.c:148-246) */
+  int32_t hrc_hesf;           /* HRC-HESF */
+  int32_t hesf_n;             /* HESFN: plates per side, 1..4 */
+  double hesf_offset_x, hesf_offset_z;   /* HESFOffsetX, HESFOffsetZ (mm) */
+  double hesf_gap_y1, hesf_gap_y2;       /* HESFGapY1, HESFGapY2 (mm) */
+  double hesf_length, hesf_cr_width;     /* HESFLength, HESFCrWidth (mm) */
+  double hesf_height[4], hesf_theta[4];  /* HESFHeight1..4 (mm), HESFTheta1..4 (deg) */
 } mx_config;
 
 /* Structure-of-arrays photon list.  3-vectors are component-major:

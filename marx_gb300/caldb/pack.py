@@ -153,6 +153,35 @@ def read_column_text(path: str, ncols: int) -> np.ndarray:
     return np.array(out, dtype=np.float64)
 
 
+def read_simple_data(path: str, names) -> dict:
+    """MARX "simple data" text file (_marx_read_simple_data_file,
+    marx/libsrc/data.c:334-393): lines "NAME v1 v2 ...", '#' comments; each
+    requested name's leading numeric fields, parsed like sscanf("%lf")."""
+    want = dict(names)
+    out = {}
+    for line in open(path):
+        f = line.split()
+        if not f or f[0].startswith("#") or f[0] not in want:
+            continue
+        out[f[0]] = [float(v) for v in f[1:1 + want[f[0]]]]
+    missing = [k for k in want if k not in out or len(out[k]) != want[k]]
+    if missing:
+        raise ValueError(f"{path}: missing {missing}")
+    return out
+
+
+# hrc_i_geom.txt fields (hrc_i_geom.c:166-175) and hrc_s_geom.txt fields
+# (hrc_s_geom.c:392-413, hrc-s.c:350-360), in the order the pack stores them
+HRC_I_GEOM = (("HRC_I_X_Pixel_Size", 1), ("HRC_I_Y_Pixel_Size", 1), ("HRC_I_LL_XYZ", 3), ("HRC_I_Center_XYZ", 3),
+              ("HRC_I_LL_to_LR_Vector", 3), ("HRC_I_Center_CXCY", 2), ("HRC_I_Aimpoint_CXCY", 2))
+HRC_S_GEOM = (("V_Pixel_Size", 1), ("V_Active", 6), ("U_Pixel_Size", 1), ("U_Active", 2), ("Aimpoint_Offset", 3),
+              ("Left_UV", 2), ("Right_UV", 2), ("Middle_UV", 2), ("Left_XYZ", 3), ("Right_XYZ", 3),
+              ("Middle_XYZ", 3), ("Left_CXCY", 2), ("Right_CXCY", 2), ("Middle_CXCY", 2), ("Left_Angle", 1),
+              ("Right_Angle", 1), ("Detector_Angle", 1), ("Ion_Shield_T", 1), ("Ion_Shield_L", 1),
+              ("Ion_Shield_R", 1), ("Ion_Shield_X", 1), ("Ion_Shield_SL", 1), ("Ion_Shield_SR", 1),
+              ("Ion_Shield_GapL", 1), ("Ion_Shield_GapR", 1))
+
+
 def read_fits_bintables(path: str):
     """Minimal FITS reader: yields (header dict, {column: ndarray}) for each
     BINTABLE extension.  Handles the scalar/vector numeric (E, D, J, I) and
@@ -272,6 +301,28 @@ def build_sections(data_dir: str) -> dict:
             names = [n.strip().upper() for n in c["AIMPOINT_NAME"]]
             S["acis/aimpt_i"] = np.asarray(c["AIMPOINT"][names.index("AI2")], dtype=np.float64)
             S["acis/aimpt_s"] = np.asarray(c["AIMPOINT"][names.index("AS1")], dtype=np.float64)
+    # HRC: geometry, CALDB origins and aimpoints, MCP and UV/ion shield
+    # efficiencies (marx.par defaults), Drake flat optical constants
+    for key, fname, fields in (("hrc/i_geom", "hrc_i_geom.txt", HRC_I_GEOM), ("hrc/s_geom", "hrc_s_geom.txt", HRC_S_GEOM)):
+        v = read_simple_data(os.path.join(data_dir, "hrc", fname), fields)
+        S[key] = np.array([x for k, _ in fields for x in v[k]], dtype=np.float64)
+    for h, c in geom:
+        if h.get("EXTNAME") == "INSTRUMENTS":
+            names = [n.strip().upper() for n in c["INSTRUMENT"]]
+            S["hrc/origin_i"] = np.asarray(c["ORIGIN"][names.index("HRC-I")], dtype=np.float64)
+            S["hrc/origin_s"] = np.asarray(c["ORIGIN"][names.index("HRC-S")], dtype=np.float64)
+    for h, c in aim:
+        if h.get("EXTNAME") == "AIMPOINTS":
+            names = [n.strip().upper() for n in c["AIMPOINT_NAME"]]
+            S["hrc/aimpt_i"] = np.asarray(c["AIMPOINT"][names.index("HI1")], dtype=np.float64)
+            S["hrc/aimpt_s"] = np.asarray(c["AIMPOINT"][names.index("HS1")], dtype=np.float64)
+    for key, fname in (("hrc/qe_i", "mcp_qe_i.v2.2.dat"), ("hrc/uvis_i", "uvis_i.v4.dat"),
+                       ("hrc/qe_s", "mcp_qe_s.v3.dat"), ("hrc/uvis_s0", "uvis_s1.v4.dat"),
+                       ("hrc/uvis_s1", "uvis_s2.v4.dat"), ("hrc/uvis_s2", "uvis_s56.v4.dat"),
+                       ("hrc/uvis_s3", "uvis_s34.v4.dat")):
+        S[key] = read_bdat(os.path.join(data_dir, "hrc", fname))[:2]
+    S["hrc/optconst_cr"] = read_bdat(os.path.join(data_dir, "hrc", "chromium.dat"))[:3]
+    S["hrc/optconst_c"] = read_bdat(os.path.join(data_dir, "hrc", "carbon.dat"))[:3]
     qe = read_fits_bintables(os.path.join(data_dir, "caldb", "acisD1997-04-17qeN0006.fits"))
     for h, c in qe:
         if h.get("EXTNAME") == "AXAF_QE":

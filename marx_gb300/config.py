@@ -54,6 +54,11 @@ class MxConfig(C.Structure):
         ("leg_coarse_bar_width", C.c_double),
         ("det_ideal", C.c_int32), ("reserved2", C.c_int32),
         ("hrc_i_blur", C.c_double * 13), ("hrc_s_blur", C.c_double * 13),
+        ("hrc_hesf", C.c_int32), ("hesf_n", C.c_int32),
+        ("hesf_offset_x", C.c_double), ("hesf_offset_z", C.c_double),
+        ("hesf_gap_y1", C.c_double), ("hesf_gap_y2", C.c_double),
+        ("hesf_length", C.c_double), ("hesf_cr_width", C.c_double),
+        ("hesf_height", C.c_double * 4), ("hesf_theta", C.c_double * 4),
     ]
 
 
@@ -105,6 +110,12 @@ def default_config() -> MxConfig:
                        10.8269, 73.3361, 63.9927, 0.0, 256.0]
     c.hrc_s_blur[:] = [13.900, 64.110, 64.530, 15.750, 4.2560, 67.420, 64.110, 0.0,
                        10.820, 53.030, 63.880, 0.0, 256.000]
+    c.hrc_hesf, c.hesf_n = 1, 2
+    c.hesf_offset_x, c.hesf_offset_z = 26.3, -5.359
+    c.hesf_gap_y1, c.hesf_gap_y2 = 28.7, 36.7
+    c.hesf_length, c.hesf_cr_width = 294.0, 15.7
+    c.hesf_height[:] = [22.3, 50.0, 0.0, 0.0]
+    c.hesf_theta[:] = [4.5, 7.0, 0.0, 0.0]
     return c
 
 
@@ -154,6 +165,14 @@ def to_par(c: MxConfig) -> dict:
     for k, name in enumerate(HRC_BLUR):
         P[f"HRC-I-Blur{name}"] = repr(c.hrc_i_blur[k])
         P[f"HRC-S-Blur{name}"] = repr(c.hrc_s_blur[k])
+    P["HRC-HESF"] = _yn(c.hrc_hesf)
+    P["HESFN"] = str(c.hesf_n)
+    P["HESFOffsetX"], P["HESFOffsetZ"] = repr(c.hesf_offset_x), repr(c.hesf_offset_z)
+    P["HESFGapY1"], P["HESFGapY2"] = repr(c.hesf_gap_y1), repr(c.hesf_gap_y2)
+    P["HESFLength"], P["HESFCrWidth"] = repr(c.hesf_length), repr(c.hesf_cr_width)
+    for k in range(4):
+        P[f"HESFHeight{k + 1}"] = repr(c.hesf_height[k])
+        P[f"HESFTheta{k + 1}"] = repr(c.hesf_theta[k])
     for i, s in enumerate(SHELLS):
         P[f"HRMA_P{s}H{s}_XOffset"] = repr(c.shell_xoffset[i])
         P[f"P{s}Blur"], P[f"H{s}Blur"] = repr(c.blur_p[i]), repr(c.blur_h[i])
@@ -225,6 +244,14 @@ def from_par(path: str, overrides: dict | None = None) -> MxConfig:
     for k, name in enumerate(HRC_BLUR):
         c.hrc_i_blur[k] = num(f"HRC-I-Blur{name}", c.hrc_i_blur[k])
         c.hrc_s_blur[k] = num(f"HRC-S-Blur{name}", c.hrc_s_blur[k])
+    c.hrc_hesf = yes("HRC-HESF", c.hrc_hesf)
+    c.hesf_n = int(num("HESFN", c.hesf_n))
+    c.hesf_offset_x, c.hesf_offset_z = num("HESFOffsetX", c.hesf_offset_x), num("HESFOffsetZ", c.hesf_offset_z)
+    c.hesf_gap_y1, c.hesf_gap_y2 = num("HESFGapY1", c.hesf_gap_y1), num("HESFGapY2", c.hesf_gap_y2)
+    c.hesf_length, c.hesf_cr_width = num("HESFLength", c.hesf_length), num("HESFCrWidth", c.hesf_cr_width)
+    for k in range(4):
+        c.hesf_height[k] = num(f"HESFHeight{k + 1}", c.hesf_height[k])
+        c.hesf_theta[k] = num(f"HESFTheta{k + 1}", c.hesf_theta[k])
     if "GratingType" in vals:
         c.grating = GRATING[vals["GratingType"]]
     c.use_sector_files = yes("Use_HETG_Sector_Files", c.use_sector_files)

@@ -44,6 +44,7 @@ static int upload_model(mx_context *c) {
          o_se = put(blob, M.sectors), o_ch = put(blob, M.chips);
   if (M.support_energy.empty()) { M.support_energy.push_back(0.f); M.support_cum.push_back(0.f); M.support_k.push_back(0.0); }
   size_t o_pe = put(blob, M.support_energy), o_pc = put(blob, M.support_cum), o_pk = put(blob, M.support_k);
+  size_t o_ht = put(blob, M.hrc_tab), o_hs = put(blob, M.hrc_slope);
   cudaError_t e = c->tables.ensure(blob.size());
   if (e != cudaSuccess) return cuda_fail(c, e, "allocating device tables");
   e = cudaMemcpy(c->tables.ptr, blob.data(), blob.size(), cudaMemcpyHostToDevice);
@@ -66,6 +67,8 @@ static int upload_model(mx_context *c) {
   c->T.support_energy = (const float *) (b + o_pe);
   c->T.support_cum = (const float *) (b + o_pc);
   c->T.support_k = (const double *) (b + o_pk);
+  c->T.hrc_tab = (const float *) (b + o_ht);
+  c->T.hrc_slope = (const double *) (b + o_hs);
   c->shared_bytes = trace_shared_bytes(c->T);
   if (c->shared_bytes > 200 * 1024) return fail(c, MX_ERANGE, "tables exceed the shared-memory budget");
   return MX_OK;
@@ -134,6 +137,12 @@ void mx_config_default(mx_config *c) {
   static const double bs[13] = {13.900, 64.110, 64.530, 15.750, 4.2560, 67.420, 64.110, 0.0,
                                 10.820, 53.030, 63.880, 0.0, 256.000};
   for (int k = 0; k < 13; k++) { c->hrc_i_blur[k] = bi[k]; c->hrc_s_blur[k] = bs[k]; }
+  c->hrc_hesf = 1; c->hesf_n = 2;
+  c->hesf_offset_x = 26.3; c->hesf_offset_z = -5.359;
+  c->hesf_gap_y1 = 28.7; c->hesf_gap_y2 = 36.7;
+  c->hesf_length = 294.0; c->hesf_cr_width = 15.7;
+  c->hesf_height[0] = 22.3; c->hesf_height[1] = 50.0;
+  c->hesf_theta[0] = 4.5; c->hesf_theta[1] = 7.0;
 }
 
 mx_context *mx_create(const char *pack_path, const mx_config *cfg) {

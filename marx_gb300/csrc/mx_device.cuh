@@ -365,8 +365,9 @@ struct Ph {
   float upix, vpix;            // HRC-S u, v pixel    (set bit 4)
 };
 #define MX_SET_SUPPORT 1u
-#define MX_SET_HRC 2u
+#define MX_SET_HRC 2u     // pulse height
 #define MX_SET_UV 4u
+#define MX_SET_REGION 8u
 
 // ------------------------------------------------------------- mirror --
 // JDMquadratic_root (qroot.c:36-70), same cancellation-free form.
@@ -1000,6 +1001,173 @@ MXD void detect_stage(const MxTables &T, const MxChipDev *chips, int nchips, Ph 
   ph.p = p;
 }
 
+// ---------------------------------------------------------------- HRC --
+MXD float hrc_interp(const MxTables &T, const MxTabDev &t, float x) {   // JDMinterpolate_f
+  return interp_f(x, T.hrc_tab + t.x_off, T.hrc_tab + t.y_off, T.hrc_slope + t.s_off, (unsigned) t.n);
+}
+
+// _marx_hrc_compute_pha (hrc-i.c:71-91): delta E / E = 1 (FWHM).
+MXD int16_t hrc_pha(double energy, Rng &rng) {
+  if (energy <= 0.5) energy = 141.582 * sqrt(energy);
+  else if (energy < 2.0) energy = 107.299 * pow(energy, 0.1);
+  else energy = 115.0;
+  energy = energy * (1.0 + 0.424661 * rng.normal());
+  if (energy < 0.0) energy = 0.0;
+  return (int16_t) energy;
+}
+
+// get_filter_region (hrc-s.c:119-185): UV/ion shield region 0..3 at (y, z)
+// in the MARX frame, or -1 in a gap.
+MXD int hrc_filter_region(const MxHrcDev &h, double y, double z) {
+  y -= h.shield_yc;
+  z -= h.shield_zc;
+  if (y < 0) {
+    y = -y;
+    if (y < h.shield_l) return 0;
+    if (y < h.shield_sl) return z >= h.shield_t ? 0 : 1;
+    if (y >= h.shield_sl_gap) return z >= h.shield_t ? 2 : 3;
+    return -1;
+  }
+  if (y < h.shield_r) return 0;
+  if (y < h.shield_sr) return z >= h.shield_t ? 0 : 1;
+  if (y >= h.shield_sr_gap) return z >= h.shield_t ? 2 : 3;
+  return -1;
+}
+
+// rand_gauss2d_radius (hrcblur.c:233-245): a draw of exactly 0 is redrawn.
+MXD double gauss2d_radius(double sigma, Rng &rng) {
+  double c;
+  int guard = 0;
+  do { c = rng.uniform(); } while (c == 0.0 && !rng.overrun && ++guard < 8);
+  return sigma * sqrt(-2 * log(c));
+}
+
+// _marx_hrc_blur_position (hrcblur.c:258-298).
+MXD void hrc_blur(const MxHrcDev &h, bool extend, double &dx, double &dy, Rng &rng) {
+  double r = rng.uniform(), x0, y0;
+  if (r < h.g1_w) { r = gauss2d_radius(h.g1_sigma, rng); x0 = 0.0; y0 = 0.0; }
+  else if (r < h.g1_w + h.g2_w) { r = gauss2d_radius(h.g2_sigma, rng); x0 = h.g2_x; y0 = h.g2_y; }
+  else {
+    double c = rng.uniform(), rmax = h.l1_rmax / h.l1_hwhm;
+    r = h.l1_hwhm * sqrt(expm1(c * log1p(rmax * rmax)));
+    x0 = h.l1_x; y0 = h.l1_y;
+  }
+  double theta = (2.0 * PI) * rng.uniform();
+  dx += x0 + r * cos(theta);
+  dy += y0 + r * sin(theta);
+  if (!extend) {
+    if (dx < 0.0) dx = 0.0;
+    if (dy < 0.0) dy = 0.0;
+  }
+}
+
+// drake_intersection + the reflection of _marx_drake_reflect (drake.c:250-351)
+// for one photon, in the MARX frame.
+MXD void drake_reflect(const MxTables &T, const MxHrcDev &h, Ph &ph, Rng &rng) {
+  const D3 x0 = ph.x, p = ph.p;
+  for (int i = 0; i < h.drake_n; i++) {
+    const MxPlateDev &r = h.plates[i];
+    const D3 nrm = mk(r.normal[0], r.normal[1], r.normal[2]), a = mk(r.a[0], r.a[1], r.a[2]);
+    double pdn = dot(p, nrm);
+    if (pdn == 0.0) continue;
+    double t = dot(a - x0, nrm) / pdn;
+    D3 nx = x0 + t * p;
+    D3 xp = nx - a;
+    double xx = dot(xp, mk(r.e1[0], r.e1[1], r.e1[2]));
+    if ((xx < 0.0) || (xx >= r.len1)) continue;
+    double yy = dot(xp, mk(r.e2[0], r.e2[1], r.e2[2]));
+    if ((yy < 0.0) || (yy >= r.len2)) continue;
+    const bool cr = xx < h.drake_cr_width;
+    ph.x = nx;
+    float fe = (float) ph.e;
+    float beta = hrc_interp(T, cr ? h.cr_beta : h.c_beta, fe), delta = hrc_interp(T, cr ? h.cr_delta : h.c_delta, fe);
+    double rfl = reflectivity(fabs(pdn), f2d(beta), f2d(delta));
+    if (rfl < rng.uniform()) { ph.flags |= MX_PHOTON_DRAKE_BLOCKED; return; }
+    ph.p = p + (-2.0 * pdn) * nrm;
+    ph.flags |= MX_PHOTON_DRAKE_REFLECTED;
+    return;
+  }
+}
+
+// _marx_hrc_i_detect / _marx_hrc_s_detect per photon (hrc-i.c:116-176,
+// hrc-s.c:254-319) with apply_hrc_qe (hrc-i.c:93-114, hrc-s.c:188-230).
+MXD void hrc_detect_stage(const MxTables &T, const MxChipDev *chips, int nchips, Ph &ph, Rng &rng) {
+  const MxHrcDev &h = T.hrc;
+  rng.window(MX_U_HRC, 6, MX_N_HRC, 2);
+  const bool hrcs = h.kind == MX_DETECTOR_HRC_S;
+  if (hrcs && h.drake_n) {
+    drake_reflect(T, h, ph, rng);
+    if (ph.flags & MX_BAD_PHOTON_MASK) return;
+  }
+  D3 off = mk(T.det_offset[0], T.det_offset[1], T.det_offset[2]);
+  D3 x = ph.x - off, p = ph.p;
+  int hit = -1;
+  D3 xh = x;
+  double dx = 0, dy = 0;
+  for (int k = 0; k < nchips; k++)
+    if (1 == chip_plane(chips[k], x, p, xh, dx, dy, true)) { hit = k; break; }
+  if (hit < 0 && T.det_extend) {
+    double best = -1;
+    for (int k = 0; k < nchips; k++) {
+      D3 xx; double ddx, ddy;
+      if (-1 == chip_plane(chips[k], x, p, xx, ddx, ddy, false)) continue;
+      double ex = ddx - 0.5 * chips[k].xlen, ey = ddy - 0.5 * chips[k].ylen, r2 = ex * ex + ey * ey;
+      if (r2 < best || hit < 0) { hit = k; xh = xx; dx = ddx; dy = ddy; best = r2; }
+    }
+  }
+  if (hit < 0) {
+    ph.flags |= MX_PHOTON_MISSED_DETECTOR;
+    ph.ccd = -1;
+    ph.x = x + off; ph.p = p;
+    return;
+  }
+  x = xh;
+  const MxChipDev &d = chips[hit];
+  const float fe = (float) ph.e;
+  bool ok = true;
+  const int m = hrcs ? d.id - 1 : 0;                     // facet index 0..2
+  const MxTabDev &mcp = h.mcp[hrcs ? 2 - m : 0];         // HRC-S MCP ids 1, 2, 3 use QE files 2, 1, 0
+  if (mcp.n && rng.uniform() >= (double) hrc_interp(T, mcp, fe)) ok = false;
+  int region = 0;
+  if (ok && hrcs) {
+    double t = (h.shield_x - x.x) / p.x;
+    region = hrc_filter_region(h, x.y + t * p.y, x.z + t * p.z);
+    if (region < 0) ok = false;
+  }
+  if (ok) {
+    const MxTabDev &f = h.filt[region];
+    if (f.n && rng.uniform() >= (double) hrc_interp(T, f, fe)) ok = false;
+  }
+  if (!ok) {
+    ph.flags |= MX_PHOTON_UNDETECTED;
+    ph.ccd = -1;
+  } else {
+    if (hrcs) { ph.region = (uint8_t) region; ph.set |= MX_SET_REGION; }
+    ph.pha = hrc_pha(ph.e, rng);
+    ph.set |= MX_SET_HRC;
+    if (h.blur && !T.det_ideal) hrc_blur(h, T.det_extend != 0, dx, dy, rng);
+    ph.ccd = d.id;
+    if (hrcs) {   // _marx_hrc_s_compute_pixel (hrc_s_geom.c:289-340)
+      double u = h.u_active0 + div_by(dx, h.pix[0], h.inv_pix[0]);
+      double v = h.v_active0[m] + div_by(dy, h.pix[1], h.inv_pix[1]);
+      ph.upix = (float) u; ph.vpix = (float) v;
+      ph.set |= MX_SET_UV;
+      ph.ypix = (float) (h.cxcy0[m][0] + (u - h.uv0[m][0]));
+      ph.zpix = (float) (h.cxcy0[m][1] + (v - h.uv0[m][1]));
+    } else {      // _marx_hrc_i_compute_pixel (hrc_i_geom.c:134-143)
+      ph.ypix = (float) (h.ll_cxcy[0] + div_by(dx, h.pix[0], h.inv_pix[0]));
+      ph.zpix = (float) (h.ll_cxcy[1] + div_by(dy, h.pix[1], h.inv_pix[1]));
+    }
+  }
+  ph.x = x + off;
+  ph.p = p;
+}
+
+MXD void any_detect_stage(const MxTables &T, const MxChipDev *chips, int nchips, Ph &ph, Rng &rng) {
+  if (T.det_kind == MX_DETECTOR_HRC_I || T.det_kind == MX_DETECTOR_HRC_S) hrc_detect_stage(T, chips, nchips, ph, rng);
+  else detect_stage(T, chips, nchips, ph, rng);
+}
+
 // The fused per-photon trace: dither at creation (source.c:357), then the
 // stages of process_photons (marx.c:240-273); a photon with a bad flag is
 // skipped by later stages as marx_prune_photons drops it, and a photon
@@ -1013,7 +1181,7 @@ MXD void trace_photon(const MxTables &T, const MxShellDev *shells, const float *
     grating_stage(T, grs, T.grating, ph, rng);
   if (rng.overrun) return;
   if ((stages & MX_STAGE_DETECT) && T.nchips && !(ph.flags & MX_BAD_PHOTON_MASK))
-    detect_stage(T, chips + T.chip_off, T.nchips, ph, rng);
+    any_detect_stage(T, chips + T.chip_off, T.nchips, ph, rng);
 }
 
 }  // namespace mx

@@ -30,6 +30,8 @@ struct HostModel {
   std::vector<MxChipDev> chips;
   std::vector<float> support_energy, support_cum;
   std::vector<double> support_k;
+  std::vector<float> hrc_tab;
+  std::vector<double> hrc_slope;
 };
 
 bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string &err);

@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_wave_c(MxTables T, TraceIO 
     if (!r.overrun && (io.stages & MX_STAGE_GRATING) && T.grating && !(q.flags & MX_BAD_PHOTON_MASK))
       grating_stage(T, gr, T.grating, q, r);
     if (!r.overrun && (io.stages & MX_STAGE_DETECT) && T.nchips && !(q.flags & MX_BAD_PHOTON_MASK))
-      detect_stage(T, ch + T.chip_off, T.nchips, q, r);
+      any_detect_stage(T, ch + T.chip_off, T.nchips, q, r);
     store_core(io, i, q, r.overrun);
     store_extra(io, i, q);
     if (q.order != unset && io.order) io.order[i] = (int8_t) q.order;

@@ -311,6 +311,255 @@ static bool build_letg(const Pack &pk, const mx_config &cfg, HostModel &M, std::
   return true;
 }
 
+// ------------------------------------------------------------------ HRC --
+static void v3_sum(double r[3], const double a[3], const double b[3]) { for (int k = 0; k < 3; k++) r[k] = a[k] + b[k]; }
+static void v3_diff(double r[3], const double a[3], const double b[3]) { for (int k = 0; k < 3; k++) r[k] = a[k] - b[k]; }
+static double v3_dot(const double a[3], const double b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+static void v3_ax_by(double r[3], double a, const double x[3], double b, const double y[3]) {  // JDMv_ax1_bx2
+  for (int k = 0; k < 3; k++) r[k] = a * x[k] + b * y[k];
+}
+static void v3_cross(double c[3], const double a[3], const double b[3]) {  // JDMv_cross_prod (vector.c:29)
+  double t[3];
+  t[2] = a[0] * b[1] - a[1] * b[0];
+  t[0] = a[1] * b[2] - a[2] * b[1];
+  t[1] = a[2] * b[0] - a[0] * b[2];
+  memcpy(c, t, sizeof(t));
+}
+
+// A facet from its four corners: the CALDB aimpoint and origin offset
+// (_marx_caldb_patch_aimpoint, caldb.c:468-491), then the basis
+// (_marx_compute_detector_basis, detector.c:383-401).
+static MxChipDev facet(int id, const double ll0[3], const double lr0[3], const double ul0[3], const double aim[3],
+                       const double orig[3]) {
+  MxChipDev c;
+  memset(&c, 0, sizeof(c));
+  c.id = id;
+  double ofs[3], ll[3], lr[3], ul[3], xh[3], yh[3];
+  v3_sum(ofs, aim, orig);
+  v3_sum(ll, ll0, ofs); v3_sum(lr, lr0, ofs); v3_sum(ul, ul0, ofs);
+  v3_diff(xh, lr, ll); v3_diff(yh, ul, ll);
+  c.xlen = vlen(xh); c.ylen = vlen(yh);
+  vnorm(xh); vnorm(yh);
+  double nrm[3];
+  v3_cross(nrm, xh, yh);
+  for (int k = 0; k < 3; k++) { c.x_ll[k] = ll[k]; c.xhat[k] = xh[k]; c.yhat[k] = yh[k]; c.normal[k] = nrm[k]; }
+  c.xpix = c.ypix = 1.0; c.inv_xpix = c.inv_ypix = 1.0;
+  for (int k = 0; k < 3; k++) {
+    c.f_ll[k] = (float) c.x_ll[k]; c.f_xhat[k] = (float) c.xhat[k];
+    c.f_yhat[k] = (float) c.yhat[k]; c.f_normal[k] = (float) c.normal[k];
+  }
+  c.f_xlen = (float) c.xlen; c.f_ylen = (float) c.ylen;
+  return c;
+}
+
+// Append a bdat table (energies, values) to the HRC float tables with the
+// interval slopes JDMinterpolate_f forms (float dy over double dx).
+static bool hrc_table(const Pack &pk, const std::string &name, int col, HostModel &M, MxTabDev &t, std::string &err) {
+  size_t cnt;
+  const float *a = pk.get<float>(name, &cnt, err);
+  if (!a) return false;
+  int ncol = name.find("optconst") != std::string::npos ? 3 : 2;
+  unsigned n = (unsigned) (cnt / ncol);
+  if (n < 1) { err = name + ": empty table"; return false; }
+  t.x_off = (int32_t) M.hrc_tab.size();
+  M.hrc_tab.insert(M.hrc_tab.end(), a, a + n);
+  t.y_off = (int32_t) M.hrc_tab.size();
+  M.hrc_tab.insert(M.hrc_tab.end(), a + (size_t) col * n, a + (size_t) (col + 1) * n);
+  t.s_off = (int32_t) M.hrc_slope.size();
+  append_slopes(M.hrc_slope, a, a + (size_t) col * n, n);
+  M.hrc_slope.push_back(0.0);
+  t.n = (int32_t) n;
+  return true;
+}
+
+// fixup_blur_parms (hrcblur.c:105-188): amplitudes to weights, pixels to mm.
+static bool hrc_blur(const double *b, double pixelsize, MxHrcDev &h, std::string &err) {
+  double g1s = b[0], g1x = b[1], g1y = b[2], g1w = b[3], g2s = b[4], g2x = b[5], g2y = b[6], g2w = b[7];
+  double l1h = b[8], l1x = b[9], l1y = b[10], l1w = b[11], l1r = b[12];
+  if (g1w < 0 || g2w < 0 || l1w < 0 || g1s <= 0 || g2s <= 0 || l1h <= 0 || l1r <= 0) {
+    err = "One or more of the HRC blur parameters has an invalid/unsupported value"; return false;
+  }
+  const double fwhm_to_sigma = 0.42466090014400953;
+  g1s *= pixelsize; g1x *= pixelsize; g1y *= pixelsize;
+  g2s *= pixelsize; g2x *= pixelsize; g2y *= pixelsize;
+  l1h *= pixelsize; l1x *= pixelsize; l1y *= pixelsize; l1r *= pixelsize;
+  g2x -= g1x; g2y -= g1y; l1x -= g1x; l1y -= g1y;
+  g1s *= fwhm_to_sigma; g2s *= fwhm_to_sigma; l1h *= 0.5;
+  double norm = 1.0 / (2 * PI_ * g1s * g1s);
+  g1w /= norm;
+  norm = 1.0 / (2 * PI_ * g2s * g2s);
+  g2w /= norm;
+  double g2 = l1h; g2 = g2 * g2;
+  norm = 1.0 / (g2 * PI_ * log(1 + l1r * l1r / g2));
+  l1w /= norm;
+  norm = g1w + g2w + l1w;
+  if (norm > 0) { g1w /= norm; g2w /= norm; l1w /= norm; }
+  h.g1_sigma = g1s; h.g1_w = g1w; h.g2_sigma = g2s; h.g2_x = g2x; h.g2_y = g2y; h.g2_w = g2w;
+  h.l1_hwhm = l1h; h.l1_x = l1x; h.l1_y = l1y; h.l1_rmax = l1r; h.l1_w = l1w;
+  return true;
+}
+
+// The HRC-I (hrc_i_geom.c:48-130, hrc-i.c:183-228) or HRC-S (hrc_s_geom.c,
+// hrc-s.c:352-441, drake.c:148-246).  Facets go to chips[10] (HRC-I) and
+// chips[11..13] (HRC-S MCPs 1, 2, 3).
+static bool build_hrc(const Pack &pk, const mx_config &cfg, HostModel &M, std::string &err) {
+  MxTables &T = M.T;
+  MxHrcDev &h = T.hrc;
+  memset(&h, 0, sizeof(h));
+  h.kind = cfg.detector;
+  h.blur = !cfg.det_ideal;
+  M.hrc_tab.clear(); M.hrc_slope.clear();
+  auto table = [&](const char *name, int col, MxTabDev &t) {
+    if (cfg.det_ideal) { memset(&t, 0, sizeof(t)); return true; }   // _marx_hrc_read_efficiencies: perfect
+    return hrc_table(pk, name, col, M, t, err);
+  };
+  double pixelsize;
+  if (cfg.detector == MX_DETECTOR_HRC_I) {
+    size_t n;
+    const double *g = pk.get<double>("hrc/i_geom", &n, err);
+    const double *aim = pk.get<double>("hrc/aimpt_i", nullptr, err), *org = pk.get<double>("hrc/origin_i", nullptr, err);
+    if (!g || !aim || !org) return false;
+    if (n != 15) { err = "hrc/i_geom malformed"; return false; }
+    const double xps = g[0], yps = g[1];
+    const double *LL_XYZ = g + 2, *Center_XYZ = g + 5, *LLtoLR = g + 8, *Center_CXCY = g + 11, *Aim_CXCY = g + 13;
+    // setup_coordinate_xforms (hrc_i_geom.c:48-101)
+    double a[3] = {LLtoLR[0], LLtoLR[1], LLtoLR[2]};
+    double len = vlen(a);
+    if (len == 0.0) { err = "Length of vector from LL to LR must be non-zero"; return false; }
+    double il = 1.0 / len;
+    for (int k = 0; k < 3; k++) a[k] = il * a[k];
+    double center[3] = {Center_XYZ[0], Center_XYZ[1], Center_XYZ[2]}, LL[3] = {LL_XYZ[0], LL_XYZ[1], LL_XYZ[2]};
+    double ll[3], lr[3], LR[3], UR[3], UL[3], t3[3];
+    v3_diff(ll, LL, center);
+    if (vlen(ll) == 0.0) { err = "The LL corner must not be the center"; return false; }
+    v3_ax_by(lr, 1.0, ll, -2.0 * v3_dot(a, ll), a);
+    v3_sum(LR, center, lr);
+    for (int k = 0; k < 3; k++) t3[k] = -1.0 * ll[k];
+    v3_sum(UR, center, t3);
+    for (int k = 0; k < 3; k++) t3[k] = -1.0 * lr[k];
+    v3_sum(UL, center, t3);
+    if (xps <= 0.0 || yps <= 0.0) { err = "X and Y Pixel sizes must be larger than 0"; return false; }
+    double b[3];
+    v3_diff(b, UL, LL);
+    vnorm(b);
+    double llc0 = Center_CXCY[0] + v3_dot(ll, a) / xps, llc1 = Center_CXCY[1] + v3_dot(ll, b) / yps;
+    double dx[3];
+    v3_ax_by(t3, (llc0 - Aim_CXCY[0]) * xps, a, (llc1 - Aim_CXCY[1]) * yps, b);
+    v3_diff(dx, t3, LL);
+    double LL2[3], LR2[3], UL2[3];
+    v3_sum(LL2, LL, dx); v3_sum(LR2, LR, dx); v3_sum(UL2, UL, dx);
+    M.chips[10] = facet(0, LL2, LR2, UL2, aim, org);
+    h.ll_cxcy[0] = llc0; h.ll_cxcy[1] = llc1;
+    h.pix[0] = xps; h.pix[1] = yps; h.inv_pix[0] = 1.0 / xps; h.inv_pix[1] = 1.0 / yps;
+    pixelsize = 0.5 * (xps * 0.25 + yps * 0.25);
+    if (!table("hrc/qe_i", 1, h.mcp[0]) || !table("hrc/uvis_i", 1, h.filt[0])) return false;
+    if (!hrc_blur(cfg.hrc_i_blur, pixelsize, h, err)) return false;
+    T.chip_off = 10; T.nchips = 1;
+  } else {
+    size_t n;
+    const double *g = pk.get<double>("hrc/s_geom", &n, err);
+    const double *aim = pk.get<double>("hrc/aimpt_s", nullptr, err), *org = pk.get<double>("hrc/origin_s", nullptr, err);
+    if (!g || !aim || !org) return false;
+    if (n != 45) { err = "hrc/s_geom malformed"; return false; }
+    const double vps = g[0], *V_Active = g + 1, ups = g[7], *U_Active = g + 8, *Aim_Off = g + 10;
+    const double *UV[3] = {g + 13, g + 17, g + 15};      // left, middle, right
+    const double *XYZ0[3] = {g + 19, g + 25, g + 22};
+    const double *CXCY[3] = {g + 28, g + 32, g + 30};
+    const double deg = PI_ / 180.0;
+    const double left_t = g[34] * deg, right_t = g[35] * deg, det_t = g[36] * deg;
+    const double *ion = g + 37;   // T L R X SL SR GapL GapR
+    // _marx_hrc_s_geom_init and setup_alphas_and_betas (hrc_s_geom.c:134-180, 446-478)
+    double xyz[3][3];
+    for (int m = 0; m < 3; m++)
+      for (int k = 0; k < 3; k++) xyz[m][k] = XYZ0[m][k] + Aim_Off[k];
+    const double alpha[3] = {0.0, 0.0, ups};
+    const double beta[3][3] = {{-1.0 * sin(left_t) * vps, -1.0 * cos(left_t) * vps, 0.0},
+                               {0.0, -1.0 * vps, 0.0},
+                               {1.0 * sin(right_t) * vps, -1.0 * cos(right_t) * vps, 0.0}};
+    auto uv_xyz = [&](int m, double u, double v, double out[3]) {   // map_uv_to_xyz (hrc_s_geom.c:98-109)
+      double du = u - UV[m][0], dv = v - UV[m][1];
+      for (int k = 0; k < 3; k++) out[k] = xyz[m][k] + du * alpha[k] + dv * beta[m][k];
+    };
+    // rotate_mcp (hrc_s_geom.c:211-224): JDMv_rotate_vector1 about (-1, 0, 0), no normalisation
+    const double st = sin(det_t), ct = cos(det_t), axis[3] = {-1, 0, 0};
+    auto rot = [&](double p[3]) {
+      double pn = v3_dot(p, axis), nxp[3];
+      v3_cross(nxp, axis, p);
+      double q[3];
+      for (int k = 0; k < 3; k++) q[k] = ct * p[k] + pn * (1.0 - ct) * axis[k] + st * nxp[k];
+      memcpy(p, q, sizeof(q));
+    };
+    for (int m = 0; m < 3; m++) {
+      double ll[3], lr[3], ul[3];
+      uv_xyz(m, U_Active[0], V_Active[2 * m + 1], ul);
+      uv_xyz(m, U_Active[0], V_Active[2 * m], ll);
+      uv_xyz(m, U_Active[1], V_Active[2 * m], lr);
+      rot(ll); rot(lr); rot(ul);
+      M.chips[11 + m] = facet(m + 1, ll, lr, ul, aim, org);
+      h.v_active0[m] = V_Active[2 * m];
+      h.uv0[m][0] = UV[m][0]; h.uv0[m][1] = UV[m][1];
+      h.cxcy0[m][0] = CXCY[m][0]; h.cxcy0[m][1] = CXCY[m][1];
+    }
+    h.u_active0 = U_Active[0];
+    h.pix[0] = ups; h.pix[1] = vps; h.inv_pix[0] = 1.0 / ups; h.inv_pix[1] = 1.0 / vps;
+    pixelsize = 0.5 * (ups * 0.25 + vps * 0.25);
+    // MCP regions: facet ids 1, 2, 3 -> QE files 2, 1, 0 (all mcp_qe_s); filters 0..3
+    for (int k = 0; k < 3; k++)
+      if (!table("hrc/qe_s", 1, h.mcp[k])) return false;
+    const char *uv[4] = {"hrc/uvis_s0", "hrc/uvis_s1", "hrc/uvis_s2", "hrc/uvis_s3"};
+    for (int k = 0; k < 4; k++)
+      if (!table(uv[k], 1, h.filt[k])) return false;
+    if (!hrc_blur(cfg.hrc_s_blur, pixelsize, h, err)) return false;
+    // geometric centre of the middle MCP (hrc-s.c:424-431), ion shield
+    const MxChipDev &mid = M.chips[12];
+    double ur[3], half[3], ur0[3], ofs[3];
+    uv_xyz(1, U_Active[1], V_Active[3], ur0);   // the middle MCP's x_ur corner, rotated and offset
+    rot(ur0);
+    v3_sum(ofs, aim, org);
+    v3_sum(ur, ur0, ofs);
+    v3_ax_by(half, 0.5, mid.x_ll, 0.5, ur);
+    double off[3] = {cfg.det_offset[0], cfg.det_offset[1], cfg.det_offset[2]}, gc[3];
+    v3_sum(gc, off, half);
+    h.shield_yc = gc[1]; h.shield_zc = gc[2];
+    h.shield_t = ion[0]; h.shield_l = ion[1]; h.shield_r = ion[2]; h.shield_x = ion[3];
+    h.shield_sl = ion[4]; h.shield_sr = ion[5];
+    h.shield_sr_gap = ion[5] + ion[7];
+    h.shield_sl_gap = ion[4] + ion[6];
+    // Drake flat (_marx_drake_flat_init, drake.c:148-246)
+    h.drake_n = 0;
+    if (cfg.hrc_hesf) {
+      int np = cfg.hesf_n;
+      if (np <= 0 || np > 4) { err = "HESFN must lie in 1..4"; return false; }
+      double cx = cfg.hesf_offset_x, cz = cfg.hesf_offset_z;
+      for (int i = 0; i < np; i++) {
+        double ang = cfg.hesf_theta[i] * (PI_ / 180.0);
+        double hh = cfg.hesf_height[i], htt = hh * tan(ang);
+        for (int side = 0; side < 2; side++) {
+          MxPlateDev &r = h.plates[i + side * np];
+          double e1[3] = {0.0, side ? -1.0 : 1.0, 0.0}, e2[3] = {hh, 0.0, -htt}, nrm[3], a[3];
+          double l2 = vlen(e2);
+          vnorm(e2);
+          if (side == 0) v3_cross(nrm, e1, e2); else v3_cross(nrm, e2, e1);
+          double corner[3] = {cx, side ? -cfg.hesf_gap_y2 : cfg.hesf_gap_y1, cz};
+          v3_sum(a, gc, corner);
+          for (int k = 0; k < 3; k++) { r.a[k] = a[k]; r.e1[k] = e1[k]; r.e2[k] = e2[k]; r.normal[k] = nrm[k]; }
+          r.len1 = cfg.hesf_length; r.len2 = l2;
+        }
+        cz -= htt;
+        cx += hh;
+      }
+      h.drake_n = 2 * np;
+      h.drake_cr_width = cfg.hesf_cr_width;
+      if (!hrc_table(pk, "hrc/optconst_c", 1, M, h.c_beta, err) || !hrc_table(pk, "hrc/optconst_c", 2, M, h.c_delta, err) ||
+          !hrc_table(pk, "hrc/optconst_cr", 1, M, h.cr_beta, err) || !hrc_table(pk, "hrc/optconst_cr", 2, M, h.cr_delta, err))
+        return false;
+    }
+    T.chip_off = 11; T.nchips = 3;
+  }
+  if (M.hrc_tab.empty()) { M.hrc_tab.push_back(0.f); M.hrc_slope.push_back(0.0); }
+  return true;
+}
+
 bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string &err) {
   M = HostModel();
   MxTables &T = M.T;
@@ -526,9 +775,8 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
   // ---- detector chips: ACIS-I (ids 0-3, aimpoint AI2) then ACIS-S (ids
   // 4-9, aimpoint AS1), each set as the reference builds it for that
   // detector; a chip's index in the table is its id.
-  if (cfg.detector != MX_DETECTOR_NONE && cfg.detector != MX_DETECTOR_ACIS_I && cfg.detector != MX_DETECTOR_ACIS_S) {
-    err = "unsupported detector"; return false;
-  }
+  if (cfg.detector < MX_DETECTOR_NONE || cfg.detector > MX_DETECTOR_HRC_S) { err = "unsupported detector"; return false; }
+  const bool acis = cfg.detector == MX_DETECTOR_ACIS_I || cfg.detector == MX_DETECTOR_ACIS_S;
   {
     size_t ng = 0;
     const double *geom = pk.get<double>("acis/geom", &ng, err);
@@ -572,11 +820,18 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
       c.f_xlen = (float) c.xlen; c.f_ylen = (float) c.ylen;
       M.chips.push_back(c);
     }
-    if (cfg.detector != MX_DETECTOR_NONE && cfg.acis_exposure_time <= 0) {
+    if (acis && cfg.acis_exposure_time <= 0) {
       err = "ACIS_Exposure_Time must be greater than 0"; return false;
     }
+    M.chips.resize(MX_MAX_CHIPS);
     T.chip_off = cfg.detector == MX_DETECTOR_ACIS_S ? 4 : 0;
     T.nchips = cfg.detector == MX_DETECTOR_NONE ? 0 : (cfg.detector == MX_DETECTOR_ACIS_I ? 4 : 6);
+    T.det_kind = cfg.detector;
+    T.det_ideal = cfg.det_ideal != 0;
+    M.hrc_tab.clear(); M.hrc_slope.clear();
+    memset(&T.hrc, 0, sizeof(T.hrc));
+    if (!acis && cfg.detector != MX_DETECTOR_NONE && !build_hrc(pk, cfg, M, err)) return false;
+    if (M.hrc_tab.empty()) { M.hrc_tab.push_back(0.f); M.hrc_slope.push_back(0.0); }
     T.det_extend = cfg.det_extend != 0;
     for (int k = 0; k < 3; k++) T.det_offset[k] = cfg.det_offset[k];
     T.frame_transfer = cfg.acis_frame_transfer_time < 0.0 ? 0.0 : cfg.acis_frame_transfer_time;

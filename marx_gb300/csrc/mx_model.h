@@ -6,7 +6,7 @@
 
 #define MX_FOLD_MAX 256      // WFold arrays per table (the HRMA tables hold 200)
 #define MX_FOLD_THETA 208    // angles per WFold array (the HRMA tables hold 201)
-#define MX_MAX_CHIPS 10
+#define MX_MAX_CHIPS 14       // ACIS ids 0-9, then HRC-I (id 0) and HRC-S (ids 1-3)
 #define MX_MAX_SECTORS 64
 #define MX_MAX_GRATINGS 8     // HETG shells 1,3,4,6 then LETG shells 1,3,4,6
 
@@ -37,6 +37,41 @@ struct MxSupportDev {
   int32_t cum_off, norders;    // cumulative efficiencies [energy][order] on the shared energy grid
   int32_t order_off, rotate;   // order constants in support_k; rotate: the angle is not zero
   double cos_t, sin_t;         // cos and sin of the angle
+};
+
+// A float table lookup (JDMinterpolate_f) in the HRC tables: abscissae at
+// hrc_tab + x_off, ordinates at hrc_tab + y_off, interval slopes at
+// hrc_slope + s_off; n = 0 means a perfect efficiency (no table).
+struct MxTabDev {
+  int32_t x_off, y_off, s_off, n;
+};
+
+// One Drake-flat plate section (drake.c:48-58, 188-230).
+struct MxPlateDev {
+  double a[3], e1[3], e2[3], normal[3];
+  double len1, len2;
+};
+
+// The configured HRC (hrc-i.c, hrc-s.c, hrc_i_geom.c, hrc_s_geom.c,
+// hrcblur.c, drake.c), everything the detector stage reads.
+struct MxHrcDev {
+  int32_t kind;                 // MX_DETECTOR_HRC_I or MX_DETECTOR_HRC_S
+  int32_t blur;                 // position blur on (not DetIdeal)
+  // pixel mapping: HRC-I y = ll_cxcy + d / size; HRC-S per MCP (facets ids 1..3)
+  double ll_cxcy[2], pix[2], inv_pix[2];       // HRC-I pixel sizes, HRC-S U and V sizes
+  double u_active0, v_active0[3], uv0[3][2], cxcy0[3][2];
+  // efficiencies: MCP per facet (HRC-S: facet id k uses MCP region map[k]), filter per region
+  MxTabDev mcp[3], filt[4];
+  // HRC-S UV/ion shield (hrc-s.c:119-185, 410-418)
+  double shield_yc, shield_zc, shield_t, shield_l, shield_r, shield_sl, shield_sr, shield_sl_gap, shield_sr_gap,
+      shield_x;
+  // position blur (hrcblur.c:105-188), mm, centred on the first gaussian
+  double g1_sigma, g1_w, g2_sigma, g2_x, g2_y, g2_w, l1_hwhm, l1_x, l1_y, l1_rmax, l1_w;
+  // Drake flat (HRC-S): 2 x plates sections, carbon and chromium constants
+  int32_t drake_n, pad;
+  double drake_cr_width;
+  MxPlateDev plates[8];
+  MxTabDev c_beta, c_delta, cr_beta, cr_delta;
 };
 
 struct MxChipDev {
@@ -90,4 +125,9 @@ struct MxTables {
   int32_t chip_off, pad_chip;
   double det_offset[3], frame_transfer, frame_time, exposure, focal_length;
   double inv_frame_time;
+  int32_t det_kind, det_ideal;  // MX_DETECTOR_* of the configuration, DetIdeal
+  // HRC tables (global memory) and parameters
+  const float *hrc_tab;
+  const double *hrc_slope;
+  MxHrcDev hrc;
 };

@@ -94,10 +94,8 @@ __device__ __forceinline__ void store_extra(const TraceIO &io, uint32_t i, const
   const size_t n = io.stride;
   if ((q.set & MX_SET_SUPPORT) && io.support)
     for (int k = 0; k < 4; k++) io.support[k * n + i] = q.sup[k];
-  if (q.set & MX_SET_HRC) {
-    if (io.pha) io.pha[i] = q.pha;
-    if (io.region) io.region[i] = q.region;
-  }
+  if ((q.set & MX_SET_HRC) && io.pha) io.pha[i] = q.pha;
+  if ((q.set & MX_SET_REGION) && io.region) io.region[i] = q.region;
   if (q.set & MX_SET_UV) {
     if (io.upix) io.upix[i] = q.upix;
     if (io.vpix) io.vpix[i] = q.vpix;

@@ -10,6 +10,9 @@ plain_hetg      2e7 photons, power law (photon index 1.7) on 0.4-8 keV
                 absorbed by NH = 1e21 cm^-2, HETG orders -3..+3, ACIS-S.
 plain_letg      4e6 photons of the same spectrum through the LETG and its
                 support gratings, ACIS-S.
+plain_hrci      4e6 photons of plain_scatter's source on the HRC-I.
+letg_hrcs       4e6 photons of plain_hetg's spectrum through the LETG onto
+                the HRC-S behind its Drake flat.
 batched         256 sources (see marx_gb300.batched).
 differentiable  4e6 weighted rays (see marx_gb300.adjoint).
 
@@ -97,7 +100,8 @@ def _hetg(w, n, seed):
     return ph
 
 
-GENERATORS = {"plain_onaxis": _onaxis, "plain_scatter": _scatter, "plain_hetg": _hetg, "plain_letg": _hetg}
+GENERATORS = {"plain_onaxis": _onaxis, "plain_scatter": _scatter, "plain_hetg": _hetg, "plain_letg": _hetg,
+              "plain_hrci": _scatter, "letg_hrcs": _hetg}
 
 
 def plain_onaxis(parity: bool = False) -> Workload:
@@ -144,8 +148,24 @@ def plain_letg(parity: bool = False) -> Workload:
     return Workload("plain_letg", 4_000_000, c, seed=404, stages=15)
 
 
+def plain_hrci(parity: bool = False) -> Workload:
+    """The plain_scatter source and mirror on the HRC-I (MCP and UV/ion
+    shield efficiencies, position blur, pulse height)."""
+    w = plain_scatter(parity)
+    w.cfg.detector = DETECTOR["HRC-I"]
+    return Workload("plain_hrci", 4_000_000, w.cfg, seed=505, stages=15)
+
+
+def letg_hrcs(parity: bool = False) -> Workload:
+    """LETG on the HRC-S: Drake flat, MCP and shield-region efficiencies,
+    u/v pixels."""
+    w = plain_letg(parity)
+    w.cfg.detector = DETECTOR["HRC-S"]
+    return Workload("letg_hrcs", 4_000_000, w.cfg, seed=606, stages=15)
+
+
 PLAIN = {"plain_onaxis": plain_onaxis, "plain_scatter": plain_scatter, "plain_hetg": plain_hetg}
 # Workloads of the stages the C++ restatement does not cover (LETG, HRC):
 # their parity is pinned to the reference's own outputs only.
-EXTRA = {"plain_letg": plain_letg}
+EXTRA = {"plain_letg": plain_letg, "plain_hrci": plain_hrci, "letg_hrcs": letg_hrcs}
 ALL = {**PLAIN, **EXTRA}

@@ -8,10 +8,12 @@
  * and the per-photon body of _marx_acis_i_detect / _marx_acis_s_detect
  * (marx/libsrc/acis-i.c:96-160, acis-s.c:177-248) through the exported
  * pieces that body calls (_marx_transform_ray, _marx_intersect_with_detector,
- * _marx_acis_apply_streak).  marx_detector_init itself cannot run here: it
- * loads the ACIS FEF calibration file unconditionally and that file is not
- * shipped with the reference, so QE and pulse height are not exercised
- * (DetIdeal semantics; pulse height left at 0).
+ * _marx_acis_apply_streak).  For the ACIS marx_detector_init itself cannot
+ * run here: it loads the ACIS FEF calibration file unconditionally and that
+ * file is not shipped with the reference, so QE and pulse height are not
+ * exercised (DetIdeal semantics; pulse height left at 0).  The HRC
+ * detectors need no missing file: marx_detector_init and marx_detect
+ * (detector.c:298-378) run as they are.
  *
  * Built twice:
  *   MXREF_INTERPOSE=1  the jdmath generator is replaced by per-photon
@@ -142,7 +144,17 @@ int mxref_setup(const char *parfile, const char *datadir, int nover,
    Det_Kind = 0; Det = NULL;
    if (0 == strcmp(buf, "ACIS-I")) Det_Kind = 1;
    else if (0 == strcmp(buf, "ACIS-S")) Det_Kind = 2;
+   else if (0 == strcmp(buf, "HRC-I")) Det_Kind = 3;
+   else if (0 == strcmp(buf, "HRC-S")) Det_Kind = 4;
    else if (0 != strcmp(buf, "NONE")) { set_err("unsupported DetectorType"); return -1; }
+   if (Det_Kind >= 3)
+     {
+        /* The HRC needs no file that is missing here: the reference's own
+         * marx_detector_init runs as it is. */
+        if (-1 == marx_detector_init(Pf)) { set_err("detector init failed"); return -1; }
+        if (NULL == (Det = marx_get_detector_info(buf, 0))) { set_err("detector geometry"); return -1; }
+        return 0;
+     }
    if (Det_Kind)
      {
         double *m = _Marx_Det_XForm_Matrix.matrix;
@@ -337,7 +349,14 @@ int mxref_trace_slots(int n, const double *energy, const double *p_in, const dou
              us[4] = U_pos - (Grating_Is_LETG ? MX_U_LETG : MX_U_GRATING);
              us[5] = N_pos - (Grating_Is_LETG ? MX_N_LETG : MX_N_GRATING);
           }
-        if ((stages & ST_DETECT) && Det_Kind)
+        if ((stages & ST_DETECT) && Det_Kind >= 3)
+          {
+             rng_window(u, MX_U_HRC, MX_U_HRC_N, g, MX_N_HRC, MX_N_HRC_N);
+             pt.history &= ~MARX_DET_NUM_OK;
+             if (-1 == marx_detect(&pt, 0)) { set_err("detect"); return -1; }
+             us[6] = U_pos - MX_U_HRC; us[7] = N_pos - MX_N_HRC;
+          }
+        else if ((stages & ST_DETECT) && Det_Kind)
           {
              rng_window(u, MX_U_DETECT, MX_U_DETECT_N, g, MX_N_DETECT, MX_N_DETECT_N);
              detect_photons(&pt);
@@ -389,7 +408,8 @@ double mxref_trace_batch(int n, const double *energy, const double *p_in, const 
    if ((stages & ST_DITHER) && Have_Dither) _marx_dither_photons(pt, &num);
    if ((stages & ST_MIRROR) && (-1 == marx_mirror_reflect(pt, 0))) goto fail;
    if ((stages & ST_GRATING) && Have_Grating && (-1 == marx_grating_diffract(pt, 0))) goto fail;
-   if ((stages & ST_DETECT) && Det_Kind) detect_photons(pt);
+   if ((stages & ST_DETECT) && Det_Kind >= 3) { if (-1 == marx_detect(pt, 0)) goto fail; }
+   else if ((stages & ST_DETECT) && Det_Kind) detect_photons(pt);
    clock_gettime(CLOCK_MONOTONIC, &t1);
    secs = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
 

@@ -63,6 +63,10 @@ def summarize(q, w):
             else:
                 out["order_hist"] = np.bincount(orders + 11, minlength=23)
         out["ccd_hist"] = np.bincount(q.ccd_num[good].astype(int) + 1, minlength=11)
+        if w.cfg.detector >= 3:     # HRC: pulse heights in bins of 16, shield regions
+            out["pha_hist"] = np.bincount(q.pulse_height[good].astype(int) // 16, minlength=40)[:40]
+            if w.cfg.detector == 4:
+                out["region_hist"] = np.bincount(q.detector_region[good].astype(int), minlength=4)
     return out
 
 

@@ -50,7 +50,7 @@ EXTRA_FIELDS = ("support_orders", "pulse_height", "u_pixel", "v_pixel", "detecto
 
 def assert_parity(q, ref, where=""):
     keys = getattr(ref, "files", None) or [k for k in EXTRA_FIELDS if hasattr(ref, k)]
-    extra = tuple(k for k in EXTRA_FIELDS if k in keys)
+    extra = tuple(k for k in EXTRA_FIELDS if k in keys and hasattr(q, k))
     r = compare(q, ref, exact_fields=("flags", "mirror_shell", "order", "ccd_num", "y_pixel", "z_pixel",
                                       "dither_state") + extra)
     assert r["dx"] <= X_TOL_MM, (where, r)

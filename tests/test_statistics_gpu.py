@@ -51,12 +51,18 @@ def test_survivor_fraction_and_histograms(cuda, name):
         m = (len(ref["order_hist"]) - 1) // 2
         orders = np.bincount(q.order[good].astype(int) + m, minlength=2 * m + 1)
         assert chi2_p(orders, ref["order_hist"]) > 1e-4
+    if "pha_hist" in ref:       # HRC pulse heights
+        pha = np.bincount(q.pulse_height[good].astype(int) // 16, minlength=40)[:40]
+        assert chi2_p(pha, ref["pha_hist"]) > 1e-4
+    if "region_hist" in ref:    # HRC-S UV/ion shield regions
+        reg = np.bincount(q.detector_region[good].astype(int), minlength=4)
+        assert chi2_p(reg, ref["region_hist"]) > 1e-4
     if "fine_hist" in ref:      # LETG fine support grating orders
         fine = np.bincount(q.support_orders[0][good].astype(int) + 9, minlength=19)
         assert chi2_p(fine, ref["fine_hist"]) > 1e-4
 
 
-@pytest.mark.parametrize("name", ["plain_onaxis", "plain_scatter"])
+@pytest.mark.parametrize("name", ["plain_onaxis", "plain_scatter", "plain_hrci"])
 def test_psf_encircled_energy(cuda, name):
     ref = np.load(os.path.join(GOLDEN, f"stats_{name}.npz"))
     w, q = run_gpu(name)
