@@ -401,6 +401,42 @@ void *mx_stream(mx_context *ctx);
 /* Photons flagged MX_PHOTON_VARIATE_OVERRUN since the last reset. */
 int mx_overrun_count(mx_context *ctx, unsigned long long *count, int reset);
 
+/* ------------------------------------------------------------ output --
+ * MARX's output directory format (marx_write_photons, marxio.c:395-478):
+ * one big-endian column file per attribute (xpos.dat, energy.dat,
+ * detector.dat, ...), rows for the photons without a MX_BAD_PHOTON_MASK
+ * bit.  history holds the MX_OUT_* bits of the columns the stages made
+ * valid (the reference's Marx_Photon_Type.history); write_mask the columns
+ * wanted (marx.par OutputVectors); with dither != 0 the dither-state
+ * columns are written whenever asked for.  append != 0 adds rows to the
+ * files already in dir.  The list is in HOST memory.  Bit values as
+ * marx.h:128-147. */
+#define MX_OUT_ENERGY      0x00000001u
+#define MX_OUT_TIME        0x00000002u
+#define MX_OUT_X           0x00000004u
+#define MX_OUT_P           0x00000008u
+#define MX_OUT_TAG         0x00000010u
+#define MX_OUT_PHA         0x00000020u
+#define MX_OUT_PI          0x00000040u
+#define MX_OUT_DET_PIXEL   0x00000080u
+#define MX_OUT_DET_NUM     0x00000100u
+#define MX_OUT_DET_REGION  0x00000200u
+#define MX_OUT_DET_UV      0x00000400u
+#define MX_OUT_SHELL       0x00000800u
+#define MX_OUT_SKY_DITHER  0x00001000u
+#define MX_OUT_DET_DITHER  0x00002000u
+#define MX_OUT_ORDER       0x00100000u
+#define MX_OUT_ORDER1      0x00200000u
+#define MX_OUT_ORDER2      0x00400000u
+#define MX_OUT_ORDER3      0x00800000u
+#define MX_OUT_ORDER4      0x01000000u
+int mx_write_photons(const mx_photons *host, uint32_t history, uint32_t write_mask, int dither, const char *dir,
+                     int append, double total_time);
+const char *mx_write_error(void);   /* message of the last mx_write_photons failure (this thread) */
+/* The history bits a trace of cfg through `stages` makes valid, as the
+ * reference's stages set them. */
+uint32_t mx_output_history(const mx_config *cfg, uint32_t stages);
+
 /* Measured FP64 fused-multiply-add throughput of the current device
  * (TFLOP/s), the denominator of the trace kernels' roofline. */
 int mx_probe_fp64(double *tflops, double *ms);

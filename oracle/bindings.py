@@ -192,6 +192,21 @@ class Reference:
             raise RuntimeError("reference trace: " + self.lib.mxref_last_error().decode())
         return self._to_list(ph, o), used, r
 
+    def write_photons(self, ph: PhotonList, history: int, write_mask: int, out_dir: str, new: bool = True,
+                      total_time: float = 0.0):
+        """The reference's marx_write_photons over ph (host columns)."""
+        c = lambda a, dt: np.ascontiguousarray(a, dtype=dt)
+        f = self.lib.mxref_write_photons
+        f.argtypes = [C.c_char_p, C.c_int] + [C.c_void_p] * 17 + [C.c_ulong, C.c_ulong, C.c_int, C.c_double]
+        cols = [c(ph.energy, np.float64), c(ph.x, np.float64), c(ph.p, np.float64), c(ph.arrival_time, np.float64),
+                c(ph.flags, np.uint32), c(ph.tag, np.uint32), c(ph.mirror_shell, np.int8), c(ph.order, np.int8),
+                c(ph.ccd_num, np.int8), c(ph.y_pixel, np.float32), c(ph.z_pixel, np.float32),
+                c(ph.dither_state, np.float32), c(ph.support_orders, np.int8), c(ph.pulse_height, np.int16),
+                c(ph.u_pixel, np.float32), c(ph.v_pixel, np.float32), c(ph.detector_region, np.uint8)]
+        r = f(out_dir.encode(), ph.n, *[_p(a) for a in cols], history, write_mask, 1 if new else 0, total_time)
+        if r != 0:
+            raise RuntimeError("reference writer failed: " + self.lib.mxref_last_error().decode())
+
     def trace_batch(self, ph: PhotonList, stages: int = 15):
         """Whole batch with the reference's own generator; returns (list, seconds)."""
         assert self.native

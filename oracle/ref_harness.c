@@ -422,3 +422,46 @@ fail:
    return -1;
 }
 #endif
+
+/* ------------------------------------------------------------- output -- */
+/* The reference's own writer (marx_write_photons, marxio.c:395-478) over a
+ * photon list given as columns (component-major x, p, dither state and
+ * support orders as in the engine's lists), for byte comparisons of the
+ * output files.  open_mode 1 creates the files, 0 appends. */
+int mxref_write_photons(const char *dir, int n, const double *energy, const double *x, const double *p,
+                        const double *t, const unsigned int *flags, const unsigned int *tag,
+                        const signed char *shell, const signed char *order, const signed char *ccd,
+                        const float *ypix, const float *zpix, const float *dith, const signed char *sup,
+                        const short *pha, const float *upix, const float *vpix, const unsigned char *region,
+                        unsigned long history, unsigned long write_mask, int open_mode, double total_time)
+{
+   Marx_Photon_Type *pt;
+   int i, k, r;
+
+   if (NULL == (pt = marx_alloc_photon_type((unsigned int) (n > 0 ? n : 1)))) return -1;
+   for (i = 0; i < n; i++)
+     {
+        Marx_Photon_Attr_Type *at = pt->attributes + i;
+        memset(at, 0, sizeof(*at));
+        at->energy = energy[i];
+        at->x.x = x[i]; at->x.y = x[n + i]; at->x.z = x[2 * n + i];
+        at->p.x = p[i]; at->p.y = p[n + i]; at->p.z = p[2 * n + i];
+        at->arrival_time = t[i];
+        at->flags = flags[i];
+        at->tag = tag[i];
+        at->mirror_shell = (unsigned int) shell[i];
+        at->order = order[i];
+        at->ccd_num = ccd[i];
+        at->y_pixel = ypix[i]; at->z_pixel = zpix[i];
+        at->dither_state.ra = dith[i]; at->dither_state.dec = dith[n + i]; at->dither_state.roll = dith[2 * n + i];
+        for (k = 0; k < 4; k++) at->support_orders[k] = sup[k * n + i];
+        at->pulse_height = pha[i];
+        at->u_pixel = upix[i]; at->v_pixel = vpix[i];
+        at->detector_region = region[i];
+     }
+   pt->n_photons = (unsigned int) n;
+   pt->history = history;
+   r = marx_write_photons(pt, write_mask, (char *) dir, open_mode, total_time);
+   marx_dealloc_photon_type(pt);
+   return r;
+}

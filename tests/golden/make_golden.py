@@ -13,6 +13,9 @@ oracle/Makefile compiles them in place into oracle/_ref.  Writes:
   stats_<workload>.npz   seeded statistical fixtures from the reference's own
                          generator: encircled-energy curve, chip/pixel and
                          order histograms, survivor fractions.
+  dat_<workload>.npz     the reference's output files (marx_write_photons)
+                         for the photons of trace_<workload>.npz, written
+                         then appended to (--dat).
   diff_rays.npz          focal-plane positions of the differentiable form's
                          rays traced by the reference's mirror stage, at
                          theta = 0 and at the workload's perturbation written
@@ -103,6 +106,34 @@ def main(names=None):
         print(name, "good fraction", float(s["good_fraction"]), f"reference {N_STATS / secs:.3g} photons/s")
 
 
+DAT_WORKLOADS = ("plain_scatter", "letg_hrcs")
+
+
+def dat_fixture(name):
+    """The reference's own writer (marx_write_photons) on a trace fixture's
+    output photons: a new output directory, then a second batch appended.
+    Runs in a process of its own: the reference keeps each file's row count
+    in a static that no later directory resets."""
+    from helpers import load_trace_fixture
+    from marx_gb300 import output as O
+    w, ph, U, N, z = load_trace_fixture(name)
+    q = ph.copy()
+    for k in z.files:
+        if hasattr(q, k) and k != "energy":
+            getattr(q, k)[...] = z[k]
+    h = O.history(w.cfg)
+    ref = Reference(w.cfg)
+    d = tempfile.mkdtemp()
+    try:
+        ref.write_photons(q, h, O.ALL, d, new=True, total_time=12.5)
+        ref.write_photons(q, h, O.ALL, d, new=False, total_time=100.0)
+        files = {f: np.frombuffer(open(os.path.join(d, f), "rb").read(), dtype=np.uint8) for f in os.listdir(d)}
+    finally:
+        shutil.rmtree(d)
+    np.savez_compressed(os.path.join(HERE, f"dat_{name}.npz"), history=np.array(h), **files)
+    print(name, "output files", len(files))
+
+
 N_DIFF = 4000
 RDB = "EKCHDOS06.rdb"
 SHELL_OF = {"1": 0, "3": 1, "4": 2, "6": 3}
@@ -178,9 +209,17 @@ def diff_rays():
 
 
 if __name__ == "__main__":
+    sys.path.insert(0, os.path.dirname(HERE))
     names = [a for a in sys.argv[1:] if not a.startswith("-")]
     if "--diff" in sys.argv:
         diff_rays()
+    elif "--dat" in sys.argv:
+        if names:
+            dat_fixture(names[0])
+        else:
+            import subprocess
+            for n in DAT_WORKLOADS:
+                subprocess.run([sys.executable, __file__, "--dat", n], check=True)
     elif names:
         main(names)
     else:
