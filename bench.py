@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-source batched comparison")
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiable-form gradient comparison")
+    ap.add_argument("--no-workloads", action="store_true", help="skip the per-workload throughput table")
     return ap.parse_args()
 
 
@@ -291,6 +292,44 @@ def bench_diff(a, fp64_peak):
             }
 
 
+def bench_workloads(a, skip):
+    """Photons/s of every other named workload (device-resident batch, the
+    kernels alone): the plain configurations, the LETG and the HRC."""
+    import torch
+    from marx_gb300 import workloads as W
+    from marx_gb300._native import Engine, DevicePhotons
+    out = {}
+    stream = torch.cuda.current_stream()
+    for name, make in W.ALL.items():
+        if name == skip:
+            continue
+        w = make()
+        n = min(w.n, 4_000_000)
+        eng = Engine(w.cfg)
+        d = DevicePhotons.from_host(w.photons(n, seed=w.seed + 5))
+        p0, f0 = d.p.clone(), d.flags.clone()
+        for s in range(2):
+            d.p.copy_(p0); d.flags.copy_(f0)
+            eng.trace(d, stages=w.stages, seed=700 + s)
+        torch.cuda.synchronize()
+        k = max(3, min(a.steps, 5))
+        ms = 0.0
+        for s in range(k):
+            d.p.copy_(p0); d.flags.copy_(f0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            eng.trace(d, stages=w.stages, seed=s)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms += e0.elapsed_time(e1)
+        ms /= k
+        good = float(((d.flags & 0xFF) == 0).float().mean().item())
+        out[name] = {"photons": n, "ms": ms, "photons_per_s": n / (ms * 1e-3), "detected_fraction": good}
+        eng.close()
+        del d
+    return out
+
+
 def run_reference(a):
     """Reference arm: the CPU implementation of the path on the host cores."""
     from marx_gb300 import workloads as W
@@ -424,6 +463,7 @@ def main():
     cpu_rate = cpu_sample(w, 200_000, os.cpu_count() or 1)
     batched = None if a.no_batched else bench_batched(a)
     differentiable = None if a.no_diff else bench_diff(a, fp64_peak)
+    workloads = None if a.no_workloads else bench_workloads(a, a.workload)
 
     line = {
         "metric": METRIC, "value": value, "unit": "photons/s", "n_gpus": world, "steps": a.steps,
@@ -446,6 +486,7 @@ def main():
         "clocks": clocks.summary(),
         "batched": batched,
         "differentiable": differentiable,
+        "workloads": workloads,
     }
     print(json.dumps(line))
     if world > 1:

@@ -821,7 +821,7 @@ MXD int diffract_photon(const MxTables &T, const MxGratingDev &g, int order_idx,
 // capped at n-1; each order's value rounded to float) and the order choice
 // of diffract_photon_from_grating (diffract.c:828-849): the first index
 // whose cumulative efficiency reaches r, or -1.  cum is [energy][order].
-MXD int choose_order(const float *ge, unsigned n, const float *cum, int norders, float fe, double r) {
+MXD int choose_order(const float *ge, unsigned n, const float *cum, int norders, bool monotone, float fe, double r) {
   unsigned lo = 1, hi = n - 1;
   while (lo < hi) {
     unsigned mid = (lo + hi) >> 1;
@@ -831,15 +831,24 @@ MXD int choose_order(const float *ge, unsigned n, const float *cum, int norders,
   double x0 = MX_LDG(ge + idx - 1), x1 = MX_LDG(ge + idx), dx = MX_DADD(x1, -x0);
   double w = MX_DADD((double) fe, -x0);
   const float *c0 = cum + (size_t) (idx - 1) * norders;
-  for (int k = 0; k < norders; k++) {
-    float ck;
-    if (dx == 0.0) ck = MX_LDG(c0 + k);
-    else {
-      double y0 = MX_LDG(c0 + k), y1 = MX_LDG(c0 + norders + k);
-      ck = (float) MX_DADD(y0, MX_DDIV(MX_DMUL(MX_DADD(y1, -y0), w), dx));
+  auto ck = [&](int k) -> float {
+    if (dx == 0.0) return MX_LDG(c0 + k);
+    double y0 = MX_LDG(c0 + k), y1 = MX_LDG(c0 + norders + k);
+    return (float) MX_DADD(y0, MX_DDIV(MX_DMUL(MX_DADD(y1, -y0), w), dx));
+  };
+  if (monotone && (dx == 0.0 || (w >= 0.0 && w <= dx))) {
+    // Between two rows that are non-decreasing in the order index the
+    // interpolated row is too (rounding to float keeps the order), so the
+    // first index reaching r is found by bisection over the same values.
+    int a = 0, b = norders;
+    while (a < b) {
+      int m = (a + b) >> 1;
+      if (r <= (double) ck(m)) b = m; else a = m + 1;
     }
-    if (r <= (double) ck) return k;
+    return a < norders ? a : -1;
   }
+  for (int k = 0; k < norders; k++)
+    if (r <= (double) ck(k)) return k;
   return -1;
 }
 
@@ -883,8 +892,8 @@ MXD void grating_stage(const MxTables &T, const MxGratingDev *grs, int kind, Ph 
   D3 x = rot_x(ph.x, g.cos_m, g.sin_m), p = rot_x(ph.p, g.cos_m, g.sin_m);
   if (-1 == rowland_intersect(x, p, g.rowland)) ph.flags |= MX_PHOTON_UNDIFFRACTED;
   float fe = (float) ph.e;
-  int chosen = choose_order(T.geff_energy + g.geff_off, (unsigned) g.nenergy, T.geff_cum + g.cum_off, g.norders, fe,
-                            rng.uniform());
+  int chosen = choose_order(T.geff_energy + g.geff_off, (unsigned) g.nenergy, T.geff_cum + g.cum_off, g.norders,
+                            g.monotone != 0, fe, rng.uniform());
   if (chosen < 0) ph.flags |= MX_PHOTON_UNDIFFRACTED;
   else {
     ph.order = chosen - g.max_order;
@@ -895,8 +904,8 @@ MXD void grating_stage(const MxTables &T, const MxGratingDev *grs, int kind, Ph 
       const MxSupportDev &sg = T.supports[s];
       if (!sg.norders) continue;
       if (ph.flags & MX_BAD_PHOTON_MASK) continue;
-      int k = choose_order(T.support_energy, (unsigned) T.support_nenergy, T.support_cum + sg.cum_off, sg.norders, fe,
-                           rng.uniform());
+      int k = choose_order(T.support_energy, (unsigned) T.support_nenergy, T.support_cum + sg.cum_off, sg.norders,
+                           sg.monotone != 0, fe, rng.uniform());
       if (k < 0) { ph.flags |= MX_PHOTON_UNDIFFRACTED; continue; }
       // order list 0, +1, -1, +2, -2, ... (init_one_grating, diffract.c:392-405)
       ph.sup[s] = (int8_t) ((k & 1) ? (k + 1) / 2 : -(k / 2));

@@ -108,6 +108,15 @@ static void append_slopes(std::vector<double> &out, const float *x, const float 
   }
 }
 
+// True if every energy row of a cumulative table [energy][order] is
+// non-decreasing in the order index (the trace may then bisect it).
+static bool rows_monotone(const float *cum, size_t nenergy, int norders) {
+  for (size_t j = 0; j < nenergy; j++)
+    for (int k = 0; k + 1 < norders; k++)
+      if (!(cum[j * norders + k] <= cum[j * norders + k + 1])) return false;
+  return true;
+}
+
 // JDMbinary_search_f (finterpo.c:37-57): the first index with xp >= x (an
 // equal element returns its index), n if every element is smaller.
 static unsigned jdm_bsearch_f(float x, const float *xp, unsigned n) {
@@ -264,6 +273,7 @@ static bool build_letg(const Pack &pk, const mx_config &cfg, HostModel &M, std::
     for (unsigned j = 0; j < ne; j++)
       for (unsigned k = 0; k < no; k++) M.geff_cum.push_back(cum[k * ne + j]);   // [energy][order]
     g.nenergy = (int32_t) ne; g.norders = (int32_t) no; g.max_order = max_order;
+    g.monotone = rows_monotone(M.geff_cum.data() + g.cum_off, ne, (int) no);
     g.order_off = (int32_t) M.order_k.size();
     for (unsigned k = 0; k < no; k++) {
       int order = (int) k - max_order;
@@ -304,6 +314,7 @@ static bool build_letg(const Pack &pk, const mx_config &cfg, HostModel &M, std::
     d.cum_off = isf ? pf.first : pc.first;
     d.order_off = isf ? pf.second : pc.second;
     d.norders = isf ? nf : nc;
+    d.monotone = rows_monotone(M.support_cum.data() + d.cum_off, NE, d.norders);
     d.rotate = angle[s] != 0.0;
     d.cos_t = cos(angle[s]); d.sin_t = sin(angle[s]);
   }
@@ -730,6 +741,7 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
       for (unsigned j = 0; j < ne; j++)
         for (unsigned k = 0; k < no; k++) M.geff_cum.push_back(cum[k * ne + j]);   // [energy][order]
       g.nenergy = (int32_t) ne; g.norders = (int32_t) no; g.max_order = max_order;
+      g.monotone = rows_monotone(M.geff_cum.data() + g.cum_off, ne, (int) no);
       g.order_off = (int32_t) M.order_k.size();
       for (unsigned k = 0; k < no; k++) {
         int order = (int) k - max_order;

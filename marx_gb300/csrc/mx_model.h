@@ -29,6 +29,7 @@ struct MxGratingDev {
   double cos_m, sin_m, cos_p, sin_p;           // rotation by -/+ dispersion angle
   int32_t geff_off, cum_off, nenergy, norders; // cumulative efficiencies [energy][order]
   int32_t max_order, order_off, sec_off, nsec; // order_k offset; sectors [6][nsec]
+  int32_t monotone, pad;                       // every energy row non-decreasing in the order index
 };
 
 // One LETG support grating as the trace meets it (diffract.c:1097-1114):
@@ -37,6 +38,7 @@ struct MxSupportDev {
   int32_t cum_off, norders;    // cumulative efficiencies [energy][order] on the shared energy grid
   int32_t order_off, rotate;   // order constants in support_k; rotate: the angle is not zero
   double cos_t, sin_t;         // cos and sin of the angle
+  int32_t monotone, pad;       // every energy row non-decreasing in the order index
 };
 
 // A float table lookup (JDMinterpolate_f) in the HRC tables: abscissae at
