@@ -255,20 +255,32 @@ int mx_trace_static(mx_context *ctx, const mx_photons *ph, uint32_t stages, cons
 int mx_trace_host(mx_context *ctx, const mx_photons *host, uint32_t stages,
                   const mx_variates *host_var, uint64_t seed);
 
-/* ------------------------------------------------------ point sources --
- * A point source at infinity with a flat spectrum: the input producer of
- * the trace (point_create_photons, marx/libsrc/s-point.c:59, with
- * flat_energy, spectrum.c:138).  Photon k gets tag first_tag + k, energy
- * emin + (emax - emin) u with u the Philox draw of that tag in the
- * source domain, direction p, arrival time 0 and flags 0. */
+/* ------------------------------------------------------------ sources --
+ * A source at infinity: the input producer of the trace (the create_photons
+ * functions of s-point.c:59, s-gauss.c, s-beta.c, s-disk.c, s-line.c, with
+ * flat_energy and file_energy, spectrum.c:138-190).  Photon k gets tag
+ * first_tag + k; its energy and direction come from the Philox draws of
+ * that tag in the source domain (draw 0: energy, then the source's own
+ * draws in the reference's order); arrival time 0 and flags 0. */
 typedef struct mx_source {
   double p[3];              /* unit direction of travel (toward the mirror) */
-  double energy_min, energy_max;   /* keV */
+  double energy_min, energy_max;   /* keV, FLAT spectrum */
   uint32_t num_photons;
   int32_t grating;          /* MX_GRATING_NONE or MX_GRATING_HETG */
   int32_t detector;         /* MX_DETECTOR_ACIS_I or MX_DETECTOR_ACIS_S */
   uint32_t reserved;
+  /* Extended sources (s-gauss.c, s-beta.c, s-disk.c, s-line.c) about p:
+   *   MX_SOURCE_GAUSS  param[0] S-GaussSigma (arcsec)
+   *   MX_SOURCE_BETA   param[0] S-BetaCoreRadius (arcsec), param[1] S-BetaBeta (> 1/2)
+   *   MX_SOURCE_DISK   param[0] S-DiskTheta0, param[1] S-DiskTheta1 (arcsec)
+   *   MX_SOURCE_LINE   param[0] S-LinePhi (deg), param[1] S-LineTheta (arcsec) */
+  int32_t kind;             /* MX_SOURCE_* */
+  uint32_t spectrum_n;      /* > 0: FILE spectrum of spectrum_n rows (spectrum.c:182-274), else FLAT */
+  double param[4];
+  const double *spectrum_energy;   /* HOST arrays: energy (keV, non-decreasing) and flux density */
+  const double *spectrum_flux;
 } mx_source;
+enum { MX_SOURCE_POINT = 0, MX_SOURCE_GAUSS = 1, MX_SOURCE_BETA = 2, MX_SOURCE_DISK = 3, MX_SOURCE_LINE = 4 };
 
 /* Fill energy, p, arrival_time, flags and tag of dev (device pointers,
  * dev->n = src->num_photons) with the source's photons. */

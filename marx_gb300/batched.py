@@ -23,7 +23,35 @@ ARCMIN = math.pi / (180.0 * 60.0)
 class MxSource(C.Structure):
     _fields_ = [("p", C.c_double * 3), ("energy_min", C.c_double), ("energy_max", C.c_double),
                 ("num_photons", C.c_uint32), ("grating", C.c_int32), ("detector", C.c_int32),
-                ("reserved", C.c_uint32)]
+                ("reserved", C.c_uint32), ("kind", C.c_int32), ("spectrum_n", C.c_uint32),
+                ("param", C.c_double * 4), ("spectrum_energy", C.c_void_p), ("spectrum_flux", C.c_void_p)]
+
+
+# source models (MX_SOURCE_* in include/marx_gb300.h) and their parameters
+SOURCE = {"POINT": 0, "GAUSS": 1, "BETA": 2, "DISK": 3, "LINE": 4}
+
+
+def make_source(p, kind="POINT", param=(), energy=(1.0, 1.0), spectrum=None, num_photons=0,
+                grating="NONE", detector="ACIS-I") -> MxSource:
+    """One source: p the unit direction of travel, kind and param as
+    mx_source documents them, a FLAT spectrum (energy_min, energy_max) or a
+    FILE spectrum (energies, flux) that the returned struct references (keep
+    the arrays alive while it is used)."""
+    s = MxSource()
+    s.p[:] = list(p)
+    s.kind = SOURCE[kind]
+    for k, v in enumerate(param):
+        s.param[k] = v
+    s.energy_min, s.energy_max = energy
+    s.num_photons = int(num_photons)
+    s.grating, s.detector = GRATING[grating], DETECTOR[detector]
+    if spectrum is not None:
+        e = np.ascontiguousarray(spectrum[0], dtype=np.float64)
+        f = np.ascontiguousarray(spectrum[1], dtype=np.float64)
+        s._keep = (e, f)
+        s.spectrum_n = len(e)
+        s.spectrum_energy, s.spectrum_flux = e.ctypes.data, f.ctypes.data
+    return s
 
 
 class MxBatchParams(C.Structure):

@@ -19,14 +19,18 @@ namespace cg = cooperative_groups;
 
 // One source as the kernels read it.
 struct MxSourceDev {
-  double p[3];
-  double emin, de;          // energy = emin + de * u
+  double p[3], pn[3];       // direction of travel; the normal to it in the x-y plane (source.c:206-209)
+  double emin, de;          // FLAT: energy = emin + de * u
+  double a, b, c;           // GAUSS: a = sigma; BETA: a = core radius, b = 1 / (1 - alpha);
+                            // DISK: a = theta1, b = (theta0/theta1)^2, c = 1 - b; LINE: a = theta, b, c = cos, sin phi
+  double axis[3], cos_al, sin_al;   // LINE: rotation from -x to p (JDMv_find_rotation_axis)
+  int32_t kind, spec_off;   // MX_SOURCE_*; FILE spectrum rows [spec_off, spec_off + spec_n) of the table
+  int32_t spec_n;           // 0: FLAT
   int32_t grating;          // 1: HETG
   int32_t chip_off, nchips; // chips[chip_off .. chip_off + nchips)
-  int32_t pad;
-  double pad2;
+  int32_t pad[2];
 };
-static_assert(sizeof(MxSourceDev) == 64, "source record size");
+static_assert(sizeof(MxSourceDev) % 16 == 0, "source record size");
 
 #define MX_BATCH_MAX_SOURCES 4096
 
@@ -39,14 +43,66 @@ struct BatchIO {
   unsigned int *ctr;            // [0] q1 entries [1] q2 entries [2..4] work counters of phases A, B, C
                                 // [5] q1 entries of phase B (q1 reused) [6] work counter of phase T
   const uint64_t *seed;         // device scalar, written before each graph launch
+  const double *spec;           // FILE spectra of the sources (energies then cumulative flux, per source)
 };
 
-// point_create_photons (s-point.c:59) with flat_energy (spectrum.c:138)
-// for one photon of a source.
-__device__ __forceinline__ void generate_photon(const MxSourceDev &S, uint64_t seed, uint32_t tag, Ph &q) {
-  q.e = MX_DADD(S.emin, MX_DMUL(S.de, source_uniform(seed, tag, 0)));   // rounded as written, no contraction
+// JDMinterpolate_d (dinterpo.c:52-82) of the inverse cumulative spectrum:
+// energies at spec[0..n), normalised cumulative flux at spec[n..2n).
+__device__ double interp_d(double x, const double *xp, const double *yp, unsigned n) {
+  if (n == 1) return __ldg(yp);
+  unsigned n1 = bsearch_d(x, xp, n), n0 = n1 - 1;
+  if (n1 < n && x == __ldg(xp + n1)) return __ldg(yp + n1);
+  if (n1 == n) { n1--; n0--; }
+  if (n1 == 0) n0 = 1;
+  double x0 = __ldg(xp + n0), x1 = __ldg(xp + n1);
+  if (x1 == x0) return __ldg(yp + n1);
+  double y0 = __ldg(yp + n0), y1 = __ldg(yp + n1);
+  return MX_DADD(y0, MX_DMUL(MX_DDIV(MX_DADD(y1, -y0), MX_DADD(x1, -x0)), MX_DADD(x, -x0)));
+}
+
+// The create_photons function of the source's model for one photon:
+// point_create_photons (s-point.c:59), gauss_create_photons
+// (s-gauss.c:76-130), beta_create_photons (s-beta.c:74-120),
+// disk_create_photons (s-disk.c:63-105), line_create_photons
+// (s-line.c:64-100), with flat_energy or file_energy (spectrum.c:138-190)
+// first.  Source-domain draw 0 is the energy; the model's draws follow in
+// the reference's order.  GAUSS, BETA and DISK rotate the source's fixed
+// normal by each photon's own azimuth (the reference carries the rotated
+// normal from one photon to the next; each photon's azimuth is uniform
+// either way).
+__device__ __forceinline__ void generate_photon(const MxSourceDev &S, const double *spec, uint64_t seed, uint32_t tag,
+                                                Ph &q) {
+  if (S.spec_n > 0) {
+    const double *e = spec + S.spec_off, *cum = e + S.spec_n;
+    q.e = interp_d(source_uniform(seed, tag, 0), cum, e, (unsigned) S.spec_n);
+  } else
+    q.e = MX_DADD(S.emin, MX_DMUL(S.de, source_uniform(seed, tag, 0)));   // rounded as written, no contraction
+  const D3 p = mk(S.p[0], S.p[1], S.p[2]);
+  if (S.kind == MX_SOURCE_POINT) q.p = p;
+  else if (S.kind == MX_SOURCE_LINE) {
+    double theta = S.a * (-1.0 + 2.0 * source_uniform(seed, tag, 1));
+    double st, ct;
+    sincos(theta, &st, &ct);
+    double sin_theta = -st;
+    D3 p0 = mk(-ct, sin_theta * S.b, sin_theta * S.c);
+    q.p = rotate_unit(p0, mk(S.axis[0], S.axis[1], S.axis[2]), S.cos_al, S.sin_al);
+  } else {
+    double sphi, cphi;
+    sincos(2.0 * PI * source_uniform(seed, tag, 1), &sphi, &cphi);
+    D3 normal = rotate_unit(mk(S.pn[0], S.pn[1], S.pn[2]), p, cphi, sphi);
+    double ang;
+    if (S.kind == MX_SOURCE_DISK)
+      ang = S.a * sqrt(S.b + S.c * source_uniform(seed, tag, 2));
+    else {
+      double rnd = source_uniform(seed, tag, 2);
+      for (uint32_t k = 3; rnd == 0.0 && k < 8; k++) rnd = source_uniform(seed, tag, k);
+      ang = S.kind == MX_SOURCE_GAUSS ? S.a * sqrt(-log(rnd)) : S.a * sqrt(pow(rnd, S.b) - 1.0);
+    }
+    double sa, ca;
+    sincos(ang, &sa, &ca);
+    q.p = rotate_unit(p, normal, ca, sa);
+  }
   q.t = 0.0;
-  q.p = mk(S.p[0], S.p[1], S.p[2]);
   q.x = mk(0.0, 0.0, 0.0);
   q.flags = 0u;
   q.shell = 0; q.order = 0; q.ccd = -1; q.ypix = q.zpix = 0.f;
@@ -55,13 +111,13 @@ __device__ __forceinline__ void generate_photon(const MxSourceDev &S, uint64_t s
   for (int k = 0; k < 4; k++) q.sup[k] = 0;
 }
 
-__global__ void __launch_bounds__(256) mx_generate_kernel(MxSourceDev S, uint32_t first_tag, uint64_t seed,
-                                                           double *energy, double *p, double *t, uint32_t *flags,
-                                                           uint32_t *tag, uint32_t n, uint32_t stride) {
+__global__ void __launch_bounds__(256) mx_generate_kernel(MxSourceDev S, const double *spec, uint32_t first_tag,
+                                                           uint64_t seed, double *energy, double *p, double *t,
+                                                           uint32_t *flags, uint32_t *tag, uint32_t n, uint32_t stride) {
   const size_t nn = stride;
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     Ph q;
-    generate_photon(S, seed, first_tag + k, q);
+    generate_photon(S, spec, seed, first_tag + k, q);
     energy[k] = q.e;
     p[k] = q.p.x; p[nn + k] = q.p.y; p[2 * nn + k] = q.p.z;
     if (t) t[k] = 0.0;
@@ -121,7 +177,7 @@ __global__ void __launch_bounds__(256) mx_batch_kernel(MxTables T, BatchIO b) {
       if (i < end) {
         const int s = source_of(i, sstart, b.nsrc);
         Ph q;
-        generate_photon(ssrc[s], seed, i, q);
+        generate_photon(ssrc[s], b.spec, seed, i, q);
         clear_extra(io, i);
         io.energy[i] = q.e;
         if (io.t) io.t[i] = 0.0;
@@ -235,6 +291,8 @@ struct mx_batch {
   mx_context *ctx = nullptr;
   std::vector<mx_source> src;
   std::vector<MxSourceDev> dsrc;
+  std::vector<double> spec;     // FILE spectra of the sources (host copy)
+  DevBuf d_spec;
   std::vector<uint32_t> start;
   uint64_t total = 0;
   DevBuf d_src;                 // sources then starts
@@ -302,6 +360,7 @@ static int build_graph(mx_batch *b) {
   io.q1 = (MxRec *) b->queues.ptr;
   io.q2 = (MxRec *) ((char *) b->queues.ptr + qbytes);
   io.ctr = (unsigned int *) b->ctr.ptr;
+  io.spec = (const double *) b->d_spec.ptr;
   io.seed = (const uint64_t *) ((char *) b->ctr.ptr + 64);
   MxTables T = c->T;
 
@@ -354,6 +413,94 @@ static std::string batch_key(mx_batch *b) {
   return buf;
 }
 
+// ------------------------------------------------------ source set-up --
+static double src_len(const double a[3]) {   // JDMv_length (vector.c:77)
+  double x = fabs(a[0]), y = fabs(a[1]), z = fabs(a[2]), t;
+  if (z < x) { t = z; z = x; x = t; }
+  if (z < y) { t = z; z = y; y = t; }
+  if (z == 0.0) return 0.0;
+  x = x / z; y = y / z;
+  return z * sqrt(1.0 + x * x + y * y);
+}
+
+// The per-source constants of the source models' set-up (select_source,
+// source.c:136-232; gauss/beta/disk/line select functions; the spectrum
+// set-up of spectrum.c:145-274).  FILE spectra are appended to spec as
+// energies then normalised cumulative flux (compute_cumulated_vector,
+// spectrum.c:40-97).
+static bool source_dev(const mx_source &q, MxSourceDev &S, std::vector<double> &spec, std::string &err) {
+  const double PI_ = 3.14159265358979323846264338327950288;
+  memset(&S, 0, sizeof(S));
+  for (int k = 0; k < 3; k++) S.p[k] = q.p[k];
+  if (!(q.p[0] < 0.0)) { err = "source direction must travel toward the mirror (p.x < 0)"; return false; }
+  // the normal to the unnegated direction u = -p in the x-y plane
+  double u[3] = {-q.p[0], -q.p[1], -q.p[2]};
+  double pn[3] = {-u[1] / u[0], 1.0, 0.0};
+  double l = src_len(pn);
+  if (l != 0.0) { pn[0] = pn[0] / l; pn[1] = pn[1] / l; pn[2] = pn[2] / l; }
+  for (int k = 0; k < 3; k++) S.pn[k] = pn[k];
+  S.kind = q.kind;
+  if (q.spectrum_n > 0) {
+    if (!q.spectrum_energy || !q.spectrum_flux) { err = "FILE spectrum arrays missing"; return false; }
+    const unsigned n = q.spectrum_n;
+    std::vector<double> cum(n);
+    double tot = 0.0, prev = q.spectrum_energy[0];
+    for (unsigned i = 0; i < n; i++) {
+      double x = q.spectrum_energy[i];
+      if (x - prev < 0.0) { err = "Your file spectrum appears corrupt.  Perhaps you are using a wavelength grid"; return false; }
+      tot += q.spectrum_flux[i] * (x - prev);
+      cum[i] = tot;
+      prev = x;
+    }
+    if (tot == 0.0) { err = "Your file spectrum seems to have zero flux in it"; return false; }
+    for (unsigned i = 0; i < n; i++) cum[i] = cum[i] / tot;
+    S.spec_off = (int32_t) spec.size();
+    S.spec_n = (int32_t) n;
+    spec.insert(spec.end(), q.spectrum_energy, q.spectrum_energy + n);
+    spec.insert(spec.end(), cum.begin(), cum.end());
+  } else {
+    if (!(q.energy_max >= q.energy_min) || !(q.energy_min > 0)) { err = "need 0 < energy_min <= energy_max"; return false; }
+    S.emin = q.energy_min; S.de = q.energy_max - q.energy_min;
+  }
+  const double arcsec = 1.0 / 3600.0 * PI_ / 180.0;
+  switch (q.kind) {
+    case MX_SOURCE_POINT: break;
+    case MX_SOURCE_GAUSS: S.a = q.param[0] * arcsec; break;
+    case MX_SOURCE_BETA: {
+      double alpha = 3 * q.param[1] - 0.5;
+      if ((alpha <= 1.0) || (q.param[0] <= 0.0)) { err = "Beta parameters out of range.  Must be greater than 1/2."; return false; }
+      S.a = q.param[0] * (1.0 / 3600.0) * (PI_ / 180.0);
+      S.b = 1.0 / (1.0 - alpha);
+      break;
+    }
+    case MX_SOURCE_DISK: {
+      double th = q.param[1] * arcsec, th0 = q.param[0] * arcsec;
+      double x0 = th0 / th;
+      x0 = x0 * x0;
+      S.a = th; S.b = x0; S.c = 1.0 - x0;
+      break;
+    }
+    case MX_SOURCE_LINE: {
+      double phi = q.param[0] * (PI_ / 180.0);
+      S.a = q.param[1] * arcsec;
+      S.b = cos(phi); S.c = sin(phi);
+      // JDMv_find_rotation_axis ((-1, 0, 0), p) (vector.c:289-330)
+      double a[3] = {-1.0, 0.0, 0.0};
+      double th = a[0] * q.p[0] + a[1] * q.p[1] + a[2] * q.p[2];
+      if (fabs(th) > 1.0) th = th > 1.0 ? 1.0 : -1.0;
+      th = acos(th);
+      double cc[3] = {a[1] * q.p[2] - a[2] * q.p[1], a[2] * q.p[0] - a[0] * q.p[2], a[0] * q.p[1] - a[1] * q.p[0]};
+      double len = src_len(cc);
+      if (len > 0.0) { for (int k = 0; k < 3; k++) S.axis[k] = cc[k] / len; }
+      else { S.axis[0] = -a[1]; S.axis[1] = -a[0]; S.axis[2] = 0.0; }
+      S.cos_al = cos(th); S.sin_al = sin(th);
+      break;
+    }
+    default: err = "unknown source model"; return false;
+  }
+  return true;
+}
+
 static std::mutex g_tune_mu;
 static std::map<std::string, mx_batch_params> g_tune_cache;
 
@@ -364,17 +511,22 @@ int mx_generate_source(mx_context *c, const mx_source *s, uint32_t first_tag, ui
   if (!c || !s || !d) return mx_fail(c, MX_EINVAL, "mx_generate_source: null argument");
   if (d->n == 0) return MX_OK;
   if (!d->energy || !d->p) return mx_fail(c, MX_EINVAL, "mx_generate_source: energy and p are required");
-  if (!(s->energy_max >= s->energy_min) || !(s->energy_min > 0))
-    return mx_fail(c, MX_EINVAL, "mx_generate_source: need 0 < energy_min <= energy_max");
   MxSourceDev S;
-  memset(&S, 0, sizeof(S));
-  for (int k = 0; k < 3; k++) S.p[k] = s->p[k];
-  S.emin = s->energy_min; S.de = s->energy_max - s->energy_min;
+  std::vector<double> spec;
+  std::string err;
+  if (!source_dev(*s, S, spec, err)) return mx_fail(c, MX_EINVAL, "mx_generate_source: " + err);
+  const double *dspec = nullptr;
+  if (!spec.empty()) {
+    cudaError_t e = c->spec.ensure(spec.size() * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpy(c->spec.ptr, spec.data(), spec.size() * sizeof(double), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return mx_cuda_fail(c, e, "mx_generate_source: uploading the spectrum");
+    dspec = (const double *) c->spec.ptr;
+  }
   int grid = std::max(1, std::min((int) ((d->n + 255) / 256), c->num_sms * 8));
   uint32_t stride = d->stride ? d->stride : d->n;
   if (stride < d->n) return mx_fail(c, MX_EINVAL, "mx_generate_source: stride below n");
-  mx_generate_kernel<<<grid, 256, 0, (cudaStream_t) stream>>>(S, first_tag, seed, d->energy, d->p, d->arrival_time,
-                                                              d->flags, d->tag, d->n, stride);
+  mx_generate_kernel<<<grid, 256, 0, (cudaStream_t) stream>>>(S, dspec, first_tag, seed, d->energy, d->p,
+                                                              d->arrival_time, d->flags, d->tag, d->n, stride);
   c->launches++;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MX_OK : mx_cuda_fail(c, e, "launching photon generation");
@@ -390,17 +542,14 @@ mx_batch *mx_batch_create(mx_context *c, const mx_source *sources, int nsrc) {
   uint64_t tot = 0;
   for (int s = 0; s < nsrc; s++) {
     const mx_source &q = sources[s];
-    if (!(q.energy_min > 0) || !(q.energy_max >= q.energy_min) ||
-        (q.grating != MX_GRATING_NONE && q.grating != MX_GRATING_HETG) ||
-        (q.detector != MX_DETECTOR_ACIS_I && q.detector != MX_DETECTOR_ACIS_S)) {
-      g_create_err = "mx_batch_create: source " + std::to_string(s) + " is malformed";
+    MxSourceDev S;
+    std::string err;
+    if ((q.grating != MX_GRATING_NONE && q.grating != MX_GRATING_HETG) ||
+        (q.detector != MX_DETECTOR_ACIS_I && q.detector != MX_DETECTOR_ACIS_S) || !source_dev(q, S, b->spec, err)) {
+      g_create_err = "mx_batch_create: source " + std::to_string(s) + " is malformed" + (err.empty() ? "" : ": " + err);
       delete b;
       return nullptr;
     }
-    MxSourceDev S;
-    memset(&S, 0, sizeof(S));
-    for (int k = 0; k < 3; k++) S.p[k] = q.p[k];
-    S.emin = q.energy_min; S.de = q.energy_max - q.energy_min;
     S.grating = q.grating == MX_GRATING_HETG;
     S.chip_off = q.detector == MX_DETECTOR_ACIS_S ? 4 : 0;
     S.nchips = q.detector == MX_DETECTOR_ACIS_S ? 6 : 4;
@@ -417,6 +566,9 @@ mx_batch *mx_batch_create(mx_context *c, const mx_source *sources, int nsrc) {
   for (int k = 0; k < 12 && e == cudaSuccess; k++) e = b->cols[k].ensure(std::max<size_t>(16, tot * elem[k]));
   if (e == cudaSuccess) e = b->queues.ensure(std::max<size_t>(256, 2 * tot * sizeof(MxRec)));
   if (e == cudaSuccess) e = b->ctr.ensure(128);
+  if (e == cudaSuccess) e = b->d_spec.ensure(std::max<size_t>(16, b->spec.size() * sizeof(double)));
+  if (e == cudaSuccess && !b->spec.empty())
+    e = cudaMemcpy(b->d_spec.ptr, b->spec.data(), b->spec.size() * sizeof(double), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMallocHost((void **) &b->h_seed, sizeof(uint64_t));
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMemcpy(b->d_src.ptr, b->dsrc.data(), b->dsrc.size() * sizeof(MxSourceDev), cudaMemcpyHostToDevice);
@@ -453,6 +605,7 @@ void mx_batch_destroy(mx_batch *b) {
   for (auto &col : b->cols) col.release();
   b->queues.release();
   b->ctr.release();
+  b->d_spec.release();
   if (b->h_seed) cudaFreeHost(b->h_seed);
   if (b->done) cudaEventDestroy(b->done);
   delete b;

@@ -183,6 +183,7 @@ void mx_destroy(mx_context *c) {
   for (auto &b : c->io) b.release();
   c->scan.release();
   c->wave.release();
+  c->spec.release();
   if (c->d_overrun) cudaFree(c->d_overrun);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;

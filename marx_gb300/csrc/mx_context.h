@@ -38,6 +38,7 @@ struct mx_context {
   DevBuf io[19];           // staging for mx_trace_host: 17 columns, U, N
   DevBuf scan;             // compaction block counts
   DevBuf wave;             // wavefront record queues
+  DevBuf spec;             // FILE spectrum of the last mx_generate_source call
   int wave_blocks = 0;     // resident blocks per SM for the wavefront kernels
   int mode = MX_MODE_AUTO;
   unsigned long long *d_overrun = nullptr;

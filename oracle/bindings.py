@@ -132,7 +132,8 @@ class Reference:
     """The reference MARX library compiled from its own sources (only in a
     checkout that has them).  ``native=True`` keeps its own generator."""
 
-    def __init__(self, cfg: MxConfig, native: bool = False, seed: int = 1, datadir: str | None = None):
+    def __init__(self, cfg: MxConfig, native: bool = False, seed: int = 1, datadir: str | None = None,
+                 extra_par: dict | None = None):
         so = REF_NATIVE_SO if native else REF_SLOTS_SO
         if not os.path.exists(so):
             if not build_reference():
@@ -143,6 +144,7 @@ class Reference:
         L.mxref_last_error.restype = C.c_char_p
         L.mxref_focal_length.restype = C.c_double
         par = to_par(cfg)
+        par.update(extra_par or {})
         names = (C.c_char_p * len(par))(*[k.encode() for k in par])
         vals = (C.c_char_p * len(par))(*[v.encode() for v in par.values()])
         parfile = os.path.join(REF_ROOT, "marx", "par", "marx.par").encode()
@@ -206,6 +208,20 @@ class Reference:
         r = f(out_dir.encode(), ph.n, *[_p(a) for a in cols], history, write_mask, 1 if new else 0, total_time)
         if r != 0:
             raise RuntimeError("reference writer failed: " + self.lib.mxref_last_error().decode())
+
+    def source_photons(self, n: int, U=None):
+        """(source direction st->p, energies, directions (3, n)) of n photons
+        of the source the parameters describe, one create_photons call per
+        photon; U (4, n) slot-major uniforms for the slot build."""
+        p0 = np.zeros(3)
+        if self.lib.mxref_source_setup(_p(p0)) != 0:
+            raise RuntimeError("reference source: " + self.lib.mxref_last_error().decode())
+        e = np.zeros(n)
+        p = np.zeros((n, 3))
+        Up = np.ascontiguousarray(U.T) if U is not None else np.zeros((n, 4))
+        if self.lib.mxref_source_photons(n, _p(Up), _p(e), _p(p)) != 0:
+            raise RuntimeError("reference source photons: " + self.lib.mxref_last_error().decode())
+        return p0, e, np.ascontiguousarray(p.T)
 
     def trace_batch(self, ph: PhotonList, stages: int = 15):
         """Whole batch with the reference's own generator; returns (list, seconds)."""

@@ -465,3 +465,51 @@ int mxref_write_photons(const char *dir, int n, const double *energy, const doub
    marx_dealloc_photon_type(pt);
    return r;
 }
+
+/* ------------------------------------------------------------ sources -- */
+/* The reference's source models (marx_create_source, source.c:388-420, and
+ * the create_photons functions of s-*.c) for the parameters of the last
+ * mxref_setup call.  p_out receives the source direction st->p. */
+static Marx_Source_Type *Src;
+int mxref_source_setup(double *p_out)
+{
+   if (Pf == NULL) { set_err("mxref_setup first"); return -1; }
+   if (Src != NULL) { marx_close_source(Src); Src = NULL; }
+   if (NULL == (Src = marx_create_source(Pf))) { set_err("source set-up failed"); return -1; }
+   if (-1 == marx_open_source(Src)) { set_err("source open failed"); return -1; }
+   p_out[0] = Src->p.x; p_out[1] = Src->p.y; p_out[2] = Src->p.z;
+   return 0;
+}
+
+/* One photon per create_photons call.  With the slot build, photon i's
+ * uniforms come from U[i*4 .. i*4+4) in the order the model draws them
+ * (spectrum first); with the native build, from the reference's own
+ * generator.  Energies and directions (n x 3) out. */
+int mxref_source_photons(int n, const double *U, double *energy, double *p)
+{
+   Marx_Photon_Type pt;
+   Marx_Photon_Attr_Type at;
+   unsigned int num;
+   int i;
+   if (Src == NULL) { set_err("no source"); return -1; }
+   for (i = 0; i < n; i++)
+     {
+        memset(&pt, 0, sizeof(pt));
+        memset(&at, 0, sizeof(at));
+        pt.attributes = &at; pt.max_n_photons = 1;
+#if MXREF_INTERPOSE
+        rng_window(U + 4 * (size_t) i, 0, 4, NULL, 0, 0);
+        Rng_Overrun = 0;
+#else
+        (void) U;
+#endif
+        if (-1 == (*Src->create_photons)(Src, &pt, 1, &num)) { set_err("create_photons"); return -1; }
+#if MXREF_INTERPOSE
+        rng_window(NULL, 0, 0, NULL, 0, 0);
+        if (Rng_Overrun) { set_err("source drew more than 4 uniforms"); return -1; }
+#endif
+        energy[i] = at.energy;
+        p[3 * i] = at.p.x; p[3 * i + 1] = at.p.y; p[3 * i + 2] = at.p.z;
+     }
+   return 0;
+}

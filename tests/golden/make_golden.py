@@ -16,6 +16,10 @@ oracle/Makefile compiles them in place into oracle/_ref.  Writes:
   dat_<workload>.npz     the reference's output files (marx_write_photons)
                          for the photons of trace_<workload>.npz, written
                          then appended to (--dat).
+  sources.npz            energies and directions of the reference's source
+                         models (POINT, GAUSS, BETA, DISK, LINE; FLAT and
+                         FILE spectra) for the engine's source uniforms
+                         (--sources).
   diff_rays.npz          focal-plane positions of the differentiable form's
                          rays traced by the reference's mirror stage, at
                          theta = 0 and at the workload's perturbation written
@@ -134,6 +138,60 @@ def dat_fixture(name):
     print(name, "output files", len(files))
 
 
+N_SRC = 2000
+# source models of the sources fixture: (name, SourceType, parameter overrides, mx_source param)
+SOURCE_CASES = (
+    ("point", "POINT", {}, ()),
+    ("gauss", "GAUSS", {"S-GaussSigma": "20.0"}, (20.0,)),
+    ("beta", "BETA", {"S-BetaCoreRadius": "12.5", "S-BetaBeta": "0.8"}, (12.5, 0.8)),
+    ("disk", "DISK", {"S-DiskTheta0": "15.0", "S-DiskTheta1": "75.0"}, (15.0, 75.0)),
+    ("line", "LINE", {"S-LinePhi": "30.0", "S-LineTheta": "300.0"}, (30.0, 300.0)),
+    ("gauss_file", "GAUSS", {"S-GaussSigma": "5.0"}, (5.0,)),
+)
+
+
+def source_spectrum():
+    """A smooth absorbed power law on 0.2-9 keV, 400 rows: the FILE
+    spectrum of the gauss_file case."""
+    e = np.linspace(0.2, 9.0, 400)
+    f = e ** -1.7 * np.exp(-0.3 * e ** (-8.0 / 3.0))
+    return e, f
+
+
+def sources_fixture():
+    """The reference's source models, one create_photons call per photon,
+    with the Philox source-domain uniforms the engine draws for the same
+    tags (draw k of tag i in slot k)."""
+    w = W.plain_onaxis(parity=True)
+    oracle = Oracle(w.cfg)
+    seed = 4321
+    tags = np.arange(N_SRC, dtype=np.uint32)
+    U = np.array([[oracle.source_uniform(seed, int(i), k) for i in tags] for k in range(4)])
+    out = {"seed": np.array(seed), "n": np.array(N_SRC), "U": U}
+    e_spec, f_spec = source_spectrum()
+    out["spectrum_energy"], out["spectrum_flux"] = e_spec, f_spec
+    tmp = tempfile.mkdtemp()
+    try:
+        spec_file = os.path.join(tmp, "spectrum.dat")
+        with open(spec_file, "w") as fh:
+            for a, b in zip(e_spec, f_spec):
+                fh.write(f"{float(a)!r} {float(b)!r}\n")
+        for name, kind, over, param in SOURCE_CASES:
+            par = {"SourceType": kind, "SourceRA": "250.25", "SourceDEC": "-53.73", "MinEnergy": "0.5",
+                   "MaxEnergy": "7.0", "SpectrumType": "FILE" if name.endswith("_file") else "FLAT",
+                   "SpectrumFile": spec_file, **over}
+            ref = Reference(w.cfg, extra_par=par)
+            p0, e, p = ref.source_photons(N_SRC, U)
+            out[f"{name}_src"] = p0
+            out[f"{name}_param"] = np.array(param, dtype=np.float64)
+            out[f"{name}_energy"] = e
+            out[f"{name}_p"] = p
+            print("source", name, p0, e[:2])
+    finally:
+        shutil.rmtree(tmp)
+    np.savez_compressed(os.path.join(HERE, "sources.npz"), **out)
+
+
 N_DIFF = 4000
 RDB = "EKCHDOS06.rdb"
 SHELL_OF = {"1": 0, "3": 1, "4": 2, "6": 3}
@@ -213,6 +271,8 @@ if __name__ == "__main__":
     names = [a for a in sys.argv[1:] if not a.startswith("-")]
     if "--diff" in sys.argv:
         diff_rays()
+    elif "--sources" in sys.argv:
+        sources_fixture()
     elif "--dat" in sys.argv:
         if names:
             dat_fixture(names[0])
