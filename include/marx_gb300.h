@@ -154,6 +154,9 @@ typedef struct mx_config {
   double hesf_gap_y1, hesf_gap_y2;       /* HESFGapY1, HESFGapY2 (mm) */
   double hesf_length, hesf_cr_width;     /* HESFLength, HESFCrWidth (mm) */
   double hesf_height[4], hesf_theta[4];  /* HESFHeight1..4 (mm), HESFTheta1..4 (deg) */
+  /* Pointing (dither.c:85-160) */
+  double ra_nom, dec_nom;     /* RA_Nom, Dec_Nom (deg) */
+  double pointing_offset[2];  /* PointingOffsetY, PointingOffsetZ (arcsec) */
 } mx_config;
 
 /* Structure-of-arrays photon list.  3-vectors are component-major:
@@ -281,6 +284,13 @@ typedef struct mx_source {
   const double *spectrum_flux;
 } mx_source;
 enum { MX_SOURCE_POINT = 0, MX_SOURCE_GAUSS = 1, MX_SOURCE_BETA = 2, MX_SOURCE_DISK = 3, MX_SOURCE_LINE = 4 };
+
+/* The direction of travel p of the photons of a source at (ra, dec)
+ * (degrees) for the configuration's pointing (RA_Nom, Dec_Nom, Roll_Nom,
+ * PointingOffsetY/Z): setup_pointing_ra_dec (dither.c:125-155),
+ * marx_compute_elaz (source.c:108-134) and select_source (source.c:136-232).
+ * MX_EINVAL if the source lies behind the telescope. */
+int mx_source_direction(const mx_config *cfg, double ra, double dec, double p[3]);
 
 /* Fill energy, p, arrival_time, flags and tag of dev (device pointers,
  * dev->n = src->num_photons) with the source's photons. */

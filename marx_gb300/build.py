@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libmarx_gb300.so")
 SOURCES = ["mx_capi.cu", "mx_kernels.cu", "mx_batch.cu", "mx_static.cu", "mx_diff.cu", "mx_model.cpp",
-           "mx_output.cpp"]
+           "mx_output.cpp", "mx_source.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

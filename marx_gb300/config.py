@@ -59,6 +59,7 @@ class MxConfig(C.Structure):
         ("hesf_gap_y1", C.c_double), ("hesf_gap_y2", C.c_double),
         ("hesf_length", C.c_double), ("hesf_cr_width", C.c_double),
         ("hesf_height", C.c_double * 4), ("hesf_theta", C.c_double * 4),
+        ("ra_nom", C.c_double), ("dec_nom", C.c_double), ("pointing_offset", C.c_double * 2),
     ]
 
 
@@ -116,6 +117,8 @@ def default_config() -> MxConfig:
     c.hesf_length, c.hesf_cr_width = 294.0, 15.7
     c.hesf_height[:] = [22.3, 50.0, 0.0, 0.0]
     c.hesf_theta[:] = [4.5, 7.0, 0.0, 0.0]
+    c.ra_nom, c.dec_nom = 250.2134679741175, -53.75743813458669
+    c.pointing_offset[:] = [0.0, 0.0]
     return c
 
 
@@ -165,6 +168,8 @@ def to_par(c: MxConfig) -> dict:
     for k, name in enumerate(HRC_BLUR):
         P[f"HRC-I-Blur{name}"] = repr(c.hrc_i_blur[k])
         P[f"HRC-S-Blur{name}"] = repr(c.hrc_s_blur[k])
+    P["RA_Nom"], P["Dec_Nom"] = repr(c.ra_nom), repr(c.dec_nom)
+    P["PointingOffsetY"], P["PointingOffsetZ"] = repr(c.pointing_offset[0]), repr(c.pointing_offset[1])
     P["HRC-HESF"] = _yn(c.hrc_hesf)
     P["HESFN"] = str(c.hesf_n)
     P["HESFOffsetX"], P["HESFOffsetZ"] = repr(c.hesf_offset_x), repr(c.hesf_offset_z)
@@ -244,6 +249,9 @@ def from_par(path: str, overrides: dict | None = None) -> MxConfig:
     for k, name in enumerate(HRC_BLUR):
         c.hrc_i_blur[k] = num(f"HRC-I-Blur{name}", c.hrc_i_blur[k])
         c.hrc_s_blur[k] = num(f"HRC-S-Blur{name}", c.hrc_s_blur[k])
+    c.ra_nom, c.dec_nom = num("RA_Nom", c.ra_nom), num("Dec_Nom", c.dec_nom)
+    c.pointing_offset[0] = num("PointingOffsetY", c.pointing_offset[0])
+    c.pointing_offset[1] = num("PointingOffsetZ", c.pointing_offset[1])
     c.hrc_hesf = yes("HRC-HESF", c.hrc_hesf)
     c.hesf_n = int(num("HESFN", c.hesf_n))
     c.hesf_offset_x, c.hesf_offset_z = num("HESFOffsetX", c.hesf_offset_x), num("HESFOffsetZ", c.hesf_offset_z)

@@ -143,6 +143,7 @@ void mx_config_default(mx_config *c) {
   c->hesf_length = 294.0; c->hesf_cr_width = 15.7;
   c->hesf_height[0] = 22.3; c->hesf_height[1] = 50.0;
   c->hesf_theta[0] = 4.5; c->hesf_theta[1] = 7.0;
+  c->ra_nom = 250.2134679741175; c->dec_nom = -53.75743813458669;
 }
 
 mx_context *mx_create(const char *pack_path, const mx_config *cfg) {

@@ -100,3 +100,47 @@ def test_default_config_matches_c_defaults():
     c = cfgmod.MxConfig()
     L.mx_config_default(C.byref(c))
     assert bytes(c) == bytes(cfgmod.default_config())
+
+
+def _source_direction(cfg, ra, dec):
+    import ctypes as C
+    from marx_gb300.config import MxConfig
+    L = _native().load_library()
+    L.mx_source_direction.argtypes = [C.POINTER(MxConfig), C.c_double, C.c_double, C.POINTER(C.c_double)]
+    out = (C.c_double * 3)()
+    r = L.mx_source_direction(C.byref(cfg), ra, dec, out)
+    return r, np.array(out[:])
+
+
+def test_source_direction_matches_reference_fixture():
+    """The source direction st->p the reference computed from SourceRA/Dec
+    and the pointing (tests/golden/sources.npz)."""
+    import os
+    from marx_gb300 import workloads as W
+    from helpers import GOLDEN
+    z = np.load(os.path.join(GOLDEN, "sources.npz"))
+    cfg = W.plain_onaxis(parity=True).cfg
+    r, p = _source_direction(cfg, 250.25, -53.73)
+    assert r == 0
+    assert np.abs(p - z["point_src"]).max() <= 1e-15, (p, z["point_src"])
+
+
+def test_source_direction_matches_reference_live():
+    import pytest
+    from oracle.bindings import Reference, reference_available
+    from marx_gb300 import workloads as W
+    from marx_gb300.config import DITHER
+    if not reference_available():
+        pytest.skip("reference sources not present")
+    cases = [(250.20, -53.70, 0.0, 0.0, 0.0), (250.31, -53.80, 237.36968458476, 3.0, -2.0),
+             (250.2134679741175, -53.75743813458669, 90.0, 0.0, 0.0)]
+    for ra, dec, roll, oy, oz in cases:
+        for dither in ("NONE", "INTERNAL"):
+            cfg = W.plain_onaxis(parity=True).cfg
+            cfg.roll_nom = roll
+            cfg.pointing_offset[:] = [oy, oz]
+            cfg.dither = DITHER[dither]
+            ref = Reference(cfg, extra_par={"SourceRA": repr(ra), "SourceDEC": repr(dec)})
+            p_ref, _, _ = ref.source_photons(1, np.full((4, 1), 0.5))
+            r, p = _source_direction(cfg, ra, dec)
+            assert r == 0 and np.abs(p - p_ref).max() <= 1e-15, (ra, dec, roll, dither, p, p_ref)
