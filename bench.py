@@ -126,13 +126,8 @@ def barrier(world):
 
 
 def max_over_ranks(v, world):
-    if world == 1:
-        return v
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from marx_gb300.replicas import max_over_ranks as mor
+    return mor(v, world, "cuda")
 
 
 def cpu_sample(w, n, threads):
@@ -370,8 +365,8 @@ def main():
     n = a.n or w.n
     eng = Engine(w.cfg)
 
-    host = w.photons(n, seed=w.seed + rank)
-    host.tag[:] = np.arange(n, dtype=np.uint64).astype(np.uint32) + np.uint32(rank * n)
+    from marx_gb300.replicas import rank_photons
+    host = rank_photons(w, n, rank)
     d = DevicePhotons.from_host(host)
     p0, flags0 = d.p.clone(), d.flags.clone()
     stream = torch.cuda.current_stream()
