@@ -53,12 +53,21 @@ MXD D3 normalized(D3 a) {
   if (d == 0.0) return a;
   return mx_rsqrt(d) * a;
 }
+// a / |a| for a vector whose length is 1 to within 1e-8 (a rotation of a
+// unit vector): with |a|^2 = 1 + e, 1/|a| = 1 - e/2 + 3e^2/8 - ..., and
+// 1.5 - |a|^2 / 2 leaves out 3e^2/8 < 4e-17, below half an ulp.  Longer or
+// shorter vectors take the full reciprocal square root.
+MXD D3 normalized_unit(D3 a) {
+  double d = dot(a, a);
+  if (fabs(d - 1.0) < 1e-8) return (1.5 - 0.5 * d) * a;
+  return normalized(a);
+}
 // JDMv_rotate_unit_vector1 (vector.c:198): Rodrigues rotation of p about
 // unit n by (c, s), renormalised.
 MXD D3 rotate_unit(D3 p, D3 n, double c, double s) {
   double pn = dot(p, n);
   D3 u = c * p + (pn * (1.0 - c)) * n + s * cross(n, p);
-  return normalized(u);
+  return normalized_unit(u);
 }
 // sin and cos of an angle that is usually tiny (mirror blur, aspect blur,
 // dither offsets, facet misalignment, scattering): below 1e-3 rad the Taylor
@@ -426,7 +435,7 @@ MXD void blur_normal(D3 &n, double blur_rad, Rng &rng) {
   sincos_small(ang, &sa, &ca);
   const double nxy = n.x * n.y, nxz = n.x * n.z;
   const D3 w = mk(c * len, (s * n.z - c * nxy) * inv, (-s * n.y - c * nxz) * inv);   // perp x n
-  n = normalized(ca * n + sa * w);
+  n = normalized_unit(ca * n + sa * w);
 }
 
 // marx_reflectivity (reflect.c:39-77): polarisation-averaged Fresnel
@@ -456,6 +465,30 @@ MXD double reflectivity(double cos_t, double beta, double delta) {
   double a2 = (pr - rr) * (pr - rr) + (pi_ - ri) * (pi_ - ri);
   double b2 = (pr + rr) * (pr + rr) + (pi_ + ri) * (pi_ + ri);
   return 0.5 * (a1 * b2 + a2 * b1) / (b1 * b2);
+}
+// The same reflectivity as num / den (den > 0).
+MXD void reflectivity_parts(double cos_t, double beta, double delta, double &num, double &den) {
+  double nr = 1.0 - delta, ni = beta;
+  double sin2 = 1.0 - cos_t * cos_t;
+  double sr = nr * nr - ni * ni, si = 2.0 * nr * ni;
+  double wr = sr - sin2, wi = si;
+  double rr, ri;
+  double r = sqrt(wr * wr + wi * wi);
+  if (r == 0.0) { rr = wr; ri = wi; }
+  else if (wr >= 0.0) {
+    double h = 0.5 * (r + wr), inv = mx_rsqrt(h);
+    rr = h * inv; ri = 0.5 * wi * inv;
+  } else {
+    double h = 0.5 * (r - wr), inv = mx_rsqrt(h);
+    rr = 0.5 * wi * inv; ri = h * inv;
+    if (rr < 0.0) { rr = -rr; ri = -ri; }
+  }
+  double a1 = (cos_t - rr) * (cos_t - rr) + ri * ri, b1 = (cos_t + rr) * (cos_t + rr) + ri * ri;
+  double pr = cos_t * sr, pi_ = cos_t * si;
+  double a2 = (pr - rr) * (pr - rr) + (pi_ - ri) * (pi_ - ri);
+  double b2 = (pr + rr) * (pr + rr) + (pi_ + ri) * (pi_ + ri);
+  num = 0.5 * (a1 * b2 + a2 * b1);
+  den = b1 * b2;
 }
 
 // interpolate_theta (wfold.c:304-332) on one fold array.
@@ -501,8 +534,11 @@ MXD bool reflect_test(const MxTables &T, const MxShellDev &h, int o, D3 p, D3 &n
   pdn = dot(p, n);
   if (!T.ideal) {
     double r = rng.uniform();
-    double rfl = reflectivity(fabs(pdn), beta, delta);
-    if (r >= rfl * corr) return false;
+    double num, den;
+    reflectivity_parts(fabs(pdn), beta, delta, num, den);
+    // r >= rfl * corr with rfl = num / den, den > 0, decided without the
+    // division (the two differ only for r within an ulp of the threshold)
+    if (r * den >= num * corr) return false;
   }
   return true;
 }
@@ -522,7 +558,7 @@ MXD int reflect_finish(const MxTables &T, const MxShellDev &h, int o, int table,
   double sg, cg;
   sincos_small(dg, &sg, &cg);
   const double pn = dot(p, n);
-  p = normalized(cg * p + sg * (n + (-pn) * p));
+  p = normalized_unit(cg * p + sg * (n + (-pn) * p));
   return 0;
 }
 
@@ -701,7 +737,7 @@ MXD void mirror_stage(const MxTables &T, const MxShellDev *shells, const float *
 // ------------------------------------------------------------- dither --
 // rotate_unit about the x axis: n = (1, 0, 0), n x p = (0, -p.z, p.y).
 MXD D3 rotate_x(D3 p, double c, double s) {
-  return normalized(mk(c * p.x + p.x * (1.0 - c), c * p.y - s * p.z, c * p.z + s * p.y));
+  return normalized_unit(mk(c * p.x + p.x * (1.0 - c), c * p.y - s * p.z, c * p.z + s * p.y));
 }
 
 // get_internal_dither + dither_ray + apply_dither (dither.c:167-182,
@@ -741,7 +777,7 @@ MXD void dither_stage(const MxTables &T, Ph &ph, Rng &rng) {
   // unit axis: cos p + ((p.n)(1 - cos) / s^2) n + n x p, n.x = 0
   const double pn = p.y * n.y + p.z * n.z;
   const double k = pn * (1.0 - cos_theta) / s2;
-  ph.p = normalized(mk(cos_theta * p.x + (n.y * p.z - n.z * p.y), cos_theta * p.y + k * n.y + n.z * p.x,
+  ph.p = normalized_unit(mk(cos_theta * p.x + (n.y * p.z - n.z * p.y), cos_theta * p.y + k * n.y + n.z * p.x,
                        cos_theta * p.z + k * n.z - n.y * p.x));
 }
 
