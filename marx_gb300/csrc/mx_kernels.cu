@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK, 3) mx_wave_b(MxTables T, Trace
             [&](Ph &q, Rng &r, MirrorState &m) { return mirror_middle(T, sh, q, r, m); });
 }
 
-__global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_wave_c(MxTables T, TraceIO io, WaveBufs w) {
+__global__ void __launch_bounds__(MX_TRACE_BLOCK, 3) mx_wave_c(MxTables T, TraceIO io, WaveBufs w) {
   MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
   stage_tables(T, sh, gr, ch, optc, slope);
   const uint32_t count = *(volatile unsigned int *) &w.counts[2];
