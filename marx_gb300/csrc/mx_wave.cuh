@@ -13,9 +13,9 @@ __host__ __device__ static inline size_t align16(size_t x) { return (x + 15) & ~
 
 // Bytes of dynamic shared memory stage_tables fills.
 __host__ __device__ static inline size_t tables_shared_bytes(const MxTables &T) {
+  (void) T;
   return align16(4 * sizeof(MxShellDev)) + align16(MX_MAX_GRATINGS * sizeof(MxGratingDev)) +
-         align16(MX_MAX_CHIPS * sizeof(MxChipDev)) + align16((size_t) T.optc_len * sizeof(float)) +
-         align16((size_t) T.slope_len * sizeof(double));
+         align16(MX_MAX_CHIPS * sizeof(MxChipDev));
 }
 
 __device__ __forceinline__ void copy_words(uint32_t *dst, const uint32_t *src, size_t words) {
@@ -29,18 +29,14 @@ __device__ __forceinline__ void stage_tables(const MxTables &T, MxShellDev *&sh,
   extern __shared__ __align__(16) unsigned char smem[];
   size_t o_gr = align16(4 * sizeof(MxShellDev));
   size_t o_ch = o_gr + align16(MX_MAX_GRATINGS * sizeof(MxGratingDev));
-  size_t o_op = o_ch + align16(MX_MAX_CHIPS * sizeof(MxChipDev));
-  size_t o_sl = o_op + align16((size_t) T.optc_len * sizeof(float));
   sh = (MxShellDev *) smem;
   gr = (MxGratingDev *) (smem + o_gr);
   ch = (MxChipDev *) (smem + o_ch);
-  optc = (float *) (smem + o_op);
-  slope = (double *) (smem + o_sl);
-  copy_words((uint32_t *) slope, (const uint32_t *) T.optc_slope, (size_t) T.slope_len * 2);
+  optc = (float *) T.optc;
+  slope = (double *) T.optc_slope;
   copy_words((uint32_t *) sh, (const uint32_t *) T.shells, 4 * sizeof(MxShellDev) / 4);
   copy_words((uint32_t *) gr, (const uint32_t *) T.gratings, MX_MAX_GRATINGS * sizeof(MxGratingDev) / 4);
   copy_words((uint32_t *) ch, (const uint32_t *) T.chips, MX_MAX_CHIPS * sizeof(MxChipDev) / 4);
-  copy_words((uint32_t *) optc, (const uint32_t *) T.optc, (size_t) T.optc_len);
   __syncthreads();
 }
 
