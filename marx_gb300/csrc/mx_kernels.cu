@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_trace_kernel(MxTables T, Tr
 // detector.  Appends are warp-aggregated (one atomic per warp); the order
 // of records in a queue does not affect any photon's result.
 
-__global__ void __launch_bounds__(MX_TRACE_BLOCK, 3) mx_wave_a(MxTables T, TraceIO io, WaveBufs w) {
+__global__ void __launch_bounds__(MX_WAVE_BLOCK, MX_WAVE_MIN_BLOCKS) mx_wave_a(MxTables T, TraceIO io, WaveBufs w) {
   MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
   stage_tables(T, sh, gr, ch, optc, slope);
   const size_t n = io.stride;   // component stride of the 3-vector columns
@@ -151,21 +151,21 @@ __device__ __forceinline__ void wave_pass(const TraceIO &io, const MxRec *in, co
   }
 }
 
-__global__ void __launch_bounds__(MX_TRACE_BLOCK, 3) mx_wave_t(MxTables T, TraceIO io, WaveBufs w) {
+__global__ void __launch_bounds__(MX_WAVE_BLOCK, MX_WAVE_MIN_BLOCKS) mx_wave_t(MxTables T, TraceIO io, WaveBufs w) {
   MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
   stage_tables(T, sh, gr, ch, optc, slope);
   wave_pass(io, w.q1, &w.counts[0], w.q2, &w.counts[1],
             [&](Ph &q, Rng &r, MirrorState &m) { return mirror_ptest(T, sh, q, r, m); });
 }
 
-__global__ void __launch_bounds__(MX_TRACE_BLOCK, 3) mx_wave_b(MxTables T, TraceIO io, WaveBufs w) {
+__global__ void __launch_bounds__(MX_WAVE_BLOCK, MX_WAVE_MIN_BLOCKS) mx_wave_b(MxTables T, TraceIO io, WaveBufs w) {
   MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
   stage_tables(T, sh, gr, ch, optc, slope);
   wave_pass(io, w.q2, &w.counts[1], w.q1, &w.counts[2],
             [&](Ph &q, Rng &r, MirrorState &m) { return mirror_middle(T, sh, q, r, m); });
 }
 
-__global__ void __launch_bounds__(MX_TRACE_BLOCK, 3) mx_wave_c(MxTables T, TraceIO io, WaveBufs w) {
+__global__ void __launch_bounds__(MX_WAVE_BLOCK, MX_WAVE_MIN_BLOCKS) mx_wave_c(MxTables T, TraceIO io, WaveBufs w) {
   MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
   stage_tables(T, sh, gr, ch, optc, slope);
   const uint32_t count = *(volatile unsigned int *) &w.counts[2];
@@ -205,7 +205,7 @@ cudaError_t wave_occupancy(int shared_bytes, int *blocks_per_sm) {
     int b = 0;
     cudaError_t e = cudaFuncSetAttribute(f[k], cudaFuncAttributeMaxDynamicSharedMemorySize, shared_bytes);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f[k], MX_TRACE_BLOCK, shared_bytes);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f[k], MX_WAVE_BLOCK, shared_bytes);
     if (e != cudaSuccess) return e;
     if (b < best) best = b;
   }
@@ -215,15 +215,15 @@ cudaError_t wave_occupancy(int shared_bytes, int *blocks_per_sm) {
 
 cudaError_t launch_wavefront(const MxTables &T, const TraceIO &io, const WaveBufs &w, int grid, int shared_bytes,
                              cudaStream_t st) {
-  uint32_t need = (io.n + MX_TRACE_BLOCK - 1) / MX_TRACE_BLOCK;
+  uint32_t need = (io.n + MX_WAVE_BLOCK - 1) / MX_WAVE_BLOCK;
   int ga = (uint32_t) grid > need ? (int) need : grid;
   if (ga < 1) ga = 1;
   cudaError_t e = cudaMemsetAsync(w.counts, 0, 3 * sizeof(unsigned int), st);
   if (e != cudaSuccess) return e;
-  mx_wave_a<<<ga, MX_TRACE_BLOCK, shared_bytes, st>>>(T, io, w);
-  mx_wave_t<<<ga, MX_TRACE_BLOCK, shared_bytes, st>>>(T, io, w);
-  mx_wave_b<<<ga, MX_TRACE_BLOCK, shared_bytes, st>>>(T, io, w);
-  mx_wave_c<<<ga, MX_TRACE_BLOCK, shared_bytes, st>>>(T, io, w);
+  mx_wave_a<<<ga, MX_WAVE_BLOCK, shared_bytes, st>>>(T, io, w);
+  mx_wave_t<<<ga, MX_WAVE_BLOCK, shared_bytes, st>>>(T, io, w);
+  mx_wave_b<<<ga, MX_WAVE_BLOCK, shared_bytes, st>>>(T, io, w);
+  mx_wave_c<<<ga, MX_WAVE_BLOCK, shared_bytes, st>>>(T, io, w);
   return cudaGetLastError();
 }
 

@@ -7,6 +7,8 @@
 #include "mx_model.h"
 
 #define MX_TRACE_BLOCK 256
+#define MX_WAVE_BLOCK 256         // threads per block of the wavefront kernels
+#define MX_WAVE_MIN_BLOCKS 2     // resident blocks per SM they are compiled for: up to 128 registers, no spills (256 x 3 with 80 registers and 256 x 4, 128 x 5 and 128 x 7 measured no faster)
 #define MX_WAVE_KERNELS 4        // kernels of one wavefront trace
 #define MX_COMPACT_THREADS 256
 #define MX_COMPACT_ITEMS 16
