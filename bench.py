@@ -41,12 +41,17 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "photons/s HRMA+grating+ACIS trace"
+# DRAM bytes the four wavefront kernels move per photon of plain_scatter
+# (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture of 2e6
+# photons, profiles/wave_kernels_plain_scatter.md); the traffic of a step
+# grows with its photon count.
+TRAFFIC_BYTES_PER_PHOTON = 559.0
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--workload", default="plain_scatter")
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
@@ -70,7 +75,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -471,7 +476,10 @@ def main():
         "gpu_launches": launches,
         "kernel_ms": kernel_ms,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp64_peak, "traffic": None,
+                     "frac": achieved / fp64_peak,
+                     "traffic": TRAFFIC_BYTES_PER_PHOTON * n if a.workload == "plain_scatter" else None,
+                     "traffic_note": "bytes per step of the four wavefront kernels, scaled from an ncu capture "
+                                     "of 2e6 photons",
                      "algorithmic_flops_per_photon": flops_per_photon,
                      "peak_source": "measured live: mx_probe_fp64 DFMA kernel (MEASURED_PEAKS.json has no FP64 figure)",
                      "hbm": {"achieved_gbs": hbm_achieved, "peak_gbs": hbm_peak, "frac": hbm_achieved / hbm_peak,
