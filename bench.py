@@ -45,7 +45,7 @@ METRIC = "photons/s HRMA+grating+ACIS trace"
 # (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture of 2e6
 # photons, profiles/wave_kernels_plain_scatter.md); the traffic of a step
 # grows with its photon count.
-TRAFFIC_BYTES_PER_PHOTON = 559.0
+TRAFFIC_BYTES_PER_PHOTON = 552.0
 
 
 def parse():
@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-source batched comparison")
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiable-form gradient comparison")
     ap.add_argument("--no-workloads", action="store_true", help="skip the per-workload throughput table")
+    ap.add_argument("--no-events", action="store_true", help="skip the marx2fits event-coordinate pass")
     return ap.parse_args()
 
 
@@ -330,6 +331,73 @@ def bench_workloads(a, skip):
     return out
 
 
+EVENT_BYTES = 1 + 4 + 4 + 4 + 12 + 4 + 4 + 4 + 8 + 8 + 8 + 8 + 4 + 4 + 4 + 2 + 2   # columns read + written
+
+
+def bench_events(a):
+    """The marx2fits event pass (mx_event_coords) on 1e7 ACIS-I events in
+    device memory: EDSER sub-pixel positions, INTERNAL dither with frames of
+    ~30 events, Philox grade draws; the oracle restatement timed on a sample
+    of the same events on one host core."""
+    import torch
+    from marx_gb300 import workloads as W, events as E
+    from marx_gb300._native import Engine
+    n = 10_000_000
+    g = torch.Generator(device="cuda").manual_seed(31)
+    dev = "cuda"
+    frame = E.ACIS_FRAME_TIME
+    t = torch.sort(torch.rand(n, generator=g, device=dev) * (n / 30 * frame)).values.float()
+    arc = 3.141592653589793 / 648000.0
+    ev = {"ccd": torch.randint(0, 4, (n,), generator=g, device=dev, dtype=torch.int8),
+          "xpixel": torch.rand(n, generator=g, device=dev) * 1024, "ypixel": torch.rand(n, generator=g, device=dev) * 1024,
+          "time": t, "sky_ra": (8 * arc * torch.sin(t / 159.0)).float(), "sky_dec": (8 * arc * torch.sin(t / 112.5)).float(),
+          "sky_roll": torch.full((n,), 4.137, device=dev), "b_energy": 0.3 + 9.7 * torch.rand(n, generator=g, device=dev)}
+    eng = Engine(W.ALL["plain_scatter"]().cfg)
+    p = E.params(roll_nom=237.36968458476, dithered=True, pixel_adjust="EDSER")
+    stream = torch.cuda.current_stream()
+    for s in range(3):
+        E.event_coords(eng, p, ev, n, seed=s)
+    torch.cuda.synchronize()
+    k = max(3, min(a.steps, 10))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = eng.launch_count()
+    e0.record(stream)
+    for s in range(k):
+        E.event_coords(eng, p, ev, n, seed=100 + s)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / k
+    launches = (eng.launch_count() - l0) // k
+    hbm_peak = 6800.0
+    try:
+        hbm_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    except (OSError, KeyError, ValueError):
+        pass
+    gbs = EVENT_BYTES * n / (ms * 1e-3) / 1e9
+    # the oracle restatement on a sample of the same events (checker only)
+    import numpy as np
+    from oracle.event_coords import event_coords as oracle_events, subpix_tables
+    from marx_gb300.caldb.pack import DEFAULT_PACK, read_pack
+    z = np.load(os.path.join(ROOT, "tests", "golden", "events_acis_i.npz"))
+    m = 200_000
+    host = {k: v[:m].cpu().numpy() for k, v in ev.items()}
+    for c in ("det_dy", "det_dz", "det_theta"):
+        host[c] = np.zeros(m, np.float32)
+    sub = subpix_tables(read_pack(DEFAULT_PACK))
+    prm = dict(focal_length=10070.0, det_offset=(0.0, 0.0, 0.0), roll_nom=237.36968458476, frame_time=frame,
+               dithered=True, pixel_adjust=0)
+    c0 = time.perf_counter()
+    oracle_events("ACIS-I", z["geom"], z["tdet"], z["fp"], prm, host, np.random.default_rng(1).random((3, m)), sub)
+    cpu_rate = m / (time.perf_counter() - c0)
+    eng.close()
+    return {"workload": "1e7 ACIS-I events, EDSER, INTERNAL dither, frames of ~30 events, device-resident",
+            "events": n, "ms": ms, "events_per_s": n / (ms * 1e-3), "gpu_launches_per_step": launches,
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                         "bytes_per_event": EVENT_BYTES},
+            "cpu_baseline": {"value": cpu_rate, "unit": "events/s", "cores": 1, "kind": "port",
+                             "sample": f"{m} of the same events through the numpy restatement"}}
+
+
 def run_reference(a):
     """Reference arm: the CPU implementation of the path on the host cores."""
     from marx_gb300 import workloads as W
@@ -464,6 +532,7 @@ def main():
     batched = None if a.no_batched else bench_batched(a)
     differentiable = None if a.no_diff else bench_diff(a, fp64_peak)
     workloads = None if a.no_workloads else bench_workloads(a, a.workload)
+    events = None if a.no_events else bench_events(a)
 
     line = {
         "metric": METRIC, "value": value, "unit": "photons/s", "n_gpus": world, "steps": a.steps,
@@ -490,6 +559,7 @@ def main():
         "batched": batched,
         "differentiable": differentiable,
         "workloads": workloads,
+        "events": events,
     }
     print(json.dumps(line))
     if world > 1:

@@ -459,6 +459,74 @@ const char *mx_write_error(void);   /* message of the last mx_write_photons fail
  * reference's stages set them. */
 uint32_t mx_output_history(const mx_config *cfg, uint32_t stages);
 
+/* ------------------------------------------------ event coordinates --
+ * The per-event columns marx2fits derives from an output directory
+ * (marx/src/marx2fits.c), for the context's detector:
+ *   CHIPX, CHIPY   xpixel + 1 in single precision (read_float32_add_1, :3460)
+ *   EXPNO          ACIS frame number (compute_expno, :3741)
+ *   FLTGRADE,GRADE ACIS sub-pixel grade draw (compute_fltgrade, :3854;
+ *                  compute_grade, :3813)
+ *   DETX, DETY     focal-plane pixel (compute_detxy, :3676, through
+ *                  marx_init_chip_to_mnc / marx_chip_to_mnc, pixlib.c:135-222,
+ *                  and marx_mnc_to_fpc, detpix.c:182)
+ *   X, Y           sky pixel (compute_xy_sky, :3869; marx_undither_mnc,
+ *                  dither.c:703; marx_mnc_to_ra_dec and
+ *                  marx_compute_ra_dec_offsets, pixlib.c:499-570)
+ *   TDETX, TDETY   tiled detector pixel (compute_tdetxy, :3584)
+ * On an ACIS run every event of one frame uses the dither state of the
+ * frame's first event unless the pixel adjustment is EXACT
+ * (read_dither_value, :3567).  Pixel adjustments as marx2fits --pixadj
+ * (:3240-3275); EDSER takes the sub-pixel offsets of the ACIS subpix CALDB
+ * file (marx_compute_acis_subpix, acis_subpix.c:284) and means RANDOMIZE
+ * on an HRC, as in marx2fits. */
+#define MX_PIXADJ_EDSER      0
+#define MX_PIXADJ_RANDOMIZE  1
+#define MX_PIXADJ_NONE       2
+#define MX_PIXADJ_EXACT      3
+
+typedef struct mx_event_params {
+  double focal_length;     /* marx.par FocalLength (mm) */
+  double det_offset[3];    /* marx.par DetOffsetX, DetOffsetY, DetOffsetZ (mm) */
+  double roll_nom;         /* obs.par Roll_Nom (degrees): the sky rotation of an undithered run */
+  double frame_time;       /* ACIS frame period: ACIS_Exposure_Time plus ACIS_Frame_Transfer_Time
+                              when both are > 0; <= 0: every event is a frame of its own */
+  double time_offset;      /* added to time64 before its single-precision rounding */
+  int32_t dithered;        /* the run used a dither model (DitherModel != NONE) */
+  int32_t pixel_adjust;    /* MX_PIXADJ_* */
+} mx_event_params;
+
+typedef struct mx_events {
+  uint32_t n;              /* events */
+  uint32_t reserved;
+  const uint32_t *index;   /* event k reads row index[k] of the input columns; NULL: row k */
+  /* inputs: the columns of an output directory (all device memory) */
+  const int8_t *ccd_id;    /* detector.dat: chip / facet id */
+  const float *xpixel, *ypixel;               /* xpixel.dat, ypixel.dat: 0-based chip pixels */
+  const float *time;       /* time.dat; NULL: time64[row] + time_offset, rounded to single precision */
+  const double *time64;
+  const float *sky_ra, *sky_dec, *sky_roll;   /* dither state (radians); NULL reads 0 */
+  const float *det_dy, *det_dz, *det_theta;   /* detector motion (mm, mm, radians); NULL reads 0 */
+  const float *b_energy;   /* b_energy.dat (keV) for EDSER; NULL reads 0 */
+  const double *uniforms;  /* [3][n] per event, slot-major: grade draw, x and y randomisation;
+                              NULL: Philox4x32-10 keyed by seed */
+  /* outputs, one per event (device memory); NULL columns are skipped */
+  float *chipx, *chipy;
+  double *detx, *dety, *x, *y;
+  int32_t *tdetx, *tdety, *expno;             /* expno: ACIS only, 0 on an HRC */
+  int16_t *fltgrade, *grade;                  /* ACIS only, 0 on an HRC */
+} mx_events;
+
+/* Events whose chip id is not a facet of the detector, or whose ray has no
+ * focal-plane position, get NaN coordinates and count as bad
+ * (mx_event_bad_count); marx2fits stops at the first such event. */
+int mx_event_coords(mx_context *ctx, const mx_event_params *params, const mx_events *ev, uint64_t seed,
+                    void *stream);
+/* The same with every column in HOST memory; copies inside, synchronous.
+ * Returns MX_EINVAL when an event was bad. */
+int mx_event_coords_host(mx_context *ctx, const mx_event_params *params, const mx_events *host_ev,
+                         uint64_t seed);
+int mx_event_bad_count(mx_context *ctx, unsigned long long *count, int reset);
+
 /* Measured FP64 fused-multiply-add throughput of the current device
  * (TFLOP/s), the denominator of the trace kernels' roofline. */
 int mx_probe_fp64(double *tflops, double *ms);

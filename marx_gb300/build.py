@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libmarx_gb300.so")
 SOURCES = ["mx_capi.cu", "mx_kernels.cu", "mx_batch.cu", "mx_static.cu", "mx_diff.cu", "mx_model.cpp",
-           "mx_output.cpp", "mx_source.cpp"]
+           "mx_output.cpp", "mx_source.cpp", "mx_events.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -37,6 +37,9 @@ def _flags(src: str, verbose: bool):
          "--expt-relaxed-constexpr"]
     if src.endswith(".cu"):
         f += ARCH
+        if os.path.basename(src) == "mx_events.cu":
+            # no multiply-add contraction: DETX/DETY round like the reference's
+            f += ["--fmad=false"]
         if verbose:
             f += ["-Xptxas", "-v"]
     else:

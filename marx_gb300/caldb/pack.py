@@ -4,7 +4,8 @@ The trace needs the HRMA shell geometry, the iridium optical constants, the
 per-shell effective-area correction factors, the WFold scattering tables, the
 HETG and LETG grating efficiencies, the grating optical constants (for the
 LETG support gratings), the HETG facet sector tables, the ACIS chip corners
-and the HRC geometry and efficiency tables.
+the HRC geometry and efficiency tables, and the ACIS sub-pixel offsets of
+marx2fits's EDSER pixel adjustment.
 MARX reads them at init from its data directory in four formats (RDB text,
 big-endian "bdat" float tables, the WFold binary format and FITS binary
 tables).  ``build_pack`` reads those files once and writes every table into a
@@ -184,14 +185,17 @@ HRC_S_GEOM = (("V_Pixel_Size", 1), ("V_Active", 6), ("U_Pixel_Size", 1), ("U_Act
 
 def read_fits_bintables(path: str):
     """Minimal FITS reader: yields (header dict, {column: ndarray}) for each
-    BINTABLE extension.  Handles the scalar/vector numeric (E, D, J, I) and
-    character (A) columns the CALDB files use."""
+    BINTABLE extension.  Handles the scalar/vector numeric (E, D, J, I, K, B),
+    character (A) and bit (X, as bytes) columns the CALDB files and event
+    lists use."""
     b = open(path, "rb").read()
     off, hdus = 0, []
     while off < len(b):
         hdr = {}
         while True:
             blk = b[off:off + 2880]
+            if len(blk) < 2880:
+                raise ValueError(f"{path}: truncated FITS header")
             off += 2880
             done = False
             for i in range(36):
@@ -231,12 +235,16 @@ def read_fits_bintables(path: str):
                 j += 1
             rep = int(form[:j]) if j else 1
             code = form[j]
-            sz = {"E": 4, "D": 8, "J": 4, "I": 2, "A": 1, "K": 8}[code]
+            sz = {"E": 4, "D": 8, "J": 4, "I": 2, "A": 1, "K": 8, "B": 1, "X": 1}[code]
             name = hdr[f"TTYPE{i}"].strip()
-            if code == "A":
+            if code == "X":   # bit array: its bytes, rows x ceil(rep / 8)
+                rep = (rep + 7) // 8
+                vals = np.array([np.frombuffer(raw, dtype=np.uint8, count=rep, offset=r * rowlen + pos)
+                                 for r in range(nrows)]).reshape(nrows, rep)
+            elif code == "A":
                 vals = [raw[r * rowlen + pos:r * rowlen + pos + rep].decode().rstrip(" \0") for r in range(nrows)]
             else:
-                dt = {"E": ">f4", "D": ">f8", "J": ">i4", "I": ">i2", "K": ">i8"}[code]
+                dt = {"E": ">f4", "D": ">f8", "J": ">i4", "I": ">i2", "K": ">i8", "B": ">u1"}[code]
                 a = np.empty((nrows, rep), dtype=dt)
                 for r in range(nrows):
                     a[r] = np.frombuffer(raw, dtype=dt, count=rep, offset=r * rowlen + pos)
@@ -323,6 +331,18 @@ def build_sections(data_dir: str) -> dict:
         S[key] = read_bdat(os.path.join(data_dir, "hrc", fname))[:2]
     S["hrc/optconst_cr"] = read_bdat(os.path.join(data_dir, "hrc", "chromium.dat"))[:3]
     S["hrc/optconst_c"] = read_bdat(os.path.join(data_dir, "hrc", "carbon.dat"))[:3]
+    # ACIS sub-pixel event positions (read_subpix_ext, acis_subpix.c:96-186):
+    # per flight grade its number of points, then energies, CHIPX and CHIPY
+    # offsets padded to the column's repeat count
+    sub = read_fits_bintables(os.path.join(data_dir, "caldb", "acisD1999-07-22subpixN0001_marx.fits"))
+    for h, c in sub:
+        kind = {"MARX_ACIS_SUBPIX_FI": "fi", "MARX_ACIS_SUBPIX_BI": "bi"}.get(h.get("EXTNAME"))
+        if kind is None:
+            continue
+        cols = {k.upper(): v for k, v in c.items()}
+        S[f"acis/subpix_{kind}/rows"] = np.stack([cols["FLTGRADE"], cols["NPOINTS"]], axis=1).astype(np.int32)
+        S[f"acis/subpix_{kind}/table"] = np.stack([cols["ENERGY"], cols["CHIPX_OFFSET"],
+                                                   cols["CHIPY_OFFSET"]]).astype(np.float32)
     qe = read_fits_bintables(os.path.join(data_dir, "caldb", "acisD1997-04-17qeN0006.fits"))
     for h, c in qe:
         if h.get("EXTNAME") == "AXAF_QE":

@@ -78,6 +78,7 @@ static int configure(mx_context *c, const mx_config *cfg) {
   std::string err;
   if (!build_model(c->pack, *cfg, c->hm, err)) return fail(c, MX_EINVAL, err);
   c->cfg = *cfg;
+  c->events_ready = false;
   int r = upload_model(c);
   if (r) return r;
   for (int s = 0; s < 2; s++) {
@@ -156,6 +157,8 @@ mx_context *mx_create(const char *pack_path, const mx_config *cfg) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc((void **) &c->d_overrun, sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMemset(c->d_overrun, 0, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc((void **) &c->d_event_bad, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(c->d_event_bad, 0, sizeof(unsigned long long));
   if (e != cudaSuccess) { g_create_err = std::string("CUDA: ") + cudaGetErrorString(e); mx_destroy(c); return nullptr; }
   if (configure(c, cfg) != MX_OK) { g_create_err = c->err; mx_destroy(c); return nullptr; }
   return c;
@@ -185,7 +188,11 @@ void mx_destroy(mx_context *c) {
   c->scan.release();
   c->wave.release();
   c->spec.release();
+  c->ev_tab.release();
+  c->ev_scan.release();
+  c->ev_io.release();
   if (c->d_overrun) cudaFree(c->d_overrun);
+  if (c->d_event_bad) cudaFree(c->d_event_bad);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }

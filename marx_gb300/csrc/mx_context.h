@@ -43,6 +43,11 @@ struct mx_context {
   int mode = MX_MODE_AUTO;
   unsigned long long *d_overrun = nullptr;
   unsigned long long launches = 0;
+  // event coordinates (mx_events.cu): tables built on first use per configuration
+  bool events_ready = false;
+  alignas(16) char ev_geom[2048];   // the launch copy of the facet geometry
+  DevBuf ev_tab, ev_scan, ev_io;
+  unsigned long long *d_event_bad = nullptr;
 };
 
 // Record an error on the context (or as the creation error when c is null)

@@ -64,6 +64,7 @@ template <class T> const T *Pack::get(const std::string &name, size_t *count, st
 }
 template const double *Pack::get<double>(const std::string &, size_t *, std::string &) const;
 template const float *Pack::get<float>(const std::string &, size_t *, std::string &) const;
+template const int32_t *Pack::get<int32_t>(const std::string &, size_t *, std::string &) const;
 
 // ---------------------------------------------------------------- matrices --
 static void rot_z(double m[9], double theta) {

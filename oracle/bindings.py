@@ -29,7 +29,7 @@ def reference_available() -> bool:
 def build_reference() -> bool:
     if not reference_available():
         return False
-    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_ROOT}"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "ref", "m2f", f"REF={REF_ROOT}"], check=True)
     return True
 
 
@@ -159,6 +159,17 @@ class Reference:
         g = np.zeros((10, 20))
         n = self.lib.mxref_detector_geometry(_p(g), 10)
         return g[:n]
+
+    def facet_tdet(self) -> np.ndarray:
+        t = np.zeros((10, 2))
+        n = self.lib.mxref_facet_tdet(_p(t), 10)
+        return t[:n]
+
+    def fp_system(self) -> np.ndarray:
+        f = np.zeros(3)
+        if self.lib.mxref_fp_system(_p(f)) != 0:
+            raise RuntimeError("no focal-plane system")
+        return f
 
     def _outs(self, n):
         o = dict(x=np.zeros((n, 3)), p=np.zeros((n, 3)), flags=np.zeros(n, np.uint32),

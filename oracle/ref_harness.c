@@ -33,6 +33,7 @@
 
 #include <jdmath.h>
 #include <pfile.h>
+#include "acis.h"   /* the facets' tdet offsets (MARX_DET_FACET_PRIVATE_DATA) */
 #include "marx.h"
 #include "_marx.h"
 
@@ -197,6 +198,32 @@ int mxref_detector_geometry(double *out, int max_chips)
 }
 
 double mxref_focal_length(void) { return Marx_Focal_Length; }
+
+/* The tiled-detector offsets of each facet (tdet_xoff, tdet_yoff), as
+ * marx2fits's compute_tdetxy reads them. */
+int mxref_facet_tdet(double *out, int max_chips)
+{
+   Marx_Detector_Geometry_Type *g;
+   int n = 0;
+   if (Det == NULL) return 0;
+   for (g = Det->facet_list; g != NULL && n < max_chips; g = g->next, n++)
+     {
+        out[2 * n] = g->tdet_xoff;
+        out[2 * n + 1] = g->tdet_yoff;
+     }
+   return n;
+}
+
+/* The detector's focal-plane system: fp_delta_s0 (radians), fp_x0, fp_y0
+ * (detpix.c:42-63). */
+int mxref_fp_system(double *out)
+{
+   if (Det == NULL || Det->fp_coord_info == NULL) return -1;
+   out[0] = Det->fp_coord_info->fp_delta_s0;
+   out[1] = Det->fp_coord_info->fp_x0;
+   out[2] = Det->fp_coord_info->fp_y0;
+   return 0;
+}
 
 /* ---------------------------------------------------------- detection -- */
 /* Per-photon body of _marx_acis_i_detect (acis-i.c:124-157); the acis-s

@@ -20,6 +20,12 @@ oracle/Makefile compiles them in place into oracle/_ref.  Writes:
                          models (POINT, GAUSS, BETA, DISK, LINE; FLAT and
                          FILE spectra) for the engine's source uniforms
                          (--sources).
+  events_<case>.npz      the reference's marx2fits program (oracle/Makefile
+                         target m2f) run on a synthetic output directory:
+                         the event columns it read, the facet geometry, and
+                         CHIPX/CHIPY, EXPNO, FLTGRADE/GRADE, TDETX/TDETY,
+                         DETX/DETY and X/Y of its FITS event list for each
+                         pixel adjustment (--events).
   diff_rays.npz          focal-plane positions of the differentiable form's
                          rays traced by the reference's mirror stage, at
                          theta = 0 and at the workload's perturbation written
@@ -192,6 +198,182 @@ def sources_fixture():
     np.savez_compressed(os.path.join(HERE, "sources.npz"), **out)
 
 
+# ----------------------------------------------------------- event lists --
+# (workload whose configuration names the detector, marx2fits inputs)
+EVENT_CASES = {
+    "acis_i": dict(workload="plain_scatter", detector="ACIS-I", dithered=True, roll_nom=237.36968458476,
+                   det_offset=(0.0, 0.0, 0.0), motion=False, focal=10070.0),
+    "acis_s": dict(workload="plain_hetg", detector="ACIS-S", dithered=True, roll_nom=112.25,
+                   det_offset=(0.2, -0.35, 0.15), motion=True, focal=10079.77),
+    "acis_i_nodither": dict(workload="plain_onaxis", detector="ACIS-I", dithered=False, roll_nom=37.5,
+                            det_offset=(0.0, 0.1, 0.0), motion=False, focal=10070.0),
+    "hrc_i": dict(workload="plain_hrci", detector="HRC-I", dithered=True, roll_nom=10.0,
+                  det_offset=(0.0, 0.0, 0.0), motion=False, focal=10070.0),
+    "hrc_s": dict(workload="letg_hrcs", detector="HRC-S", dithered=True, roll_nom=300.0,
+                  det_offset=(0.0, 0.1, -0.2), motion=False, focal=10070.0),
+}
+N_EVENTS = 4000
+FRAME_TIME = 3.2 + 0.041          # marx.par ACIS_Exposure_Time + ACIS_Frame_Transfer_Time
+PIXADJ_MODES = ("EXACT", "NONE", "RANDOMIZE", "EDSER")
+
+
+def write_dat(path, name, typ, values):
+    """One column file of a MARX output directory (marx/data/FORMAT.TXT)."""
+    dt = {"E": ">f4", "J": ">i4", "I": ">i2", "A": ">i1"}[typ]
+    v = np.asarray(values).astype(dt)
+    hdr = bytearray(32)
+    hdr[0:4] = bytes([0x83, 0x13, 0x89, 0x8D])
+    hdr[4] = ord(typ)
+    hdr[5:5 + len(name)] = name.encode()
+    hdr[20:24] = len(v).to_bytes(4, "big")
+    with open(path, "wb") as f:
+        f.write(bytes(hdr) + v.tobytes())
+
+
+def par_set(text, name, value):
+    """Set the value field of one parameter line of a .par file."""
+    out = []
+    for line in text.splitlines():
+        if line.split(",", 1)[0] == name:
+            f = line.split(",")
+            f[3] = value
+            line = ",".join(f)
+        out.append(line)
+    return "\n".join(out) + "\n"
+
+
+def synth_events(case, geom, seed):
+    rng = np.random.default_rng(seed)
+    n = N_EVENTS
+    ids = geom[:, 0].astype(np.int64)
+    ccd = ids[rng.integers(0, len(ids), n)]
+    det = case["detector"]
+    nx, ny = {"ACIS-I": (1024, 1024), "ACIS-S": (1024, 1024), "HRC-I": (16384, 16384),
+              "HRC-S": (4096, 16456)}[det]
+    xp = rng.uniform(0, nx, n)
+    yp = rng.uniform(0, ny, n)
+    # whole pixels and sub-pixel thirds, where floor and the grade split change
+    m = rng.random(n) < 0.1
+    xp[m] = np.floor(xp[m])
+    m = rng.random(n) < 0.1
+    yp[m] = np.floor(yp[m]) + rng.choice([1.0 / 3.0, 2.0 / 3.0, 0.5], int(m.sum()))
+    t = np.sort(rng.uniform(0.0, n / 30.0 * FRAME_TIME, n)).astype(np.float32)
+    arc = np.pi / (180.0 * 3600.0)
+    ra = 8.0 * arc * np.sin(2 * np.pi * t / 1000.0) + rng.normal(0, 0.2 * arc, n)
+    dec = 8.0 * arc * np.sin(2 * np.pi * t / 707.0) + rng.normal(0, 0.2 * arc, n)
+    roll = np.deg2rad(case["roll_nom"]) + rng.normal(0, 1e-5, n)
+    z = np.zeros(n)
+    dy = rng.normal(0, 0.02, n) if case["motion"] else z
+    dz = rng.normal(0, 0.02, n) if case["motion"] else z
+    dth = rng.normal(0, 2e-4, n) if case["motion"] else z
+    be = rng.uniform(0.2, 12.0, n)
+    be[:20] = [0.0, 20.0, 0.3, 1.0, 2.0, 0.5, 5.0, 10.0, 1.5, 0.25] * 2   # table nodes and ends
+    U = rng.random((3, n))
+    U[:, :8] = [[0.0] * 8, [0.0] * 8, [0.999999] * 8]
+    f = np.float32
+    return dict(ccd=ccd.astype(np.int8), xpixel=xp.astype(f), ypixel=yp.astype(f), time=t,
+                sky_ra=ra.astype(f), sky_dec=dec.astype(f), sky_roll=roll.astype(f), det_dy=dy.astype(f),
+                det_dz=dz.astype(f), det_theta=dth.astype(f), b_energy=be.astype(f)), U
+
+
+def run_marx2fits(case, ev, U, mode, workdir):
+    """The reference's marx2fits on one synthetic output directory."""
+    import subprocess
+    from marx_gb300.caldb.pack import read_fits_bintables
+    exe = os.path.join(ROOT, "oracle", "_ref", "marx2fits")
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "m2f", f"REF={REF_ROOT}"], check=True)
+    d = os.path.join(workdir, f"sim_{mode}")
+    os.makedirs(d, exist_ok=True)
+    n = len(ev["ccd"])
+    acis = case["detector"].startswith("ACIS")
+    z = np.zeros(n)
+    cols = [("time.dat", "TIME", "E", ev["time"]), ("energy.dat", "ENERGY", "E", z + 1.0),
+            ("b_energy.dat", "B_ENERGY", "E", ev["b_energy"]),
+            ("xpos.dat", "XPOS", "E", z), ("ypos.dat", "YPOS", "E", z), ("zpos.dat", "ZPOS", "E", z),
+            ("xcos.dat", "COSX", "E", z - 1.0), ("ycos.dat", "COSY", "E", z), ("zcos.dat", "COSZ", "E", z),
+            ("pha.dat", "PHA", "I", z), ("detector.dat", "CCDID", "A", ev["ccd"]),
+            ("xpixel.dat", "CHIPX", "E", ev["xpixel"]), ("ypixel.dat", "CHIPY", "E", ev["ypixel"]),
+            ("mirror.dat", "MIRROR", "I", z), ("tag.dat", "TAG", "J", np.arange(n)),
+            ("sky_ra.dat", "RA", "E", ev["sky_ra"]), ("sky_dec.dat", "DEC", "E", ev["sky_dec"]),
+            ("sky_roll.dat", "ROLL", "E", ev["sky_roll"]), ("det_dy.dat", "DET_DY", "E", ev["det_dy"]),
+            ("det_dz.dat", "DET_DZ", "E", ev["det_dz"]), ("det_theta.dat", "DET_THETA", "E", ev["det_theta"])]
+    if case["detector"] == "HRC-S":
+        cols += [("hrc_u.dat", "U", "E", z), ("hrc_v.dat", "V", "E", z)]
+    for fn, name, typ, v in cols:
+        write_dat(os.path.join(d, fn), name, typ, v)
+    par = open(os.path.join(REF_ROOT, "marx", "par", "marx.par")).read()
+    for k, v in (("DetectorType", f'"{case["detector"]}"'), ("GratingType", '"NONE"'),
+                 ("DitherModel", '"INTERNAL"' if case["dithered"] else '"NONE"'),
+                 ("FocalLength", repr(case["focal"])), ("DetOffsetX", repr(case["det_offset"][0])),
+                 ("DetOffsetY", repr(case["det_offset"][1])), ("DetOffsetZ", repr(case["det_offset"][2])),
+                 ("ACIS_Exposure_Time", "3.2"), ("ACIS_Frame_Transfer_Time", "0.041")):
+        par = par_set(par, k, v)
+    open(os.path.join(d, "marx.par"), "w").write(par)
+    obs_t = {"ACIS-I": "acis_i_obs.par", "ACIS-S": "acis_s_obs.par", "HRC-I": "hrc_i_obs.par",
+             "HRC-S": "hrc_s_obs.par"}[case["detector"]]
+    obs = open(os.path.join(REF_ROOT, "marx", "data", "obs", obs_t)).read()
+    # the values marx's write_obs_par learns into the template (marx.c:1152-1180)
+    for k, v in (("EXPOSURE", 1000.0), ("ra_nom", 250.2), ("dec_nom", -53.75), ("roll_nom", case["roll_nom"]),
+                 ("tstart", 0.0), ("tstop", 1000.0), ("sim_x", 0.0), ("sim_y", 0.0), ("sim_z", 0.0)):
+        obs = par_set(obs, k, repr(v))
+    open(os.path.join(d, "obs.par"), "w").write(obs)
+    # the uniforms in the order marx2fits draws them
+    padj = mode if (acis or mode != "EDSER") else "RANDOMIZE"
+    seq = []
+    for k in range(n):
+        if acis:
+            seq.append(U[0, k])
+        if padj == "RANDOMIZE":
+            seq += [U[1, k], U[2, k]]
+    ufile = os.path.join(workdir, f"u_{mode}.bin")
+    np.asarray(seq, dtype=np.float64).tofile(ufile)
+    out = os.path.join(workdir, f"evt_{mode}.fits")
+    env = dict(os.environ, MARX_DATA_DIR=os.path.join(REF_ROOT, "marx", "data"), MXREF_UNIFORMS=ufile)
+    r = subprocess.run([exe, f"--pixadj={mode}", d, out], env=env, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"marx2fits failed: {r.stdout[-2000:]}\n{r.stderr[-2000:]}")
+    drawn = [ln for ln in r.stderr.splitlines() if ln.startswith("mxref uniforms drawn:")]
+    got = int(drawn[-1].split(":")[1]) if drawn else 0
+    if got != len(seq):
+        raise RuntimeError(f"marx2fits drew {got} uniforms, expected {len(seq)}")
+    for hdr, c in read_fits_bintables(out):
+        if hdr.get("EXTNAME") == "EVENTS":
+            return c
+    raise RuntimeError("no EVENTS table")
+
+
+def events_fixture(name):
+    """The reference's marx2fits on a synthetic event list (one process per
+    case: the reference keeps detector state in statics)."""
+    case = EVENT_CASES[name]
+    w = W.ALL[case["workload"]]()
+    ref = Reference(w.cfg)
+    geom, tdet, fp = ref.detector_geometry(), ref.facet_tdet(), ref.fp_system()
+    import zlib
+    ev, U = synth_events(case, geom, seed=zlib.crc32(name.encode()))
+    out = dict(geom=geom, tdet=tdet, fp=fp, uniforms=U, **ev)
+    if case["detector"] == "HRC-I":
+        # marx2fits cannot open an HRC-I run in this MARX: the detector set-up
+        # it calls (patch_hrc_i_geom, hrc_i_geom.c:119) reads Verbose from a
+        # null parameter file (hrc_i_geom.c:190) and fails.  The fixture keeps
+        # the inputs and the reference's facet geometry only.
+        out["marx2fits"] = np.array("fails: DetectorType HRC-I not supported")
+        modes = ()
+    else:
+        modes = PIXADJ_MODES
+    with tempfile.TemporaryDirectory() as tmp:
+        for mode in modes:
+            c = run_marx2fits(case, ev, U, mode, tmp)
+            for col in ("EXPNO", "CHIPX", "CHIPY", "TDETX", "TDETY", "DETX", "DETY", "X", "Y", "FLTGRADE", "GRADE"):
+                if col in c:
+                    out[f"{mode}_{col.lower()}"] = np.asarray(c[col])
+    out["params"] = np.array([case["focal"], *case["det_offset"], case["roll_nom"], FRAME_TIME,
+                              float(case["dithered"])])
+    out["detector"] = np.array(case["detector"])
+    np.savez_compressed(os.path.join(HERE, f"events_{name}.npz"), **out)
+    print(name, "events", N_EVENTS, "columns", sorted(k for k in out if k.startswith("EXACT_")))
+
+
 N_DIFF = 4000
 RDB = "EKCHDOS06.rdb"
 SHELL_OF = {"1": 0, "3": 1, "4": 2, "6": 3}
@@ -271,6 +453,13 @@ if __name__ == "__main__":
     names = [a for a in sys.argv[1:] if not a.startswith("-")]
     if "--diff" in sys.argv:
         diff_rays()
+    elif "--events" in sys.argv:
+        if names:
+            events_fixture(names[0])
+        else:
+            import subprocess
+            for n in EVENT_CASES:
+                subprocess.run([sys.executable, __file__, "--events", n], check=True)
     elif "--sources" in sys.argv:
         sources_fixture()
     elif "--dat" in sys.argv:
