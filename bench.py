@@ -392,8 +392,10 @@ def bench_events(a):
     eng.close()
     return {"workload": "1e7 ACIS-I events, EDSER, INTERNAL dither, frames of ~30 events, device-resident",
             "events": n, "ms": ms, "events_per_s": n / (ms * 1e-3), "gpu_launches_per_step": launches,
-            "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
-                         "bytes_per_event": EVENT_BYTES},
+            "roofline": {"bound": "fp64", "note": "sin, cos, acos, asin, atan and six divisions per event; "
+                                                  "ncu: FP64 pipe 87% busy (profiles/event_kernel_acis_i.md)",
+                         "hbm": {"achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                                 "bytes_per_event": EVENT_BYTES}},
             "cpu_baseline": {"value": cpu_rate, "unit": "events/s", "cores": 1, "kind": "port",
                              "sample": f"{m} of the same events through the numpy restatement"}}
 

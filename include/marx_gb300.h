@@ -260,7 +260,7 @@ int mx_trace_host(mx_context *ctx, const mx_photons *host, uint32_t stages,
 
 /* ------------------------------------------------------------ sources --
  * A source at infinity: the input producer of the trace (the create_photons
- * functions of s-point.c:59, s-gauss.c, s-beta.c, s-disk.c, s-line.c, with
+ * functions of s-point.c:59, s-gauss.c, s-beta.c, s-disk.c, s-line.c, s-image.c, with
  * flat_energy and file_energy, spectrum.c:138-190).  Photon k gets tag
  * first_tag + k; its energy and direction come from the Philox draws of
  * that tag in the source domain (draw 0: energy, then the source's own
@@ -276,14 +276,20 @@ typedef struct mx_source {
    *   MX_SOURCE_GAUSS  param[0] S-GaussSigma (arcsec)
    *   MX_SOURCE_BETA   param[0] S-BetaCoreRadius (arcsec), param[1] S-BetaBeta (> 1/2)
    *   MX_SOURCE_DISK   param[0] S-DiskTheta0, param[1] S-DiskTheta1 (arcsec)
-   *   MX_SOURCE_LINE   param[0] S-LinePhi (deg), param[1] S-LineTheta (arcsec) */
+   *   MX_SOURCE_LINE   param[0] S-LinePhi (deg), param[1] S-LineTheta (arcsec)
+   *   MX_SOURCE_IMAGE  param[0], param[1] degrees per pixel along NAXIS1 and NAXIS2
+   *                    (|CDELT1|, |CDELT2|, or the CD matrix's row lengths; 0: 0.5 arcsec),
+   *                    image: image_ny rows of image_nx pixel values (s-image.c:91-330) */
   int32_t kind;             /* MX_SOURCE_* */
   uint32_t spectrum_n;      /* > 0: FILE spectrum of spectrum_n rows (spectrum.c:182-274), else FLAT */
   double param[4];
   const double *spectrum_energy;   /* HOST arrays: energy (keV, non-decreasing) and flux density */
   const double *spectrum_flux;
+  uint32_t image_nx, image_ny;     /* IMAGE: NAXIS1, NAXIS2 */
+  const float *image;              /* HOST array, row-major (NAXIS2 rows of NAXIS1 pixels) */
 } mx_source;
-enum { MX_SOURCE_POINT = 0, MX_SOURCE_GAUSS = 1, MX_SOURCE_BETA = 2, MX_SOURCE_DISK = 3, MX_SOURCE_LINE = 4 };
+enum { MX_SOURCE_POINT = 0, MX_SOURCE_GAUSS = 1, MX_SOURCE_BETA = 2, MX_SOURCE_DISK = 3, MX_SOURCE_LINE = 4,
+       MX_SOURCE_IMAGE = 5 };
 
 /* The direction of travel p of the photons of a source at (ra, dec)
  * (degrees) for the configuration's pointing (RA_Nom, Dec_Nom, Roll_Nom,

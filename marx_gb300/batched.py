@@ -24,19 +24,22 @@ class MxSource(C.Structure):
     _fields_ = [("p", C.c_double * 3), ("energy_min", C.c_double), ("energy_max", C.c_double),
                 ("num_photons", C.c_uint32), ("grating", C.c_int32), ("detector", C.c_int32),
                 ("reserved", C.c_uint32), ("kind", C.c_int32), ("spectrum_n", C.c_uint32),
-                ("param", C.c_double * 4), ("spectrum_energy", C.c_void_p), ("spectrum_flux", C.c_void_p)]
+                ("param", C.c_double * 4), ("spectrum_energy", C.c_void_p), ("spectrum_flux", C.c_void_p),
+                ("image_nx", C.c_uint32), ("image_ny", C.c_uint32), ("image", C.c_void_p)]
 
 
 # source models (MX_SOURCE_* in include/marx_gb300.h) and their parameters
-SOURCE = {"POINT": 0, "GAUSS": 1, "BETA": 2, "DISK": 3, "LINE": 4}
+SOURCE = {"POINT": 0, "GAUSS": 1, "BETA": 2, "DISK": 3, "LINE": 4, "IMAGE": 5}
 
 
 def make_source(p, kind="POINT", param=(), energy=(1.0, 1.0), spectrum=None, num_photons=0,
-                grating="NONE", detector="ACIS-I") -> MxSource:
+                grating="NONE", detector="ACIS-I", image=None) -> MxSource:
     """One source: p the unit direction of travel, kind and param as
     mx_source documents them, a FLAT spectrum (energy_min, energy_max) or a
-    FILE spectrum (energies, flux) that the returned struct references (keep
-    the arrays alive while it is used)."""
+    FILE spectrum (energies, flux), and for an IMAGE source the pixel array
+    (NAXIS2 rows of NAXIS1, e.g. from ``read_image_fits``) with param the
+    degrees per pixel; the returned struct references the arrays (keep it
+    alive while it is used)."""
     s = MxSource()
     s.p[:] = list(p)
     s.kind = SOURCE[kind]
@@ -51,7 +54,53 @@ def make_source(p, kind="POINT", param=(), energy=(1.0, 1.0), spectrum=None, num
         s._keep = (e, f)
         s.spectrum_n = len(e)
         s.spectrum_energy, s.spectrum_flux = e.ctypes.data, f.ctypes.data
+    if image is not None:
+        im = np.ascontiguousarray(image, dtype=np.float32)
+        s._keep_image = im
+        s.image_ny, s.image_nx = im.shape
+        s.image = im.ctypes.data
     return s
+
+
+def read_image_fits(path: str):
+    """The primary image of a FITS file as the IMAGE source reads it
+    (open_image_fits_file and read_image, s-image.c:46-232): pixel values as
+    float32 (BITPIX 8, 16, 32, -32 or -64; no BSCALE/BZERO), and the degrees
+    per pixel from CDELT1/CDELT2, else the CD matrix, else (0, 0) for the
+    model's 0.5 arcsec default.  Returns (image[NAXIS2, NAXIS1], (s1, s2))."""
+    b = open(path, "rb").read()
+    hdr, off = {}, 0
+    while True:
+        blk = b[off:off + 2880]
+        if len(blk) < 2880:
+            raise ValueError(f"{path}: truncated FITS header")
+        off += 2880
+        done = False
+        for i in range(36):
+            card = blk[i * 80:(i + 1) * 80].decode("ascii", "replace")
+            key = card[:8].strip()
+            if key == "END":
+                done = True
+                break
+            if card[8:10] == "= ":
+                hdr[key] = card[10:].split("/")[0].strip()
+        if done:
+            break
+    nx, ny, bitpix = int(hdr["NAXIS1"]), int(hdr["NAXIS2"]), int(hdr["BITPIX"])
+    dt = {8: ">u1", 16: ">i2", 32: ">i4", -32: ">f4", -64: ">f8"}.get(bitpix)
+    if dt is None:
+        raise ValueError(f"BITPIX = {bitpix} is not supported")
+    img = np.frombuffer(b, dtype=dt, count=nx * ny, offset=off).astype(np.float32).reshape(ny, nx)
+    num = lambda k: float(hdr[k].replace("D", "E"))
+    if "CDELT1" in hdr:
+        s1, s2 = abs(num("CDELT1")), abs(num("CDELT2"))
+    elif "CD1_1" in hdr:
+        a, b2, c, d = num("CD1_1"), num("CD1_2"), num("CD2_1"), num("CD2_2")
+        s1 = math.sqrt(a * a + b2 * b2)
+        s2 = math.sqrt(c * c + d * d)
+    else:
+        s1 = s2 = 0.0
+    return img, (s1, s2)
 
 
 class MxBatchParams(C.Structure):

@@ -28,7 +28,8 @@ struct MxSourceDev {
   int32_t spec_n;           // 0: FLAT
   int32_t grating;          // 1: HETG
   int32_t chip_off, nchips; // chips[chip_off .. chip_off + nchips)
-  int32_t pad[2];
+  int32_t img_off, img_nx;  // IMAGE: cumulative distribution rows [img_off, img_off + nx * ny) of the table
+  int32_t img_ny, pad[3];   //        (a, b: radians per pixel along x and y; axis, cos_al, sin_al: the rotation)
 };
 static_assert(sizeof(MxSourceDev) % 16 == 0, "source record size");
 
@@ -60,6 +61,23 @@ __device__ double interp_d(double x, const double *xp, const double *yp, unsigne
   return MX_DADD(y0, MX_DMUL(MX_DDIV(MX_DADD(y1, -y0), MX_DADD(x1, -x0)), MX_DADD(x, -x0)));
 }
 
+// JDMbinary_search_f (finterpo.c:37-57) over single-precision values held in
+// the double table: the same bisection and comparisons.
+__device__ __forceinline__ unsigned bsearch_cdf(float x, const double *xp, unsigned n) {
+  unsigned n0 = 0, n1 = n;
+  while (n1 > n0 + 1) {
+    unsigned n2 = (n0 + n1) / 2;
+    const float v = (float) __ldg(xp + n2);
+    if (v >= x) {
+      if (v == x) return n2;
+      n1 = n2;
+    } else
+      n0 = n2;
+  }
+  if (x >= (float) __ldg(xp + n0)) return n1;
+  return n0;
+}
+
 // The create_photons function of the source's model for one photon:
 // point_create_photons (s-point.c:59), gauss_create_photons
 // (s-gauss.c:76-130), beta_create_photons (s-beta.c:74-120),
@@ -79,6 +97,22 @@ __device__ __forceinline__ void generate_photon(const MxSourceDev &S, const doub
     q.e = MX_DADD(S.emin, MX_DMUL(S.de, source_uniform(seed, tag, 0)));   // rounded as written, no contraction
   const D3 p = mk(S.p[0], S.p[1], S.p[2]);
   if (S.kind == MX_SOURCE_POINT) q.p = p;
+  else if (S.kind == MX_SOURCE_IMAGE) {
+    // image_create_photons (s-image.c:290-350): a pixel by the image's
+    // cumulative distribution, a uniform position in it, about the centre
+    const unsigned n = (unsigned) S.img_nx * (unsigned) S.img_ny;
+    const unsigned ofs = bsearch_cdf((float) source_uniform(seed, tag, 1), spec + S.img_off, n);
+    double y = (double) (ofs / (unsigned) S.img_nx);
+    double x = (double) (ofs % (unsigned) S.img_nx);
+    y = MX_DADD(y, MX_DADD(MX_DMUL(-0.5, (double) S.img_ny), MX_DADD(source_uniform(seed, tag, 2), -0.5)));
+    x = MX_DADD(x, MX_DADD(MX_DMUL(-0.5, (double) S.img_nx), MX_DADD(source_uniform(seed, tag, 3), -0.5)));
+    y = MX_DMUL(y, S.b);
+    x = MX_DMUL(x, S.a);
+    double sy, cy, sx, cx;
+    sincos(y, &sy, &cy);
+    sincos(x, &sx, &cx);
+    q.p = rotate_unit(mk(-cy * cx, cy * sx, -sy), mk(S.axis[0], S.axis[1], S.axis[2]), S.cos_al, S.sin_al);
+  }
   else if (S.kind == MX_SOURCE_LINE) {
     double theta = S.a * (-1.0 + 2.0 * source_uniform(seed, tag, 1));
     double st, ct;
@@ -493,6 +527,41 @@ static bool source_dev(const mx_source &q, MxSourceDev &S, std::vector<double> &
       double len = src_len(cc);
       if (len > 0.0) { for (int k = 0; k < 3; k++) S.axis[k] = cc[k] / len; }
       else { S.axis[0] = -a[1]; S.axis[1] = -a[0]; S.axis[2] = 0.0; }
+      S.cos_al = cos(th); S.sin_al = sin(th);
+      break;
+    }
+    case MX_SOURCE_IMAGE: {
+      // read_image (s-image.c:46-148): a float image, its running double sum
+      // stored back as float, then each entry divided by the total
+      if (!q.image || q.image_nx == 0 || q.image_ny == 0) { err = "IMAGE source without an image"; return false; }
+      const size_t n = (size_t) q.image_nx * q.image_ny;
+      if (n > (size_t) 1 << 30) { err = "image too large"; return false; }
+      std::vector<float> cdf(n);
+      double sum = 0;
+      for (size_t i = 0; i < n; i++) {
+        sum += (double) q.image[i];
+        cdf[i] = (float) sum;
+      }
+      if (!(sum > 0.0)) { err = "IMAGE source with no positive flux"; return false; }
+      S.img_off = (int32_t) spec.size();
+      S.img_nx = (int32_t) q.image_nx;
+      S.img_ny = (int32_t) q.image_ny;
+      for (size_t i = 0; i < n; i++) spec.push_back((double) (float) (cdf[i] / sum));
+      // open_image_fits_file (s-image.c:190-232): 0.5 arcsec when no scale is given
+      double s1 = fabs(q.param[0]), s2 = fabs(q.param[1]);
+      if (s1 == 0.0 || s2 == 0.0) s1 = s2 = 0.5 / 3600.0;
+      S.a = s1 * PI_ / 180.0;
+      S.b = s2 * PI_ / 180.0;
+      // the rotation of (-1, 0, 0) into p (s-image.c:297-318)
+      double th = -1.0 * q.p[0] + 0.0 * q.p[1] + 0.0 * q.p[2];
+      if (fabs(th) > 1.0) th = th < 0 ? -1.0 : 1.0;
+      th = acos(th);
+      double nrm[3] = {0.0 * q.p[2] - 0.0 * q.p[1], 0.0 * q.p[0] - -1.0 * q.p[2], -1.0 * q.p[1] - 0.0 * q.p[0]};
+      if (th != 0.0) {
+        double l = src_len(nrm);
+        if (l != 0.0) for (int k = 0; k < 3; k++) nrm[k] = nrm[k] / l;
+      }
+      for (int k = 0; k < 3; k++) S.axis[k] = nrm[k];
       S.cos_al = cos(th); S.sin_al = sin(th);
       break;
     }

@@ -215,6 +215,7 @@ __global__ void __launch_bounds__(EV_BLOCK) mx_event_kernel(EvArgs a, EvGeom G, 
   const mx_events &e = a.e;
   const mx_event_params &p = a.p;
   const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  double last_roll = nan, roll_s = 0.0, roll_c = 1.0;   // NaN never equals a roll: the first event computes
   for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const uint32_t k = t * EV_BLOCK + threadIdx.x;
     uint32_t first = k;   // the event whose dither state this event uses
@@ -342,22 +343,27 @@ __global__ void __launch_bounds__(EV_BLOCK) mx_event_kernel(EvArgs a, EvGeom G, 
         n = mk(n.x / sin_t, n.y / sin_t, n.z / sin_t);
         mnc = jdm_rotate_unit(mnc, n, cos_t, sin_t);
       }
-      double sr, cr;
-      sincos(d_roll, &sr, &cr);
-      mnc = jdm_rotate_unit(mnc, mk(1.0, 0.0, 0.0), cr, sr);
+      if (d_roll != last_roll) {   // one roll for a whole run under INTERNAL dither
+        sincos(d_roll, &roll_s, &roll_c);
+        last_roll = d_roll;
+      }
+      mnc = jdm_rotate_unit(mnc, mk(1.0, 0.0, 0.0), roll_c, roll_s);
       // marx_mnc_to_ra_dec (pixlib.c:499-523)
       double perp = sqrt(mnc.x * mnc.x + mnc.y * mnc.y);
       if (perp > 1.0) perp = 1.0;
       const double dec = mnc.z <= 0 ? acos(perp) : -acos(perp);
       const double q = -mnc.x / perp;
       const double ra = mnc.y <= 0.0 ? acos(q) : -acos(q);
-      // marx_compute_ra_dec_offsets (pixlib.c:531-570) about (0, 0)
-      const double c = cos(dec);
-      const double factor = c * (1 - cos(ra));
-      double sin_dd = sin(dec) + factor * 0.0;
+      // marx_compute_ra_dec_offsets (pixlib.c:531-570) about (0, 0): cos(dec)
+      // and cos(d_dec) are the same value there
+      double sdec_s, c, sra_s, cra_s;
+      sincos(dec, &sdec_s, &c);
+      sincos(ra, &sra_s, &cra_s);
+      const double factor = c * (1 - cra_s);
+      double sin_dd = sdec_s + factor * 0.0;
       if (fabs(sin_dd) > 1.0) sin_dd = sin_dd < 0 ? -1.0 : 1.0;
       const double ddec = asin(sin_dd);
-      const double num = c * sin(ra), den = cos(dec) - factor * 1.0;
+      const double num = c * sra_s, den = c - factor * 1.0;
       double dra;
       if (den >= 0) dra = atan(num / den);
       else dra = num >= 0 ? atan(num / den) + PI : atan(num / den) - PI;
@@ -548,7 +554,7 @@ int mx_event_coords(mx_context *c, const mx_event_params *params, const mx_event
   if (!c) return MX_EINVAL;
   int rc = check_params(c, params, ev);
   if (rc != MX_OK || ev->n == 0) return rc;
-  return launch_events(c, params, ev, seed, stream ? (cudaStream_t) stream : c->stream);
+  return launch_events(c, params, ev, seed, (cudaStream_t) stream);
 }
 
 int mx_event_coords_host(mx_context *c, const mx_event_params *params, const mx_events *h, uint64_t seed) {

@@ -220,13 +220,18 @@ class Reference:
         if r != 0:
             raise RuntimeError("reference writer failed: " + self.lib.mxref_last_error().decode())
 
-    def source_photons(self, n: int, U=None):
+    def source_photons(self, n: int, U=None, direction=None):
         """(source direction st->p, energies, directions (3, n)) of n photons
         of the source the parameters describe, one create_photons call per
-        photon; U (4, n) slot-major uniforms for the slot build."""
+        photon; U (4, n) slot-major uniforms for the slot build; direction
+        replaces st->p after the source's set-up."""
         p0 = np.zeros(3)
         if self.lib.mxref_source_setup(_p(p0)) != 0:
             raise RuntimeError("reference source: " + self.lib.mxref_last_error().decode())
+        if direction is not None:
+            p0 = np.ascontiguousarray(direction, dtype=np.float64)
+            if self.lib.mxref_source_set_direction(_p(p0)) != 0:
+                raise RuntimeError("reference source: " + self.lib.mxref_last_error().decode())
         e = np.zeros(n)
         p = np.zeros((n, 3))
         Up = np.ascontiguousarray(U.T) if U is not None else np.zeros((n, 4))

@@ -508,6 +508,16 @@ int mxref_source_setup(double *p_out)
    return 0;
 }
 
+/* Replace the source's direction st->p (select_source, source.c:158-201,
+ * leaves an IMAGE source's p pointing from the origin to the sky; its
+ * image_create_photons expects the direction of travel). */
+int mxref_source_set_direction(const double *p)
+{
+   if (Src == NULL) { set_err("no source"); return -1; }
+   Src->p.x = p[0]; Src->p.y = p[1]; Src->p.z = p[2];
+   return 0;
+}
+
 /* One photon per create_photons call.  With the slot build, photon i's
  * uniforms come from U[i*4 .. i*4+4) in the order the model draws them
  * (spectrum first); with the native build, from the reference's own

@@ -153,7 +153,34 @@ SOURCE_CASES = (
     ("disk", "DISK", {"S-DiskTheta0": "15.0", "S-DiskTheta1": "75.0"}, (15.0, 75.0)),
     ("line", "LINE", {"S-LinePhi": "30.0", "S-LineTheta": "300.0"}, (30.0, 300.0)),
     ("gauss_file", "GAUSS", {"S-GaussSigma": "5.0"}, (5.0,)),
+    ("image", "IMAGE", {}, (0.6 / 3600.0, 0.6 / 3600.0)),   # S-ImageFile: source_image() as FITS
 )
+
+
+def source_image():
+    """A 48 x 64 image for the IMAGE case: two Gaussian blobs on a floor,
+    a block of empty pixels (flat runs in the cumulative distribution) and
+    one bright pixel; 0.6 arcsec pixels."""
+    ny, nx = 48, 64
+    yy, xx = np.mgrid[0:ny, 0:nx].astype(np.float64)
+    im = 50 * np.exp(-((xx - 20) ** 2 + (yy - 30) ** 2) / 18.0) + 20 * np.exp(-((xx - 45) ** 2 + (yy - 12) ** 2) / 40.0)
+    im += 0.3
+    im[5:15, 50:60] = 0.0
+    im[40, 8] = 400.0
+    return im.astype(np.float32), (0.6 / 3600.0, 0.6 / 3600.0)
+
+
+def write_image_fits(path, im, scale):
+    """A primary-HDU FITS image (BITPIX -32) with CDELT1/CDELT2."""
+    ny, nx = im.shape
+    cards = [("SIMPLE", "T"), ("BITPIX", "-32"), ("NAXIS", "2"), ("NAXIS1", str(nx)), ("NAXIS2", str(ny)),
+             ("CDELT1", repr(-scale[0])), ("CDELT2", repr(scale[1]))]
+    h = "".join(f"{k:<8}= {v:>20}" .ljust(80) for k, v in cards) + "END".ljust(80)
+    h = h.ljust((len(h) + 2879) // 2880 * 2880)
+    data = im.astype(">f4").tobytes()
+    data += b"\0" * ((-len(data)) % 2880)
+    with open(path, "wb") as f:
+        f.write(h.encode("ascii") + data)
 
 
 def source_spectrum():
@@ -182,12 +209,19 @@ def sources_fixture():
         with open(spec_file, "w") as fh:
             for a, b in zip(e_spec, f_spec):
                 fh.write(f"{float(a)!r} {float(b)!r}\n")
+        img_file = os.path.join(tmp, "image.fits")
+        im, scale = source_image()
+        write_image_fits(img_file, im, scale)
+        out["image"] = im
+        out["image_scale"] = np.array(scale)
         for name, kind, over, param in SOURCE_CASES:
             par = {"SourceType": kind, "SourceRA": "250.25", "SourceDEC": "-53.73", "MinEnergy": "0.5",
                    "MaxEnergy": "7.0", "SpectrumType": "FILE" if name.endswith("_file") else "FLAT",
-                   "SpectrumFile": spec_file, **over}
+                   "SpectrumFile": spec_file, "S-ImageFile": img_file, **over}
             ref = Reference(w.cfg, extra_par=par)
-            p0, e, p = ref.source_photons(N_SRC, U)
+            # an IMAGE source's st->p is left pointing to the sky (source.c:158-201);
+            # its photons are drawn about the point source's direction of travel instead
+            p0, e, p = ref.source_photons(N_SRC, U, direction=out.get("point_src") if kind == "IMAGE" else None)
             out[f"{name}_src"] = p0
             out[f"{name}_param"] = np.array(param, dtype=np.float64)
             out[f"{name}_energy"] = e

@@ -55,3 +55,18 @@ def test_write_mask_and_empty_list(tmp_path):
     O.write_photons(q, O.history(w.cfg), O.OUT["X"] | O.OUT["ENERGY"], str(tmp_path), dither=False)
     assert sorted(os.listdir(tmp_path)) == ["energy.dat", "xpos.dat", "ypos.dat", "zpos.dat"]
     assert len(O.read_column(str(tmp_path / "xpos.dat"))[1]) == 0
+
+
+def test_image_fits_reader(tmp_path):
+    """The IMAGE source's FITS reader: pixels and scale as the reference's
+    open_image_fits_file reads them (CDELT, else the CD matrix, else none)."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_golden import source_image, write_image_fits
+    from marx_gb300.batched import read_image_fits
+    im, scale = source_image()
+    f = tmp_path / "im.fits"
+    write_image_fits(str(f), im, scale)
+    got, sc = read_image_fits(str(f))
+    assert got.dtype == np.float32 and got.shape == im.shape and np.array_equal(got, im)
+    assert sc == (abs(-scale[0]), scale[1])

@@ -1,6 +1,6 @@
 """Source models on the GPU (mx_generate_source) against the reference's
-own create_photons functions (POINT, GAUSS, BETA, DISK, LINE; FLAT and FILE
-spectra) fed the same uniforms: tests/golden/sources.npz.  Energies exact;
+own create_photons functions (POINT, GAUSS, BETA, DISK, LINE, IMAGE; FLAT and
+FILE spectra) fed the same uniforms: tests/golden/sources.npz.  Energies exact;
 directions within 1e-12 (library sine and cosine of the same arguments)."""
 import os
 
@@ -12,7 +12,8 @@ from marx_gb300 import batched as B
 from helpers import GOLDEN, P_TOL, assert_parity
 
 pytestmark = pytest.mark.gpu
-CASES = {"point": "POINT", "gauss": "GAUSS", "beta": "BETA", "disk": "DISK", "line": "LINE", "gauss_file": "GAUSS"}
+CASES = {"point": "POINT", "gauss": "GAUSS", "beta": "BETA", "disk": "DISK", "line": "LINE", "gauss_file": "GAUSS",
+         "image": "IMAGE"}
 
 
 def fixture():
@@ -22,7 +23,7 @@ def fixture():
 def source_of(z, name, n):
     spec = (z["spectrum_energy"], z["spectrum_flux"]) if name.endswith("_file") else None
     return B.make_source(z[f"{name}_src"], CASES[name], tuple(z[f"{name}_param"]), energy=(0.5, 7.0),
-                         spectrum=spec, num_photons=n)
+                         spectrum=spec, num_photons=n, image=z["image"] if name == "image" else None)
 
 
 def generate(eng, src, n, seed, first_tag=0):
