@@ -2,7 +2,9 @@
 
 ``write_photons`` is the C ABI's ``mx_write_photons`` (the reference's
 marx_write_photons, marx/libsrc/marxio.c:395-478); ``read_column`` and
-``read_dir`` read such files back (any MARX output directory).
+``read_dir`` read such files back (any MARX output directory);
+``write_run_files`` adds the marx.par and obs.par that marx2fits reads
+beside the column files.
 """
 from __future__ import annotations
 
@@ -72,3 +74,77 @@ def read_dir(out_dir: str) -> dict:
         if f.endswith(".dat"):
             out[f[:-4]] = read_column(os.path.join(out_dir, f))[1]
     return out
+
+
+def _par_lines(text: str):
+    return [ln for ln in text.splitlines() if ln.strip()]   # pfile reading stops at a blank line
+
+
+def _value_span(ln: str):
+    """Start and end of the value field (the fourth) of a .par line."""
+    pos = 0
+    for _ in range(3):
+        pos = ln.index(",", pos) + 1
+    if ln[pos:pos + 1] == '"':
+        end = ln.index('"', pos + 1) + 1
+    else:
+        end = ln.find(",", pos)
+        end = len(ln) if end < 0 else end
+    return pos, end
+
+
+def _par_set(lines, name, value, kind="r"):
+    """Set the value of parameter `name` (names compare without case, as
+    pfile's do); append a hidden parameter when the file lacks it."""
+    for i, ln in enumerate(lines):
+        if ln.startswith("#") or ln.count(",") < 3:
+            continue
+        if ln.split(",", 1)[0].strip().lower() == name.lower():
+            quoted = ln.split(",", 2)[1].strip()[:1] in ("s", "f")
+            a, b = _value_span(ln)
+            lines[i] = ln[:a] + (f'"{value}"' if quoted else str(value)) + ln[b:]
+            return
+    v = f'"{value}"' if kind in ("s", "f") else str(value)
+    lines.append(f'{name},{kind},h,{v},,,""')
+
+
+def write_run_files(out_dir: str, cfg: MxConfig, par_template: str, data_dir: str, total_time: float,
+                    source_name: str = "POINT") -> None:
+    """marx.par and obs.par of a run, so that marx2fits, marxcat and the
+    other readers take the output directory as marx's own: the user's
+    parameter file with the configuration's values (marx copies it,
+    marx.c:475-503), and the detector's observation template from the MARX
+    data directory (obs/<detector>_obs.par) with the pointing, instrument,
+    focal length, offsets and times write_obs_par learns into it
+    (marx.c:999-1196; the dither averages, zero for INTERNAL dither, and the
+    calendar dates from TStart are left at the template's)."""
+    from .config import to_par
+    os.makedirs(out_dir, exist_ok=True)
+    lines = _par_lines(open(par_template).read())
+    names = {ln.split(",", 1)[0].strip().lower() for ln in lines if not ln.startswith("#")}
+    for k, v in to_par(cfg).items():
+        if k.lower() in names:
+            _par_set(lines, k, v)
+    with open(os.path.join(out_dir, "marx.par"), "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+    det = {1: "ACIS-I", 2: "ACIS-S", 3: "HRC-I", 4: "HRC-S"}.get(int(cfg.detector), "NONE")
+    grat = {1: "HETG", 2: "LETG"}.get(int(cfg.grating), "NONE")
+    tmpl = {"ACIS-I": "acis_i_obs.par", "ACIS-S": "acis_s_obs.par", "HRC-I": "hrc_i_obs.par",
+            "HRC-S": "hrc_s_obs.par"}.get(det, "generic_obs.par")
+    obs = _par_lines(open(os.path.join(data_dir, "obs", tmpl)).read())
+    norm = lambda a: a % 360.0
+    datamode = "GRADED" if det.startswith("ACIS") else ("SPECTROSCOPIC" if grat != "NONE" else "IMAGING")
+    for k, v, kind in (("ra_nom", norm(cfg.ra_nom), "r"), ("roll_nom", norm(cfg.roll_nom), "r"),
+                       ("dec_nom", cfg.dec_nom, "r"), ("ra_pnt", norm(cfg.ra_nom), "r"),
+                       ("roll_pnt", norm(cfg.roll_nom), "r"), ("dec_pnt", cfg.dec_nom, "r"),
+                       ("foc_len", cfg.focal_length, "r"), ("datamode", datamode, "s"), ("detnam", det, "s"),
+                       ("grating", grat, "s"), ("object", source_name, "s"), ("title", source_name, "s"),
+                       ("tstart", 0.0, "r"), ("tstop", total_time, "r"),
+                       ("sim_x", cfg.det_offset[0], "r"), ("sim_y", cfg.det_offset[1], "r"),
+                       ("sim_z", cfg.det_offset[2], "r"), ("defocus", cfg.det_offset[0], "r"),
+                       ("DY_AVG", 0.0, "r"), ("DZ_AVG", 0.0, "r"), ("DTH_AVG", 0.0, "r"),
+                       ("LIVETIME", total_time, "r"), ("ONTIME", total_time, "r"),
+                       ("EXPOSURE", total_time, "r"), ("TELAPSE", total_time, "r")):
+        _par_set(obs, k, repr(float(v)) if kind == "r" else v, kind)
+    with open(os.path.join(out_dir, "obs.par"), "w") as fh:
+        fh.write("\n".join(obs) + "\n")

@@ -120,3 +120,54 @@ def test_subpix_tables_in_the_pack():
     for d in t.values():
         for e, dx, dy in d.values():
             assert len(e) >= 2 and np.all(np.diff(e) > 0)
+
+
+def test_marx2fits_reads_the_engines_output_directory(tmp_path):
+    """The traced photons of a parity fixture (which the device trace
+    reproduces bit for bit), written by mx_write_photons with the run's
+    marx.par and obs.par (write_run_files): the reference's own marx2fits
+    reads the directory unchanged, and its event columns equal the oracle's
+    on the columns read back."""
+    from oracle import bindings
+    if not bindings.reference_available():
+        pytest.skip("needs the reference's sources to build marx2fits")
+    bindings.build_reference()
+    from helpers import load_trace_fixture
+    from marx_gb300 import output as O
+    from marx_gb300.caldb.pack import read_fits_bintables
+    w, ph, U, N, z = load_trace_fixture("plain_scatter")
+    q = ph.copy()
+    for k in z.files:
+        if hasattr(q, k) and k != "energy":
+            getattr(q, k)[...] = z[k]
+    d = str(tmp_path / "sim")
+    O.write_photons(q, O.history(w.cfg), O.ALL, d, total_time=0.0)
+    ref_root = bindings.REF_ROOT
+    O.write_run_files(d, w.cfg, os.path.join(ref_root, "marx", "par", "marx.par"),
+                      os.path.join(ref_root, "marx", "data"), 1000.0)
+    cols = O.read_dir(d)
+    n = len(cols["time"])
+    assert n > 100
+    u = np.random.default_rng(2).random((3, n))
+    ufile = tmp_path / "u.bin"
+    u[0].astype(np.float64).tofile(ufile)              # one grade draw per ACIS event (EXACT)
+    out = tmp_path / "evt.fits"
+    env = dict(os.environ, MARX_DATA_DIR=os.path.join(ref_root, "marx", "data"), MXREF_UNIFORMS=str(ufile))
+    r = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "marx2fits"), "--pixadj=EXACT", d, str(out)],
+                       env=env, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    ev_fits = next(c for h, c in read_fits_bintables(str(out)) if h.get("EXTNAME") == "EVENTS")
+    zc, det, _, _ = load_case("acis_i")
+    zero = np.zeros(n, np.float32)
+    ev = dict(ccd=cols["detector"], xpixel=cols["xpixel"], ypixel=cols["ypixel"], time=cols["time"],
+              sky_ra=cols["sky_ra"], sky_dec=cols["sky_dec"], sky_roll=cols["sky_roll"], det_dy=zero, det_dz=zero,
+              det_theta=zero, b_energy=zero)
+    params = dict(focal_length=10070.0, det_offset=tuple(w.cfg.det_offset), roll_nom=w.cfg.roll_nom,
+                  frame_time=3.2 + 0.041, dithered=True, pixel_adjust=PIXADJ["EXACT"])
+    o = event_coords("ACIS-I", zc["geom"], zc["tdet"], zc["fp"], params, ev, u)
+    for c in ("DETX", "DETY", "X", "Y"):
+        np.testing.assert_array_equal(o[c.lower()].astype(np.float32), ev_fits[c], err_msg=c)
+    for c in ("CHIPX", "CHIPY"):
+        np.testing.assert_array_equal(o[c.lower()].astype(np.int16), ev_fits[c], err_msg=c)
+    for c in ("TDETX", "TDETY", "EXPNO", "FLTGRADE", "GRADE"):
+        np.testing.assert_array_equal(o[c.lower()].astype(np.int64), ev_fits[c].astype(np.int64), err_msg=c)
