@@ -191,6 +191,10 @@ void mx_destroy(mx_context *c) {
   c->ev_tab.release();
   c->ev_scan.release();
   c->ev_io.release();
+  for (int k = 0; k < MX_PIPE_STREAMS; k++) {
+    c->pipe_wave[k].release();
+    if (c->pipe[k]) cudaStreamDestroy(c->pipe[k]);
+  }
   if (c->d_overrun) cudaFree(c->d_overrun);
   if (c->d_event_bad) cudaFree(c->d_event_bad);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -218,6 +222,13 @@ int mx_set_trace_mode(mx_context *c, int mode) {
 
 int mx_trace_tables(mx_context *c, const MxTables &T, const mx_photons *ph, uint32_t stages, const double *U,
                     const double *N, uint64_t seed, cudaStream_t st, bool fresh) {
+  return mx_trace_queues(c, T, ph, stages, U, N, seed, st, fresh, c->wave);
+}
+
+}  // extern "C"
+
+int mx_trace_queues(mx_context *c, const MxTables &T, const mx_photons *ph, uint32_t stages, const double *U,
+                    const double *N, uint64_t seed, cudaStream_t st, bool fresh, DevBuf &queues) {
   if (!ph) return fail(c, MX_EINVAL, "mx_trace: null photon list");
   if (ph->n == 0) return MX_OK;
   if (!ph->energy || !ph->p) return fail(c, MX_EINVAL, "mx_trace: energy and p are required");
@@ -240,12 +251,12 @@ int mx_trace_tables(mx_context *c, const MxTables &T, const mx_photons *ph, uint
   cudaError_t e;
   if (wave) {
     size_t qbytes = (size_t) ph->n * sizeof(MxRec);
-    e = c->wave.ensure(2 * qbytes + 256);
+    e = queues.ensure(2 * qbytes + 256);
     if (e != cudaSuccess) return cuda_fail(c, e, "allocating wavefront queues");
     WaveBufs w;
-    w.q1 = (MxRec *) c->wave.ptr;
-    w.q2 = (MxRec *) ((char *) c->wave.ptr + qbytes);
-    w.counts = (unsigned int *) ((char *) c->wave.ptr + 2 * qbytes);
+    w.q1 = (MxRec *) queues.ptr;
+    w.q2 = (MxRec *) ((char *) queues.ptr + qbytes);
+    w.counts = (unsigned int *) ((char *) queues.ptr + 2 * qbytes);
     e = launch_wavefront(T, io, w, c->num_sms * c->wave_blocks, (int) c->shared_bytes, st);
     c->launches += MX_WAVE_KERNELS;
   } else {
@@ -256,11 +267,109 @@ int mx_trace_tables(mx_context *c, const MxTables &T, const mx_photons *ph, uint
   return MX_OK;
 }
 
+extern "C" {
+
 int mx_trace(mx_context *c, const mx_photons *ph, uint32_t stages, const mx_variates *var, uint64_t seed,
              void *stream) {
   if (!c) return MX_EINVAL;
   return mx_trace_tables(c, c->T, ph, stages, var ? var->U : nullptr, var ? var->N : nullptr, seed,
                          (cudaStream_t) stream, false);
+}
+
+// The host columns of mx_trace_host: pointer, element size, components,
+// copied in, copied out.
+struct HostCol { const void *host; size_t elem; int comps; bool in, out; };
+static int host_columns(const mx_photons *h, HostCol cols[17]) {
+  const HostCol c[17] = {
+      {h->energy, 8, 1, true, false},     {h->x, 8, 3, false, true},         {h->p, 8, 3, true, true},
+      {h->arrival_time, 8, 1, true, false}, {h->flags, 4, 1, true, true},   {h->tag, 4, 1, true, false},
+      {h->mirror_shell, 1, 1, false, true}, {h->order, 1, 1, false, true},   {h->ccd_num, 1, 1, false, true},
+      {h->y_pixel, 4, 1, false, true},    {h->z_pixel, 4, 1, false, true},   {h->dither_state, 4, 3, false, true},
+      {h->support_orders, 1, 4, false, true}, {h->pulse_height, 2, 1, false, true}, {h->u_pixel, 4, 1, false, true},
+      {h->v_pixel, 4, 1, false, true},    {h->detector_region, 1, 1, false, true}};
+  for (int k = 0; k < 17; k++) cols[k] = c[k];
+  return 17;
+}
+
+// mx_trace_host for a large list: MX_PIPE_CHUNKS chunks of consecutive
+// photons, chunk j on stream j % MX_PIPE_STREAMS with its own wavefront
+// queues, each chunk's copies in, trace and copies out queued in order on
+// its stream; the copy engines then move one chunk while the SMs trace
+// another.  Photons are independent and draw by tag, so the results equal
+// the single-pass trace's.  Multi-component columns keep the list's own
+// component stride on the device; a chunk's pre-drawn variates are packed
+// slot-major for its own length.
+static int trace_host_pipelined(mx_context *c, const mx_photons *h, uint32_t stages, const mx_variates *hv,
+                                uint64_t seed) {
+  const size_t n = h->n;
+  HostCol cols[17];
+  const int NC = host_columns(h, cols);
+  cudaError_t e = cudaSuccess;
+  for (int s = 0; s < MX_PIPE_STREAMS && e == cudaSuccess; s++)
+    if (!c->pipe[s]) e = cudaStreamCreateWithFlags(&c->pipe[s], cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_fail(c, e, "creating the copy-overlap streams");
+  char *dev[17];
+  for (int k = 0; k < NC; k++) {
+    dev[k] = nullptr;
+    if (!cols[k].host) continue;
+    if ((e = c->io[k].ensure(n * cols[k].elem * cols[k].comps)) != cudaSuccess)
+      return cuda_fail(c, e, "allocating staging buffers");
+    dev[k] = (char *) c->io[k].ptr;
+  }
+  const bool slots = hv && hv->U && hv->N;
+  if (slots && ((e = c->io[NC].ensure(n * MX_NUM_U * 8)) != cudaSuccess ||
+                (e = c->io[NC + 1].ensure(n * MX_NUM_N * 8)) != cudaSuccess))
+    return cuda_fail(c, e, "allocating variate buffers");
+  // the queues are per stream; the photons' own columns were written before
+  // by whatever last used them, so wait for the context's stream first
+  cudaEvent_t ready;
+  if ((e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming)) != cudaSuccess) return cuda_fail(c, e, "event");
+  cudaEventRecord(ready, c->stream);
+  for (int s = 0; s < MX_PIPE_STREAMS; s++) cudaStreamWaitEvent(c->pipe[s], ready, 0);
+  cudaEventDestroy(ready);
+  const size_t chunk = ((n + MX_PIPE_CHUNKS - 1) / MX_PIPE_CHUNKS + 255) & ~(size_t) 255;
+  for (size_t i0 = 0, j = 0; i0 < n; i0 += chunk, j++) {
+    const size_t m = std::min(chunk, n - i0);
+    cudaStream_t st = c->pipe[j % MX_PIPE_STREAMS];
+    for (int k = 0; k < NC && e == cudaSuccess; k++) {
+      if (!cols[k].host || !cols[k].in) continue;
+      const size_t el = cols[k].elem;
+      e = cudaMemcpy2DAsync(dev[k] + i0 * el, n * el, (const char *) cols[k].host + i0 * el, n * el, m * el,
+                            cols[k].comps, cudaMemcpyHostToDevice, st);
+    }
+    const double *dU = nullptr, *dN = nullptr;
+    if (slots && e == cudaSuccess) {
+      double *u = (double *) c->io[NC].ptr + i0 * MX_NUM_U, *v = (double *) c->io[NC + 1].ptr + i0 * MX_NUM_N;
+      e = cudaMemcpy2DAsync(u, m * 8, hv->U + i0, n * 8, m * 8, MX_NUM_U, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess)
+        e = cudaMemcpy2DAsync(v, m * 8, hv->N + i0, n * 8, m * 8, MX_NUM_N, cudaMemcpyHostToDevice, st);
+      dU = u; dN = v;
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "copying photons to the device");
+    mx_photons d;
+    memset(&d, 0, sizeof(d));
+    d.n = (uint32_t) m;
+    d.stride = (uint32_t) n;
+    auto at = [&](int k) { return dev[k] ? (void *) (dev[k] + i0 * cols[k].elem) : nullptr; };
+    d.energy = (double *) at(0); d.x = (double *) at(1); d.p = (double *) at(2);
+    d.arrival_time = (double *) at(3); d.flags = (uint32_t *) at(4); d.tag = (uint32_t *) at(5);
+    d.mirror_shell = (int8_t *) at(6); d.order = (int8_t *) at(7); d.ccd_num = (int8_t *) at(8);
+    d.y_pixel = (float *) at(9); d.z_pixel = (float *) at(10); d.dither_state = (float *) at(11);
+    d.support_orders = (int8_t *) at(12); d.pulse_height = (int16_t *) at(13); d.u_pixel = (float *) at(14);
+    d.v_pixel = (float *) at(15); d.detector_region = (uint8_t *) at(16);
+    int r = mx_trace_queues(c, c->T, &d, stages, dU, dN, seed, st, true, c->pipe_wave[j % MX_PIPE_STREAMS]);
+    if (r) return r;
+    for (int k = 0; k < NC && e == cudaSuccess; k++) {
+      if (!cols[k].host || !cols[k].out) continue;
+      const size_t el = cols[k].elem;
+      e = cudaMemcpy2DAsync((char *) cols[k].host + i0 * el, n * el, dev[k] + i0 * el, n * el, m * el,
+                            cols[k].comps, cudaMemcpyDeviceToHost, st);
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "copying photons to the host");
+  }
+  for (int s = 0; s < MX_PIPE_STREAMS && e == cudaSuccess; s++) e = cudaStreamSynchronize(c->pipe[s]);
+  if (e != cudaSuccess) return cuda_fail(c, e, "trace");
+  return MX_OK;
 }
 
 int mx_trace_host(mx_context *c, const mx_photons *h, uint32_t stages, const mx_variates *hv, uint64_t seed) {
@@ -279,6 +388,7 @@ int mx_trace_host(mx_context *c, const mx_photons *h, uint32_t stages, const mx_
       {h->y_pixel, 4, 1, false, true},    {h->z_pixel, 4, 1, false, true},   {h->dither_state, 4, 3, false, true},
       {h->support_orders, 1, 4, false, true}, {h->pulse_height, 2, 1, false, true}, {h->u_pixel, 4, 1, false, true},
       {h->v_pixel, 4, 1, false, true},    {h->detector_region, 1, 1, false, true}};
+  if (n >= MX_PIPE_MIN_PHOTONS && (stages & MX_STAGE_MIRROR)) return trace_host_pipelined(c, h, stages, hv, seed);
   void *dev[NC];
   cudaStream_t st = c->stream;
   cudaError_t e;

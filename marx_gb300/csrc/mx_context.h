@@ -48,7 +48,14 @@ struct mx_context {
   alignas(16) char ev_geom[2048];   // the launch copy of the facet geometry
   DevBuf ev_tab, ev_scan, ev_io;
   unsigned long long *d_event_bad = nullptr;
+  // mx_trace_host on large lists: chunks on MX_PIPE_STREAMS streams so that
+  // copies in, kernels and copies out of different chunks overlap
+  cudaStream_t pipe[3] = {nullptr, nullptr, nullptr};
+  DevBuf pipe_wave[3];
 };
+#define MX_PIPE_STREAMS 3
+#define MX_PIPE_CHUNKS 8
+#define MX_PIPE_MIN_PHOTONS (2u << 20)
 
 // Record an error on the context (or as the creation error when c is null)
 // and return code.
@@ -61,3 +68,7 @@ extern thread_local std::string g_create_err;
 // columns start from their defaults instead of being read.
 extern "C" __attribute__((visibility("hidden"))) int mx_trace_tables(mx_context *c, const MxTables &T, const mx_photons *ph, uint32_t stages,
                                const double *U, const double *N, uint64_t seed, cudaStream_t st, bool fresh);
+// The same with the wavefront queues in `queues` instead of the context's own.
+__attribute__((visibility("hidden"))) int mx_trace_queues(mx_context *c, const MxTables &T, const mx_photons *ph,
+                                                          uint32_t stages, const double *U, const double *N,
+                                                          uint64_t seed, cudaStream_t st, bool fresh, DevBuf &queues);

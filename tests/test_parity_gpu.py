@@ -171,3 +171,22 @@ def test_launch_count_tracks_kernels(cuda):
     eng.set_mode(MODES["wavefront"])
     device_trace(eng, w.photons(1000))
     assert eng.launch_count() == before + 1 + 4   # phases A, T, B and C
+
+
+@pytest.mark.parametrize("slots", [False, True])
+def test_pipelined_host_entry_equals_device_trace(cuda, slots):
+    """mx_trace_host on a list large enough to be cut into chunks on
+    several streams (copies overlapping the trace): every column equals the
+    one-pass device trace of the same photons, with Philox draws and with
+    pre-drawn variates (packed per chunk)."""
+    w = W.ALL["plain_scatter"]()
+    n = (1 << 21) + 12345
+    ph = w.photons(n, seed=9)
+    U, N = predraw_variates(n, 3) if slots else (None, None)
+    eng = engine(w.cfg)
+    a = ph.copy()
+    eng.trace_host(a, U=U, N=N, seed=5)
+    b = device_trace(eng, ph, U, N, seed=5)
+    for k in ("x", "p", "flags", "mirror_shell", "order", "ccd_num", "y_pixel", "z_pixel", "dither_state"):
+        assert np.array_equal(getattr(a, k), getattr(b, k)), k
+    assert int(((a.flags & BAD_PHOTON_MASK) == 0).sum()) > n // 10
