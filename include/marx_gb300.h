@@ -61,26 +61,31 @@ extern "C" {
  *                     per optic P then H: [blur phi] [reflectivity] [wfold p, sign]
  *           N[2..3] : per optic [blur angle]
  *   HETG    U[12..13]: vignetting, order;  N[4..5]: dtheta, dP/P
- *   ACIS    U[14..15]: [QE] [streak row];  N[6..7]: reserved (pulse height)
+ *   ACIS    U[14..15]: [QE] [streak row];  N[6..7]: reserved
+ *           U[28..35], N[20..23]: the FEF pulse height (marx_apply_acis_rmf):
+ *                      gaussian choice, its normal or tail draws, rejection
+ *                      draws, the PI randomisation
  *   LETG    U[16..21]: vignetting, order, support orders (fine, coarse x3);
  *           N[8..17] : dtheta, dP/P of the primary, then of each support
  *   HRC     U[22..27]: MCP QE, UV/ion shield QE, blur component, radius,
  *                      azimuth (one spare);  N[18..19]: pulse height (one spare)
  *   dither  N[0..1]  : aspect blur ra, dec
  * Slot arrays are slot-major: U[k * n + i] is uniform k of photon i. */
-#define MX_NUM_U 28
-#define MX_NUM_N 20
+#define MX_NUM_U 36
+#define MX_NUM_N 24
 #define MX_U_MIRROR   0
 #define MX_U_GRATING 12
 #define MX_U_DETECT  14
 #define MX_U_LETG    16
 #define MX_U_HRC     22
+#define MX_U_FEF     28
 #define MX_N_DITHER   0
 #define MX_N_MIRROR   2
 #define MX_N_GRATING  4
 #define MX_N_DETECT   6
 #define MX_N_LETG     8
 #define MX_N_HRC     18
+#define MX_N_FEF     20
 
 enum { MX_GRATING_NONE = 0, MX_GRATING_HETG = 1, MX_GRATING_LETG = 2 };
 enum { MX_DETECTOR_NONE = 0, MX_DETECTOR_ACIS_I = 1, MX_DETECTOR_ACIS_S = 2, MX_DETECTOR_HRC_I = 3,
@@ -181,10 +186,11 @@ typedef struct mx_photons {
   float    *z_pixel;       /* chip y (0-based) */
   float    *dither_state;  /* 3n: ra, dec, roll (rad), as Marx_Dither_Type */
   int8_t   *support_orders;/* 4n: LETG fine and three coarse support orders */
-  int16_t  *pulse_height;  /* HRC pulse height */
+  int16_t  *pulse_height;  /* HRC pulse height; ACIS PHA from the FEF (-1: no response) */
   float    *u_pixel;       /* HRC-S u, v pixel */
   float    *v_pixel;
   uint8_t  *detector_region; /* HRC-S UV/ion shield region */
+  float    *pi;            /* ACIS PI energy (keV) from the FEF (Marx_Photon_Attr_Type.pi, b_energy.dat) */
 } mx_photons;
 
 /* Pre-drawn variates (device pointers for mx_trace).  When both are NULL

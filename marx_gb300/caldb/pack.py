@@ -255,6 +255,34 @@ def read_fits_bintables(path: str):
     return hdus
 
 
+def read_fef(path: str) -> dict:
+    """The acis/fef sections from an ACIS FEF file (its FUNCTION table, as
+    read_fef_file reads it, acis_fef.c:819-874): rows = CCD_ID, CHIPX_LO,
+    CHIPX_HI, CHIPY_LO, CHIPY_HI, REGNUM; vals = ENERGY, CHANNEL, then
+    G<k>_FWHM, G<k>_POS, G<k>_AMPL for each gaussian the file has, in row
+    order."""
+    for h, c in read_fits_bintables(path):
+        if h.get("EXTNAME", "").upper() != "FUNCTION":
+            continue
+        cols = {k.upper(): v for k, v in c.items()}
+        ng = 0
+        while all(f"G{ng + 1}_{x}" in cols for x in ("FWHM", "POS", "AMPL")):
+            ng += 1
+        rows = np.stack([np.asarray(cols[k]) for k in ("CCD_ID", "CHIPX_LO", "CHIPX_HI", "CHIPY_LO", "CHIPY_HI",
+                                                       "REGNUM")], axis=1).astype(np.int32)
+        vals = [cols["ENERGY"], cols["CHANNEL"]] + [cols[f"G{k + 1}_{x}"] for k in range(ng)
+                                                    for x in ("FWHM", "POS", "AMPL")]
+        return {"acis/fef/rows": rows, "acis/fef/vals": np.stack([np.asarray(v) for v in vals], axis=1).astype(np.float32)}
+    raise ValueError(f"{path}: no FUNCTION table")
+
+
+def pack_with_fef(pack_in: str, fef_path: str, pack_out: str) -> None:
+    """A copy of a table pack with the ACIS FEF of fef_path added."""
+    S = read_pack(pack_in)
+    S.update(read_fef(fef_path))
+    write_pack(pack_out, S)
+
+
 # ---------------------------------------------------------------- builder --
 def build_sections(data_dir: str) -> dict:
     """Collect every table from a MARX data directory (marx/data)."""
@@ -343,6 +371,9 @@ def build_sections(data_dir: str) -> dict:
         S[f"acis/subpix_{kind}/rows"] = np.stack([cols["FLTGRADE"], cols["NPOINTS"]], axis=1).astype(np.int32)
         S[f"acis/subpix_{kind}/table"] = np.stack([cols["ENERGY"], cols["CHIPX_OFFSET"],
                                                    cols["CHIPY_OFFSET"]]).astype(np.float32)
+    fef = os.path.join(data_dir, "caldb", "acisfef.fits")     # the ACISFEF entry of marxcaldb.par
+    if os.path.exists(fef):
+        S.update(read_fef(fef))
     qe = read_fits_bintables(os.path.join(data_dir, "caldb", "acisD1997-04-17qeN0006.fits"))
     for h, c in qe:
         if h.get("EXTNAME") == "AXAF_QE":

@@ -384,6 +384,7 @@ static int build_graph(mx_batch *b) {
   io.io.ypix = d.y_pixel; io.io.zpix = d.z_pixel; io.io.dith = d.dither_state;
   io.io.support = d.support_orders; io.io.pha = d.pulse_height; io.io.upix = d.u_pixel; io.io.vpix = d.v_pixel;
   io.io.region = d.detector_region;
+  io.io.pi = d.pi;
   io.io.U = nullptr; io.io.N = nullptr; io.io.n = d.n; io.io.stride = d.n; io.io.stages = MX_STAGE_ALL; io.io.fresh = 1;
   io.io.overrun = c->d_overrun;
   io.src = (const MxSourceDev *) b->d_src.ptr;
@@ -418,6 +419,8 @@ static int build_graph(mx_batch *b) {
     lc.numAttrs = 1;
     e = cudaLaunchKernelEx(&lc, mx_batch_kernel, T, io);
   }
+  // with an FEF: the pulse heights and streaks of the photons on a chip
+  if (e == cudaSuccess && T.acis_fef) e = launch_acis_fef(T, io.io, c->num_sms * 8, st, io.seed);
   cudaGraph_t g = nullptr;
   cudaError_t e2 = cudaStreamEndCapture(st, &g);
   cudaStreamDestroy(st);
@@ -712,7 +715,7 @@ int mx_batch_run(mx_batch *b, uint64_t seed, void *stream) {
   *b->h_seed = seed;
   e = cudaGraphLaunch(b->exec, (cudaStream_t) stream);
   if (e == cudaSuccess) e = cudaEventRecord(b->done, (cudaStream_t) stream);
-  b->ctx->launches++;
+  b->ctx->launches += b->ctx->T.acis_fef ? 2 : 1;
   return e == cudaSuccess ? MX_OK : mx_cuda_fail(b->ctx, e, "launching the batch graph");
 }
 

@@ -45,6 +45,7 @@ static int upload_model(mx_context *c) {
   if (M.support_energy.empty()) { M.support_energy.push_back(0.f); M.support_cum.push_back(0.f); M.support_k.push_back(0.0); }
   size_t o_pe = put(blob, M.support_energy), o_pc = put(blob, M.support_cum), o_pk = put(blob, M.support_k);
   size_t o_ht = put(blob, M.hrc_tab), o_hs = put(blob, M.hrc_slope);
+  size_t o_fm = put(blob, M.fef_map), o_fr = put(blob, M.fef), o_ff = put(blob, M.fef_f), o_fs = put(blob, M.fef_slope);
   cudaError_t e = c->tables.ensure(blob.size());
   if (e != cudaSuccess) return cuda_fail(c, e, "allocating device tables");
   e = cudaMemcpy(c->tables.ptr, blob.data(), blob.size(), cudaMemcpyHostToDevice);
@@ -69,6 +70,10 @@ static int upload_model(mx_context *c) {
   c->T.support_k = (const double *) (b + o_pk);
   c->T.hrc_tab = (const float *) (b + o_ht);
   c->T.hrc_slope = (const double *) (b + o_hs);
+  c->T.fef_map = (const int32_t *) (b + o_fm);
+  c->T.fef = (const MxFefDev *) (b + o_fr);
+  c->T.fef_f = (const float *) (b + o_ff);
+  c->T.fef_slope = (const double *) (b + o_fs);
   c->shared_bytes = trace_shared_bytes(c->T);
   if (c->shared_bytes > 200 * 1024) return fail(c, MX_ERANGE, "tables exceed the shared-memory budget");
   return MX_OK;
@@ -241,6 +246,7 @@ int mx_trace_queues(mx_context *c, const MxTables &T, const mx_photons *ph, uint
   io.ypix = ph->y_pixel; io.zpix = ph->z_pixel; io.dith = ph->dither_state;
   io.support = ph->support_orders; io.pha = ph->pulse_height; io.upix = ph->u_pixel; io.vpix = ph->v_pixel;
   io.region = ph->detector_region;
+  io.pi = ph->pi;
   io.U = U; io.N = N; io.n = ph->n; io.seed = seed; io.stages = stages; io.fresh = fresh ? 1 : 0;
   io.stride = ph->stride ? ph->stride : ph->n;
   if (io.stride < io.n) return fail(c, MX_EINVAL, "mx_trace: stride below n");
@@ -263,6 +269,10 @@ int mx_trace_queues(mx_context *c, const MxTables &T, const mx_photons *ph, uint
     e = launch_trace(T, io, c->num_sms * c->trace_blocks[slots ? 0 : 1], (int) c->shared_bytes, slots != 0, st);
     c->launches++;
   }
+  if (e == cudaSuccess && (stages & MX_STAGE_DETECT) && T.acis_fef) {
+    e = launch_acis_fef(T, io, c->num_sms * 8, st);
+    c->launches++;
+  }
   if (e != cudaSuccess) return cuda_fail(c, e, "launching the trace kernels");
   return MX_OK;
 }
@@ -279,16 +289,16 @@ int mx_trace(mx_context *c, const mx_photons *ph, uint32_t stages, const mx_vari
 // The host columns of mx_trace_host: pointer, element size, components,
 // copied in, copied out.
 struct HostCol { const void *host; size_t elem; int comps; bool in, out; };
-static int host_columns(const mx_photons *h, HostCol cols[17]) {
-  const HostCol c[17] = {
+static int host_columns(const mx_photons *h, HostCol cols[18]) {
+  const HostCol c[18] = {
       {h->energy, 8, 1, true, false},     {h->x, 8, 3, false, true},         {h->p, 8, 3, true, true},
       {h->arrival_time, 8, 1, true, false}, {h->flags, 4, 1, true, true},   {h->tag, 4, 1, true, false},
       {h->mirror_shell, 1, 1, false, true}, {h->order, 1, 1, false, true},   {h->ccd_num, 1, 1, false, true},
       {h->y_pixel, 4, 1, false, true},    {h->z_pixel, 4, 1, false, true},   {h->dither_state, 4, 3, false, true},
       {h->support_orders, 1, 4, false, true}, {h->pulse_height, 2, 1, false, true}, {h->u_pixel, 4, 1, false, true},
-      {h->v_pixel, 4, 1, false, true},    {h->detector_region, 1, 1, false, true}};
-  for (int k = 0; k < 17; k++) cols[k] = c[k];
-  return 17;
+      {h->v_pixel, 4, 1, false, true},    {h->detector_region, 1, 1, false, true}, {h->pi, 4, 1, false, true}};
+  for (int k = 0; k < 18; k++) cols[k] = c[k];
+  return 18;
 }
 
 // mx_trace_host for a large list: MX_PIPE_CHUNKS chunks of consecutive
@@ -302,13 +312,13 @@ static int host_columns(const mx_photons *h, HostCol cols[17]) {
 static int trace_host_pipelined(mx_context *c, const mx_photons *h, uint32_t stages, const mx_variates *hv,
                                 uint64_t seed) {
   const size_t n = h->n;
-  HostCol cols[17];
+  HostCol cols[18];
   const int NC = host_columns(h, cols);
   cudaError_t e = cudaSuccess;
   for (int s = 0; s < MX_PIPE_STREAMS && e == cudaSuccess; s++)
     if (!c->pipe[s]) e = cudaStreamCreateWithFlags(&c->pipe[s], cudaStreamNonBlocking);
   if (e != cudaSuccess) return cuda_fail(c, e, "creating the copy-overlap streams");
-  char *dev[17];
+  char *dev[18];
   for (int k = 0; k < NC; k++) {
     dev[k] = nullptr;
     if (!cols[k].host) continue;
@@ -356,7 +366,7 @@ static int trace_host_pipelined(mx_context *c, const mx_photons *h, uint32_t sta
     d.mirror_shell = (int8_t *) at(6); d.order = (int8_t *) at(7); d.ccd_num = (int8_t *) at(8);
     d.y_pixel = (float *) at(9); d.z_pixel = (float *) at(10); d.dither_state = (float *) at(11);
     d.support_orders = (int8_t *) at(12); d.pulse_height = (int16_t *) at(13); d.u_pixel = (float *) at(14);
-    d.v_pixel = (float *) at(15); d.detector_region = (uint8_t *) at(16);
+    d.v_pixel = (float *) at(15); d.detector_region = (uint8_t *) at(16); d.pi = (float *) at(17);
     int r = mx_trace_queues(c, c->T, &d, stages, dU, dN, seed, st, true, c->pipe_wave[j % MX_PIPE_STREAMS]);
     if (r) return r;
     for (int k = 0; k < NC && e == cudaSuccess; k++) {
@@ -380,14 +390,14 @@ int mx_trace_host(mx_context *c, const mx_photons *h, uint32_t stages, const mx_
   if (!h->energy || !h->p) return fail(c, MX_EINVAL, "mx_trace_host: energy and p are required");
   if (h->stride && h->stride != h->n) return fail(c, MX_EINVAL, "mx_trace_host: host lists must be contiguous (stride 0 or n)");
   struct Col { const void *host; size_t elem; int comps; bool in, out; };
-  const int NC = 17;
+  const int NC = 18;
   const Col cols[NC] = {
       {h->energy, 8, 1, true, false},     {h->x, 8, 3, false, true},         {h->p, 8, 3, true, true},
       {h->arrival_time, 8, 1, true, false}, {h->flags, 4, 1, true, true},   {h->tag, 4, 1, true, false},
       {h->mirror_shell, 1, 1, false, true}, {h->order, 1, 1, false, true},   {h->ccd_num, 1, 1, false, true},
       {h->y_pixel, 4, 1, false, true},    {h->z_pixel, 4, 1, false, true},   {h->dither_state, 4, 3, false, true},
       {h->support_orders, 1, 4, false, true}, {h->pulse_height, 2, 1, false, true}, {h->u_pixel, 4, 1, false, true},
-      {h->v_pixel, 4, 1, false, true},    {h->detector_region, 1, 1, false, true}};
+      {h->v_pixel, 4, 1, false, true},    {h->detector_region, 1, 1, false, true}, {h->pi, 4, 1, false, true}};
   if (n >= MX_PIPE_MIN_PHOTONS && (stages & MX_STAGE_MIRROR)) return trace_host_pipelined(c, h, stages, hv, seed);
   void *dev[NC];
   cudaStream_t st = c->stream;
@@ -417,7 +427,7 @@ int mx_trace_host(mx_context *c, const mx_photons *h, uint32_t stages, const mx_
   d.mirror_shell = (int8_t *) dev[6]; d.order = (int8_t *) dev[7]; d.ccd_num = (int8_t *) dev[8];
   d.y_pixel = (float *) dev[9]; d.z_pixel = (float *) dev[10]; d.dither_state = (float *) dev[11];
   d.support_orders = (int8_t *) dev[12]; d.pulse_height = (int16_t *) dev[13]; d.u_pixel = (float *) dev[14];
-  d.v_pixel = (float *) dev[15]; d.detector_region = (uint8_t *) dev[16];
+  d.v_pixel = (float *) dev[15]; d.detector_region = (uint8_t *) dev[16]; d.pi = (float *) dev[17];
   int r = mx_trace_tables(c, c->T, &d, stages, dU, dN, seed, st, true);
   if (r) return r;
   for (int k = 0; k < NC; k++) {

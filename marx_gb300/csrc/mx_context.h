@@ -35,7 +35,7 @@ struct mx_context {
   size_t shared_bytes = 0;
   int trace_blocks[2] = {0, 0};   // resident blocks per SM for the slot / Philox kernels
   cudaStream_t stream = nullptr;
-  DevBuf io[19];           // staging for mx_trace_host: 17 columns, U, N
+  DevBuf io[20];           // staging for mx_trace_host: 18 columns, U, N
   DevBuf scan;             // compaction block counts
   DevBuf wave;             // wavefront record queues
   DevBuf spec;             // FILE spectrum of the last mx_generate_source call

@@ -372,11 +372,13 @@ struct Ph {
   uint8_t region;              // HRC-S shield region (set bit 2)
   uint8_t set;
   float upix, vpix;            // HRC-S u, v pixel    (set bit 4)
+  float pi;                    // ACIS PI energy      (set bit 16)
 };
 #define MX_SET_SUPPORT 1u
-#define MX_SET_HRC 2u     // pulse height
+#define MX_SET_HRC 2u     // pulse height (HRC, or ACIS with an FEF)
 #define MX_SET_UV 4u
 #define MX_SET_REGION 8u
+#define MX_SET_PI 16u
 
 // ------------------------------------------------------------- mirror --
 // JDMquadratic_root (qroot.c:36-70), same cancellation-free form.
@@ -995,6 +997,150 @@ MXD int chip_screen(const MxChipDev &g, float x0, float x1, float x2, float p0, 
 // _marx_acis_apply_streak (acis-i.c:60-93).  QE and pulse height are not
 // modelled (DetIdeal); the detector frame is the identity rotation plus the
 // DetOffset translation (INTERNAL dither has no detector motion).
+// _marx_acis_apply_streak (acis-i.c:60-100): a photon arriving during the
+// frame transfer lands on a random row of its column.  x, p in the
+// detector frame.
+MXD void acis_streak(const MxTables &T, const MxChipDev &d, Ph &ph, D3 &x, D3 &p, Rng &rng) {
+  if (!(T.frame_transfer > 0.0)) return;
+  double t = fmod_pos(T.start_time + ph.t, T.frame_time, T.inv_frame_time);
+  if (t > T.exposure) {
+    ph.zpix = (float) (1.0 + 1022.0 * rng.uniform());
+    double xp = ((double) ph.ypix - d.xoff) * d.xpix, yp = ((double) ph.zpix - d.yoff) * d.ypix;
+    x = mk(d.x_ll[0] + (xp * d.xhat[0] + yp * d.yhat[0]), d.x_ll[1] + (xp * d.xhat[1] + yp * d.yhat[1]),
+           d.x_ll[2] + (xp * d.xhat[2] + yp * d.yhat[2]));
+    p = normalized(x - mk(T.focal_length, 0, 0));
+    ph.flags |= MX_PHOTON_ACIS_STREAKED;
+  }
+}
+
+// ------------------------------------------------------------ ACIS FEF --
+constexpr int MX_FEF_MAX_GAUSS = MX_FEF_GAUSSIANS;
+
+// gaussian_integral (acis_fef.c:380-392) over [0, inf) and (-inf, 0]: the
+// erf of the upper (lower) infinite bound is 1 (-1).
+MXD void fef_areas(float amp, float center, float sigma, double &above, double &below) {
+  const double s = (double) sigma * 1.4142135623730951;
+  if (s == 0.0) { above = below = 0.0; return; }
+  const double e0 = erf((0 - (double) center) / s), w = 2.5066282746310002 * (double) sigma;
+  above = 0.5 * amp * (1.0 - e0) * w;
+  below = 0.5 * amp * (e0 - -1.0) * w;
+}
+
+// marx_apply_acis_rmf (acis_fef.c:910-1079) for a photon at chip pixel
+// (x, y): the region's gaussians interpolated in energy and normalised
+// (normalize_gaussians, :509-579), a pulse height drawn from them
+// (compute_pha_with_pos_amps, :407-469; compute_pha_with_neg_amps,
+// :471-507), and its PI energy.  False where the reference returns -1.
+// Draws come from the FEF window; the reference's unbounded loops stop at
+// its end (the photon is then flagged as a variate overrun).
+MXD bool acis_fef(const MxTables &T, int ccd, float x, float y, double energy, Rng &rng, int16_t &pha_out,
+                  float &pi_out) {
+  // find_fef
+  if (x < 0) { if (!T.det_extend) return false; x = 0; }
+  else if (x >= 1024.0f) { if (!T.det_extend) return false; x = 1023.0f; }
+  if (y < 0) { if (!T.det_extend) return false; y = 0; }
+  else if (y >= 1024.0f) { if (!T.det_extend) return false; y = 1023.0f; }
+  const unsigned ci = (unsigned) (x / 32.0f), cj = (unsigned) (y / 32.0f);
+  if (ci >= 32 || cj >= 32 || ccd < 0 || ccd >= 10) return false;
+  const int idx = T.fef_map[((unsigned) ccd * 32 + ci) * 32 + cj];
+  if (idx < 0) return false;
+  const MxFefDev f = T.fef[idx];
+  const float *E = T.fef_f + f.e_off, *CH = E + f.n_e, *G = T.fef_f + f.g_off;
+  const unsigned n = (unsigned) f.n_e;
+  const int ng = f.n_g;
+  unsigned k = bsearch_f((float) energy, E, n);
+  if (k == 0) k++;
+  if (k == n) k--;
+  const double t = (energy - (double) E[k - 1]) / (double) (E[k] - E[k - 1]);
+  const float *g0 = G + 3 * (size_t) (k - 1) * ng, *g1 = g0 + 3 * ng;
+  float amp[MX_FEF_MAX_GAUSS], cen[MX_FEF_MAX_GAUSS], sig[MX_FEF_MAX_GAUSS], cum[MX_FEF_MAX_GAUSS];
+  bool tail[MX_FEF_MAX_GAUSS];
+  double pos = 0.0, neg = 0.0;
+#pragma unroll
+  for (int g = 0; g < MX_FEF_MAX_GAUSS; g++) {
+    amp[g] = cen[g] = sig[g] = cum[g] = 0.0f;
+    tail[g] = false;
+    if (g >= ng) continue;
+    const float a0 = g0[3 * g], c0 = g0[3 * g + 1], s0 = g0[3 * g + 2];
+    const float a1 = g1[3 * g], c1 = g1[3 * g + 1], s1 = g1[3 * g + 2];
+    cen[g] = (float) ((double) c0 + t * (double) (c1 - c0));
+    double v = (double) s0 + t * (double) (s1 - s0);
+    if (v > 0.0) {
+      sig[g] = (float) v;
+      v = (double) a0 + t * (double) (a1 - a0);
+      if ((v < 0.0) && ((a1 > 0.0f) || (a0 > 0.0f))) v = 0.0;
+      amp[g] = (float) v;
+    }
+    double above, below;
+    fef_areas(amp[g], cen[g], sig[g], above, below);
+    if (below > above) tail[g] = above / below < 0.1;
+    if (above >= 0) pos += above;
+    else neg -= above;
+    cum[g] = (float) pos;
+  }
+  if (pos <= neg) return false;               // HAS_TOTAL_NEG_AREA
+  if (pos > 0) {
+#pragma unroll
+    for (int g = 0; g < MX_FEF_MAX_GAUSS; g++) cum[g] = (float) ((double) cum[g] / pos);
+  }
+  double pha = -1.0;
+  for (int tries = 0; tries < 100; tries++) {   // compute_pha_with_neg_amps (one pass when no amplitude is negative)
+    // compute_pha_with_pos_amps
+    for (;;) {
+      const double r = rng.uniform();
+      if (rng.overrun) return false;
+      pha = -1.0;
+      bool drawn = false;
+#pragma unroll
+      for (int g = 0; g < MX_FEF_MAX_GAUSS; g++) {
+        if (drawn || g >= ng || (double) cum[g] <= r) continue;
+        drawn = true;
+        if (!tail[g]) {
+          int count = 0;
+          do {
+            pha = (double) cen[g] + (double) sig[g] * rng.normal();
+            count++;
+          } while ((pha < 0) && (count < 100) && !rng.overrun);
+        } else {
+          const double s = (double) ((0.0f - cen[g]) / sig[g]);
+          double u, xx;
+          do {
+            u = rng.uniform();
+            double vv;
+            do { vv = rng.uniform(); } while (vv == 0.0 && !rng.overrun);
+            xx = sqrt(s * s - 2 * log(vv));
+          } while ((xx * u > s) && !rng.overrun);
+          pha = (double) cen[g] + xx * (double) sig[g];
+        }
+      }
+      if (rng.overrun) return false;
+      if (drawn && !(pha < 0)) break;           // else: a new choice of gaussian
+    }
+    if (neg == 0.0) break;
+    double psum = 0.0, sum = 0.0;
+#pragma unroll
+    for (int g = 0; g < MX_FEF_MAX_GAUSS; g++) {
+      if (g >= ng || sig[g] == 0.0f) continue;   // evaluate_gaussian
+      const double xx = (pha - (double) cen[g]) / (double) sig[g];
+      const double d = amp[g] * exp(-0.5 * xx * xx);
+      sum += d;
+      if (d > 0) psum += d;
+    }
+    const double u = rng.uniform();
+    if (rng.overrun) return false;
+    if (u * psum < sum) break;
+    if (tries == 99) return false;
+  }
+  const int16_t ipha = (int16_t) pha;
+  const double ph2 = (double) ipha - rng.uniform();
+  if (rng.overrun) return false;
+  const float pi = interp_f((float) ph2, CH, E, T.fef_slope + f.s_off, n);
+  if (pi < 0) return false;
+  pha_out = ipha;
+  pi_out = pi;
+  return true;
+}
+
 MXD void detect_stage(const MxTables &T, const MxChipDev *chips, int nchips, Ph &ph, Rng &rng) {
   rng.window(MX_U_DETECT, 2, MX_N_DETECT, 2);
   D3 off = mk(T.det_offset[0], T.det_offset[1], T.det_offset[2]);
@@ -1030,17 +1176,9 @@ MXD void detect_stage(const MxTables &T, const MxChipDev *chips, int nchips, Ph 
     ph.ccd = d.id;
     ph.ypix = (float) div_by(dx, d.xpix, d.inv_xpix);
     ph.zpix = (float) div_by(dy, d.ypix, d.inv_ypix);
-    if (T.frame_transfer > 0.0) {
-      double t = fmod_pos(T.start_time + ph.t, T.frame_time, T.inv_frame_time);
-      if (t > T.exposure) {
-        ph.zpix = (float) (1.0 + 1022.0 * rng.uniform());
-        double xp = ((double) ph.ypix - d.xoff) * d.xpix, yp = ((double) ph.zpix - d.yoff) * d.ypix;
-        x = mk(d.x_ll[0] + (xp * d.xhat[0] + yp * d.yhat[0]), d.x_ll[1] + (xp * d.xhat[1] + yp * d.yhat[1]),
-               d.x_ll[2] + (xp * d.xhat[2] + yp * d.yhat[2]));
-        p = normalized(x - mk(T.focal_length, 0, 0));
-        ph.flags |= MX_PHOTON_ACIS_STREAKED;
-      }
-    }
+    // with an FEF the pulse height, PI and streak are a pass of their own
+    // over the detected photons (mx_acis_fef_kernel), after the trace
+    if (!T.acis_fef) acis_streak(T, d, ph, x, p, rng);
   }
   ph.x = x + off;
   ph.p = p;

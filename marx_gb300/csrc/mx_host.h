@@ -32,6 +32,10 @@ struct HostModel {
   std::vector<double> support_k;
   std::vector<float> hrc_tab;
   std::vector<double> hrc_slope;
+  std::vector<int32_t> fef_map;
+  std::vector<MxFefDev> fef;
+  std::vector<float> fef_f;
+  std::vector<double> fef_slope;
 };
 
 bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string &err);

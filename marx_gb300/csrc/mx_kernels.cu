@@ -65,6 +65,65 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_trace_kernel(MxTables T, Tr
   }
 }
 
+// The ACIS FEF pass: pulse height and PI of every photon the trace put on
+// a chip (_marx_acis_apply_qe_and_pha with DetIdeal, acis-s.c:136-172),
+// then the frame-transfer streak of those the FEF detected, as
+// _marx_acis_s_detect and _marx_acis_i_detect order them (acis-s.c:230-236).
+// The trace leaves these steps to this pass when the tables carry an FEF.
+__global__ void __launch_bounds__(256) mx_acis_fef_kernel(MxTables T, TraceIO io, const uint64_t *seedp) {
+  const size_t n = io.stride;
+  const uint64_t seed = seedp ? *seedp : io.seed;
+  const D3 off = mk(T.det_offset[0], T.det_offset[1], T.det_offset[2]);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < io.n; i += gridDim.x * blockDim.x) {
+    const int ccd = io.ccd[i];
+    const uint32_t f0 = io.flags ? io.flags[i] : 0u;
+    if (ccd < 0 || ccd > 9 || (f0 & (MX_BAD_PHOTON_MASK | MX_PHOTON_VARIATE_OVERRUN))) continue;
+    Ph q;
+    q.e = io.energy[i];
+    q.t = io.t ? io.t[i] : 0.0;
+    q.flags = f0;
+    q.ypix = io.ypix[i];
+    q.zpix = io.zpix[i];
+    Rng r;
+    r.U = io.U; r.N = io.N; r.seed = seed; r.n = io.n; r.i = i;
+    r.tag = io.tag ? io.tag[i] : i;
+    r.overrun = false;
+    r.window(MX_U_FEF, r.U ? 8 : 64, MX_N_FEF, r.N ? 4 : 64);
+    int16_t pha = -1;
+    float pi = 0.0f;
+    const bool ok = acis_fef(T, ccd, q.ypix, q.zpix, q.e, r, pha, pi);
+    if (r.overrun) {
+      q.flags |= MX_PHOTON_VARIATE_OVERRUN;
+      atomicAdd(io.overrun, 1ull);
+    } else if (!ok) {
+      pha = -1; pi = 0.0f;
+      q.flags |= MX_PHOTON_UNDETECTED;
+    } else {
+      r.window(MX_U_DETECT, 2, MX_N_DETECT, 2);
+      D3 x = mk(0, 0, 0), p = mk(0, 0, 0);
+      acis_streak(T, T.chips[ccd], q, x, p, r);
+      if (q.flags & MX_PHOTON_ACIS_STREAKED) {
+        x = x + off;
+        if (io.x) { io.x[i] = x.x; io.x[n + i] = x.y; io.x[2 * n + i] = x.z; }
+        io.p[i] = p.x; io.p[n + i] = p.y; io.p[2 * n + i] = p.z;
+        io.zpix[i] = q.zpix;
+      }
+    }
+    if (io.pha) io.pha[i] = pha;
+    if (io.pi) io.pi[i] = pi;
+    if (io.flags) io.flags[i] = q.flags;
+  }
+}
+
+cudaError_t launch_acis_fef(const MxTables &T, const TraceIO &io, int grid, cudaStream_t st, const uint64_t *seed_dev) {
+  if (!io.ccd || !io.ypix || !io.zpix || io.n == 0) return cudaSuccess;
+  uint32_t need = (io.n + 255) / 256;
+  if ((uint32_t) grid > need) grid = (int) need;
+  if (grid < 1) grid = 1;
+  mx_acis_fef_kernel<<<grid, 256, 0, st>>>(T, io, seed_dev);
+  return cudaGetLastError();
+}
+
 // ------------------------------------------------------------ wavefront --
 // The same trace as mx_trace_kernel split where photons are lost, so that
 // lost photons stop occupying SIMT lanes: phase A runs every photon up to

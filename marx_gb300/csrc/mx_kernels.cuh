@@ -23,6 +23,7 @@ struct TraceIO {
   int16_t *pha;                 // HRC pulse height
   float *upix, *vpix;           // HRC-S u, v pixels
   uint8_t *region;              // HRC-S shield region
+  float *pi;                    // ACIS PI energy (FEF)
   const double *U, *N;          // pre-drawn variates (slot-major) or null
   uint32_t n, stages;
   uint32_t stride;              // component stride of x, p and dither_state (>= n)
@@ -55,6 +56,11 @@ cudaError_t wave_occupancy(int shared_bytes, int *blocks_per_sm);
 cudaError_t launch_wavefront(const MxTables &T, const TraceIO &io, const WaveBufs &w, int grid, int shared_bytes,
                              cudaStream_t st);
 cudaError_t trace_occupancy(bool philox, int shared_bytes, int *blocks_per_sm);
+// The ACIS FEF pass over the photons the trace put on a chip (a no-op
+// without the chip and pixel columns); seed_dev: the Philox seed in device
+// memory instead of io.seed (a captured graph whose seed changes per run).
+cudaError_t launch_acis_fef(const MxTables &T, const TraceIO &io, int grid, cudaStream_t st,
+                            const uint64_t *seed_dev = nullptr);
 cudaError_t launch_trace(const MxTables &T, const TraceIO &io, int grid, int shared_bytes, bool slots,
                          cudaStream_t st);
 cudaError_t launch_compact(const uint32_t *flags, uint32_t n, uint32_t *idx_out, uint32_t *scan, uint32_t nblk,

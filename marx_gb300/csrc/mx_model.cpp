@@ -414,6 +414,82 @@ static bool hrc_blur(const double *b, double pixelsize, MxHrcDev &h, std::string
 // The HRC-I (hrc_i_geom.c:48-130, hrc-i.c:183-228) or HRC-S (hrc_s_geom.c,
 // hrc-s.c:352-441, drake.c:148-246).  Facets go to chips[10] (HRC-I) and
 // chips[11..13] (HRC-S MCPs 1, 2, 3).
+// The ACIS FEF regions of the detector's chips (read_fef_file,
+// process_rows, process_region_rows and map_fef_to_region,
+// acis_fef.c:194-295, 619-874).  The pack holds the FUNCTION table's rows
+// as acis/fef/rows (CCD_ID, CHIPX_LO, CHIPX_HI, CHIPY_LO, CHIPY_HI,
+// REGNUM) and acis/fef/vals (ENERGY, CHANNEL, then G<k>_FWHM, G<k>_POS,
+// G<k>_AMPL per gaussian).  Consecutive rows of one REGNUM are one region,
+// its energies ascending.
+static bool build_fef(const Pack &pk, int min_ccd, int max_ccd, HostModel &M, std::string &err) {
+  const int REG = 32, NREG = 1024 / REG;
+  const double FWHM_TO_SIGMA = 0.4246609001440095;
+  size_t nr, nv;
+  const int32_t *rows = pk.get<int32_t>("acis/fef/rows", &nr, err);
+  const float *vals = pk.get<float>("acis/fef/vals", &nv, err);
+  if (!rows || !vals) return false;
+  nr /= 6;
+  if (nr == 0 || nv % nr) { err = "acis/fef tables malformed"; return false; }
+  const size_t ncol = nv / nr;
+  if (ncol < 5 || (ncol - 2) % 3) { err = "acis/fef tables malformed"; return false; }
+  const int ng = (int) ((ncol - 2) / 3);
+  if (ng > MX_FEF_GAUSSIANS) { err = "FEF with more gaussians per row than the engine's " + std::to_string(MX_FEF_GAUSSIANS); return false; }
+  M.fef_map.assign((size_t) 10 * NREG * NREG, -1);
+  M.fef.clear(); M.fef_f.clear(); M.fef_slope.clear();
+  auto finish = [&](const std::vector<size_t> &run) -> bool {   // the rows of one region
+    const int32_t *q = rows + 6 * run[0];
+    const int ccd = q[0], xmin = q[1], xmax = q[2], ymin = q[3], ymax = q[4];
+    MxFefDev f;
+    memset(&f, 0, sizeof(f));
+    f.n_e = (int32_t) run.size();
+    f.n_g = ng;
+    f.e_off = (int32_t) M.fef_f.size();
+    for (size_t r : run) M.fef_f.push_back(vals[r * ncol]);
+    for (size_t r : run) M.fef_f.push_back(vals[r * ncol + 1]);
+    f.g_off = (int32_t) M.fef_f.size();
+    for (size_t r : run)
+      for (int k = 0; k < ng; k++) {
+        const float *g = vals + r * ncol + 2 + 3 * k;
+        M.fef_f.push_back(g[2]);                                   // amp
+        M.fef_f.push_back(g[1]);                                   // center
+        M.fef_f.push_back((float) (FWHM_TO_SIGMA * g[0]));         // sigma
+      }
+    // check_fef_validity: energies and channels increasing
+    const float *e = M.fef_f.data() + f.e_off, *ch = e + f.n_e;
+    for (int k = 0; k + 1 < f.n_e; k++)
+      if (!(e[k] < e[k + 1]) || !(ch[k] < ch[k + 1])) {
+        err = "Fef Map does not have monotonically increasing energies and PHAs"; return false;
+      }
+    f.s_off = (int32_t) M.fef_slope.size();
+    append_slopes(M.fef_slope, ch, e, (unsigned) f.n_e);
+    // check_region_values, map_fef_to_region
+    if (ccd < 0 || ccd >= 10) { err = "Invalid CCD_ID value in gain file"; return false; }
+    if (xmin < 1 || ymin < 1 || xmax > 1024 || ymax > 1024) { err = "CHIPX/Y_LO/HI value out of range"; return false; }
+    if ((xmax % REG) || (ymax % REG) || ((xmin - 1) % REG) || ((ymin - 1) % REG)) {
+      err = "Expecting ACIS gain region size to be a multiple of 32"; return false;
+    }
+    const int idx = (int) M.fef.size();
+    M.fef.push_back(f);
+    for (int i = (xmin - 1) / REG; i < xmax / REG; i++)
+      for (int j = (ymin - 1) / REG; j < ymax / REG; j++) M.fef_map[((size_t) ccd * NREG + i) * NREG + j] = idx;
+    return true;
+  };
+  // rows of other chips are skipped; a region is a run of rows with one REGNUM
+  std::vector<size_t> run;
+  int last_reg = -1;
+  for (size_t r = 0; r < nr; r++) {
+    const int ccd = rows[6 * r];
+    if (ccd < min_ccd || ccd > max_ccd) continue;
+    const int reg = rows[6 * r + 5];
+    if (!run.empty() && reg == last_reg) { run.push_back(r); continue; }
+    if (!run.empty() && !finish(run)) return false;
+    run.assign(1, r);
+    last_reg = reg;
+  }
+  if (!run.empty() && !finish(run)) return false;
+  return true;
+}
+
 static bool build_hrc(const Pack &pk, const mx_config &cfg, HostModel &M, std::string &err) {
   MxTables &T = M.T;
   MxHrcDev &h = T.hrc;
@@ -845,6 +921,20 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
     memset(&T.hrc, 0, sizeof(T.hrc));
     if (!acis && cfg.detector != MX_DETECTOR_NONE && !build_hrc(pk, cfg, M, err)) return false;
     if (M.hrc_tab.empty()) { M.hrc_tab.push_back(0.f); M.hrc_slope.push_back(0.0); }
+    // the FEF when the pack carries one (the reference's ACIS detector needs
+    // the file; without it the detection stays geometric)
+    M.fef_map.clear(); M.fef.clear(); M.fef_f.clear(); M.fef_slope.clear();
+    T.acis_fef = 0;
+    if (acis && pk.sections.count("acis/fef/rows")) {
+      if (!build_fef(pk, cfg.detector == MX_DETECTOR_ACIS_I ? 0 : 4, cfg.detector == MX_DETECTOR_ACIS_I ? 3 : 9, M, err))
+        return false;
+      T.acis_fef = M.fef.empty() ? 0 : 1;
+    }
+    T.fef_nregions = (int32_t) M.fef.size();
+    if (M.fef_map.empty()) M.fef_map.push_back(-1);
+    if (M.fef.empty()) { MxFefDev z; memset(&z, 0, sizeof(z)); M.fef.push_back(z); }
+    if (M.fef_f.empty()) M.fef_f.push_back(0.f);
+    if (M.fef_slope.empty()) M.fef_slope.push_back(0.0);
     T.det_extend = cfg.det_extend != 0;
     for (int k = 0; k < 3; k++) T.det_offset[k] = cfg.det_offset[k];
     T.frame_transfer = cfg.acis_frame_transfer_time < 0.0 ? 0.0 : cfg.acis_frame_transfer_time;

@@ -76,6 +76,16 @@ struct MxHrcDev {
   MxTabDev c_beta, c_delta, cr_beta, cr_delta;
 };
 
+// One region of the ACIS FEF (acis_fef.c Fef_Type): n_e energies and
+// channels at fef_f + e_off (energies, then channels), n_g gaussians per
+// energy at fef_f + g_off as (amp, center, sigma) triples [energy][gaussian],
+// the channel-to-energy interpolation slopes at fef_slope + s_off.
+#define MX_FEF_GAUSSIANS 6   // gaussians per FEF row the device pass holds
+struct MxFefDev {
+  int32_t e_off, n_e, g_off, n_g;
+  int32_t s_off, pad[3];
+};
+
 struct MxChipDev {
   double x_ll[3], xhat[3], yhat[3], normal[3];
   double xlen, ylen, xpix, ypix, xoff, yoff;
@@ -132,4 +142,11 @@ struct MxTables {
   const float *hrc_tab;
   const double *hrc_slope;
   MxHrcDev hrc;
+  // ACIS FEF pulse heights (acis_fef.c): 32 x 32 pixel cells of ccds 0..9 ->
+  // region index (-1: none), the regions and their tables
+  const int32_t *fef_map;
+  const MxFefDev *fef;
+  const float *fef_f;
+  const double *fef_slope;
+  int32_t acis_fef, fef_nregions;
 };

@@ -76,7 +76,7 @@ void put_value(std::vector<unsigned char> &b, int c, const mx_photons *h, size_t
   auto f32 = [&](double v) { put_be(b, f2bits((float) v), 4); };
   auto col3 = [&](const double *a, int k) { return a ? a[k * s + i] : 0.0; };
   switch (c) {
-    case 0: f32(0.0); break;                                         // PI: no ACIS pulse-height model here
+    case 0: f32(h->pi ? (double) h->pi[i] : 0.0); break;             // PI (keV) from the ACIS FEF
     case 1: f32(h->energy ? h->energy[i] : 0.0); break;
     case 2: f32((h->arrival_time ? h->arrival_time[i] : 0.0) + total_time); break;
     case 3: put_be(b, h->tag ? h->tag[i] : 0u, 4); break;

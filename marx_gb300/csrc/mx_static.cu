@@ -62,6 +62,7 @@ extern "C" int mx_trace_static(mx_context *c, const mx_photons *ph, uint32_t sta
   io.ypix = ph->y_pixel; io.zpix = ph->z_pixel; io.dith = ph->dither_state;
   io.support = ph->support_orders; io.pha = ph->pulse_height; io.upix = ph->u_pixel; io.vpix = ph->v_pixel;
   io.region = ph->detector_region;
+  io.pi = ph->pi;
   io.U = U; io.N = N; io.n = ph->n; io.seed = seed; io.stages = stages; io.fresh = 0;
   io.stride = ph->stride ? ph->stride : ph->n;
   if (io.stride < io.n) return mx_fail(c, MX_EINVAL, "mx_trace_static: stride below n");
@@ -76,5 +77,9 @@ extern "C" int mx_trace_static(mx_context *c, const mx_photons *ph, uint32_t sta
   w.counts = (unsigned int *) ((char *) scratch + 2 * qbytes);
   cudaError_t e = launch_wavefront(c->T, io, w, c->num_sms * c->wave_blocks, (int) c->shared_bytes, (cudaStream_t) stream);
   c->launches += MX_WAVE_KERNELS;
+  if (e == cudaSuccess && (stages & MX_STAGE_DETECT) && c->T.acis_fef) {
+    e = launch_acis_fef(c->T, io, c->num_sms * 8, (cudaStream_t) stream);
+    c->launches++;
+  }
   return e == cudaSuccess ? MX_OK : mx_cuda_fail(c, e, "mx_trace_static: launching the trace kernels");
 }

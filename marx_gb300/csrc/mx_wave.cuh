@@ -92,6 +92,7 @@ __device__ __forceinline__ void store_extra(const TraceIO &io, uint32_t i, const
     for (int k = 0; k < 4; k++) io.support[k * n + i] = q.sup[k];
   if ((q.set & MX_SET_HRC) && io.pha) io.pha[i] = q.pha;
   if ((q.set & MX_SET_REGION) && io.region) io.region[i] = q.region;
+  if ((q.set & MX_SET_PI) && io.pi) io.pi[i] = q.pi;
   if (q.set & MX_SET_UV) {
     if (io.upix) io.upix[i] = q.upix;
     if (io.vpix) io.vpix[i] = q.vpix;
@@ -104,6 +105,7 @@ __device__ __forceinline__ void clear_extra(const TraceIO &io, uint32_t i) {
   if (io.support) for (int k = 0; k < 4; k++) io.support[k * n + i] = 0;
   if (io.pha) io.pha[i] = 0;
   if (io.region) io.region[i] = 0;
+  if (io.pi) io.pi[i] = 0.f;
   if (io.upix) io.upix[i] = 0.f;
   if (io.vpix) io.vpix[i] = 0.f;
 }

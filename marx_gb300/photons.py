@@ -26,7 +26,7 @@ PHOTON_VARIATE_OVERRUN = 0x10000
 
 STAGE_DITHER, STAGE_MIRROR, STAGE_GRATING, STAGE_DETECT = 1, 2, 4, 8
 STAGE_ALL = 15
-NUM_U, NUM_N = 28, 20
+NUM_U, NUM_N = 36, 24
 
 
 class MxPhotons(C.Structure):
@@ -38,7 +38,7 @@ class MxPhotons(C.Structure):
         ("reserved8", C.c_void_p),
         ("y_pixel", C.c_void_p), ("z_pixel", C.c_void_p), ("dither_state", C.c_void_p),
         ("support_orders", C.c_void_p), ("pulse_height", C.c_void_p), ("u_pixel", C.c_void_p),
-        ("v_pixel", C.c_void_p), ("detector_region", C.c_void_p),
+        ("v_pixel", C.c_void_p), ("detector_region", C.c_void_p), ("pi", C.c_void_p),
     ]
 
 
@@ -53,7 +53,7 @@ COLUMNS = {
     "mirror_shell": (np.int8, 1), "order": (np.int8, 1), "ccd_num": (np.int8, 1),
     "y_pixel": (np.float32, 1), "z_pixel": (np.float32, 1), "dither_state": (np.float32, 3),
     "support_orders": (np.int8, 4), "pulse_height": (np.int16, 1), "u_pixel": (np.float32, 1),
-    "v_pixel": (np.float32, 1), "detector_region": (np.uint8, 1),
+    "v_pixel": (np.float32, 1), "detector_region": (np.uint8, 1), "pi": (np.float32, 1),
 }
 
 

@@ -38,8 +38,8 @@
 #include "_marx.h"
 
 /* Variate slot layout, shared with the engine and the port. */
-#define MX_NU 28
-#define MX_NN 20
+#define MX_NU 36
+#define MX_NN 24
 #define MX_U_MIRROR 0
 #define MX_U_MIRROR_N 12
 #define MX_U_GRATING 12
@@ -62,6 +62,10 @@
 #define MX_U_HRC_N 6
 #define MX_N_HRC 18
 #define MX_N_HRC_N 2
+#define MX_U_FEF 28
+#define MX_U_FEF_N 8
+#define MX_N_FEF 20
+#define MX_N_FEF_N 4
 
 static char Err[1024];
 static void set_err(const char *s) { strncpy(Err, s, sizeof(Err) - 1); }
@@ -103,9 +107,30 @@ uint32 JDMfast_uint32_random(void) { Rng_Unexpected++; return 0; }
 double JDMfast_random(void) { Rng_Unexpected++; return 0.5; }
 #endif
 
+/* The FEF pulse-height draws (marx_apply_acis_rmf, acis_fef.c:967-1079)
+ * come from a window of their own: the library is linked with
+ * --wrap=_marx_apply_acis_rmf, so the ACIS detector's call lands here. */
+int __real__marx_apply_acis_rmf(_Marx_Acis_Chip_Type *c, float x, float y, double energy, float *pip,
+                                short *phap);
+int __wrap__marx_apply_acis_rmf(_Marx_Acis_Chip_Type *c, float x, float y, double energy, float *pip,
+                                short *phap)
+{
+#if MXREF_INTERPOSE
+   const double *su = Cur_U, *sn = Cur_N;
+   int up = U_pos, ue = U_end, np = N_pos, ne = N_end, r;
+   rng_window(su, MX_U_FEF, MX_U_FEF_N, sn, MX_N_FEF, MX_N_FEF_N);
+   r = __real__marx_apply_acis_rmf(c, x, y, energy, pip, phap);
+   Cur_U = su; Cur_N = sn; U_pos = up; U_end = ue; N_pos = np; N_end = ne;
+   return r;
+#else
+   return __real__marx_apply_acis_rmf(c, x, y, energy, pip, phap);
+#endif
+}
+
 /* ------------------------------------------------------------- set-up -- */
 static Param_File_Type *Pf;
 static int Have_Dither, Have_Grating, Det_Kind;   /* 0 none, 1 ACIS-I, 2 ACIS-S */
+static int Acis_Fef;      /* an ACIS FEF file is present: the reference's own ACIS detector runs */
 static int Grating_Is_LETG;
 static Marx_Detector_Type *Det;
 
@@ -155,6 +180,23 @@ int mxref_setup(const char *parfile, const char *datadir, int nover,
         if (-1 == marx_detector_init(Pf)) { set_err("detector init failed"); return -1; }
         if (NULL == (Det = marx_get_detector_info(buf, 0))) { set_err("detector geometry"); return -1; }
         return 0;
+     }
+   Acis_Fef = 0;
+   if (Det_Kind)
+     {
+        char *fef = _marx_caldb_get_file("ACISFEF");
+        if ((fef != NULL) && (1 == marx_file_exists(fef)))
+          {
+             /* With an FEF (DetIdeal = yes reads nothing else) marx_detector_init
+              * runs as it is, and marx_detect applies the FEF pulse heights. */
+             marx_free(fef);
+             if (-1 == marx_detector_init(Pf)) { set_err("detector init failed"); return -1; }
+             if (NULL == (Det = marx_get_detector_info(Det_Kind == 1 ? "ACIS-I" : "ACIS-S", 0)))
+               { set_err("detector geometry"); return -1; }
+             Acis_Fef = 1;
+             return 0;
+          }
+        if (fef != NULL) marx_free(fef);
      }
    if (Det_Kind)
      {
@@ -287,6 +329,10 @@ static signed char *X_Sup;
 static short *X_Pha;
 static float *X_U, *X_V;
 static unsigned char *X_Region;
+static float *X_Pi;
+/* ACIS PI (at->pi) output column, or NULL. */
+void mxref_set_pi_output(float *pi) { X_Pi = pi; }
+
 void mxref_set_extra_outputs(signed char *sup, short *pha, float *u, float *v, unsigned char *region)
 {
    X_Sup = sup; X_Pha = pha; X_U = u; X_V = v; X_Region = region;
@@ -314,6 +360,7 @@ static void store_attr(const Marx_Photon_Attr_Type *at, int i, double *x, double
    if (X_U != NULL) X_U[i] = at->u_pixel;
    if (X_V != NULL) X_V[i] = at->v_pixel;
    if (X_Region != NULL) X_Region[i] = at->detector_region;
+   if (X_Pi != NULL) X_Pi[i] = at->pi;
 }
 
 #define ST_DITHER 1
@@ -386,7 +433,12 @@ int mxref_trace_slots(int n, const double *energy, const double *p_in, const dou
         else if ((stages & ST_DETECT) && Det_Kind)
           {
              rng_window(u, MX_U_DETECT, MX_U_DETECT_N, g, MX_N_DETECT, MX_N_DETECT_N);
-             detect_photons(&pt);
+             if (Acis_Fef)
+               {
+                  pt.history &= ~MARX_DET_NUM_OK;
+                  if (-1 == marx_detect(&pt, 0)) { set_err("detect"); return -1; }
+               }
+             else detect_photons(&pt);
              us[6] = U_pos - MX_U_DETECT; us[7] = N_pos - MX_N_DETECT;
           }
         rng_window(NULL, 0, 0, NULL, 0, 0);
@@ -436,6 +488,7 @@ double mxref_trace_batch(int n, const double *energy, const double *p_in, const 
    if ((stages & ST_MIRROR) && (-1 == marx_mirror_reflect(pt, 0))) goto fail;
    if ((stages & ST_GRATING) && Have_Grating && (-1 == marx_grating_diffract(pt, 0))) goto fail;
    if ((stages & ST_DETECT) && Det_Kind >= 3) { if (-1 == marx_detect(pt, 0)) goto fail; }
+   else if ((stages & ST_DETECT) && Det_Kind && Acis_Fef) { if (-1 == marx_detect(pt, 0)) goto fail; }
    else if ((stages & ST_DETECT) && Det_Kind) detect_photons(pt);
    clock_gettime(CLOCK_MONOTONIC, &t1);
    secs = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);

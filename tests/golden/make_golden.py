@@ -26,6 +26,15 @@ oracle/Makefile compiles them in place into oracle/_ref.  Writes:
                          CHIPX/CHIPY, EXPNO, FLTGRADE/GRADE, TDETX/TDETY,
                          DETX/DETY and X/Y of its FITS event list for each
                          pixel adjustment (--events).
+  acis_fef_synthetic.fits  a synthetic ACIS FEF (the real one is not in the
+                         reference checkout): 10 chips x 4 regions x 20
+                         energies, three gaussians per row (main peak, a
+                         shoulder that is negative on the BI chips 5 and 7,
+                         a low-channel tail) (--fef).
+  trace_fef_<workload>.npz, stats_fef_<workload>.npz
+                         the trace and statistics fixtures of a workload
+                         with the reference's ACIS detector reading that FEF
+                         (pulse height and PI) (--fef).
   diff_rays.npz          focal-plane positions of the differentiable form's
                          rays traced by the reference's mirror stage, at
                          theta = 0 and at the workload's perturbation written
@@ -408,6 +417,111 @@ def events_fixture(name):
     print(name, "events", N_EVENTS, "columns", sorted(k for k in out if k.startswith("EXACT_")))
 
 
+# ------------------------------------------------------------- ACIS FEF --
+FEF_FILE = os.path.join(HERE, "acis_fef_synthetic.fits")
+FEF_CASES = {"fef_acis_i": "plain_scatter", "fef_hetg_s": "plain_hetg"}
+
+
+def write_bintable(path, extname, columns, keys=()):
+    """A FITS file with an empty primary HDU and one binary table:
+    columns = [(name, 'J' | 'E', values)]."""
+    def block(cards):
+        h = "".join(c.ljust(80)[:80] for c in cards) + "END".ljust(80)
+        return h.ljust((len(h) + 2879) // 2880 * 2880).encode("ascii")
+    card = lambda k, v: f"{k:<8}= {v:>20}"
+    prim = block([card("SIMPLE", "T"), card("BITPIX", "8"), card("NAXIS", "0"), card("EXTEND", "T")])
+    n = len(columns[0][2])
+    dt = np.dtype([(name, {"J": ">i4", "E": ">f4"}[t]) for name, t, _ in columns])
+    rec = np.zeros(n, dtype=dt)
+    for name, t, v in columns:
+        rec[name] = v
+    cards = [card("XTENSION", "'BINTABLE'"), card("BITPIX", "8"), card("NAXIS", "2"),
+             card("NAXIS1", str(dt.itemsize)), card("NAXIS2", str(n)), card("PCOUNT", "0"), card("GCOUNT", "1"),
+             card("TFIELDS", str(len(columns)))]
+    for i, (name, t, _) in enumerate(columns):
+        cards += [card(f"TTYPE{i + 1}", f"'{name}'"), card(f"TFORM{i + 1}", f"'1{t}'")]
+    cards += [card("EXTNAME", f"'{extname}'")] + [card(k, v) for k, v in keys]
+    data = rec.tobytes()
+    data += b"\0" * ((-len(data)) % 2880)
+    with open(path, "wb") as f:
+        f.write(prim + block(cards) + data)
+
+
+def synthetic_fef():
+    """Rows of the synthetic FEF (see the module docstring)."""
+    energies = np.geomspace(0.15, 12.0, 20)
+    cols = {k: [] for k in ("CCD_ID", "CHIPX_LO", "CHIPX_HI", "CHIPY_LO", "CHIPY_HI", "REGNUM", "ENERGY", "CHANNEL",
+                            "G1_FWHM", "G1_POS", "G1_AMPL", "G2_FWHM", "G2_POS", "G2_AMPL",
+                            "G3_FWHM", "G3_POS", "G3_AMPL")}
+    reg = 0
+    for ccd in range(10):
+        for rx in range(2):
+            for ry in range(2):
+                gain = 1.0 + 0.01 * (2 * rx + ry - 1.5) + 0.004 * ccd
+                for e in energies:
+                    ch = e * 1000.0 / 14.6 * gain
+                    fwhm = (55.0 + 45.0 * np.sqrt(e)) / 14.6
+                    vals = dict(CCD_ID=ccd, CHIPX_LO=1 + 512 * rx, CHIPX_HI=512 * (rx + 1), CHIPY_LO=1 + 512 * ry,
+                                CHIPY_HI=512 * (ry + 1), REGNUM=reg, ENERGY=e, CHANNEL=ch,
+                                G1_FWHM=fwhm, G1_POS=ch, G1_AMPL=1.0,
+                                G2_FWHM=2.5 * fwhm, G2_POS=0.7 * ch,
+                                G2_AMPL=-0.004 if ccd in (5, 7) else 0.04,
+                                G3_FWHM=6.0, G3_POS=-5.0, G3_AMPL=0.8 + 0.2 * e)
+                    for k, v in vals.items():
+                        cols[k].append(v)
+                reg += 1
+    kinds = {k: ("J" if k in ("CCD_ID", "CHIPX_LO", "CHIPX_HI", "CHIPY_LO", "CHIPY_HI", "REGNUM") else "E")
+             for k in cols}
+    return [(k, kinds[k], np.array(v)) for k, v in cols.items()]
+
+
+def fef_datadir(where: str) -> str:
+    """A copy of the MARX data directory with the synthetic FEF as its
+    caldb/acisfef.fits (the ACISFEF entry of marxcaldb.par)."""
+    src = os.path.join(REF_ROOT, "marx", "data")
+    dst = os.path.join(where, "data")
+    shutil.copytree(src, dst)
+    shutil.copy(FEF_FILE, os.path.join(dst, "caldb", "acisfef.fits"))
+    return dst
+
+
+def fef_fixtures():
+    write_bintable(FEF_FILE, "FUNCTION", synthetic_fef())
+    tmp = tempfile.mkdtemp()
+    try:
+        dd = fef_datadir(tmp)
+        for name, base in FEF_CASES.items():
+            w = W.ALL[base](parity=True)
+            ph = w.photons(N_TRACE, seed=w.seed + 11)
+            U, N = predraw_variates(N_TRACE, seed=w.seed + 12)
+            ref = Reference(w.cfg, datadir=dd, extra_par={"DetIdeal": "yes"})   # QE, filter, contamination off
+            q, used, bad = ref.trace_slots(ph, U, N)
+            assert bad == 0, "reference ran past its variate slots"
+            np.savez_compressed(
+                os.path.join(HERE, f"trace_{name}.npz"),
+                energy=ph.energy, p_in=ph.p, arrival_time=ph.arrival_time, U=U, N=N,
+                x=q.x, p=q.p, flags=q.flags, mirror_shell=q.mirror_shell, order=q.order, ccd_num=q.ccd_num,
+                y_pixel=q.y_pixel, z_pixel=q.z_pixel, dither_state=q.dither_state, used=used,
+                pulse_height=q.pulse_height, pi=q.pi)
+            on_chip = q.ccd_num >= 0
+            print(name, "on chips", int(on_chip.sum()), "FEF-detected", int(((q.flags & 0xFF) == 0).sum()),
+                  "pha range", q.pulse_height[on_chip].min() if on_chip.any() else None,
+                  q.pulse_height[on_chip].max() if on_chip.any() else None)
+            ref_n = Reference(w.cfg, native=True, seed=w.seed, datadir=dd, extra_par={"DetIdeal": "yes"})
+            ph = w.photons(N_STATS, seed=w.seed + 13)
+            q, secs = ref_n.trace_batch(ph)
+            good = (q.flags & 0xFF) == 0
+            hit = q.ccd_num >= 0
+            out = {"n": np.array(q.n), "on_chip": np.array(hit.sum()), "good": np.array(good.sum()),
+                   "streaked": np.array(((q.flags & 0x200) != 0).sum()),
+                   "pha_hist": np.bincount(np.clip(q.pulse_height[good].astype(int), 0, 1023) // 8, minlength=128),
+                   "pi_hist": np.histogram(q.pi[good], bins=np.linspace(0, 12, 97))[0]}
+            np.savez_compressed(os.path.join(HERE, f"stats_fef_{name[4:]}.npz"), **out)
+            print(name, "stats", {k: int(v) for k, v in out.items() if v.ndim == 0})
+    finally:
+        shutil.rmtree(tmp)
+
+
 N_DIFF = 4000
 RDB = "EKCHDOS06.rdb"
 SHELL_OF = {"1": 0, "3": 1, "4": 2, "6": 3}
@@ -487,6 +601,8 @@ if __name__ == "__main__":
     names = [a for a in sys.argv[1:] if not a.startswith("-")]
     if "--diff" in sys.argv:
         diff_rays()
+    elif "--fef" in sys.argv:
+        fef_fixtures()
     elif "--events" in sys.argv:
         if names:
             events_fixture(names[0])
