@@ -328,7 +328,49 @@ def bench_workloads(a, skip):
         out[name] = {"photons": n, "ms": ms, "photons_per_s": n / (ms * 1e-3), "detected_fraction": good}
         eng.close()
         del d
+    out.update(bench_fef(a))
     return out
+
+
+def bench_fef(a):
+    """plain_scatter with an ACIS FEF in the tables (the synthetic FEF the
+    tests pin against the reference): the trace plus the FEF pass."""
+    import tempfile
+    import torch
+    from marx_gb300 import workloads as W
+    from marx_gb300._native import Engine, DevicePhotons
+    from marx_gb300.caldb.pack import DEFAULT_PACK, pack_with_fef
+    fef = os.path.join(ROOT, "tests", "golden", "acis_fef_synthetic.fits")
+    if not os.path.exists(fef):
+        return {}
+    with tempfile.TemporaryDirectory() as tmp:
+        pack = os.path.join(tmp, "fef.mxpack")
+        pack_with_fef(DEFAULT_PACK, fef, pack)
+        w = W.ALL["plain_scatter"]()
+        n = 4_000_000
+        eng = Engine(w.cfg, pack=pack)
+    d = DevicePhotons.from_host(w.photons(n, seed=w.seed + 6))
+    p0, f0 = d.p.clone(), d.flags.clone()
+    stream = torch.cuda.current_stream()
+    for s in range(2):
+        d.p.copy_(p0); d.flags.copy_(f0)
+        eng.trace(d, stages=w.stages, seed=800 + s)
+    torch.cuda.synchronize()
+    k = max(3, min(a.steps, 5))
+    ms = 0.0
+    for s in range(k):
+        d.p.copy_(p0); d.flags.copy_(f0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        eng.trace(d, stages=w.stages, seed=s)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms += e0.elapsed_time(e1)
+    ms /= k
+    good = float(((d.flags & 0xFF) == 0).float().mean().item())
+    eng.close()
+    return {"plain_scatter_fef": {"photons": n, "ms": ms, "photons_per_s": n / (ms * 1e-3), "detected_fraction": good,
+                                  "note": "with the synthetic ACIS FEF: trace, then the FEF pulse-height pass"}}
 
 
 EVENT_BYTES = 1 + 4 + 4 + 4 + 12 + 4 + 4 + 4 + 8 + 8 + 8 + 8 + 4 + 4 + 4 + 2 + 2   # columns read + written
@@ -392,7 +434,7 @@ def bench_events(a):
     eng.close()
     return {"workload": "1e7 ACIS-I events, EDSER, INTERNAL dither, frames of ~30 events, device-resident",
             "events": n, "ms": ms, "events_per_s": n / (ms * 1e-3), "gpu_launches_per_step": launches,
-            "roofline": {"bound": "fp64", "note": "sin, cos, acos, asin, atan and six divisions per event; "
+            "roofline": {"bound": "fp64", "note": "sin, cos, acos, asin, atan and about 26 divisions per event; "
                                                   "ncu: FP64 pipe 87% busy (profiles/event_kernel_acis_i.md)",
                          "hbm": {"achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
                                  "bytes_per_event": EVENT_BYTES}},
