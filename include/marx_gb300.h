@@ -162,6 +162,9 @@ typedef struct mx_config {
   /* Pointing (dither.c:85-160) */
   double ra_nom, dec_nom;     /* RA_Nom, Dec_Nom (deg) */
   double pointing_offset[2];  /* PointingOffsetY, PointingOffsetZ (arcsec) */
+  /* ACIS response with DetIdeal = no (acis-s.c:136-172): the CALDB QE and
+   * the contamination of the pack's ACIS contamination tables at this epoch */
+  double tstart_mjdsecs;      /* the run's start in seconds since MJDREF (marx_set_time, util.c:231) */
 } mx_config;
 
 /* Structure-of-arrays photon list.  3-vectors are component-major:

@@ -276,10 +276,47 @@ def read_fef(path: str) -> dict:
     raise ValueError(f"{path}: no FUNCTION table")
 
 
-def pack_with_fef(pack_in: str, fef_path: str, pack_out: str) -> None:
-    """A copy of a table pack with the ACIS FEF of fef_path added."""
+def read_contam(path: str) -> dict:
+    """The acis/contam<ccd>/* sections from an ACIS contamination file
+    (read_contam_file_for_ccd, aciscontam.c:315-487): per chip extension
+    ACIS<ccd>_CONTAM (or AXAF_CONTAM with CCD_ID), one row per layer:
+    rows = (component, n_energy, n_time), energy and mu [layer][repeat],
+    time [layer][repeat] (double), tau0 and tau1, and the optional fxy map
+    with its blocking factor fxyblk."""
+    S = {}
+    for h, c in read_fits_bintables(path):
+        ext = h.get("EXTNAME", "").upper()
+        if ext.startswith("ACIS") and ext.endswith("_CONTAM") and ext[4:-7].isdigit():
+            ccd = int(ext[4:-7])
+        elif ext == "AXAF_CONTAM" and "CCD_ID" in h:
+            ccd = int(h["CCD_ID"])
+        else:
+            continue
+        cols = {k.lower(): v for k, v in c.items()}
+        two = lambda a: np.asarray(a).reshape(len(np.asarray(a)), -1)
+        k = f"acis/contam{ccd}/"
+        S[k + "rows"] = np.stack([np.asarray(cols["component"]), np.asarray(cols["n_energy"]),
+                                  np.asarray(cols["n_time"])], axis=1).astype(np.int32)
+        S[k + "energy"] = two(cols["energy"]).astype(np.float32)
+        S[k + "mu"] = two(cols["mu"]).astype(np.float32)
+        S[k + "time"] = two(cols["time"]).astype(np.float64)
+        S[k + "tau0"] = two(cols["tau0"]).astype(np.float32)
+        S[k + "tau1"] = two(cols["tau1"]).astype(np.float32)
+        if "fxy" in cols:
+            S[k + "fxy"] = two(cols["fxy"]).astype(np.float32)
+            S[k + "fxyblk"] = np.array([int(h.get("FXYBLK", "1"))], dtype=np.int32)
+    if not S:
+        raise ValueError(f"{path}: no ACIS contamination tables")
+    return S
+
+
+def pack_with_fef(pack_in: str, fef_path: str, pack_out: str, contam_path: str | None = None) -> None:
+    """A copy of a table pack with the ACIS FEF of fef_path (and the ACIS
+    contamination file contam_path) added."""
     S = read_pack(pack_in)
     S.update(read_fef(fef_path))
+    if contam_path:
+        S.update(read_contam(contam_path))
     write_pack(pack_out, S)
 
 
@@ -374,6 +411,9 @@ def build_sections(data_dir: str) -> dict:
     fef = os.path.join(data_dir, "caldb", "acisfef.fits")     # the ACISFEF entry of marxcaldb.par
     if os.path.exists(fef):
         S.update(read_fef(fef))
+    contam = os.path.join(data_dir, "caldb", "acisD1999-08-13contamN0015_marx.fits")   # ACISCONTAM
+    if os.path.exists(contam):
+        S.update(read_contam(contam))
     qe = read_fits_bintables(os.path.join(data_dir, "caldb", "acisD1997-04-17qeN0006.fits"))
     for h, c in qe:
         if h.get("EXTNAME") == "AXAF_QE":

@@ -60,6 +60,7 @@ class MxConfig(C.Structure):
         ("hesf_length", C.c_double), ("hesf_cr_width", C.c_double),
         ("hesf_height", C.c_double * 4), ("hesf_theta", C.c_double * 4),
         ("ra_nom", C.c_double), ("dec_nom", C.c_double), ("pointing_offset", C.c_double * 2),
+        ("tstart_mjdsecs", C.c_double),
     ]
 
 

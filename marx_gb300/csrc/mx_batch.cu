@@ -420,7 +420,7 @@ static int build_graph(mx_batch *b) {
     e = cudaLaunchKernelEx(&lc, mx_batch_kernel, T, io);
   }
   // with an FEF: the pulse heights and streaks of the photons on a chip
-  if (e == cudaSuccess && T.acis_fef) e = launch_acis_fef(T, io.io, c->num_sms * 8, st, io.seed);
+  if (e == cudaSuccess && (T.acis_fef || T.acis_qe)) e = launch_acis_fef(T, io.io, c->num_sms * 8, st, io.seed);
   cudaGraph_t g = nullptr;
   cudaError_t e2 = cudaStreamEndCapture(st, &g);
   cudaStreamDestroy(st);
@@ -715,7 +715,7 @@ int mx_batch_run(mx_batch *b, uint64_t seed, void *stream) {
   *b->h_seed = seed;
   e = cudaGraphLaunch(b->exec, (cudaStream_t) stream);
   if (e == cudaSuccess) e = cudaEventRecord(b->done, (cudaStream_t) stream);
-  b->ctx->launches += b->ctx->T.acis_fef ? 2 : 1;
+  b->ctx->launches += (b->ctx->T.acis_fef || b->ctx->T.acis_qe) ? 2 : 1;
   return e == cudaSuccess ? MX_OK : mx_cuda_fail(b->ctx, e, "launching the batch graph");
 }
 

@@ -46,6 +46,7 @@ static int upload_model(mx_context *c) {
   size_t o_pe = put(blob, M.support_energy), o_pc = put(blob, M.support_cum), o_pk = put(blob, M.support_k);
   size_t o_ht = put(blob, M.hrc_tab), o_hs = put(blob, M.hrc_slope);
   size_t o_fm = put(blob, M.fef_map), o_fr = put(blob, M.fef), o_ff = put(blob, M.fef_f), o_fs = put(blob, M.fef_slope);
+  size_t o_co = put(blob, M.contam);
   cudaError_t e = c->tables.ensure(blob.size());
   if (e != cudaSuccess) return cuda_fail(c, e, "allocating device tables");
   e = cudaMemcpy(c->tables.ptr, blob.data(), blob.size(), cudaMemcpyHostToDevice);
@@ -74,6 +75,7 @@ static int upload_model(mx_context *c) {
   c->T.fef = (const MxFefDev *) (b + o_fr);
   c->T.fef_f = (const float *) (b + o_ff);
   c->T.fef_slope = (const double *) (b + o_fs);
+  c->T.contam = (const MxContamDev *) (b + o_co);
   c->shared_bytes = trace_shared_bytes(c->T);
   if (c->shared_bytes > 200 * 1024) return fail(c, MX_ERANGE, "tables exceed the shared-memory budget");
   return MX_OK;
@@ -269,7 +271,7 @@ int mx_trace_queues(mx_context *c, const MxTables &T, const mx_photons *ph, uint
     e = launch_trace(T, io, c->num_sms * c->trace_blocks[slots ? 0 : 1], (int) c->shared_bytes, slots != 0, st);
     c->launches++;
   }
-  if (e == cudaSuccess && (stages & MX_STAGE_DETECT) && T.acis_fef) {
+  if (e == cudaSuccess && (stages & MX_STAGE_DETECT) && (T.acis_fef || T.acis_qe)) {
     e = launch_acis_fef(T, io, c->num_sms * 8, st);
     c->launches++;
   }

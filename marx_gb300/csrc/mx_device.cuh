@@ -1013,7 +1013,54 @@ MXD void acis_streak(const MxTables &T, const MxChipDev &d, Ph &ph, D3 &x, D3 &p
   }
 }
 
-// ------------------------------------------------------------ ACIS FEF --
+// ------------------------------------------------------- ACIS QE, FEF --
+// compute_contamination (aciscontam.c:93-135) at chip pixel (cx, cy).
+MXD double acis_contam(const MxTables &T, const MxContamDev &c, double en, double cx, double cy) {
+  const float fe = (float) en;
+  double fxy = 0.0, v = 0.0;
+  if (c.mode != 2) {
+    if (c.mode == 0) {   // fxy_acis_i (aciscontam.c:140-155)
+      const double dx = cx - c.x0, dy = cy - c.y0;
+      double r = (8.0 / 1024.0) * sqrt(dx * dx + dy * dy);
+      r /= 8.07;
+      fxy = 1.29 * r * r;
+    } else {             // fxy_acis456789 (aciscontam.c:177-189)
+      const double y0 = 512.0;
+      fxy = cy <= 512.0 ? pow(fabs((cy - y0) / (64.0 - y0)), 5.5) : pow(fabs((cy - y0) / (964.0 - y0)), 4.5);
+    }
+    for (int i = 0; i < c.nl; i++) {
+      const MxTabDev &t = c.mu[i];
+      const double mu = f2d(interp_f(fe, T.fef_f + t.x_off, T.fef_f + t.y_off, T.fef_slope + t.s_off, (unsigned) t.n));
+      v += mu * (c.tau0[i] + c.tau1[i] * fxy);
+    }
+  } else {
+    if ((cx < 0) || (cx >= 1024) || (cy < 0) || (cy >= 1024)) return 0.0;
+    cx /= c.blk;
+    cy /= c.blk;
+    const unsigned ofs = (1024u / (unsigned) c.blk) * (unsigned) cy + (unsigned) cx;
+    for (int i = 0; i < c.nl; i++) {
+      const MxTabDev &t = c.mu[i];
+      const double mu = f2d(interp_f(fe, T.fef_f + t.x_off, T.fef_f + t.y_off, T.fef_slope + t.s_off, (unsigned) t.n));
+      fxy = f2d(T.fef_f[c.fxy_off[i] + ofs]);
+      v += mu * (c.tau0[i] + c.tau1[i] * fxy);
+    }
+  }
+  return exp(-v);
+}
+
+// The acceptance of _marx_acis_apply_qe_and_pha (acis-s.c:145-163): the
+// CALDB QE (no filter table: the CALDB build reads none) times the
+// contamination against one uniform.
+MXD bool acis_qe_accept(const MxTables &T, int ccd, const Ph &ph, Rng &rng) {
+  const double r = rng.uniform();
+  const MxContamDev &c = T.contam[ccd];
+  const double qe = f2d(interp_f((float) ph.e, T.fef_f + c.qe.x_off, T.fef_f + c.qe.y_off, T.fef_slope + c.qe.s_off,
+                                 (unsigned) c.qe.n));
+  const double qe_filter = 1.0;
+  const double qe_contam = acis_contam(T, c, ph.e, (double) ph.ypix, (double) ph.zpix);
+  return !(r >= qe * qe_filter * qe_contam);
+}
+
 constexpr int MX_FEF_MAX_GAUSS = MX_FEF_GAUSSIANS;
 
 // gaussian_integral (acis_fef.c:380-392) over [0, inf) and (-inf, 0]: the
@@ -1176,9 +1223,9 @@ MXD void detect_stage(const MxTables &T, const MxChipDev *chips, int nchips, Ph 
     ph.ccd = d.id;
     ph.ypix = (float) div_by(dx, d.xpix, d.inv_xpix);
     ph.zpix = (float) div_by(dy, d.ypix, d.inv_ypix);
-    // with an FEF the pulse height, PI and streak are a pass of their own
-    // over the detected photons (mx_acis_fef_kernel), after the trace
-    if (!T.acis_fef) acis_streak(T, d, ph, x, p, rng);
+    // with an FEF or the QE acceptance the response and the streak are a
+    // pass of their own over the photons on a chip (mx_acis_fef_kernel)
+    if (!T.acis_fef && !T.acis_qe) acis_streak(T, d, ph, x, p, rng);
   }
   ph.x = x + off;
   ph.p = p;

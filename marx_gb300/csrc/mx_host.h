@@ -36,6 +36,7 @@ struct HostModel {
   std::vector<MxFefDev> fef;
   std::vector<float> fef_f;
   std::vector<double> fef_slope;
+  std::vector<MxContamDev> contam;
 };
 
 bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string &err);

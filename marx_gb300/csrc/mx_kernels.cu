@@ -65,11 +65,12 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_trace_kernel(MxTables T, Tr
   }
 }
 
-// The ACIS FEF pass: pulse height and PI of every photon the trace put on
-// a chip (_marx_acis_apply_qe_and_pha with DetIdeal, acis-s.c:136-172),
-// then the frame-transfer streak of those the FEF detected, as
-// _marx_acis_s_detect and _marx_acis_i_detect order them (acis-s.c:230-236).
-// The trace leaves these steps to this pass when the tables carry an FEF.
+// The ACIS response pass over every photon the trace put on a chip
+// (_marx_acis_apply_qe_and_pha, acis-s.c:136-172): with DetIdeal = no the
+// QE x contamination acceptance, with an FEF the pulse height and PI, then
+// the frame-transfer streak of those detected, as _marx_acis_s_detect and
+// _marx_acis_i_detect order them (acis-s.c:230-236).  The trace leaves
+// these steps to this pass when the tables carry either.
 __global__ void __launch_bounds__(256) mx_acis_fef_kernel(MxTables T, TraceIO io, const uint64_t *seedp) {
   const size_t n = io.stride;
   const uint64_t seed = seedp ? *seedp : io.seed;
@@ -88,10 +89,19 @@ __global__ void __launch_bounds__(256) mx_acis_fef_kernel(MxTables T, TraceIO io
     r.U = io.U; r.N = io.N; r.seed = seed; r.n = io.n; r.i = i;
     r.tag = io.tag ? io.tag[i] : i;
     r.overrun = false;
-    r.window(MX_U_FEF, r.U ? 8 : 64, MX_N_FEF, r.N ? 4 : 64);
+    r.window(MX_U_DETECT, 2, MX_N_DETECT, 2);
+    if (T.acis_qe && !acis_qe_accept(T, ccd, q, r)) {
+      if (io.flags) io.flags[i] = q.flags | MX_PHOTON_UNDETECTED;
+      continue;
+    }
+    const int ub = r.upos, nb = r.npos;
     int16_t pha = -1;
     float pi = 0.0f;
-    const bool ok = acis_fef(T, ccd, q.ypix, q.zpix, q.e, r, pha, pi);
+    bool ok = true;
+    if (T.acis_fef) {
+      r.window(MX_U_FEF, r.U ? 8 : 64, MX_N_FEF, r.N ? 4 : 64);
+      ok = acis_fef(T, ccd, q.ypix, q.zpix, q.e, r, pha, pi);
+    }
     if (r.overrun) {
       q.flags |= MX_PHOTON_VARIATE_OVERRUN;
       atomicAdd(io.overrun, 1ull);
@@ -99,7 +109,7 @@ __global__ void __launch_bounds__(256) mx_acis_fef_kernel(MxTables T, TraceIO io
       pha = -1; pi = 0.0f;
       q.flags |= MX_PHOTON_UNDETECTED;
     } else {
-      r.window(MX_U_DETECT, 2, MX_N_DETECT, 2);
+      r.window(ub, MX_U_DETECT + 2 - ub, nb, MX_N_DETECT + 2 - nb);   // the ACIS window, after the QE draw
       D3 x = mk(0, 0, 0), p = mk(0, 0, 0);
       acis_streak(T, T.chips[ccd], q, x, p, r);
       if (q.flags & MX_PHOTON_ACIS_STREAKED) {
@@ -109,8 +119,10 @@ __global__ void __launch_bounds__(256) mx_acis_fef_kernel(MxTables T, TraceIO io
         io.zpix[i] = q.zpix;
       }
     }
-    if (io.pha) io.pha[i] = pha;
-    if (io.pi) io.pi[i] = pi;
+    if (T.acis_fef) {
+      if (io.pha) io.pha[i] = pha;
+      if (io.pi) io.pi[i] = pi;
+    }
     if (io.flags) io.flags[i] = q.flags;
   }
 }

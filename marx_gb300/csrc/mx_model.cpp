@@ -490,6 +490,110 @@ static bool build_fef(const Pack &pk, int min_ccd, int max_ccd, HostModel &M, st
   return true;
 }
 
+// JDMbinary_search_d (dinterpo.c:30): the same bisection over doubles.
+static unsigned jdm_bsearch_d(double x, const double *xp, unsigned n) {
+  unsigned n0 = 0, n1 = n;
+  while (n1 > n0 + 1) {
+    unsigned n2 = (n0 + n1) / 2;
+    if (xp[n2] >= x) {
+      if (xp[n2] == x) return n2;
+      n1 = n2;
+    } else
+      n0 = n2;
+  }
+  if (x >= xp[n0]) return n1;
+  return n0;
+}
+
+// An energy -> value table of the ACIS response in fef_f / fef_slope.
+static MxTabDev response_table(HostModel &M, const float *x, const float *y, unsigned n) {
+  MxTabDev t;
+  t.n = (int32_t) n;
+  t.x_off = (int32_t) M.fef_f.size();
+  M.fef_f.insert(M.fef_f.end(), x, x + n);
+  t.y_off = (int32_t) M.fef_f.size();
+  M.fef_f.insert(M.fef_f.end(), y, y + n);
+  t.s_off = (int32_t) M.fef_slope.size();
+  append_slopes(M.fef_slope, x, y, n);
+  return t;
+}
+
+// The chips' CALDB QE (_marx_read_acis_qe, caldb.c:504-575) and
+// contamination (read_contam_file_for_ccd and compute_tau_values,
+// aciscontam.c:236-487) for the ACIS response with DetIdeal = no.  The
+// contamination's epoch is cfg.tstart_mjdsecs.
+static bool build_contam(const Pack &pk, const mx_config &cfg, int min_ccd, int max_ccd, HostModel &M,
+                         std::string &err) {
+  MxContamDev z;
+  memset(&z, 0, sizeof(z));
+  M.contam.assign(10, z);
+  for (int ccd = min_ccd; ccd <= max_ccd; ccd++) {
+    MxContamDev &c = M.contam[ccd];
+    const std::string k = "acis/contam" + std::to_string(ccd) + "/";
+    size_t nq;
+    const float *qe = pk.get<float>("acis/qe" + std::to_string(ccd), &nq, err);
+    if (!qe) return false;
+    if (nq / 2 < 2) { err = "Expecting more than 2 rows in the ACIS QE file"; return false; }
+    c.qe = response_table(M, qe, qe + nq / 2, (unsigned) (nq / 2));
+    size_t nr, ne, nm, nt, n0, n1;
+    const int32_t *rows = pk.get<int32_t>(k + "rows", &nr, err);
+    if (!rows) { err = "Unable to open acis contam file for CCD " + std::to_string(ccd); return false; }
+    const unsigned L = (unsigned) (nr / 3);
+    if (L > MX_CONTAM_LAYERS) { err = "The number of layers in the contamination file is larger than supported"; return false; }
+    const float *en = pk.get<float>(k + "energy", &ne, err), *mu = pk.get<float>(k + "mu", &nm, err);
+    const double *tm = pk.get<double>(k + "time", &nt, err);
+    const float *t0s = pk.get<float>(k + "tau0", &n0, err), *t1s = pk.get<float>(k + "tau1", &n1, err);
+    if (!en || !mu || !tm || !t0s || !t1s || L == 0) { if (err.empty()) err = "contamination table malformed"; return false; }
+    const size_t re = ne / L, rt = nt / L;
+    if (nm / L != re || n0 / L != rt || n1 / L != rt) { err = "contamination table malformed"; return false; }
+    const bool has_fxy = pk.sections.count(k + "fxy") > 0;
+    const float *fxy = nullptr;
+    size_t nf = 0;
+    if (has_fxy) {
+      fxy = pk.get<float>(k + "fxy", &nf, err);
+      const int32_t *blk = pk.get<int32_t>(k + "fxyblk", nullptr, err);
+      if (!fxy || !blk) return false;
+      c.blk = blk[0];
+      if (c.blk <= 0 || c.blk * (1024 / c.blk) != 1024) { err = "Invalid fxyblk value"; return false; }
+      if (nf / L != (size_t) (1024 / c.blk) * (1024 / c.blk)) { err = "The FXY column has the wrong size"; return false; }
+      c.mode = 2;
+    } else if (ccd <= 3) {
+      // fxy_acis0..3 (aciscontam.c:138-156)
+      static const double cx[4] = {1024.5, 0.5, 0.5, 1024.5};
+      c.mode = 0; c.x0 = cx[ccd]; c.y0 = 1024.5;
+    } else
+      c.mode = 1;   // fxy_acis456789
+    c.nl = (int32_t) L;
+    for (unsigned l = 0; l < L; l++) {
+      if (rows[3 * l] != 0) { err = "Expecting COMPONENT=0 in the contamination file"; return false; }
+      const unsigned n_e = (unsigned) rows[3 * l + 1], n_t = (unsigned) rows[3 * l + 2];
+      if (n_t <= 1 || n_e <= 1) { err = "Expecting n_energy or n_time to be greater than 1"; return false; }
+      if (n_t > rt) { err = "n_time value is larger than data arrays"; return false; }
+      if (n_e > re) { err = "n_energy value is larger than data arrays"; return false; }
+      const double *times = tm + l * rt;
+      const float *e = en + l * re, *m = mu + l * re, *tau0s = t0s + l * rt, *tau1s = t1s + l * rt;
+      for (unsigned i = 0; i + 1 < n_t; i++)
+        if (!(times[i] < times[i + 1])) { err = "Expecting the time grid to be monotonically increasing"; return false; }
+      for (unsigned i = 0; i + 1 < n_e; i++)
+        if (!(e[i] < e[i + 1])) { err = "Expecting the ENERGY grid to be monotonically increasing"; return false; }
+      // compute_tau_values
+      unsigned b1 = jdm_bsearch_d(cfg.tstart_mjdsecs, times, n_t), b0 = b1 - 1;
+      if (b1 == n_t) { b1--; b0--; }
+      if (b1 == 0) { b1 = 1; b0 = 0; }
+      const double t = (cfg.tstart_mjdsecs - times[b0]) / (times[b1] - times[b0]);
+      c.tau0[l] = tau0s[b0] + (double) (tau0s[b1] - tau0s[b0]) * t;
+      c.tau1[l] = tau1s[b0] + (double) (tau1s[b1] - tau1s[b0]) * t;
+      c.mu[l] = response_table(M, e, m, n_e);
+      if (has_fxy) {
+        const size_t per = nf / L;
+        c.fxy_off[l] = (int32_t) M.fef_f.size();
+        M.fef_f.insert(M.fef_f.end(), fxy + l * per, fxy + (l + 1) * per);
+      }
+    }
+  }
+  return true;
+}
+
 static bool build_hrc(const Pack &pk, const mx_config &cfg, HostModel &M, std::string &err) {
   MxTables &T = M.T;
   MxHrcDev &h = T.hrc;
@@ -931,6 +1035,18 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
       T.acis_fef = M.fef.empty() ? 0 : 1;
     }
     T.fef_nregions = (int32_t) M.fef.size();
+    // the QE and contamination acceptance of DetIdeal = no, when the pack
+    // carries contamination tables (without them ACIS detection is ideal)
+    M.contam.clear();
+    T.acis_qe = 0;
+    if (acis && !cfg.det_ideal && pk.sections.count(std::string("acis/contam") +
+                                                    (cfg.detector == MX_DETECTOR_ACIS_I ? "0" : "4") + "/rows")) {
+      if (!build_contam(pk, cfg, cfg.detector == MX_DETECTOR_ACIS_I ? 0 : 4, cfg.detector == MX_DETECTOR_ACIS_I ? 3 : 9,
+                        M, err))
+        return false;
+      T.acis_qe = 1;
+    }
+    if (M.contam.empty()) { MxContamDev z; memset(&z, 0, sizeof(z)); M.contam.assign(10, z); }
     if (M.fef_map.empty()) M.fef_map.push_back(-1);
     if (M.fef.empty()) { MxFefDev z; memset(&z, 0, sizeof(z)); M.fef.push_back(z); }
     if (M.fef_f.empty()) M.fef_f.push_back(0.f);

@@ -81,6 +81,18 @@ struct MxHrcDev {
 // energy at fef_f + g_off as (amp, center, sigma) triples [energy][gaussian],
 // the channel-to-energy interpolation slopes at fef_slope + s_off.
 #define MX_FEF_GAUSSIANS 6   // gaussians per FEF row the device pass holds
+#define MX_CONTAM_LAYERS 5   // MAX_LAYERS of aciscontam.c
+
+// One chip's QE and contamination (aciscontam.c Single_Component_Contam_Type)
+// for the ACIS response with DetIdeal = no.  Tables index fef_f/fef_slope.
+struct MxContamDev {
+  int32_t nl, mode, blk, pad;   // layers; spatial term: 0 ACIS-I radial (x0, y0), 1 ACIS-S power law, 2 fxy map
+  double x0, y0;
+  double tau0[MX_CONTAM_LAYERS], tau1[MX_CONTAM_LAYERS];
+  MxTabDev mu[MX_CONTAM_LAYERS];    // energy -> mu per layer
+  int32_t fxy_off[MX_CONTAM_LAYERS], pad2[3];
+  MxTabDev qe;                      // energy -> QE (the CALDB ACIS QE)
+};
 struct MxFefDev {
   int32_t e_off, n_e, g_off, n_g;
   int32_t s_off, pad[3];
@@ -149,4 +161,7 @@ struct MxTables {
   const float *fef_f;
   const double *fef_slope;
   int32_t acis_fef, fef_nregions;
+  // ACIS QE x contamination acceptance (DetIdeal = no and contamination tables present)
+  const MxContamDev *contam;        // [10] by chip id
+  int32_t acis_qe, pad_qe;
 };

@@ -419,32 +419,77 @@ def events_fixture(name):
 
 # ------------------------------------------------------------- ACIS FEF --
 FEF_FILE = os.path.join(HERE, "acis_fef_synthetic.fits")
-FEF_CASES = {"fef_acis_i": "plain_scatter", "fef_hetg_s": "plain_hetg"}
+# name: (workload, DetIdeal): with DetIdeal = no the reference also applies
+# the CALDB QE and the (synthetic) contamination before the FEF
+FEF_CASES = {"fef_acis_i": ("plain_scatter", "yes"), "fef_hetg_s": ("plain_hetg", "yes"),
+             "qe_acis_i": ("plain_scatter", "no"), "qe_hetg_s": ("plain_hetg", "no")}
 
 
-def write_bintable(path, extname, columns, keys=()):
-    """A FITS file with an empty primary HDU and one binary table:
-    columns = [(name, 'J' | 'E', values)]."""
+def write_bintable(path, extname, columns, keys=(), tables=None):
+    """A FITS file with an empty primary HDU and binary tables:
+    columns = [(name, 'J' | 'E' | 'D', values (rows, or rows x repeat))];
+    `tables` gives several as [(extname, columns, keys)]."""
     def block(cards):
         h = "".join(c.ljust(80)[:80] for c in cards) + "END".ljust(80)
         return h.ljust((len(h) + 2879) // 2880 * 2880).encode("ascii")
     card = lambda k, v: f"{k:<8}= {v:>20}"
-    prim = block([card("SIMPLE", "T"), card("BITPIX", "8"), card("NAXIS", "0"), card("EXTEND", "T")])
-    n = len(columns[0][2])
-    dt = np.dtype([(name, {"J": ">i4", "E": ">f4"}[t]) for name, t, _ in columns])
-    rec = np.zeros(n, dtype=dt)
-    for name, t, v in columns:
-        rec[name] = v
-    cards = [card("XTENSION", "'BINTABLE'"), card("BITPIX", "8"), card("NAXIS", "2"),
-             card("NAXIS1", str(dt.itemsize)), card("NAXIS2", str(n)), card("PCOUNT", "0"), card("GCOUNT", "1"),
-             card("TFIELDS", str(len(columns)))]
-    for i, (name, t, _) in enumerate(columns):
-        cards += [card(f"TTYPE{i + 1}", f"'{name}'"), card(f"TFORM{i + 1}", f"'1{t}'")]
-    cards += [card("EXTNAME", f"'{extname}'")] + [card(k, v) for k, v in keys]
-    data = rec.tobytes()
-    data += b"\0" * ((-len(data)) % 2880)
+    out = block([card("SIMPLE", "T"), card("BITPIX", "8"), card("NAXIS", "0"), card("EXTEND", "T")])
+    for ext, cols, kv in (tables or [(extname, columns, keys)]):
+        n = len(cols[0][2])
+        vals = [np.asarray(v) for _, _, v in cols]
+        reps = [1 if v.ndim == 1 else v.shape[1] for v in vals]
+        dt = np.dtype([(name, {"J": ">i4", "E": ">f4", "D": ">f8"}[t], (r,)) if r > 1 else
+                       (name, {"J": ">i4", "E": ">f4", "D": ">f8"}[t]) for (name, t, _), r in zip(cols, reps)])
+        rec = np.zeros(n, dtype=dt)
+        for (name, t, _), v in zip(cols, vals):
+            rec[name] = v
+        cards = [card("XTENSION", "'BINTABLE'"), card("BITPIX", "8"), card("NAXIS", "2"),
+                 card("NAXIS1", str(dt.itemsize)), card("NAXIS2", str(n)), card("PCOUNT", "0"), card("GCOUNT", "1"),
+                 card("TFIELDS", str(len(cols)))]
+        for i, ((name, t, _), r) in enumerate(zip(cols, reps)):
+            cards += [card(f"TTYPE{i + 1}", f"'{name}'"), card(f"TFORM{i + 1}", f"'{r}{t}'")]
+        cards += [card("EXTNAME", f"'{ext}'")] + [card(k, v) for k, v in kv]
+        data = rec.tobytes()
+        data += b"\0" * ((-len(data)) % 2880)
+        out += block(cards) + data
     with open(path, "wb") as f:
-        f.write(prim + block(cards) + data)
+        f.write(out)
+
+
+CONTAM_FILE = os.path.join(HERE, "acis_contam_synthetic.fits")
+
+
+def synthetic_contam():
+    """Per chip two layers (component 0), 35 of 40 energy slots and 5 of 6
+    time slots used; the spatial term by the reference's own functions,
+    except on the BI chips 5 and 7, which carry an fxy map of 32 x 32
+    blocks (fxyblk = 32)."""
+    tables = []
+    e = np.zeros(40, np.float32)
+    e[:35] = np.geomspace(0.1, 12.0, 35)
+    t = np.zeros(6)
+    t[:5] = [-2.0e8, 0.5e8, 1.5e8, 3.0e8, 5.0e8]
+    for ccd in range(10):
+        mu = np.zeros((2, 40), np.float32)
+        mu[0, :35] = 2.2 * e[:35] ** -2.4          # carbon-like
+        mu[1, :35] = 0.9 * e[:35] ** -2.0 + 0.05   # a second layer
+        tau0 = np.zeros((2, 6), np.float32)
+        tau1 = np.zeros((2, 6), np.float32)
+        tau0[0, :5] = [0.02, 0.05, 0.08, 0.12, 0.16]
+        tau0[1, :5] = [0.01, 0.02, 0.03, 0.04, 0.05]
+        tau1[0, :5] = [0.01, 0.03, 0.05, 0.07, 0.09]
+        tau1[1, :5] = [0.0, 0.005, 0.01, 0.015, 0.02]
+        cols = [("component", "J", np.zeros(2)), ("n_energy", "J", np.full(2, 35)), ("energy", "E", np.tile(e, (2, 1))),
+                ("mu", "E", mu), ("n_time", "J", np.full(2, 5)), ("time", "D", np.tile(t, (2, 1))),
+                ("tau0", "E", tau0), ("tau1", "E", tau1)]
+        keys = ()
+        if ccd in (5, 7):
+            yy, xx = np.mgrid[0:32, 0:32]
+            fxy = (((xx - 15.5) ** 2 + (yy - 15.5) ** 2) / 400.0).astype(np.float32).ravel()
+            cols.append(("fxy", "E", np.tile(fxy, (2, 1)) * np.array([[1.0], [0.5]], np.float32)))
+            keys = (("FXYBLK", "32"),)
+        tables.append((f"ACIS{ccd}_CONTAM", cols, keys))
+    return tables
 
 
 def synthetic_fef():
@@ -482,19 +527,21 @@ def fef_datadir(where: str) -> str:
     dst = os.path.join(where, "data")
     shutil.copytree(src, dst)
     shutil.copy(FEF_FILE, os.path.join(dst, "caldb", "acisfef.fits"))
+    shutil.copy(CONTAM_FILE, os.path.join(dst, "caldb", "acisD1999-08-13contamN0015_marx.fits"))
     return dst
 
 
 def fef_fixtures():
     write_bintable(FEF_FILE, "FUNCTION", synthetic_fef())
+    write_bintable(CONTAM_FILE, None, None, tables=synthetic_contam())
     tmp = tempfile.mkdtemp()
     try:
         dd = fef_datadir(tmp)
-        for name, base in FEF_CASES.items():
+        for name, (base, ideal) in FEF_CASES.items():
             w = W.ALL[base](parity=True)
             ph = w.photons(N_TRACE, seed=w.seed + 11)
             U, N = predraw_variates(N_TRACE, seed=w.seed + 12)
-            ref = Reference(w.cfg, datadir=dd, extra_par={"DetIdeal": "yes"})   # QE, filter, contamination off
+            ref = Reference(w.cfg, datadir=dd, extra_par={"DetIdeal": ideal})
             q, used, bad = ref.trace_slots(ph, U, N)
             assert bad == 0, "reference ran past its variate slots"
             np.savez_compressed(
@@ -507,7 +554,7 @@ def fef_fixtures():
             print(name, "on chips", int(on_chip.sum()), "FEF-detected", int(((q.flags & 0xFF) == 0).sum()),
                   "pha range", q.pulse_height[on_chip].min() if on_chip.any() else None,
                   q.pulse_height[on_chip].max() if on_chip.any() else None)
-            ref_n = Reference(w.cfg, native=True, seed=w.seed, datadir=dd, extra_par={"DetIdeal": "yes"})
+            ref_n = Reference(w.cfg, native=True, seed=w.seed, datadir=dd, extra_par={"DetIdeal": ideal})
             ph = w.photons(N_STATS, seed=w.seed + 13)
             q, secs = ref_n.trace_batch(ph)
             good = (q.flags & 0xFF) == 0
@@ -516,7 +563,7 @@ def fef_fixtures():
                    "streaked": np.array(((q.flags & 0x200) != 0).sum()),
                    "pha_hist": np.bincount(np.clip(q.pulse_height[good].astype(int), 0, 1023) // 8, minlength=128),
                    "pi_hist": np.histogram(q.pi[good], bins=np.linspace(0, 12, 97))[0]}
-            np.savez_compressed(os.path.join(HERE, f"stats_fef_{name[4:]}.npz"), **out)
+            np.savez_compressed(os.path.join(HERE, f"stats_{name}.npz"), **out)
             print(name, "stats", {k: int(v) for k, v in out.items() if v.ndim == 0})
     finally:
         shutil.rmtree(tmp)

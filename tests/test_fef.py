@@ -5,11 +5,12 @@ import os
 
 import numpy as np
 
-from marx_gb300.caldb.pack import DEFAULT_PACK, pack_with_fef, read_fef, read_pack
+from marx_gb300.caldb.pack import DEFAULT_PACK, pack_with_fef, read_contam, read_fef, read_pack
 from marx_gb300 import workloads as W
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 FEF_FILE = os.path.join(GOLDEN, "acis_fef_synthetic.fits")
+CONTAM_FILE = os.path.join(GOLDEN, "acis_contam_synthetic.fits")
 
 
 def test_fef_sections():
@@ -42,3 +43,29 @@ def test_pack_with_fef_builds_the_engine_model(tmp_path):
     bad = str(tmp_path / "bad.mxpack")
     write_pack(bad, S)
     assert "multiple of 32" in (validate_config(W.ALL["plain_scatter"](parity=True).cfg, pack=bad) or "")
+
+
+def test_contam_sections_and_model(tmp_path):
+    """The contamination tables per chip (two layers; an fxy map on the BI
+    chips), and an engine model with the QE acceptance (DetIdeal = no)."""
+    from marx_gb300._native import validate_config
+    S = read_contam(CONTAM_FILE)
+    for ccd in range(10):
+        assert S[f"acis/contam{ccd}/rows"].shape == (2, 3)
+        assert (f"acis/contam{ccd}/fxy" in S) == (ccd in (5, 7))
+    out = str(tmp_path / "qe.mxpack")
+    pack_with_fef(DEFAULT_PACK, FEF_FILE, out, contam_path=CONTAM_FILE)
+    for name in ("plain_scatter", "plain_hetg"):
+        cfg = W.ALL[name](parity=True).cfg
+        cfg.det_ideal = 0
+        assert validate_config(cfg, pack=out) is None
+    # a layer that is not component 0 is refused, as the reference does
+    T = read_pack(out)
+    T["acis/contam0/rows"] = T["acis/contam0/rows"].copy()
+    T["acis/contam0/rows"][1, 0] = 1
+    from marx_gb300.caldb.pack import write_pack
+    bad = str(tmp_path / "bad.mxpack")
+    write_pack(bad, T)
+    cfg = W.ALL["plain_scatter"](parity=True).cfg
+    cfg.det_ideal = 0
+    assert "COMPONENT=0" in (validate_config(cfg, pack=bad) or "")
