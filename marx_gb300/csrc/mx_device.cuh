@@ -776,9 +776,13 @@ MXD void dither_stage(const MxTables &T, Ph &ph, Rng &rng) {
   double s2 = n.y * n.y + n.z * n.z;
   if (!(s2 > 1e-40)) { ph.p = p; return; }
   // rotate_unit(p, n / s, cos_theta, s) with s = |n| written without the
-  // unit axis: cos p + ((p.n)(1 - cos) / s^2) n + n x p, n.x = 0
+  // unit axis: cos p + ((p.n)(1 - cos) / s^2) n + n x p, n.x = 0.  With
+  // s^2 = sin^2 the factor (1 - cos) / s^2 is 1 / (1 + cos) = 1 / (2 - d),
+  // d = 1 - cos; for arcsecond offsets (d < 1e-6) its series
+  // 1/2 + d/4 + d^2/8 is exact to 1e-19 and saves the division.
   const double pn = p.y * n.y + p.z * n.z;
-  const double k = pn * (1.0 - cos_theta) / s2;
+  const double d = 1.0 - cos_theta;
+  const double k = d < 1e-6 ? pn * (0.5 + d * (0.25 + d * 0.125)) : pn * d / s2;
   ph.p = normalized_unit(mk(cos_theta * p.x + (n.y * p.z - n.z * p.y), cos_theta * p.y + k * n.y + n.z * p.x,
                        cos_theta * p.z + k * n.z - n.y * p.x));
 }
