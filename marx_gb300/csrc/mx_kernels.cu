@@ -71,60 +71,88 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_trace_kernel(MxTables T, Tr
 // the frame-transfer streak of those detected, as _marx_acis_s_detect and
 // _marx_acis_i_detect order them (acis-s.c:230-236).  The trace leaves
 // these steps to this pass when the tables carry either.
-__global__ void __launch_bounds__(256) mx_acis_fef_kernel(MxTables T, TraceIO io, const uint64_t *seedp) {
+// Photon i is on a chip and still to be detected.
+__device__ __forceinline__ bool acis_pending(const TraceIO &io, uint32_t i) {
+  const int ccd = io.ccd[i];
+  const uint32_t f0 = io.flags ? io.flags[i] : 0u;
+  return ccd >= 0 && ccd <= 9 && !(f0 & (MX_BAD_PHOTON_MASK | MX_PHOTON_VARIATE_OVERRUN));
+}
+
+__device__ void acis_response(const MxTables &T, const TraceIO &io, uint32_t i, uint64_t seed, D3 off) {
   const size_t n = io.stride;
+  const int ccd = io.ccd[i];
+  Ph q;
+  q.e = io.energy[i];
+  q.t = io.t ? io.t[i] : 0.0;
+  q.flags = io.flags ? io.flags[i] : 0u;
+  q.ypix = io.ypix[i];
+  q.zpix = io.zpix[i];
+  Rng r;
+  r.U = io.U; r.N = io.N; r.seed = seed; r.n = io.n; r.i = i;
+  r.tag = io.tag ? io.tag[i] : i;
+  r.overrun = false;
+  r.window(MX_U_DETECT, 2, MX_N_DETECT, 2);
+  if (T.acis_qe && !acis_qe_accept(T, ccd, q, r)) {
+    if (io.flags) io.flags[i] = q.flags | MX_PHOTON_UNDETECTED;
+    return;
+  }
+  const int ub = r.upos, nb = r.npos;
+  int16_t pha = -1;
+  float pi = 0.0f;
+  bool ok = true;
+  if (T.acis_fef) {
+    r.window(MX_U_FEF, r.U ? 8 : 64, MX_N_FEF, r.N ? 4 : 64);
+    ok = acis_fef(T, ccd, q.ypix, q.zpix, q.e, r, pha, pi);
+  }
+  if (r.overrun) {
+    q.flags |= MX_PHOTON_VARIATE_OVERRUN;
+    atomicAdd(io.overrun, 1ull);
+  } else if (!ok) {
+    pha = -1; pi = 0.0f;
+    q.flags |= MX_PHOTON_UNDETECTED;
+  } else {
+    r.window(ub, MX_U_DETECT + 2 - ub, nb, MX_N_DETECT + 2 - nb);   // the ACIS window, after the QE draw
+    D3 x = mk(0, 0, 0), p = mk(0, 0, 0);
+    acis_streak(T, T.chips[ccd], q, x, p, r);
+    if (q.flags & MX_PHOTON_ACIS_STREAKED) {
+      x = x + off;
+      if (io.x) { io.x[i] = x.x; io.x[n + i] = x.y; io.x[2 * n + i] = x.z; }
+      io.p[i] = p.x; io.p[n + i] = p.y; io.p[2 * n + i] = p.z;
+      io.zpix[i] = q.zpix;
+    }
+  }
+  if (T.acis_fef) {
+    if (io.pha) io.pha[i] = pha;
+    if (io.pi) io.pi[i] = pi;
+  }
+  if (io.flags) io.flags[i] = q.flags;
+}
+
+// A fifth or less of the photons reach a chip, and each costs several
+// hundred FP64 operations here, so each block first gathers the indices of
+// pending photons from successive 256-photon tiles into shared memory and
+// works on them 256 at a time, every lane busy.
+__global__ void __launch_bounds__(256) mx_acis_fef_kernel(MxTables T, TraceIO io, const uint64_t *seedp) {
+  __shared__ uint32_t list[512];
+  __shared__ int count;
   const uint64_t seed = seedp ? *seedp : io.seed;
   const D3 off = mk(T.det_offset[0], T.det_offset[1], T.det_offset[2]);
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < io.n; i += gridDim.x * blockDim.x) {
-    const int ccd = io.ccd[i];
-    const uint32_t f0 = io.flags ? io.flags[i] : 0u;
-    if (ccd < 0 || ccd > 9 || (f0 & (MX_BAD_PHOTON_MASK | MX_PHOTON_VARIATE_OVERRUN))) continue;
-    Ph q;
-    q.e = io.energy[i];
-    q.t = io.t ? io.t[i] : 0.0;
-    q.flags = f0;
-    q.ypix = io.ypix[i];
-    q.zpix = io.zpix[i];
-    Rng r;
-    r.U = io.U; r.N = io.N; r.seed = seed; r.n = io.n; r.i = i;
-    r.tag = io.tag ? io.tag[i] : i;
-    r.overrun = false;
-    r.window(MX_U_DETECT, 2, MX_N_DETECT, 2);
-    if (T.acis_qe && !acis_qe_accept(T, ccd, q, r)) {
-      if (io.flags) io.flags[i] = q.flags | MX_PHOTON_UNDETECTED;
-      continue;
+  if (threadIdx.x == 0) count = 0;
+  __syncthreads();
+  for (uint32_t base = blockIdx.x * 256u; base < io.n; base += gridDim.x * 256u) {
+    const uint32_t i = base + threadIdx.x;
+    if (i < io.n && acis_pending(io, i)) list[atomicAdd(&count, 1)] = i;   // count stays below 512
+    __syncthreads();
+    const int c = count;
+    if (c >= 256) {
+      acis_response(T, io, list[c - 256 + threadIdx.x], seed, off);
+      __syncthreads();
+      if (threadIdx.x == 0) count = c - 256;
     }
-    const int ub = r.upos, nb = r.npos;
-    int16_t pha = -1;
-    float pi = 0.0f;
-    bool ok = true;
-    if (T.acis_fef) {
-      r.window(MX_U_FEF, r.U ? 8 : 64, MX_N_FEF, r.N ? 4 : 64);
-      ok = acis_fef(T, ccd, q.ypix, q.zpix, q.e, r, pha, pi);
-    }
-    if (r.overrun) {
-      q.flags |= MX_PHOTON_VARIATE_OVERRUN;
-      atomicAdd(io.overrun, 1ull);
-    } else if (!ok) {
-      pha = -1; pi = 0.0f;
-      q.flags |= MX_PHOTON_UNDETECTED;
-    } else {
-      r.window(ub, MX_U_DETECT + 2 - ub, nb, MX_N_DETECT + 2 - nb);   // the ACIS window, after the QE draw
-      D3 x = mk(0, 0, 0), p = mk(0, 0, 0);
-      acis_streak(T, T.chips[ccd], q, x, p, r);
-      if (q.flags & MX_PHOTON_ACIS_STREAKED) {
-        x = x + off;
-        if (io.x) { io.x[i] = x.x; io.x[n + i] = x.y; io.x[2 * n + i] = x.z; }
-        io.p[i] = p.x; io.p[n + i] = p.y; io.p[2 * n + i] = p.z;
-        io.zpix[i] = q.zpix;
-      }
-    }
-    if (T.acis_fef) {
-      if (io.pha) io.pha[i] = pha;
-      if (io.pi) io.pi[i] = pi;
-    }
-    if (io.flags) io.flags[i] = q.flags;
+    __syncthreads();
   }
+  const int c = count;
+  if ((int) threadIdx.x < c) acis_response(T, io, list[threadIdx.x], seed, off);
 }
 
 cudaError_t launch_acis_fef(const MxTables &T, const TraceIO &io, int grid, cudaStream_t st, const uint64_t *seed_dev) {
