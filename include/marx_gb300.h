@@ -229,6 +229,11 @@ const char *mx_last_error(const mx_context *ctx);  /* ctx may be NULL */
 int mx_trace(mx_context *ctx, const mx_photons *ph, uint32_t stages,
              const mx_variates *var, uint64_t seed, void *stream);
 
+/* With an ACIS FEF or (DetIdeal = no) ACIS contamination tables in the
+ * pack, every trace that runs the detector stage ends with one more launch:
+ * the ACIS response of the photons on a chip (QE x contamination
+ * acceptance, FEF pulse height and PI, frame-transfer streak). */
+
 /* Kernel organisation for mx_trace / mx_trace_host.  FUSED runs every stage
  * of a photon in one kernel; WAVEFRONT splits the mirror at its two conic
  * intersections into three kernels with survivor queues between them (the
@@ -263,7 +268,10 @@ int mx_trace_static(mx_context *ctx, const mx_photons *ph, uint32_t stages, cons
                     uint64_t seed, void *stream);
 
 /* Same trace on HOST buffers: copies inputs to the device, traces and
- * copies results back; blocks until done. */
+ * copies results back; blocks until done.  A list of 2^21 photons or more
+ * (tracing the mirror) is cut into chunks on several streams, so that the
+ * copies of one chunk overlap the trace of another (pinned host memory lets
+ * them run asynchronously); the results are those of one pass. */
 int mx_trace_host(mx_context *ctx, const mx_photons *host, uint32_t stages,
                   const mx_variates *host_var, uint64_t seed);
 

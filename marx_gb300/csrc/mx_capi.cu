@@ -235,7 +235,7 @@ int mx_trace_tables(mx_context *c, const MxTables &T, const mx_photons *ph, uint
 }  // extern "C"
 
 int mx_trace_queues(mx_context *c, const MxTables &T, const mx_photons *ph, uint32_t stages, const double *U,
-                    const double *N, uint64_t seed, cudaStream_t st, bool fresh, DevBuf &queues) {
+                    const double *N, uint64_t seed, cudaStream_t st, bool fresh, DevBuf &queues, bool force_wave) {
   if (!ph) return fail(c, MX_EINVAL, "mx_trace: null photon list");
   if (ph->n == 0) return MX_OK;
   if (!ph->energy || !ph->p) return fail(c, MX_EINVAL, "mx_trace: energy and p are required");
@@ -255,7 +255,7 @@ int mx_trace_queues(mx_context *c, const MxTables &T, const mx_photons *ph, uint
   io.overrun = c->d_overrun;
   int slots = U != nullptr;
   bool wave = (stages & MX_STAGE_MIRROR) &&
-              (c->mode == MX_MODE_WAVEFRONT || (c->mode == MX_MODE_AUTO && ph->n >= MX_WAVEFRONT_MIN_PHOTONS));
+              (c->mode == MX_MODE_WAVEFRONT || (c->mode == MX_MODE_AUTO && (force_wave || ph->n >= MX_WAVEFRONT_MIN_PHOTONS)));
   cudaError_t e;
   if (wave) {
     size_t qbytes = (size_t) ph->n * sizeof(MxRec);
@@ -369,7 +369,7 @@ static int trace_host_pipelined(mx_context *c, const mx_photons *h, uint32_t sta
     d.y_pixel = (float *) at(9); d.z_pixel = (float *) at(10); d.dither_state = (float *) at(11);
     d.support_orders = (int8_t *) at(12); d.pulse_height = (int16_t *) at(13); d.u_pixel = (float *) at(14);
     d.v_pixel = (float *) at(15); d.detector_region = (uint8_t *) at(16); d.pi = (float *) at(17);
-    int r = mx_trace_queues(c, c->T, &d, stages, dU, dN, seed, st, true, c->pipe_wave[j % MX_PIPE_STREAMS]);
+    int r = mx_trace_queues(c, c->T, &d, stages, dU, dN, seed, st, true, c->pipe_wave[j % MX_PIPE_STREAMS], true);
     if (r) return r;
     for (int k = 0; k < NC && e == cudaSuccess; k++) {
       if (!cols[k].host || !cols[k].out) continue;

@@ -54,7 +54,7 @@ struct mx_context {
   DevBuf pipe_wave[3];
 };
 #define MX_PIPE_STREAMS 3
-#define MX_PIPE_CHUNKS 8
+#define MX_PIPE_CHUNKS 16
 #define MX_PIPE_MIN_PHOTONS (2u << 20)
 
 // Record an error on the context (or as the creation error when c is null)
@@ -68,7 +68,10 @@ extern thread_local std::string g_create_err;
 // columns start from their defaults instead of being read.
 extern "C" __attribute__((visibility("hidden"))) int mx_trace_tables(mx_context *c, const MxTables &T, const mx_photons *ph, uint32_t stages,
                                const double *U, const double *N, uint64_t seed, cudaStream_t st, bool fresh);
-// The same with the wavefront queues in `queues` instead of the context's own.
+// The same with the wavefront queues in `queues` instead of the context's
+// own; force_wave: the wavefront kernels whatever the list's length (the
+// chunks of a list that one pass would trace with them).
 __attribute__((visibility("hidden"))) int mx_trace_queues(mx_context *c, const MxTables &T, const mx_photons *ph,
                                                           uint32_t stages, const double *U, const double *N,
-                                                          uint64_t seed, cudaStream_t st, bool fresh, DevBuf &queues);
+                                                          uint64_t seed, cudaStream_t st, bool fresh, DevBuf &queues,
+                                                          bool force_wave = false);
