@@ -482,6 +482,23 @@ const char *mx_write_error(void);   /* message of the last mx_write_photons fail
  * reference's stages set them. */
 uint32_t mx_output_history(const mx_config *cfg, uint32_t stages);
 
+/* MARX ray files (DumpToRayFile and the RAYFILE source, s-rayfile.c):
+ * a native-endian unsigned long magic 0xF8161961 and the history bits, then
+ * one Marx_Photon_Attr_Type record (marx.h:51-100, 136 bytes on LP64
+ * hosts) per photon.  mx_write_rayfile writes the photons without a
+ * MX_BAD_PHOTON_MASK bit with total_time added to their arrival times
+ * (marx_dump_to_rayfile, s-rayfile.c:109-155; the list itself is not
+ * changed); append != 0 adds records to an existing file.  mx_read_rayfile
+ * reads up to max records from byte *offset (0: from the start, after
+ * checking the header) into the host columns that are not NULL, subtracts
+ * *last_time from the arrival times and leaves there the last record's
+ * time, as rayfile_create_photons does (s-rayfile.c:188-219); *offset
+ * advances past what was read and *n_read is 0 at the end of the file.
+ * Host memory. */
+int mx_write_rayfile(const mx_photons *host, uint64_t history, const char *file, int append, double total_time);
+int mx_read_rayfile(const char *file, mx_photons *host, uint32_t max, uint64_t *offset, double *last_time,
+                    uint64_t *history, uint32_t *n_read);
+
 /* ------------------------------------------------ event coordinates --
  * The per-event columns marx2fits derives from an output directory
  * (marx/src/marx2fits.c), for the context's detector:

@@ -9,7 +9,9 @@
 // and the column count (0) at byte 24 -- followed by one big-endian value
 // per written photon.  Only photons without a MX_BAD_PHOTON_MASK bit are
 // written.  Appending adds rows to existing files and rewrites the count.
+#include <algorithm>
 #include <cerrno>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -98,9 +100,126 @@ void put_value(std::vector<unsigned char> &b, int c, const mx_photons *h, size_t
   }
 }
 
+// Marx_Photon_Attr_Type (marx.h:51-100) as an LP64 compiler lays it out:
+// the record of a ray file.
+struct RayRecord {
+  double energy, x[3], p[3], arrival_time;
+  uint32_t flags;
+  float y_pixel, z_pixel, u_pixel, v_pixel;
+  float dither[6];               // Marx_Dither_Type: ra, dec, roll, dy, dz, dtheta
+  float pi;
+  int16_t pulse_height;
+  uint32_t mirror_shell;
+  int8_t ccd_num, detector_region, order, support_orders[4];
+  uint32_t tag;
+};
+static_assert(sizeof(RayRecord) == 136, "ray-file record size");
+static_assert(offsetof(RayRecord, flags) == 64 && offsetof(RayRecord, dither) == 84 && offsetof(RayRecord, pi) == 108 &&
+                  offsetof(RayRecord, pulse_height) == 112 && offsetof(RayRecord, mirror_shell) == 116 &&
+                  offsetof(RayRecord, ccd_num) == 120 && offsetof(RayRecord, tag) == 128,
+              "ray-file record layout");
+const unsigned long kRayMagic = 0xF8161961UL;   // MARX_RAYFILE_MAGIC (marx.h:479)
+
 }  // namespace
 
 extern "C" {
+
+int mx_write_rayfile(const mx_photons *h, uint64_t history, const char *file, int append, double total_time) {
+  if (!h || !file) { g_err = "mx_write_rayfile: null argument"; return MX_EINVAL; }
+  if (h->stride && h->stride < h->n) { g_err = "mx_write_rayfile: stride below n"; return MX_EINVAL; }
+  FILE *f = fopen(file, append ? "ab" : "wb");
+  if (!f) { g_err = std::string("Unable to open ") + file + " for writing"; return MX_EINVAL; }
+  bool ok = true;
+  if (!append) {
+    unsigned long hdr[2] = {kRayMagic, (unsigned long) history};
+    ok = fwrite(hdr, sizeof(unsigned long), 2, f) == 2;
+  }
+  const size_t s = h->stride ? h->stride : h->n;
+  std::vector<RayRecord> buf;
+  buf.reserve(h->n);
+  for (size_t i = 0; i < h->n && ok; i++) {
+    if (h->flags && (h->flags[i] & MX_BAD_PHOTON_MASK)) continue;
+    RayRecord r;
+    memset(&r, 0, sizeof(r));
+    r.energy = h->energy ? h->energy[i] : 0.0;
+    for (int k = 0; k < 3; k++) {
+      r.x[k] = h->x ? h->x[k * s + i] : 0.0;
+      r.p[k] = h->p ? h->p[k * s + i] : 0.0;
+      r.dither[k] = h->dither_state ? h->dither_state[k * s + i] : 0.0f;
+    }
+    r.arrival_time = (h->arrival_time ? h->arrival_time[i] : 0.0) + total_time;
+    r.flags = h->flags ? h->flags[i] : 0u;
+    r.y_pixel = h->y_pixel ? h->y_pixel[i] : 0.0f;
+    r.z_pixel = h->z_pixel ? h->z_pixel[i] : 0.0f;
+    r.u_pixel = h->u_pixel ? h->u_pixel[i] : 0.0f;
+    r.v_pixel = h->v_pixel ? h->v_pixel[i] : 0.0f;
+    r.pi = h->pi ? h->pi[i] : 0.0f;
+    r.pulse_height = h->pulse_height ? h->pulse_height[i] : (int16_t) 0;
+    r.mirror_shell = h->mirror_shell ? (uint32_t) (int32_t) h->mirror_shell[i] : 0u;
+    r.ccd_num = h->ccd_num ? h->ccd_num[i] : (int8_t) 0;
+    r.detector_region = h->detector_region ? (int8_t) h->detector_region[i] : (int8_t) 0;
+    r.order = h->order ? h->order[i] : (int8_t) 0;
+    for (int k = 0; k < 4; k++) r.support_orders[k] = h->support_orders ? h->support_orders[k * s + i] : (int8_t) 0;
+    r.tag = h->tag ? h->tag[i] : 0u;
+    buf.push_back(r);
+  }
+  if (ok && !buf.empty()) ok = fwrite(buf.data(), sizeof(RayRecord), buf.size(), f) == buf.size();
+  if (fclose(f) != 0) ok = false;
+  if (!ok) { g_err = std::string("write to ") + file + " failed"; return MX_EINVAL; }
+  return MX_OK;
+}
+
+int mx_read_rayfile(const char *file, mx_photons *h, uint32_t max, uint64_t *offset, double *last_time,
+                    uint64_t *history, uint32_t *n_read) {
+  if (!file || !h || !offset || !last_time || !n_read) { g_err = "mx_read_rayfile: null argument"; return MX_EINVAL; }
+  *n_read = 0;
+  FILE *f = fopen(file, "rb");
+  if (!f) { g_err = std::string("Unable to open rayfile ") + file; return MX_EINVAL; }
+  unsigned long hdr[2];
+  if (fread(hdr, sizeof(unsigned long), 2, f) != 2 || hdr[0] != kRayMagic) {
+    fclose(f);
+    g_err = std::string("Magic number mismatch in rayfile ") + file;
+    return MX_EINVAL;
+  }
+  if (history) *history = hdr[1];
+  if (*offset == 0) *offset = sizeof(hdr);
+  if (fseek(f, (long) *offset, SEEK_SET) != 0) { fclose(f); g_err = "mx_read_rayfile: bad offset"; return MX_EINVAL; }
+  const size_t cap = h->n ? std::min<size_t>(max, h->n) : max;
+  std::vector<RayRecord> buf(cap);
+  const size_t got = cap ? fread(buf.data(), sizeof(RayRecord), cap, f) : 0;
+  fclose(f);
+  const size_t s = h->stride ? h->stride : h->n;
+  double t = 0.0;
+  for (size_t i = 0; i < got; i++) {
+    const RayRecord &r = buf[i];
+    t = r.arrival_time;
+    if (h->energy) h->energy[i] = r.energy;
+    for (int k = 0; k < 3; k++) {
+      if (h->x) h->x[k * s + i] = r.x[k];
+      if (h->p) h->p[k * s + i] = r.p[k];
+      if (h->dither_state) h->dither_state[k * s + i] = r.dither[k];
+    }
+    if (h->arrival_time) h->arrival_time[i] = r.arrival_time - *last_time;
+    if (h->flags) h->flags[i] = r.flags;
+    if (h->tag) h->tag[i] = r.tag;
+    if (h->mirror_shell) h->mirror_shell[i] = (int8_t) r.mirror_shell;
+    if (h->order) h->order[i] = r.order;
+    if (h->ccd_num) h->ccd_num[i] = r.ccd_num;
+    if (h->y_pixel) h->y_pixel[i] = r.y_pixel;
+    if (h->z_pixel) h->z_pixel[i] = r.z_pixel;
+    if (h->u_pixel) h->u_pixel[i] = r.u_pixel;
+    if (h->v_pixel) h->v_pixel[i] = r.v_pixel;
+    if (h->pi) h->pi[i] = r.pi;
+    if (h->pulse_height) h->pulse_height[i] = r.pulse_height;
+    if (h->detector_region) h->detector_region[i] = (uint8_t) r.detector_region;
+    if (h->support_orders)
+      for (int k = 0; k < 4; k++) h->support_orders[k * s + i] = r.support_orders[k];
+  }
+  if (got) *last_time = t;
+  *offset += got * sizeof(RayRecord);
+  *n_read = (uint32_t) got;
+  return MX_OK;
+}
 
 const char *mx_write_error(void) { return g_err.c_str(); }
 

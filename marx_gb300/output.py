@@ -56,6 +56,52 @@ def write_photons(ph: PhotonList, hist: int, write_mask: int, out_dir: str, appe
         raise RuntimeError("mx_write_photons: " + L.mx_write_error().decode())
 
 
+def _ray_lib():
+    L = _lib()
+    if not getattr(L, "_mx_ray_bound", False):
+        from .photons import MxPhotons
+        L.mx_write_rayfile.argtypes = [C.POINTER(MxPhotons), C.c_uint64, C.c_char_p, C.c_int, C.c_double]
+        L.mx_read_rayfile.argtypes = [C.c_char_p, C.POINTER(MxPhotons), C.c_uint32, C.POINTER(C.c_uint64),
+                                      C.POINTER(C.c_double), C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]
+        L._mx_ray_bound = True
+    return L
+
+
+def write_rayfile(ph: PhotonList, hist: int, path: str, append: bool = False, total_time: float = 0.0) -> None:
+    """MARX's ray file of the photons without a bad flag (mx_write_rayfile;
+    marx_dump_to_rayfile, marx/libsrc/s-rayfile.c:109-155)."""
+    L = _ray_lib()
+    s = ph.struct()
+    if L.mx_write_rayfile(C.byref(s), hist, path.encode(), 1 if append else 0, total_time) != 0:
+        raise RuntimeError("mx_write_rayfile: " + L.mx_write_error().decode())
+
+
+def read_rayfile(path: str, batch: int | None = None):
+    """The photons of a ray file as PhotonLists of at most `batch` photons
+    (all at once by default), with the RAYFILE source's arrival times: each
+    batch's times relative to the last photon of the batch before
+    (rayfile_create_photons, s-rayfile.c:188-219).  Returns (history, lists)."""
+    L = _ray_lib()
+    n_all = max(0, (os.path.getsize(path) - 2 * C.sizeof(C.c_ulong)) // 136)
+    batch = batch or max(1, n_all)
+    off, last, hist, got = C.c_uint64(0), C.c_double(0.0), C.c_uint64(0), C.c_uint32(0)
+    out = []
+    while True:
+        ph = PhotonList(batch)
+        s = ph.struct()
+        if L.mx_read_rayfile(path.encode(), C.byref(s), batch, C.byref(off), C.byref(last), C.byref(hist),
+                             C.byref(got)) != 0:
+            raise RuntimeError("mx_read_rayfile: " + L.mx_write_error().decode())
+        if got.value == 0:
+            break
+        q = PhotonList(got.value)
+        for k in vars(ph):
+            if k != "n":
+                setattr(q, k, np.ascontiguousarray(getattr(ph, k)[..., :got.value]))
+        out.append(q)
+    return hist.value, out
+
+
 def read_column(path: str):
     """(column name, values) of one column file."""
     b = open(path, "rb").read()

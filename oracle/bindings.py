@@ -208,6 +208,21 @@ class Reference:
             raise RuntimeError("reference trace: " + self.lib.mxref_last_error().decode())
         return self._to_list(ph, o), used, r
 
+    def dump_rayfile(self, ph: PhotonList, history: int, path: str, new: bool = True, total_time: float = 0.0):
+        """The reference's marx_dump_to_rayfile over ph (host columns)."""
+        c = lambda a, dt: np.ascontiguousarray(a, dtype=dt)
+        f = self.lib.mxref_dump_rayfile
+        f.argtypes = [C.c_char_p, C.c_int] + [C.c_void_p] * 18 + [C.c_ulong, C.c_int, C.c_double]
+        cols = [c(ph.energy, np.float64), c(ph.x, np.float64), c(ph.p, np.float64), c(ph.arrival_time, np.float64),
+                c(ph.flags, np.uint32), c(ph.tag, np.uint32), c(ph.mirror_shell, np.int8), c(ph.order, np.int8),
+                c(ph.ccd_num, np.int8), c(ph.y_pixel, np.float32), c(ph.z_pixel, np.float32),
+                c(ph.dither_state, np.float32), c(ph.support_orders, np.int8), c(ph.pulse_height, np.int16),
+                c(ph.u_pixel, np.float32), c(ph.v_pixel, np.float32), c(ph.detector_region, np.uint8),
+                c(ph.pi, np.float32)]
+        r = f(path.encode(), ph.n, *[_p(a) for a in cols], history, 1 if new else 0, total_time)
+        if r != 0:
+            raise RuntimeError("reference ray-file writer failed: " + self.lib.mxref_last_error().decode())
+
     def write_photons(self, ph: PhotonList, history: int, write_mask: int, out_dir: str, new: bool = True,
                       total_time: float = 0.0):
         """The reference's marx_write_photons over ph (host columns)."""

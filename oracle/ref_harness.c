@@ -546,6 +546,47 @@ int mxref_write_photons(const char *dir, int n, const double *energy, const doub
    return r;
 }
 
+/* The reference's ray-file writer (marx_dump_to_rayfile, s-rayfile.c:109-155)
+ * over the same columns, with PI. */
+int mxref_dump_rayfile(const char *file, int n, const double *energy, const double *x, const double *p,
+                       const double *t, const unsigned int *flags, const unsigned int *tag,
+                       const signed char *shell, const signed char *order, const signed char *ccd,
+                       const float *ypix, const float *zpix, const float *dith, const signed char *sup,
+                       const short *pha, const float *upix, const float *vpix, const unsigned char *region,
+                       const float *pi, unsigned long history, int new_file, double total_time)
+{
+   Marx_Photon_Type *pt;
+   int i, k, r;
+
+   if (NULL == (pt = marx_alloc_photon_type((unsigned int) (n > 0 ? n : 1)))) return -1;
+   for (i = 0; i < n; i++)
+     {
+        Marx_Photon_Attr_Type *at = pt->attributes + i;
+        memset(at, 0, sizeof(*at));
+        at->energy = energy[i];
+        at->x.x = x[i]; at->x.y = x[n + i]; at->x.z = x[2 * n + i];
+        at->p.x = p[i]; at->p.y = p[n + i]; at->p.z = p[2 * n + i];
+        at->arrival_time = t[i];
+        at->flags = flags[i];
+        at->tag = tag[i];
+        at->mirror_shell = (unsigned int) shell[i];
+        at->order = order[i];
+        at->ccd_num = ccd[i];
+        at->y_pixel = ypix[i]; at->z_pixel = zpix[i];
+        at->dither_state.ra = dith[i]; at->dither_state.dec = dith[n + i]; at->dither_state.roll = dith[2 * n + i];
+        for (k = 0; k < 4; k++) at->support_orders[k] = sup[k * n + i];
+        at->pulse_height = pha[i];
+        at->u_pixel = upix[i]; at->v_pixel = vpix[i];
+        at->detector_region = (SIGNED_CHAR) region[i];
+        at->pi = pi[i];
+     }
+   pt->n_photons = (unsigned int) n;
+   pt->history = history;
+   r = marx_dump_to_rayfile((char *) file, new_file, pt, total_time);
+   marx_dealloc_photon_type(pt);
+   return r;
+}
+
 /* ------------------------------------------------------------ sources -- */
 /* The reference's source models (marx_create_source, source.c:388-420, and
  * the create_photons functions of s-*.c) for the parameters of the last
