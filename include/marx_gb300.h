@@ -47,6 +47,12 @@ extern "C" {
 #define MX_PHOTON_ACIS_STREAKED     0x200u
 /* Engine-only bit: a stage ran out of pre-drawn variate slots. */
 #define MX_PHOTON_VARIATE_OVERRUN   0x10000u
+/* Engine-only bit inside the bad mask: with DitherModel FILE the photon's
+ * time is at or past the aspect solution's last row.  The reference stops
+ * dithering there and drops the photon and every later one from its batch
+ * (get_aspsol_point, dither.c:303-306 and _marx_dither_photons, :646-656);
+ * the engine flags it and later stages skip it. */
+#define MX_PHOTON_ASPECT_END        0x80u
 
 /* Stage mask for mx_trace. */
 #define MX_STAGE_DITHER   0x1u   /* _marx_dither_photons (dither.c:630)   */
@@ -90,7 +96,7 @@ extern "C" {
 enum { MX_GRATING_NONE = 0, MX_GRATING_HETG = 1, MX_GRATING_LETG = 2 };
 enum { MX_DETECTOR_NONE = 0, MX_DETECTOR_ACIS_I = 1, MX_DETECTOR_ACIS_S = 2, MX_DETECTOR_HRC_I = 3,
        MX_DETECTOR_HRC_S = 4 };
-enum { MX_DITHER_NONE = 0, MX_DITHER_INTERNAL = 1 };
+enum { MX_DITHER_NONE = 0, MX_DITHER_INTERNAL = 1, MX_DITHER_FILE = 2 };   /* DitherModel NONE, INTERNAL, FILE */
 
 /* Simulation parameters.  Names follow marx.par; units are marx.par's. */
 typedef struct mx_config {
@@ -194,6 +200,8 @@ typedef struct mx_photons {
   float    *v_pixel;
   uint8_t  *detector_region; /* HRC-S UV/ion shield region */
   float    *pi;            /* ACIS PI energy (keV) from the FEF (Marx_Photon_Attr_Type.pi, b_energy.dat) */
+  float    *det_dither;    /* 3n: dy, dz (mm), dtheta (rad): the detector's motion of Marx_Dither_Type,
+                              written by the dither stage (zero unless DitherModel is FILE) */
 } mx_photons;
 
 /* Pre-drawn variates (device pointers for mx_trace).  When both are NULL
@@ -307,6 +315,27 @@ typedef struct mx_source {
 } mx_source;
 enum { MX_SOURCE_POINT = 0, MX_SOURCE_GAUSS = 1, MX_SOURCE_BETA = 2, MX_SOURCE_DISK = 3, MX_SOURCE_LINE = 4,
        MX_SOURCE_IMAGE = 5 };
+
+/* DitherModel = FILE (init_aspsol_dither and get_single_aspsol_point,
+ * dither.c:282-500): the rows of the aspect solution's ASPSOL table, n x 7
+ * row-major (time (s), ra, dec, roll (deg), dy, dz (mm), dtheta (deg)) in
+ * the file's order, with its RA_NOM, DEC_NOM, ROLL_NOM (deg) and TSTART (s)
+ * keywords.  Each row is converted as the reference converts it (ra, dec
+ * rolled into offsets from the nominal pointing; times relative to TSTART,
+ * the first row's taken off twice as init_aspsol_dither does) and the table
+ * kept on the device for the configuration's dither stage, which must be
+ * MX_DITHER_FILE.  A photon at time t (start_time + arrival time) takes the
+ * linear interpolation between the last row at or before t and the next one
+ * (get_aspsol_dither, :350-371); the detector stages move the detector by
+ * that row's dy, dz, dtheta (_marx_dither_detector, detector.c:275-284).
+ * record_only: the rays are already dithered (_MARX_DITHER_RECORD_ONLY):
+ * the state is recorded and the aspect blur applied, the pointing not moved.
+ * The configuration's ra_nom, dec_nom and roll_nom should carry the file's
+ * keywords, as init_aspsol_dither overrides the parameter file's.  n = 0
+ * removes the table.  Times must not decrease along the photon list for the
+ * result to equal the reference's forward-only reader. */
+int mx_set_aspect_solution(mx_context *ctx, const double *rows, uint32_t n, double ra_nom, double dec_nom,
+                           double roll_nom, double tstart, int record_only);
 
 /* The direction of travel p of the photons of a source at (ra, dec)
  * (degrees) for the configuration's pointing (RA_Nom, Dec_Nom, Roll_Nom,

@@ -11,7 +11,7 @@ import os
 import numpy as np
 
 from .config import MxConfig
-from .photons import COLUMNS, MxPhotons, MxVariates, PhotonList, NUM_U, NUM_N
+from .photons import COLUMNS, OPTIONAL_COLUMNS, MxPhotons, MxVariates, PhotonList, NUM_U, NUM_N
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libmarx_gb300.so")
@@ -52,6 +52,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.mx_overrun_count.argtypes = [C.c_void_p, C.POINTER(C.c_ulonglong), C.c_int]
     L.mx_probe_fp64.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.mx_set_trace_mode.argtypes = [C.c_void_p, C.c_int]
+    L.mx_set_aspect_solution.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_double, C.c_double, C.c_double,
+                                         C.c_double, C.c_int]
     _lib = L
     return L
 
@@ -59,7 +61,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
 class DevicePhotons:
     """Photon list resident on the GPU: one torch tensor per column."""
 
-    def __init__(self, n: int, device="cuda"):
+    def __init__(self, n: int, device="cuda", det_dither: bool = False):
         import torch
         self.n = int(n)
         tmap = {np.float64: torch.float64, np.float32: torch.float32, np.uint32: torch.int32,
@@ -67,6 +69,7 @@ class DevicePhotons:
         for k, (dt, m) in COLUMNS.items():
             shape = (m, self.n) if m > 1 else (self.n,)
             setattr(self, k, torch.zeros(shape, dtype=tmap[dt], device=device))
+        self.det_dither = torch.zeros((3, self.n), dtype=torch.float32, device=device) if det_dither else None
         self.ccd_num.fill_(-1)
 
     @classmethod
@@ -79,6 +82,8 @@ class DevicePhotons:
             if a.dtype == np.uint32:
                 a = a.view(np.int32)
             setattr(d, k, torch.from_numpy(np.ascontiguousarray(a)).to(device))
+        dd = getattr(ph, "det_dither", None)
+        d.det_dither = None if dd is None else torch.from_numpy(np.ascontiguousarray(dd)).to(device)
         return d
 
     def to_host(self) -> PhotonList:
@@ -87,12 +92,14 @@ class DevicePhotons:
         for k, (dt, m) in COLUMNS.items():
             a = getattr(self, k).cpu().numpy()
             setattr(q, k, a.view(dt) if a.dtype != dt else a)
+        dd = getattr(self, "det_dither", None)
+        q.det_dither = None if dd is None else dd.cpu().numpy()
         return q
 
     def struct(self) -> MxPhotons:
         s = MxPhotons()
         s.n = self.n
-        for k in COLUMNS:
+        for k in list(COLUMNS) + list(OPTIONAL_COLUMNS):
             t = getattr(self, k, None)
             if t is None:
                 continue
@@ -124,6 +131,18 @@ class Engine:
     def _check(self, r):
         if r != 0:
             raise RuntimeError(f"marx_gb300 error {r}: " + self.lib.mx_last_error(self.h).decode())
+
+    def set_aspect_solution(self, asp, record_only: bool = False):
+        """DitherModel FILE: the aspect solution (an ``AspectSolution``, see
+        ``marx_gb300.aspsol``) for the dither and detector stages
+        (mx_set_aspect_solution); None removes it."""
+        if asp is None:
+            self._check(self.lib.mx_set_aspect_solution(self.h, None, 0, 0.0, 0.0, 0.0, 0.0, 0))
+            return
+        rows = np.ascontiguousarray(asp.rows, dtype=np.float64)
+        assert rows.ndim == 2 and rows.shape[1] == 7
+        self._check(self.lib.mx_set_aspect_solution(self.h, rows.ctypes.data, rows.shape[0], asp.ra_nom, asp.dec_nom,
+                                                    asp.roll_nom, asp.tstart, 1 if record_only else 0))
 
     def set_mode(self, mode: int):
         """MODE_AUTO, MODE_FUSED or MODE_WAVEFRONT (include/marx_gb300.h)."""

@@ -16,7 +16,7 @@ DETECTOR = {"NONE": 0, "ACIS-I": 1, "ACIS-S": 2, "HRC-I": 3, "HRC-S": 4}
 # HRC blur parameter suffixes, in the order of mx_config.hrc_*_blur
 HRC_BLUR = ("G1FWHM", "G1Xctr", "G1Yctr", "G1Amp", "G2FWHM", "G2Xctr", "G2Yctr", "G2Amp",
             "L1FWHM", "L1Xctr", "L1Yctr", "L1Amp", "L1Rmax")
-DITHER = {"NONE": 0, "INTERNAL": 1}
+DITHER = {"NONE": 0, "INTERNAL": 1, "FILE": 2}
 
 
 class MxConfig(C.Structure):

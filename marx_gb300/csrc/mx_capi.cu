@@ -76,6 +76,10 @@ static int upload_model(mx_context *c) {
   c->T.fef_f = (const float *) (b + o_ff);
   c->T.fef_slope = (const double *) (b + o_fs);
   c->T.contam = (const MxContamDev *) (b + o_co);
+  c->T.asp_t = (const double *) c->asp.ptr;
+  c->T.asp_v = c->asp.ptr ? (const double *) c->asp.ptr + ((c->asp_n + 1 + 7) & ~7u) : nullptr;
+  c->T.asp_n = c->asp_n;
+  c->T.asp_record_only = c->asp_record_only;
   c->shared_bytes = trace_shared_bytes(c->T);
   if (c->shared_bytes > 200 * 1024) return fail(c, MX_ERANGE, "tables exceed the shared-memory budget");
   return MX_OK;
@@ -195,6 +199,7 @@ void mx_destroy(mx_context *c) {
   c->scan.release();
   c->wave.release();
   c->spec.release();
+  c->asp.release();
   c->ev_tab.release();
   c->ev_scan.release();
   c->ev_io.release();
@@ -211,6 +216,35 @@ void mx_destroy(mx_context *c) {
 const char *mx_last_error(const mx_context *c) { return c ? c->err.c_str() : g_create_err.c_str(); }
 
 void *mx_stream(mx_context *c) { return c ? (void *) c->stream : nullptr; }
+
+int mx_set_aspect_solution(mx_context *c, const double *rows, uint32_t n, double ra_nom, double dec_nom,
+                           double roll_nom, double tstart, int record_only) {
+  if (!c) return MX_EINVAL;
+  if (n && !rows) return fail(c, MX_EINVAL, "mx_set_aspect_solution: null rows");
+  cudaStreamSynchronize(c->stream);
+  if (n == 0) {
+    c->asp.release();
+    c->asp_n = 0;
+  } else {
+    // times, padded to a multiple of 8 doubles, then the rows of 8 values
+    const size_t nt = ((size_t) n + 1 + 7) & ~(size_t) 7;
+    std::vector<double> h(nt + 8 * ((size_t) n + 1), 0.0);
+    int r = mx_aspsol_convert(rows, n, ra_nom, dec_nom, roll_nom, tstart, h.data(), h.data() + nt);
+    if (r) return fail(c, r, "mx_set_aspect_solution: bad arguments");
+    for (uint32_t i = 2; i <= n; i++)   // row 1 carries TSTART twice over
+      if (!(h[i] >= h[i - 1])) return fail(c, MX_EINVAL, "mx_set_aspect_solution: times decrease");
+    cudaError_t e = c->asp.ensure(h.size() * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpy(c->asp.ptr, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(c, e, "uploading the aspect solution");
+    c->asp_n = n;
+  }
+  c->asp_record_only = record_only ? 1 : 0;
+  c->T.asp_t = (const double *) c->asp.ptr;
+  c->T.asp_v = c->asp.ptr ? (const double *) c->asp.ptr + (((size_t) c->asp_n + 1 + 7) & ~(size_t) 7) : nullptr;
+  c->T.asp_n = c->asp_n;
+  c->T.asp_record_only = c->asp_record_only;
+  return MX_OK;
+}
 
 int mx_table_bytes(const mx_context *c, size_t *shared_bytes, size_t *global_bytes) {
   if (!c) return MX_EINVAL;
@@ -241,7 +275,8 @@ int mx_trace_queues(mx_context *c, const MxTables &T, const mx_photons *ph, uint
   if (!ph->energy || !ph->p) return fail(c, MX_EINVAL, "mx_trace: energy and p are required");
   if ((U == nullptr) != (N == nullptr)) return fail(c, MX_EINVAL, "mx_trace: give both U and N or neither");
   if ((stages & MX_STAGE_DETECT) && T.nchips && (!ph->x)) return fail(c, MX_EINVAL, "mx_trace: x is required");
-  if (ph->n == 0) return MX_OK;
+  if ((stages & (MX_STAGE_DITHER | MX_STAGE_DETECT)) && T.dither_file && T.asp_n == 0)
+    return fail(c, MX_EINVAL, "mx_trace: DitherModel FILE needs mx_set_aspect_solution");
   TraceIO io;
   io.energy = ph->energy; io.x = ph->x; io.p = ph->p; io.t = ph->arrival_time; io.flags = ph->flags;
   io.tag = ph->tag; io.shell = ph->mirror_shell; io.order = ph->order; io.ccd = ph->ccd_num;
@@ -249,6 +284,7 @@ int mx_trace_queues(mx_context *c, const MxTables &T, const mx_photons *ph, uint
   io.support = ph->support_orders; io.pha = ph->pulse_height; io.upix = ph->u_pixel; io.vpix = ph->v_pixel;
   io.region = ph->detector_region;
   io.pi = ph->pi;
+  io.ddith = ph->det_dither;
   io.U = U; io.N = N; io.n = ph->n; io.seed = seed; io.stages = stages; io.fresh = fresh ? 1 : 0;
   io.stride = ph->stride ? ph->stride : ph->n;
   if (io.stride < io.n) return fail(c, MX_EINVAL, "mx_trace: stride below n");
@@ -291,16 +327,17 @@ int mx_trace(mx_context *c, const mx_photons *ph, uint32_t stages, const mx_vari
 // The host columns of mx_trace_host: pointer, element size, components,
 // copied in, copied out.
 struct HostCol { const void *host; size_t elem; int comps; bool in, out; };
-static int host_columns(const mx_photons *h, HostCol cols[18]) {
-  const HostCol c[18] = {
+static int host_columns(const mx_photons *h, HostCol cols[19]) {
+  const HostCol c[19] = {
       {h->energy, 8, 1, true, false},     {h->x, 8, 3, false, true},         {h->p, 8, 3, true, true},
       {h->arrival_time, 8, 1, true, false}, {h->flags, 4, 1, true, true},   {h->tag, 4, 1, true, false},
       {h->mirror_shell, 1, 1, false, true}, {h->order, 1, 1, false, true},   {h->ccd_num, 1, 1, false, true},
       {h->y_pixel, 4, 1, false, true},    {h->z_pixel, 4, 1, false, true},   {h->dither_state, 4, 3, false, true},
       {h->support_orders, 1, 4, false, true}, {h->pulse_height, 2, 1, false, true}, {h->u_pixel, 4, 1, false, true},
-      {h->v_pixel, 4, 1, false, true},    {h->detector_region, 1, 1, false, true}, {h->pi, 4, 1, false, true}};
-  for (int k = 0; k < 18; k++) cols[k] = c[k];
-  return 18;
+      {h->v_pixel, 4, 1, false, true},    {h->detector_region, 1, 1, false, true}, {h->pi, 4, 1, false, true},
+      {h->det_dither, 4, 3, false, true}};
+  for (int k = 0; k < 19; k++) cols[k] = c[k];
+  return 19;
 }
 
 // mx_trace_host for a large list: MX_PIPE_CHUNKS chunks of consecutive
@@ -314,13 +351,13 @@ static int host_columns(const mx_photons *h, HostCol cols[18]) {
 static int trace_host_pipelined(mx_context *c, const mx_photons *h, uint32_t stages, const mx_variates *hv,
                                 uint64_t seed) {
   const size_t n = h->n;
-  HostCol cols[18];
+  HostCol cols[19];
   const int NC = host_columns(h, cols);
   cudaError_t e = cudaSuccess;
   for (int s = 0; s < MX_PIPE_STREAMS && e == cudaSuccess; s++)
     if (!c->pipe[s]) e = cudaStreamCreateWithFlags(&c->pipe[s], cudaStreamNonBlocking);
   if (e != cudaSuccess) return cuda_fail(c, e, "creating the copy-overlap streams");
-  char *dev[18];
+  char *dev[19];
   for (int k = 0; k < NC; k++) {
     dev[k] = nullptr;
     if (!cols[k].host) continue;
@@ -369,6 +406,7 @@ static int trace_host_pipelined(mx_context *c, const mx_photons *h, uint32_t sta
     d.y_pixel = (float *) at(9); d.z_pixel = (float *) at(10); d.dither_state = (float *) at(11);
     d.support_orders = (int8_t *) at(12); d.pulse_height = (int16_t *) at(13); d.u_pixel = (float *) at(14);
     d.v_pixel = (float *) at(15); d.detector_region = (uint8_t *) at(16); d.pi = (float *) at(17);
+    d.det_dither = (float *) at(18);
     int r = mx_trace_queues(c, c->T, &d, stages, dU, dN, seed, st, true, c->pipe_wave[j % MX_PIPE_STREAMS], true);
     if (r) return r;
     for (int k = 0; k < NC && e == cudaSuccess; k++) {
@@ -392,14 +430,15 @@ int mx_trace_host(mx_context *c, const mx_photons *h, uint32_t stages, const mx_
   if (!h->energy || !h->p) return fail(c, MX_EINVAL, "mx_trace_host: energy and p are required");
   if (h->stride && h->stride != h->n) return fail(c, MX_EINVAL, "mx_trace_host: host lists must be contiguous (stride 0 or n)");
   struct Col { const void *host; size_t elem; int comps; bool in, out; };
-  const int NC = 18;
+  const int NC = 19;
   const Col cols[NC] = {
       {h->energy, 8, 1, true, false},     {h->x, 8, 3, false, true},         {h->p, 8, 3, true, true},
       {h->arrival_time, 8, 1, true, false}, {h->flags, 4, 1, true, true},   {h->tag, 4, 1, true, false},
       {h->mirror_shell, 1, 1, false, true}, {h->order, 1, 1, false, true},   {h->ccd_num, 1, 1, false, true},
       {h->y_pixel, 4, 1, false, true},    {h->z_pixel, 4, 1, false, true},   {h->dither_state, 4, 3, false, true},
       {h->support_orders, 1, 4, false, true}, {h->pulse_height, 2, 1, false, true}, {h->u_pixel, 4, 1, false, true},
-      {h->v_pixel, 4, 1, false, true},    {h->detector_region, 1, 1, false, true}, {h->pi, 4, 1, false, true}};
+      {h->v_pixel, 4, 1, false, true},    {h->detector_region, 1, 1, false, true}, {h->pi, 4, 1, false, true},
+      {h->det_dither, 4, 3, false, true}};
   if (n >= MX_PIPE_MIN_PHOTONS && (stages & MX_STAGE_MIRROR)) return trace_host_pipelined(c, h, stages, hv, seed);
   void *dev[NC];
   cudaStream_t st = c->stream;
@@ -430,6 +469,7 @@ int mx_trace_host(mx_context *c, const mx_photons *h, uint32_t stages, const mx_
   d.y_pixel = (float *) dev[9]; d.z_pixel = (float *) dev[10]; d.dither_state = (float *) dev[11];
   d.support_orders = (int8_t *) dev[12]; d.pulse_height = (int16_t *) dev[13]; d.u_pixel = (float *) dev[14];
   d.v_pixel = (float *) dev[15]; d.detector_region = (uint8_t *) dev[16]; d.pi = (float *) dev[17];
+  d.det_dither = (float *) dev[18];
   int r = mx_trace_tables(c, c->T, &d, stages, dU, dN, seed, st, true);
   if (r) return r;
   for (int k = 0; k < NC; k++) {

@@ -35,7 +35,7 @@ struct mx_context {
   size_t shared_bytes = 0;
   int trace_blocks[2] = {0, 0};   // resident blocks per SM for the slot / Philox kernels
   cudaStream_t stream = nullptr;
-  DevBuf io[20];           // staging for mx_trace_host: 18 columns, U, N
+  DevBuf io[22];           // staging for mx_trace_host: 19 columns, U, N
   DevBuf scan;             // compaction block counts
   DevBuf wave;             // wavefront record queues
   DevBuf spec;             // FILE spectrum of the last mx_generate_source call
@@ -52,6 +52,10 @@ struct mx_context {
   // copies in, kernels and copies out of different chunks overlap
   cudaStream_t pipe[3] = {nullptr, nullptr, nullptr};
   DevBuf pipe_wave[3];
+  // DitherModel FILE: the converted aspect solution (mx_set_aspect_solution)
+  DevBuf asp;
+  uint32_t asp_n = 0;
+  int asp_record_only = 0;
 };
 #define MX_PIPE_STREAMS 3
 #define MX_PIPE_CHUNKS 16
@@ -75,3 +79,9 @@ __attribute__((visibility("hidden"))) int mx_trace_queues(mx_context *c, const M
                                                           uint32_t stages, const double *U, const double *N,
                                                           uint64_t seed, cudaStream_t st, bool fresh, DevBuf &queues,
                                                           bool force_wave = false);
+
+// The rows of an ASPSOL table converted as the reference's reader converts
+// them (mx_source.cpp): out is (n + 1) x 8, row 0 the reader's zero start
+// state; times go to out_t (n + 1).
+int mx_aspsol_convert(const double *rows, uint32_t n, double ra_nom, double dec_nom, double roll_nom, double tstart,
+                      double *out_t, double *out_v);

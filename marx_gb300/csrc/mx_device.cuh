@@ -742,21 +742,55 @@ MXD D3 rotate_x(D3 p, double c, double s) {
   return normalized_unit(mk(c * p.x + p.x * (1.0 - c), c * p.y - s * p.z, c * p.z + s * p.y));
 }
 
-// get_internal_dither + dither_ray + apply_dither (dither.c:167-182,
-// 551-581, 609-628).  The dither angles pass through float as they do in
-// Marx_Dither_Type.
+// get_aspsol_point + get_aspsol_dither (dither.c:342-371) at time t
+// (start_time + arrival time): the rows j - 1, j around t, j the first row
+// later than t as the forward reader leaves them, interpolated linearly and
+// stored in float as Marx_Dither_Type holds them (ra, dec, roll, dy, dz,
+// dtheta).  False when no row is later than t: the reader has run off the
+// end of the file.
+MXD bool aspsol_state(const MxTables &T, double t, float s[6]) {
+  const uint32_t n = T.asp_n;
+  if (n == 0 || !(t < T.asp_t[n])) return false;
+  uint32_t lo = 1, hi = n;   // asp_t[hi] > t
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (T.asp_t[mid] > t) hi = mid; else lo = mid + 1;
+  }
+  const double t0 = T.asp_t[lo - 1], t1 = T.asp_t[lo];
+  double dt = MX_DADD(t1, -t0);
+  if (dt != 0) dt = MX_DDIV(MX_DADD(t, -t0), dt);
+  const double *a = T.asp_v + 8 * (size_t) (lo - 1), *b = a + 8;
+  for (int k = 0; k < 6; k++) s[k] = (float) MX_DADD(a[k], MX_DMUL(dt, MX_DADD(b[k], -a[k])));
+  return true;
+}
+
+// get_internal_dither / get_aspsol_dither + dither_ray + apply_dither
+// (dither.c:167-182, 350-389, 551-581, 609-628).  The dither angles pass
+// through float as they do in Marx_Dither_Type.
 MXD void dither_stage(const MxTables &T, Ph &ph, Rng &rng) {
   rng.window(0, 0, MX_N_DITHER, 2);
-  double t = (2.0 * PI) * (T.start_time + ph.t);
-  // A zero amplitude makes amp * sin(...) zero whatever the sine; skip it.
-  double v[3];
-  for (int k = 0; k < 3; k++)
-    v[k] = T.dith_amp[k] != 0.0 ? T.dith_amp[k] * sin(div_by(t, T.dith_period[k], T.dith_inv_period[k]) +
-                                                      T.dith_phase[k]) : 0.0;
-  float fra = (float) v[0];
-  float fdec = (float) v[1];
-  float froll = (float) (T.nominal_roll + v[2]);
-  ph.dith[0] = fra; ph.dith[1] = fdec; ph.dith[2] = froll;
+  float fra, fdec, froll;
+  if (T.dither_file) {
+    float s[6];
+    if (!aspsol_state(T, T.start_time + ph.t, s)) { ph.flags |= MX_PHOTON_ASPECT_END; return; }
+    ph.dith[0] = s[0]; ph.dith[1] = s[1]; ph.dith[2] = s[2];
+    // record only (get_aspsol_dither_record_only, :404-418): the rays are
+    // already dithered; the aspect blur still applies
+    fra = T.asp_record_only ? 0.0f : s[0];
+    fdec = T.asp_record_only ? 0.0f : s[1];
+    froll = T.asp_record_only ? 0.0f : s[2];
+  } else {
+    double t = (2.0 * PI) * (T.start_time + ph.t);
+    // A zero amplitude makes amp * sin(...) zero whatever the sine; skip it.
+    double v[3];
+    for (int k = 0; k < 3; k++)
+      v[k] = T.dith_amp[k] != 0.0 ? T.dith_amp[k] * sin(div_by(t, T.dith_period[k], T.dith_inv_period[k]) +
+                                                        T.dith_phase[k]) : 0.0;
+    fra = (float) v[0];
+    fdec = (float) v[1];
+    froll = (float) (T.nominal_roll + v[2]);
+    ph.dith[0] = fra; ph.dith[1] = fdec; ph.dith[2] = froll;
+  }
   double ra = f2d(fra) + T.aspect_blur * rng.normal();
   double dec = f2d(fdec) + T.aspect_blur * rng.normal();
   // roll about the x axis (JDMv_rotate_unit_vector with n = x); a fixed
@@ -996,6 +1030,44 @@ MXD int chip_screen(const MxChipDev &g, float x0, float x1, float x2, float p0, 
   return 1;
 }
 
+// The detector frame of a photon: _marx_dither_detector then
+// _marx_transform_ray (detector.c:244-284, trans.c:40-77).  DetOffset plus,
+// with DitherModel FILE, the aspect solution's dy, dz at the photon's time,
+// and a rotation by its dtheta about x (rotate_matrix of the identity: rows
+// (1,0,0), (0,c,s), (0,-s,c)).  The reference moves one global matrix there
+// and back per photon; here each photon has its own.
+struct DetFrame { D3 off; double c, s; };
+MXD DetFrame det_frame(const MxTables &T, double t) {
+  DetFrame f;
+  f.off = mk(T.det_offset[0], T.det_offset[1], T.det_offset[2]);
+  f.c = 1.0; f.s = 0.0;
+  float s[6];
+  if (T.dither_file && aspsol_state(T, T.start_time + t, s)) {
+    f.off.y = T.det_offset[1] + f2d(s[3]);
+    f.off.z = T.det_offset[2] + f2d(s[4]);
+    const double th = f2d(s[5]);
+    if (th != 0.0) sincos_small(th, &f.s, &f.c);
+  }
+  return f;
+}
+// rotate_vector and rotate_vector_inv (trans.c:40-66) with that matrix;
+// the x row is the identity's.
+MXD D3 det_rotate(const DetFrame &f, D3 v) {
+  return mk(v.x, MX_DADD(MX_DMUL(f.c, v.y), MX_DMUL(f.s, v.z)), MX_DADD(MX_DMUL(-f.s, v.y), MX_DMUL(f.c, v.z)));
+}
+MXD D3 det_rotate_inv(const DetFrame &f, D3 v) {
+  return mk(v.x, MX_DADD(MX_DMUL(f.c, v.y), MX_DMUL(-f.s, v.z)), MX_DADD(MX_DMUL(f.s, v.y), MX_DMUL(f.c, v.z)));
+}
+// into the frame: x - offset, then rotated (T.dither_file only)
+MXD void det_enter(const MxTables &T, const DetFrame &f, D3 &x, D3 &p) {
+  x = x - f.off;
+  if (T.dither_file) { x = det_rotate(f, x); p = det_rotate(f, p); }
+}
+MXD void det_leave(const MxTables &T, const DetFrame &f, D3 &x, D3 &p) {
+  if (T.dither_file) { p = det_rotate_inv(f, p); x = det_rotate_inv(f, x); }
+  x = x + f.off;
+}
+
 // _marx_acis_i_detect / _marx_acis_s_detect per photon (acis-i.c:124-157,
 // acis-s.c:203-239), _marx_intersect_with_detector (detector.c:112-168),
 // _marx_acis_apply_streak (acis-i.c:60-93).  QE and pulse height are not
@@ -1194,8 +1266,9 @@ MXD bool acis_fef(const MxTables &T, int ccd, float x, float y, double energy, R
 
 MXD void detect_stage(const MxTables &T, const MxChipDev *chips, int nchips, Ph &ph, Rng &rng) {
   rng.window(MX_U_DETECT, 2, MX_N_DETECT, 2);
-  D3 off = mk(T.det_offset[0], T.det_offset[1], T.det_offset[2]);
-  D3 x = ph.x - off, p = ph.p;
+  const DetFrame fr = det_frame(T, ph.t);
+  D3 x = ph.x, p = ph.p;
+  det_enter(T, fr, x, p);
   int hit = -1;
   D3 xh = x;
   double dx = 0, dy = 0;
@@ -1231,7 +1304,8 @@ MXD void detect_stage(const MxTables &T, const MxChipDev *chips, int nchips, Ph 
     // pass of their own over the photons on a chip (mx_acis_fef_kernel)
     if (!T.acis_fef && !T.acis_qe) acis_streak(T, d, ph, x, p, rng);
   }
-  ph.x = x + off;
+  det_leave(T, fr, x, p);
+  ph.x = x;
   ph.p = p;
 }
 
@@ -1333,8 +1407,9 @@ MXD void hrc_detect_stage(const MxTables &T, const MxChipDev *chips, int nchips,
     drake_reflect(T, h, ph, rng);
     if (ph.flags & MX_BAD_PHOTON_MASK) return;
   }
-  D3 off = mk(T.det_offset[0], T.det_offset[1], T.det_offset[2]);
-  D3 x = ph.x - off, p = ph.p;
+  const DetFrame fr = det_frame(T, ph.t);
+  D3 x = ph.x, p = ph.p;
+  det_enter(T, fr, x, p);
   int hit = -1;
   D3 xh = x;
   double dx = 0, dy = 0;
@@ -1352,7 +1427,8 @@ MXD void hrc_detect_stage(const MxTables &T, const MxChipDev *chips, int nchips,
   if (hit < 0) {
     ph.flags |= MX_PHOTON_MISSED_DETECTOR;
     ph.ccd = -1;
-    ph.x = x + off; ph.p = p;
+    det_leave(T, fr, x, p);
+    ph.x = x; ph.p = p;
     return;
   }
   x = xh;
@@ -1393,7 +1469,8 @@ MXD void hrc_detect_stage(const MxTables &T, const MxChipDev *chips, int nchips,
       ph.zpix = (float) (h.ll_cxcy[1] + div_by(dy, h.pix[1], h.inv_pix[1]));
     }
   }
-  ph.x = x + off;
+  det_leave(T, fr, x, p);
+  ph.x = x;
   ph.p = p;
 }
 

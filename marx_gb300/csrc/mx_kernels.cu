@@ -12,6 +12,18 @@ using namespace mx;
 // searches run on these).
 size_t trace_shared_bytes(const MxTables &T) { return tables_shared_bytes(T); }
 
+// The detector part of the dither state the dither stage recorded (dy, dz,
+// dtheta of Marx_Dither_Type): the aspect solution's at the photon's time,
+// zero with the INTERNAL model.  Taken again from the table here instead of
+// being carried through the trace.
+__device__ __forceinline__ void store_det_dither(const MxTables &T, const TraceIO &io, size_t n, uint32_t i, double t,
+                                                 uint32_t flags) {
+  if (!io.ddith || !((io.stages & MX_STAGE_DITHER) && T.dither)) return;
+  float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (T.dither_file && !(flags & MX_PHOTON_ASPECT_END)) aspsol_state(T, T.start_time + t, s);
+  io.ddith[i] = s[3]; io.ddith[n + i] = s[4]; io.ddith[2 * n + i] = s[5];
+}
+
 // Fused dither -> mirror -> grating -> detector trace, one photon per
 // thread, grid-stride over the photon list with a resident grid.
 __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_trace_kernel(MxTables T, TraceIO io) {
@@ -61,6 +73,7 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_trace_kernel(MxTables T, Tr
     if (io.ypix) io.ypix[i] = q.ypix;
     if (io.zpix) io.zpix[i] = q.zpix;
     if (io.dith) for (int k = 0; k < 3; k++) io.dith[k * n + i] = q.dith[k];
+    store_det_dither(T, io, n, i, q.t, q.flags);
     store_extra(io, i, q);
   }
 }
@@ -76,6 +89,13 @@ __device__ __forceinline__ bool acis_pending(const TraceIO &io, uint32_t i) {
   const int ccd = io.ccd[i];
   const uint32_t f0 = io.flags ? io.flags[i] : 0u;
   return ccd >= 0 && ccd <= 9 && !(f0 & (MX_BAD_PHOTON_MASK | MX_PHOTON_VARIATE_OVERRUN));
+}
+
+// Back from the detector frame of a photon with DitherModel FILE (kept out
+// of line: the frame's search and rotation are not on the common path).
+__device__ __noinline__ void leave_dithered_frame(const MxTables &T, double t, D3 &x, D3 &p) {
+  const DetFrame f = det_frame(T, t);
+  det_leave(T, f, x, p);
 }
 
 __device__ void acis_response(const MxTables &T, const TraceIO &io, uint32_t i, uint64_t seed, D3 off) {
@@ -115,7 +135,8 @@ __device__ void acis_response(const MxTables &T, const TraceIO &io, uint32_t i, 
     D3 x = mk(0, 0, 0), p = mk(0, 0, 0);
     acis_streak(T, T.chips[ccd], q, x, p, r);
     if (q.flags & MX_PHOTON_ACIS_STREAKED) {
-      x = x + off;
+      if (T.dither_file) leave_dithered_frame(T, q.t, x, p);
+      else x = x + off;
       if (io.x) { io.x[i] = x.x; io.x[n + i] = x.y; io.x[2 * n + i] = x.z; }
       io.p[i] = p.x; io.p[n + i] = p.y; io.p[2 * n + i] = p.z;
       io.zpix[i] = q.zpix;
@@ -213,6 +234,7 @@ __global__ void __launch_bounds__(MX_WAVE_BLOCK, MX_WAVE_MIN_BLOCKS) mx_wave_a(M
       r.overrun = false;
       if ((io.stages & MX_STAGE_DITHER) && T.dither) dither_stage(T, q, r);
       if (io.dith) for (int k = 0; k < 3; k++) io.dith[k * n + i] = q.dith[k];
+      store_det_dither(T, io, n, i, q.t, q.flags);
       MirrorState m;
       if (!(q.flags & MX_BAD_PHOTON_MASK) && mirror_front(T, sh, optc, slope, q, r, m)) {
         keep = true;

@@ -19,6 +19,7 @@ struct TraceIO {
   uint32_t *flags, *tag;
   int8_t *shell, *order, *ccd;
   float *ypix, *zpix, *dith;
+  float *ddith;                 // detector dither dy, dz, dtheta (3 components), or null
   int8_t *support;              // 4 components (stride): LETG support orders
   int16_t *pha;                 // HRC pulse height
   float *upix, *vpix;           // HRC-S u, v pixels

@@ -1061,14 +1061,16 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
   }
 
   // ---- dither
-  T.dither = cfg.dither == MX_DITHER_INTERNAL;
+  if (cfg.dither < MX_DITHER_NONE || cfg.dither > MX_DITHER_FILE) { err = "unknown dither model"; return false; }
+  T.dither = cfg.dither != MX_DITHER_NONE;
+  T.dither_file = cfg.dither == MX_DITHER_FILE;
   T.aspect_blur = cfg.aspect_blur * (PI_ / (180.0 * 3600.0));
   if (T.aspect_blur < 0) T.aspect_blur = 0.0;
   for (int k = 0; k < 3; k++) {
     T.dith_amp[k] = cfg.dither_amp[k] * (PI_ / (180.0 * 3600));
     T.dith_period[k] = cfg.dither_period[k];
     T.dith_phase[k] = cfg.dither_phase[k];
-    if (T.dither && !(cfg.dither_period[k] > 0)) { err = "dither periods must be > 0"; return false; }
+    if (cfg.dither == MX_DITHER_INTERNAL && !(cfg.dither_period[k] > 0)) { err = "dither periods must be > 0"; return false; }
     T.dith_inv_period[k] = cfg.dither_period[k] > 0 ? 1.0 / cfg.dither_period[k] : 0.0;
   }
   double roll = cfg.roll_nom * (PI_ / 180.0);
@@ -1079,7 +1081,7 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
   // With no roll amplitude every photon is rolled by the same float angle
   // (get_internal_dither, dither.c:175): its sine and cosine are taken once
   // here as the per-photon code would take them (series below 1e-3 rad).
-  T.roll_fixed = T.dith_amp[2] == 0.0;
+  T.roll_fixed = !T.dither_file && T.dith_amp[2] == 0.0;
   {
     double a = -(double) (float) (T.nominal_roll + 0.0);
     T.roll_zero = T.roll_fixed && a == 0.0;

@@ -144,6 +144,12 @@ struct MxTables {
   double dith_inv_period[3];    // correctly rounded 1 / dith_period
   int32_t roll_fixed, roll_zero;// roll amplitude 0: the roll angle is the same for every photon (zero: no roll)
   double roll_cos, roll_sin;    // cos and sin of -(float) nominal_roll, when roll_fixed
+  // DitherModel FILE (mx_set_aspect_solution): rows 0 .. asp_n of the
+  // aspect solution, row 0 the zero state the reference's reader starts from
+  int32_t dither_file, asp_record_only;
+  const double *asp_t;          // [asp_n + 1] times (s, relative to TSTART)
+  const double *asp_v;          // [asp_n + 1][8]: ra, dec, roll (rad), dy, dz (mm), dtheta (rad), 0, 0
+  uint32_t asp_n, pad_asp;
   // detector
   int32_t nchips, det_extend;   // configured detector's chips: chips[chip_off .. chip_off + nchips)
   int32_t chip_off, pad_chip;

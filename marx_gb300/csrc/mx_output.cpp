@@ -96,7 +96,8 @@ void put_value(std::vector<unsigned char> &b, int c, const mx_photons *h, size_t
     case 19: case 20: case 21: case 22:
       put_be(b, (uint8_t) (h->support_orders ? h->support_orders[(c - 19) * s + i] : 0), 1); break;
     case 23: case 24: case 25: f32(h->dither_state ? (double) h->dither_state[(c - 23) * s + i] : 0.0); break;
-    default: f32(0.0); break;                                        // detector dither: none with INTERNAL
+    case 26: case 27: case 28: f32(h->det_dither ? (double) h->det_dither[(c - 26) * s + i] : 0.0); break;
+    default: f32(0.0); break;
   }
 }
 
@@ -146,6 +147,7 @@ int mx_write_rayfile(const mx_photons *h, uint64_t history, const char *file, in
       r.x[k] = h->x ? h->x[k * s + i] : 0.0;
       r.p[k] = h->p ? h->p[k * s + i] : 0.0;
       r.dither[k] = h->dither_state ? h->dither_state[k * s + i] : 0.0f;
+      r.dither[3 + k] = h->det_dither ? h->det_dither[k * s + i] : 0.0f;
     }
     r.arrival_time = (h->arrival_time ? h->arrival_time[i] : 0.0) + total_time;
     r.flags = h->flags ? h->flags[i] : 0u;
@@ -198,6 +200,7 @@ int mx_read_rayfile(const char *file, mx_photons *h, uint32_t max, uint64_t *off
       if (h->x) h->x[k * s + i] = r.x[k];
       if (h->p) h->p[k * s + i] = r.p[k];
       if (h->dither_state) h->dither_state[k * s + i] = r.dither[k];
+      if (h->det_dither) h->det_dither[k * s + i] = r.dither[3 + k];
     }
     if (h->arrival_time) h->arrival_time[i] = r.arrival_time - *last_time;
     if (h->flags) h->flags[i] = r.flags;

@@ -68,13 +68,36 @@ double normalize_angle(double x) {   // dither.c:113-122
   if (x < -PI_) x += (2 * PI_);
   return x;
 }
+// marx_compute_ra_dec_offsets (pixlib.c:525-572): (ra, dec) as offsets
+// from (ra0, dec0).
+void ra_dec_offsets(double ra0, double dec0, double ra, double dec, double *dra, double *ddec) {
+  double d_ra = ra - ra0, d_dec = dec - dec0, c = cos(dec), factor = c * (1 - cos(d_ra));
+  double sdd = sin(d_dec) + factor * sin(dec0);
+  if (fabs(sdd) > 1.0) sdd = sdd < 0 ? -1 : 1;
+  double new_dec = asin(sdd), num = c * sin(d_ra), den = cos(d_dec) - factor * cos(dec0), new_ra;
+  if (den >= 0) new_ra = atan(num / den);
+  else new_ra = num >= 0 ? atan(num / den) + PI_ : atan(num / den) - PI_;
+  *dra = new_ra; *ddec = new_dec;
+}
+// The nominal pointing of init_aspsol_dither (dither.c:455-464): the file's
+// keywords in radians, moved below pi (no fmod, unlike the parameter file's
+// roll).
+double aspsol_nominal(double deg) {
+  double a = deg * (PI_ / 180.0);
+  if (a >= PI_) a -= (2.0 * PI_);
+  return a;
+}
 
 }  // namespace
 
 extern "C" int mx_source_direction(const mx_config *cfg, double ra, double dec, double out[3]) {
   if (!cfg || !out) return MX_EINVAL;
-  const double nom_ra = cfg->ra_nom * (PI_ / 180.0), nom_dec = cfg->dec_nom * (PI_ / 180.0);
-  const double nom_roll = normalize_angle(cfg->roll_nom * (PI_ / 180.0));
+  // DitherModel FILE: init_aspsol_dither replaces the nominal pointing by
+  // the aspect solution's keywords (carried in cfg) with its own reduction
+  const bool file = cfg->dither == MX_DITHER_FILE;
+  const double nom_ra = file ? aspsol_nominal(cfg->ra_nom) : cfg->ra_nom * (PI_ / 180.0);
+  const double nom_dec = file ? aspsol_nominal(cfg->dec_nom) : cfg->dec_nom * (PI_ / 180.0);
+  const double nom_roll = file ? aspsol_nominal(cfg->roll_nom) : normalize_angle(cfg->roll_nom * (PI_ / 180.0));
   const double yoff = cfg->pointing_offset[0] * (PI_ / (180.0 * 3600.0));
   const double zoff = cfg->pointing_offset[1] * (PI_ / (180.0 * 3600.0));
   // setup_pointing_ra_dec: the pointing from the nominal direction and the offsets
@@ -95,15 +118,7 @@ extern "C" int mx_source_direction(const mx_config *cfg, double ra, double dec, 
   double el, az;
   to_spherical(src, &el, &az);
   el = PI_ / 2.0 - el;
-  {   // marx_compute_ra_dec_offsets (pra, pdec, az, el)
-    double d_ra = az - pra, d_dec = el - pdec, c = cos(el), factor = c * (1 - cos(d_ra));
-    double sdd = sin(d_dec) + factor * sin(pdec);
-    if (fabs(sdd) > 1.0) sdd = sdd < 0 ? -1 : 1;
-    double new_el = asin(sdd), num = c * sin(d_ra), den = cos(d_dec) - factor * cos(pdec), new_az;
-    if (den >= 0) new_az = atan(num / den);
-    else new_az = num >= 0 ? atan(num / den) + PI_ : atan(num / den) - PI_;
-    az = new_az; el = new_el;
-  }
+  ra_dec_offsets(pra, pdec, az, el, &az, &el);
   // select_source
   V q = spherical(0.5 * PI_ - zoff, yoff);
   q = rotate_unit(q, V{0, -1, 0}, el);
@@ -111,5 +126,41 @@ extern "C" int mx_source_direction(const mx_config *cfg, double ra, double dec, 
   q = rotate_unit(q, V{1, 0, 0}, nom_roll);
   if (q.x <= 0.0) return MX_EINVAL;   // "Rays will not hit the telescope"
   out[0] = -q.x; out[1] = -q.y; out[2] = -q.z;
+  return MX_OK;
+}
+
+// init_aspsol_dither and get_single_aspsol_point (dither.c:282-340,
+// 438-500): each row's pointing (ra, dec) is unrolled about the nominal
+// pointing by the row's roll and taken as offsets from it; angles reduced
+// to [-pi, pi); times relative to TSTART, which init_aspsol_dither takes off
+// the first row a second time.  Row 0 of the output is the reader's static
+// start state (all zero), the left end of the first interval.
+int mx_aspsol_convert(const double *rows, uint32_t n, double ra_nom, double dec_nom, double roll_nom, double tstart,
+                      double *out_t, double *out_v) {
+  if (!rows || !out_t || !out_v) return MX_EINVAL;
+  const double nra = aspsol_nominal(ra_nom), ndec = aspsol_nominal(dec_nom);
+  (void) roll_nom;   // the unrolled rows keep their own roll (Aspsol.roll1 -= Nominal_Roll is left out there)
+  const V nominal = spherical(PI_ / 2.0 - ndec, nra);
+  for (int k = 0; k < 8; k++) out_v[k] = 0.0;
+  out_t[0] = 0.0;
+  for (uint32_t i = 0; i < n; i++) {
+    const double *b = rows + 7 * (size_t) i;
+    double t = b[0], ra = b[1] * (PI_ / 180.0), dec = b[2] * (PI_ / 180.0), roll = b[3] * (PI_ / 180.0);
+    double dth = b[6] * (PI_ / 180.0);
+    V p = spherical(PI_ / 2.0 - dec, ra);
+    p = rotate_unit(p, nominal, -roll);
+    to_spherical(p, &dec, &ra);
+    dec = PI_ / 2.0 - dec;
+    ra = normalize_angle(ra);
+    dec = normalize_angle(dec);
+    roll = normalize_angle(roll);
+    dth = normalize_angle(dth);
+    ra_dec_offsets(nra, ndec, ra, dec, &ra, &dec);
+    t -= tstart;
+    if (i == 0) t -= tstart;
+    double *v = out_v + 8 * (size_t) (i + 1);
+    out_t[i + 1] = t;
+    v[0] = ra; v[1] = dec; v[2] = roll; v[3] = b[4]; v[4] = b[5]; v[5] = dth; v[6] = 0.0; v[7] = 0.0;
+  }
   return MX_OK;
 }

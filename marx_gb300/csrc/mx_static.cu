@@ -63,6 +63,7 @@ extern "C" int mx_trace_static(mx_context *c, const mx_photons *ph, uint32_t sta
   io.support = ph->support_orders; io.pha = ph->pulse_height; io.upix = ph->u_pixel; io.vpix = ph->v_pixel;
   io.region = ph->detector_region;
   io.pi = ph->pi;
+  io.ddith = ph->det_dither;
   io.U = U; io.N = N; io.n = ph->n; io.seed = seed; io.stages = stages; io.fresh = 0;
   io.stride = ph->stride ? ph->stride : ph->n;
   if (io.stride < io.n) return mx_fail(c, MX_EINVAL, "mx_trace_static: stride below n");

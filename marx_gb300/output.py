@@ -87,7 +87,7 @@ def read_rayfile(path: str, batch: int | None = None):
     off, last, hist, got = C.c_uint64(0), C.c_double(0.0), C.c_uint64(0), C.c_uint32(0)
     out = []
     while True:
-        ph = PhotonList(batch)
+        ph = PhotonList(batch, det_dither=True)
         s = ph.struct()
         if L.mx_read_rayfile(path.encode(), C.byref(s), batch, C.byref(off), C.byref(last), C.byref(hist),
                              C.byref(got)) != 0:
@@ -96,7 +96,7 @@ def read_rayfile(path: str, batch: int | None = None):
             break
         q = PhotonList(got.value)
         for k in vars(ph):
-            if k != "n":
+            if k != "n" and getattr(ph, k) is not None:
                 setattr(q, k, np.ascontiguousarray(getattr(ph, k)[..., :got.value]))
         out.append(q)
     return hist.value, out

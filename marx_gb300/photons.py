@@ -39,6 +39,7 @@ class MxPhotons(C.Structure):
         ("y_pixel", C.c_void_p), ("z_pixel", C.c_void_p), ("dither_state", C.c_void_p),
         ("support_orders", C.c_void_p), ("pulse_height", C.c_void_p), ("u_pixel", C.c_void_p),
         ("v_pixel", C.c_void_p), ("detector_region", C.c_void_p), ("pi", C.c_void_p),
+        ("det_dither", C.c_void_p),
     ]
 
 
@@ -55,16 +56,20 @@ COLUMNS = {
     "support_orders": (np.int8, 4), "pulse_height": (np.int16, 1), "u_pixel": (np.float32, 1),
     "v_pixel": (np.float32, 1), "detector_region": (np.uint8, 1), "pi": (np.float32, 1),
 }
+# Columns a list carries only when asked for (None otherwise): the detector
+# dither dy, dz, dtheta, non-zero with DitherModel FILE only.
+OPTIONAL_COLUMNS = {"det_dither": (np.float32, 3)}
 
 
 class PhotonList:
     """Host photon list: one numpy column per attribute."""
 
-    def __init__(self, n: int):
+    def __init__(self, n: int, det_dither: bool = False):
         self.n = int(n)
         for k, (dt, m) in COLUMNS.items():
             shape = (m, self.n) if m > 1 else (self.n,)
             setattr(self, k, np.zeros(shape, dtype=dt))
+        self.det_dither = np.zeros((3, self.n), np.float32) if det_dither else None
         self.ccd_num[:] = -1
         self.tag[:] = np.arange(self.n, dtype=np.uint32)
 
@@ -84,12 +89,14 @@ class PhotonList:
         q.n = self.n
         for k in COLUMNS:
             setattr(q, k, getattr(self, k).copy())
+        dd = getattr(self, "det_dither", None)
+        q.det_dither = None if dd is None else dd.copy()
         return q
 
     def struct(self) -> MxPhotons:
         s = MxPhotons()
         s.n = self.n
-        for k in COLUMNS:
+        for k in list(COLUMNS) + list(OPTIONAL_COLUMNS):
             a = getattr(self, k, None)
             if a is None:
                 continue

@@ -177,15 +177,18 @@ class Reference:
                  ypix=np.zeros(n, np.float32), zpix=np.zeros(n, np.float32),
                  dith=np.zeros((n, 3), np.float32), sup=np.zeros((n, 4), np.int8), pha=np.zeros(n, np.int16),
                  u=np.zeros(n, np.float32), v=np.zeros(n, np.float32), region=np.zeros(n, np.uint8),
-                 pi=np.zeros(n, np.float32))
+                 pi=np.zeros(n, np.float32), ddith=np.zeros((n, 3), np.float32))
         self.lib.mxref_set_extra_outputs(_p(o["sup"]), _p(o["pha"]), _p(o["u"]), _p(o["v"]), _p(o["region"]))
         self.lib.mxref_set_pi_output(_p(o["pi"]))
+        self.lib.mxref_set_det_dither_output(_p(o["ddith"]))
         return o
 
     def _to_list(self, ph: PhotonList, o: dict) -> PhotonList:
         self.lib.mxref_set_extra_outputs(None, None, None, None, None)
         self.lib.mxref_set_pi_output(None)
+        self.lib.mxref_set_det_dither_output(None)
         q = ph.copy()
+        q.det_dither = np.ascontiguousarray(o["ddith"].T)
         q.x[:] = o["x"].T; q.p[:] = o["p"].T; q.flags[:] = o["flags"]
         q.mirror_shell[:] = o["shell"]; q.order[:] = o["order"]; q.ccd_num[:] = o["ccd"]
         q.y_pixel[:] = o["ypix"]; q.z_pixel[:] = o["zpix"]; q.dither_state[:] = o["dith"].T

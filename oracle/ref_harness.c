@@ -156,7 +156,7 @@ int mxref_setup(const char *parfile, const char *datadir, int nover,
      { set_err("dither init failed"); return -1; }
    if (-1 == pf_get_string(Pf, "DitherModel", buf, sizeof(buf)))
      return -1;
-   Have_Dither = (0 == strcmp(buf, "INTERNAL"));
+   Have_Dither = (0 == strcmp(buf, "INTERNAL")) || (0 == strcmp(buf, "FILE"));
 
    if (-1 == marx_mirror_init(Pf)) { set_err("mirror init failed"); return -1; }
    if (-1 == marx_grating_init(Pf)) { set_err("grating init failed"); return -1; }
@@ -332,6 +332,9 @@ static unsigned char *X_Region;
 static float *X_Pi;
 /* ACIS PI (at->pi) output column, or NULL. */
 void mxref_set_pi_output(float *pi) { X_Pi = pi; }
+/* The detector dither (dy, dz, dtheta of at->dither_state, 3 per photon), or NULL. */
+static float *X_Det;
+void mxref_set_det_dither_output(float *d) { X_Det = d; }
 
 void mxref_set_extra_outputs(signed char *sup, short *pha, float *u, float *v, unsigned char *region)
 {
@@ -361,6 +364,11 @@ static void store_attr(const Marx_Photon_Attr_Type *at, int i, double *x, double
    if (X_V != NULL) X_V[i] = at->v_pixel;
    if (X_Region != NULL) X_Region[i] = at->detector_region;
    if (X_Pi != NULL) X_Pi[i] = at->pi;
+   if (X_Det != NULL)
+     {
+        X_Det[3*i] = at->dither_state.dy; X_Det[3*i+1] = at->dither_state.dz;
+        X_Det[3*i+2] = at->dither_state.dtheta;
+     }
 }
 
 #define ST_DITHER 1
@@ -406,6 +414,7 @@ int mxref_trace_slots(int n, const double *energy, const double *p_in, const dou
              rng_window(u, 0, 0, g, MX_N_DITHER, MX_N_DITHER_N);
              _marx_dither_photons(&pt, &num);
              us[1] = N_pos - MX_N_DITHER;
+             if (num == 0) us[1] = -1;     /* the dither model gave no state (past the aspect solution) */
           }
         if (stages & ST_MIRROR)
           {

@@ -35,6 +35,11 @@ oracle/Makefile compiles them in place into oracle/_ref.  Writes:
                          the trace and statistics fixtures of a workload
                          with the reference's ACIS detector reading that FEF
                          (pulse height and PI) (--fef).
+  aspsol_synthetic.fits, trace_aspsol_<case>.npz
+                         a synthetic ASPSOL aspect solution and the trace of
+                         a workload's photons by the reference with
+                         DitherModel = FILE reading it (sky and detector
+                         dither state recorded) (--aspsol).
   diff_rays.npz          focal-plane positions of the differentiable form's
                          rays traced by the reference's mirror stage, at
                          theta = 0 and at the workload's perturbation written
@@ -569,6 +574,58 @@ def fef_fixtures():
         shutil.rmtree(tmp)
 
 
+ASPSOL_FILE = os.path.join(HERE, "aspsol_synthetic.fits")
+ASPSOL_CASES = {"aspsol_scatter": "plain_scatter", "aspsol_hrci": "plain_hrci"}
+ASPSOL_KEYS = (("RA_NOM", "83.8221"), ("DEC_NOM", "-5.3911"), ("ROLL_NOM", "250.37"), ("TSTART", "300000000.5"))
+ASPSOL_SPAN = 200.0   # s of photon arrival times covered by the table
+
+
+def synthetic_aspsol():
+    """An aspect solution at 0.256 s steps from TSTART - 1 s to TSTART +
+    ASPSOL_SPAN + 2 s: Lissajous pointing (8 arcsec, periods 707 and 1000 s)
+    about the nominal pointing with a slow roll wobble, and a detector
+    drifting by tens of microns and turning by a few arcsec."""
+    kv = {k: float(v) for k, v in ASPSOL_KEYS}
+    t = kv["TSTART"] - 1.0 + 0.256 * np.arange(int((ASPSOL_SPAN + 3.0) / 0.256))
+    s = t - kv["TSTART"]
+    a = 8.0 / 3600.0
+    ra = kv["RA_NOM"] + a * np.sin(2 * np.pi * s / 707.0) / np.cos(np.radians(kv["DEC_NOM"]))
+    dec = kv["DEC_NOM"] + a * np.sin(2 * np.pi * s / 1000.0 + 0.3)
+    roll = kv["ROLL_NOM"] + (10.0 / 3600.0) * np.sin(2 * np.pi * s / 150.0)
+    dy = 0.02 * np.sin(2 * np.pi * s / 90.0)
+    dz = -0.015 * np.cos(2 * np.pi * s / 130.0)
+    dth = (4.0 / 3600.0) * np.sin(2 * np.pi * s / 60.0)
+    cols = [("time", "D", t), ("ra", "D", ra), ("dec", "D", dec), ("roll", "D", roll), ("dy", "D", dy),
+            ("dz", "D", dz), ("dtheta", "D", dth)]
+    return cols, list(ASPSOL_KEYS)
+
+
+def aspsol_fixture(name):
+    """trace_<name>.npz: the workload's photons at arrival times spread over
+    the aspect solution, traced by the reference with DitherModel = FILE;
+    the dither state (sky and detector parts) is recorded with the rest."""
+    from marx_gb300.aspsol import read_aspsol, apply_to_config
+    cols, keys = synthetic_aspsol()
+    write_bintable(ASPSOL_FILE, "ASPSOL", cols, keys)
+    asp = read_aspsol(ASPSOL_FILE)
+    w = W.ALL[ASPSOL_CASES[name]](parity=True)
+    cfg = apply_to_config(w.cfg, asp)
+    ph = w.photons(N_TRACE, seed=w.seed + 21)
+    ph.arrival_time[:] = np.sort(np.random.default_rng(w.seed + 22).uniform(0.0, ASPSOL_SPAN, N_TRACE))
+    U, N = predraw_variates(N_TRACE, seed=w.seed + 23)
+    ref = Reference(cfg, extra_par={"DitherModel": "FILE", "DitherFile": ASPSOL_FILE})
+    q, used, bad = ref.trace_slots(ph, U, N)
+    assert bad == 0, "reference ran past its variate slots"
+    assert (used[:, 1] >= 0).all(), "a photon fell outside the aspect solution"
+    np.savez_compressed(
+        os.path.join(HERE, f"trace_{name}.npz"),
+        energy=ph.energy, p_in=ph.p, arrival_time=ph.arrival_time, U=U, N=N,
+        x=q.x, p=q.p, flags=q.flags, mirror_shell=q.mirror_shell, order=q.order, ccd_num=q.ccd_num,
+        y_pixel=q.y_pixel, z_pixel=q.z_pixel, dither_state=q.dither_state, det_dither=q.det_dither, used=used)
+    print(name, "detected", int(((q.flags & 0xFF) == 0).sum()), "det dither range",
+          np.abs(q.det_dither).max(axis=1))
+
+
 N_DIFF = 4000
 RDB = "EKCHDOS06.rdb"
 SHELL_OF = {"1": 0, "3": 1, "4": 2, "6": 3}
@@ -650,6 +707,13 @@ if __name__ == "__main__":
         diff_rays()
     elif "--fef" in sys.argv:
         fef_fixtures()
+    elif "--aspsol" in sys.argv:
+        if names:
+            aspsol_fixture(names[0])
+        else:
+            import subprocess
+            for n in ASPSOL_CASES:
+                subprocess.run([sys.executable, __file__, "--aspsol", n], check=True)
     elif "--events" in sys.argv:
         if names:
             events_fixture(names[0])
