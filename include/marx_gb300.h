@@ -337,6 +337,31 @@ enum { MX_SOURCE_POINT = 0, MX_SOURCE_GAUSS = 1, MX_SOURCE_BETA = 2, MX_SOURCE_D
 int mx_set_aspect_solution(mx_context *ctx, const double *rows, uint32_t n, double ra_nom, double dec_nom,
                            double roll_nom, double tstart, int record_only);
 
+/* USER sources (marx/libsrc/s-user.c): a plug-in shared object exporting
+ * user_open_source(argv, argc, area, px, py, pz), user_create_ray(&t,
+ * &energy, &p1, &p2, &p3), user_close_source() and optionally
+ * user_start_iteration().  Host-side, as in the reference.
+ *
+ * mx_user_source_open: marx_select_user_source + open_source (s-user.c:
+ * 158-167, 250-300): dlopen `file`, split `args` (UserSourceArgs) at blanks
+ * into argv and call user_open_source with the mirror's geometric area
+ * (cm^2) and the source direction p.  NULL on failure (mx_user_source_error). */
+typedef struct mx_user_source mx_user_source;
+mx_user_source *mx_user_source_open(const char *file, const char *args, double geometric_area, const double p[3]);
+/* create_photons (s-user.c:168-232) over a HOST list: host->energy holds
+ * the spectrum's draws on entry; per photon user_create_ray gets the draw
+ * and may replace it (a negative energy keeps the draw); p is the ray's,
+ * flags 0, and while the plug-in hands back t >= 0 the arrival time is the
+ * running sum of those t (times_set = 1; otherwise arrival times are left to
+ * the caller, as the reference leaves them to marx_create_photons).  Stops at
+ * the first ray the plug-in refuses; user_start_iteration returning -1 gives
+ * no photons.  *n_created = photons made. */
+int mx_user_source_create(mx_user_source *src, const mx_photons *host, uint32_t n, uint32_t *n_created,
+                          int *times_set);
+/* close_source: user_close_source, then the plug-in is unloaded. */
+void mx_user_source_close(mx_user_source *src);
+const char *mx_user_source_error(void);
+
 /* The direction of travel p of the photons of a source at (ra, dec)
  * (degrees) for the configuration's pointing (RA_Nom, Dec_Nom, Roll_Nom,
  * PointingOffsetY/Z): setup_pointing_ra_dec (dither.c:125-155),

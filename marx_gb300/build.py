@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libmarx_gb300.so")
 SOURCES = ["mx_capi.cu", "mx_kernels.cu", "mx_batch.cu", "mx_static.cu", "mx_diff.cu", "mx_model.cpp",
-           "mx_output.cpp", "mx_source.cpp", "mx_events.cu"]
+           "mx_output.cpp", "mx_source.cpp", "mx_events.cu", "mx_user_source.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -69,7 +69,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     with ThreadPoolExecutor(len(srcs)) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB + ".tmp"
-    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
