@@ -9,7 +9,7 @@ axis, 8 arcsec Lissajous dither, mirror blur and WFold scattering, ACIS-I).
 
 value     photons/s with the batch resident in HBM (inputs > L2, so no flush);
           each step restores the batch's input directions and flags, then
-          launches the fused trace kernel.
+          traces it (from 65536 photons: the four wavefront kernels).
 e2e       the same metric through mx_trace_host: pinned host buffers in,
           host buffers out, copies inside the timed region.
 roofline  the trace kernel against the measured FP64 FMA peak (it is FP64
@@ -17,6 +17,9 @@ roofline  the trace kernel against the measured FP64 FMA peak (it is FP64
           oracle's counting arithmetic on a sample of the same batch.
 cpu_baseline  the CPU oracle (a restatement of the reference) on a bounded
           sample, all host threads.
+configs   the on-axis (plain_onaxis, 1e6 photons) and HETG (plain_hetg,
+          2e7 photons) configurations at their full sizes, each with its own
+          value, roofline, e2e and cpu_baseline.
 batched   the 256-source workload: one persistent cooperative launch in a
           CUDA graph against 256 sequential plain traces.
 differentiable  4e6 weighted rays: gradients/s of forward + MSE + adjoint
@@ -42,9 +45,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "photons/s HRMA+grating+ACIS trace"
 # DRAM bytes the four wavefront kernels move per photon of plain_scatter
-# (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture of 2e6
-# photons, profiles/wave_kernels_plain_scatter.md); the traffic of a step
-# grows with its photon count.
+# (dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of 2e6
+# photons); the traffic of a step grows with its photon count.
 TRAFFIC_BYTES_PER_PHOTON = 552.0
 
 
@@ -61,6 +63,7 @@ def parse():
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiable-form gradient comparison")
     ap.add_argument("--no-workloads", action="store_true", help="skip the per-workload throughput table")
     ap.add_argument("--no-events", action="store_true", help="skip the marx2fits event-coordinate pass")
+    ap.add_argument("--no-configs", action="store_true", help="skip the full-size on-axis and HETG configurations")
     return ap.parse_args()
 
 
@@ -302,7 +305,7 @@ def bench_workloads(a, skip):
     out = {}
     stream = torch.cuda.current_stream()
     for name, make in W.ALL.items():
-        if name == skip:
+        if name in skip:
             continue
         w = make()
         n = min(w.n, 4_000_000)
@@ -435,7 +438,7 @@ def bench_events(a):
     return {"workload": "1e7 ACIS-I events, EDSER, INTERNAL dither, frames of ~30 events, device-resident",
             "events": n, "ms": ms, "events_per_s": n / (ms * 1e-3), "gpu_launches_per_step": launches,
             "roofline": {"bound": "fp64", "note": "sin, cos, acos, asin, atan and about 26 divisions per event; "
-                                                  "ncu: FP64 pipe 87% busy (profiles/event_kernel_acis_i.md)",
+                                                  "ncu: FP64 pipe 87% busy",
                          "hbm": {"achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
                                  "bytes_per_event": EVENT_BYTES}},
             "cpu_baseline": {"value": cpu_rate, "unit": "events/s", "cores": 1, "kind": "port",
@@ -465,16 +468,121 @@ def run_reference(a):
     print(json.dumps(line))
 
 
+def e2e_host(eng, host, w, n, steps, warmup, world=1):
+    """The metric through mx_trace_host: pinned host buffers in, every
+    output column back in host memory, wall clock around each blocking
+    call."""
+    import numpy as np
+    import torch
+    from marx_gb300.photons import PhotonList
+    pin = {}
+    for k in ("energy", "p", "arrival_time", "flags", "tag", "x", "mirror_shell", "order", "ccd_num",
+              "y_pixel", "z_pixel", "dither_state"):
+        src = getattr(host, k)
+        t = torch.empty(src.shape, dtype=getattr(torch, str(src.dtype).replace("uint32", "int32")), pin_memory=True)
+        t.numpy()[...] = src.view(np.int32) if src.dtype == np.uint32 else src
+        pin[k] = t
+    hp = PhotonList.__new__(PhotonList)
+    hp.n = n
+    for k, t in pin.items():
+        arr = t.numpy()
+        setattr(hp, k, arr.view(np.uint32) if k in ("flags", "tag") else arr)
+    p_in = pin["p"].clone()
+    in_b = sum(pin[k].numel() * pin[k].element_size() for k in ("energy", "p", "arrival_time", "flags", "tag"))
+    out_b = sum(pin[k].numel() * pin[k].element_size() for k in ("x", "p", "flags", "mirror_shell", "order",
+                                                                 "ccd_num", "y_pixel", "z_pixel", "dither_state"))
+    for s in range(max(1, warmup)):
+        pin["p"].copy_(p_in); pin["flags"].zero_()
+        eng.trace_host(hp, stages=w.stages, seed=2000 + s)
+    barrier(world)
+    e2e_s = 0.0
+    for s in range(steps):
+        # the step's inputs are put back in the pinned buffers outside the
+        # timed region; each timed call copies them in, traces and copies
+        # every output column back
+        pin["p"].copy_(p_in); pin["flags"].zero_()
+        t0 = time.perf_counter()
+        eng.trace_host(hp, stages=w.stages, seed=s)
+        e2e_s += time.perf_counter() - t0
+    e2e_s = max_over_ranks(e2e_s, world)
+    barrier(world)
+    return {"value": world * n * steps / e2e_s, "unit": "photons/s",
+            "h2d_bytes_per_step": in_b, "d2h_bytes_per_step": out_b,
+            "note": "pinned host buffers; wall clock around each blocking mx_trace_host call (copies in, "
+                    "trace, copies out; the host-side reset of the step's inputs is not timed)"}
+
+
+def flops_per_photon(w):
+    """Algorithmic FP64 operations per photon: the oracle's counting
+    arithmetic on 2e4 photons of the workload."""
+    from oracle.bindings import Oracle
+    sample = w.photons(20_000, seed=w.seed + 99)
+    ops, cnt = Oracle(w.cfg).count_flops(sample, seed=5)
+    return ops / cnt
+
+
+def bench_config(a, name, fp64_peak):
+    """One configuration at its full size on one GPU: photons/s with the
+    batch resident (every launch timed with CUDA events on the launching
+    stream), the FP64 roofline of the trace, the same through
+    mx_trace_host, and the oracle on a sample."""
+    import torch
+    from marx_gb300 import workloads as W
+    from marx_gb300._native import Engine, DevicePhotons
+    w = W.PLAIN[name]()
+    n = w.n
+    eng = Engine(w.cfg)
+    host = w.photons(n)
+    d = DevicePhotons.from_host(host)
+    p0, f0 = d.p.clone(), d.flags.clone()
+    stream = torch.cuda.current_stream()
+    for s in range(max(3, a.warmup)):
+        d.p.copy_(p0); d.flags.copy_(f0)
+        eng.trace(d, stages=w.stages, seed=1000 + s)
+    torch.cuda.synchronize()
+    k = max(3, min(a.steps, 10))
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = eng.launch_count()
+    t0.record(stream)
+    for s in range(k):
+        d.p.copy_(p0); d.flags.copy_(f0)
+        ev[s][0].record(stream)
+        eng.trace(d, stages=w.stages, seed=s)
+        ev[s][1].record(stream)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    launches = (eng.launch_count() - l0) // k
+    ms_step = t0.elapsed_time(t1) / k
+    kernel_ms = statistics.mean(e0.elapsed_time(e1) for e0, e1 in ev)
+    good = float(((d.flags & 0xFF) == 0).float().mean().item())
+    del d, p0, f0
+    e2e = e2e_host(eng, host, w, n, k, 1)
+    fpp = flops_per_photon(w)
+    achieved = fpp * n / (kernel_ms * 1e-3) / 1e12
+    cpu_n = 200_000
+    cpu_rate = cpu_sample(w, cpu_n, os.cpu_count() or 1)
+    eng.close()
+    torch.cuda.empty_cache()
+    return {"workload": name, "photons_per_step": n, "steps": k, "value": n / (ms_step * 1e-3), "unit": "photons/s",
+            "ms_per_step": ms_step, "kernel_ms": kernel_ms, "gpu_launches_per_step": launches,
+            "detected_fraction": good,
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": achieved / fp64_peak, "traffic": None,
+                         "algorithmic_flops_per_photon": fpp,
+                         "peak_source": "measured live: mx_probe_fp64 DFMA kernel"},
+            "e2e": e2e,
+            "cpu_baseline": {"value": cpu_rate, "unit": "photons/s", "cores": os.cpu_count() or 1, "kind": "port",
+                             "sample": f"{cpu_n} photons of {name}"}}
+
+
 def main():
     a = parse()
     if a.impl == "reference":
         return run_reference(a)
-    import numpy as np
     import torch
     from marx_gb300 import workloads as W
     from marx_gb300._native import Engine, DevicePhotons, probe_fp64
-    from marx_gb300.photons import PhotonList
-    from oracle.bindings import Oracle
 
     rank, world = dist_init(a.gpus)
     dev = torch.cuda.current_device()
@@ -521,43 +629,7 @@ def main():
     good = float(((d.flags & 0xFF) == 0).float().mean().item())
 
     # end to end through the host entry point, pinned buffers
-    e2e = None
-    if not a.no_e2e:
-        pin = {}
-        for k in ("energy", "p", "arrival_time", "flags", "tag", "x", "mirror_shell", "order", "ccd_num",
-                  "y_pixel", "z_pixel", "dither_state"):
-            src = getattr(host, k)
-            t = torch.empty(src.shape, dtype=getattr(torch, str(src.dtype).replace("uint32", "int32")), pin_memory=True)
-            t.numpy()[...] = src.view(np.int32) if src.dtype == np.uint32 else src
-            pin[k] = t
-        hp = PhotonList.__new__(PhotonList)
-        hp.n = n
-        for k, t in pin.items():
-            arr = t.numpy()
-            setattr(hp, k, arr.view(np.uint32) if k in ("flags", "tag") else arr)
-        p_in = pin["p"].clone()
-        in_b = sum(pin[k].numel() * pin[k].element_size() for k in ("energy", "p", "arrival_time", "flags", "tag"))
-        out_b = sum(pin[k].numel() * pin[k].element_size() for k in ("x", "p", "flags", "mirror_shell", "order",
-                                                                     "ccd_num", "y_pixel", "z_pixel", "dither_state"))
-        for s in range(max(1, a.warmup)):
-            pin["p"].copy_(p_in); pin["flags"].zero_()
-            eng.trace_host(hp, stages=w.stages, seed=2000 + s)
-        barrier(world)
-        e2e_s = 0.0
-        for s in range(a.steps):
-            # the step's inputs are put back in the pinned buffers outside the
-            # timed region; each timed call copies them in, traces and copies
-            # every output column back
-            pin["p"].copy_(p_in); pin["flags"].zero_()
-            t0 = time.perf_counter()
-            eng.trace_host(hp, stages=w.stages, seed=s)
-            e2e_s += time.perf_counter() - t0
-        e2e_s = max_over_ranks(e2e_s, world)
-        barrier(world)
-        e2e = {"value": world * n * a.steps / e2e_s, "unit": "photons/s",
-               "h2d_bytes_per_step": in_b, "d2h_bytes_per_step": out_b,
-               "note": "pinned host buffers; wall clock around each blocking mx_trace_host call (copies in, "
-                       "trace, copies out; the host-side reset of the step's inputs is not timed)"}
+    e2e = None if a.no_e2e else e2e_host(eng, host, w, n, a.steps, a.warmup, world)
 
     if rank != 0:
         if world > 1:
@@ -566,11 +638,9 @@ def main():
         return
 
     # roofline: algorithmic FP64 operations per photon from the oracle's counting arithmetic
-    sample = w.photons(20_000, seed=w.seed + 99)
-    ops, cnt = Oracle(w.cfg).count_flops(sample, seed=5)
-    flops_per_photon = ops / cnt
+    fpp = flops_per_photon(w)
     fp64_peak = probe_fp64()
-    achieved = flops_per_photon * n / (kernel_ms * 1e-3) / 1e12
+    achieved = fpp * n / (kernel_ms * 1e-3) / 1e12
     bytes_per_photon = 8 + 24 + 8 + 4 + 4 + 24 + 24 + 4 + 3 + 8 + 12 + 24   # SoA columns read + written
     hbm_peak = None
     try:
@@ -579,9 +649,14 @@ def main():
         hbm_peak = 6800.0
     hbm_achieved = bytes_per_photon * n / (kernel_ms * 1e-3) / 1e9
     cpu_rate = cpu_sample(w, 200_000, os.cpu_count() or 1)
+    del d, p0, flags0
+    torch.cuda.empty_cache()
+    configs = None if a.no_configs else {c: bench_config(a, c, fp64_peak) for c in ("plain_onaxis", "plain_hetg")
+                                         if c != a.workload}
     batched = None if a.no_batched else bench_batched(a)
     differentiable = None if a.no_diff else bench_diff(a, fp64_peak)
-    workloads = None if a.no_workloads else bench_workloads(a, a.workload)
+    workloads = None if a.no_workloads else bench_workloads(
+        a, {a.workload} | (set() if a.no_configs else {"plain_onaxis", "plain_hetg"}))
     events = None if a.no_events else bench_events(a)
 
     line = {
@@ -599,13 +674,14 @@ def main():
                      "traffic": TRAFFIC_BYTES_PER_PHOTON * n if a.workload == "plain_scatter" else None,
                      "traffic_note": "bytes per step of the four wavefront kernels, scaled from an ncu capture "
                                      "of 2e6 photons",
-                     "algorithmic_flops_per_photon": flops_per_photon,
+                     "algorithmic_flops_per_photon": fpp,
                      "peak_source": "measured live: mx_probe_fp64 DFMA kernel (MEASURED_PEAKS.json has no FP64 figure)",
                      "hbm": {"achieved_gbs": hbm_achieved, "peak_gbs": hbm_peak, "frac": hbm_achieved / hbm_peak,
                              "bytes_per_photon": bytes_per_photon}},
         "cpu_baseline": {"value": cpu_rate, "unit": "photons/s", "cores": os.cpu_count() or 1, "kind": "port",
                          "sample": f"200000 photons of {a.workload}"},
         "clocks": clocks.summary(),
+        "configs": configs,
         "batched": batched,
         "differentiable": differentiable,
         "workloads": workloads,

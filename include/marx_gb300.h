@@ -266,7 +266,12 @@ int mx_set_trace_mode(mx_context *ctx, int mode);
  *   - at most MX_STATIC_MAX_PHOTONS photons per call (MX_ERANGE beyond);
  *     the array (2 x 128 bytes per photon, 32 MiB) is held by every GPU
  *     that loads the library until the process exits;
- *   - stages must include MX_STAGE_MIRROR; pointers as for mx_trace;
+ *   - stages must include MX_STAGE_MIRROR: this entry point always runs
+ *     the wavefront kernels, whatever mx_set_trace_mode set; pointers and
+ *     argument checks as for mx_trace, except that x is always required
+ *     (also without MX_STAGE_DETECT);
+ *   - the current device must be the one the context was created on
+ *     (MX_EINVAL otherwise);
  *   - the first call on a device looks up the array's address there, with
  *     that device current; make that first call before any stream capture;
  *   - every call shares the one array: calls that overlap on the GPU (other

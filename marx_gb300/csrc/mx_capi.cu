@@ -268,16 +268,16 @@ int mx_trace_tables(mx_context *c, const MxTables &T, const mx_photons *ph, uint
 
 }  // extern "C"
 
-int mx_trace_queues(mx_context *c, const MxTables &T, const mx_photons *ph, uint32_t stages, const double *U,
-                    const double *N, uint64_t seed, cudaStream_t st, bool fresh, DevBuf &queues, bool force_wave) {
-  if (!ph) return fail(c, MX_EINVAL, "mx_trace: null photon list");
-  if (ph->n == 0) return MX_OK;
-  if (!ph->energy || !ph->p) return fail(c, MX_EINVAL, "mx_trace: energy and p are required");
-  if ((U == nullptr) != (N == nullptr)) return fail(c, MX_EINVAL, "mx_trace: give both U and N or neither");
-  if ((stages & MX_STAGE_DETECT) && T.nchips && (!ph->x)) return fail(c, MX_EINVAL, "mx_trace: x is required");
+int mx_trace_io(mx_context *c, const MxTables &T, const mx_photons *ph, uint32_t stages, const double *U,
+                const double *N, uint64_t seed, bool fresh, TraceIO &io, const char *who) {
+  const std::string w(who);
+  if (!ph) return fail(c, MX_EINVAL, w + ": null photon list");
+  if (!ph->energy || !ph->p) return fail(c, MX_EINVAL, w + ": energy and p are required");
+  if ((U == nullptr) != (N == nullptr)) return fail(c, MX_EINVAL, w + ": give both U and N or neither");
+  if ((stages & MX_STAGE_DETECT) && T.nchips && (!ph->x)) return fail(c, MX_EINVAL, w + ": x is required");
   if ((stages & (MX_STAGE_DITHER | MX_STAGE_DETECT)) && T.dither_file && T.asp_n == 0)
-    return fail(c, MX_EINVAL, "mx_trace: DitherModel FILE needs mx_set_aspect_solution");
-  TraceIO io;
+    return fail(c, MX_EINVAL, w + ": DitherModel FILE needs mx_set_aspect_solution");
+  memset(&io, 0, sizeof(io));
   io.energy = ph->energy; io.x = ph->x; io.p = ph->p; io.t = ph->arrival_time; io.flags = ph->flags;
   io.tag = ph->tag; io.shell = ph->mirror_shell; io.order = ph->order; io.ccd = ph->ccd_num;
   io.ypix = ph->y_pixel; io.zpix = ph->z_pixel; io.dith = ph->dither_state;
@@ -287,8 +287,18 @@ int mx_trace_queues(mx_context *c, const MxTables &T, const mx_photons *ph, uint
   io.ddith = ph->det_dither;
   io.U = U; io.N = N; io.n = ph->n; io.seed = seed; io.stages = stages; io.fresh = fresh ? 1 : 0;
   io.stride = ph->stride ? ph->stride : ph->n;
-  if (io.stride < io.n) return fail(c, MX_EINVAL, "mx_trace: stride below n");
+  if (io.stride < io.n) return fail(c, MX_EINVAL, w + ": stride below n");
   io.overrun = c->d_overrun;
+  return MX_OK;
+}
+
+int mx_trace_queues(mx_context *c, const MxTables &T, const mx_photons *ph, uint32_t stages, const double *U,
+                    const double *N, uint64_t seed, cudaStream_t st, bool fresh, DevBuf &queues, bool force_wave) {
+  if (!ph) return fail(c, MX_EINVAL, "mx_trace: null photon list");
+  if (ph->n == 0) return MX_OK;
+  TraceIO io;
+  int r = mx_trace_io(c, T, ph, stages, U, N, seed, fresh, io, "mx_trace");
+  if (r) return r;
   int slots = U != nullptr;
   bool wave = (stages & MX_STAGE_MIRROR) &&
               (c->mode == MX_MODE_WAVEFRONT || (c->mode == MX_MODE_AUTO && (force_wave || ph->n >= MX_WAVEFRONT_MIN_PHOTONS)));

@@ -80,6 +80,13 @@ __attribute__((visibility("hidden"))) int mx_trace_queues(mx_context *c, const M
                                                           uint64_t seed, cudaStream_t st, bool fresh, DevBuf &queues,
                                                           bool force_wave = false);
 
+// The checks every trace entry point makes on its arguments, and the kernel
+// view of the photon list built from them (who: the entry point's name for
+// the messages).  MX_OK, or MX_EINVAL with the reason on the context.
+__attribute__((visibility("hidden"))) int mx_trace_io(mx_context *c, const MxTables &T, const mx_photons *ph,
+                                                      uint32_t stages, const double *U, const double *N, uint64_t seed,
+                                                      bool fresh, TraceIO &io, const char *who);
+
 // The rows of an ASPSOL table converted as the reference's reader converts
 // them (mx_source.cpp): out is (n + 1) x 8, row 0 the reader's zero start
 // state; times go to out_t (n + 1).

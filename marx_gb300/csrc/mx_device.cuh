@@ -442,8 +442,9 @@ MXD void blur_normal(D3 &n, double blur_rad, Rng &rng) {
 
 // marx_reflectivity (reflect.c:39-77): polarisation-averaged Fresnel
 // |r|^2 for n = 1 - delta + i beta (Jackson 7.39, 7.41), with
-// |num/den|^2 = |num|^2 / |den|^2.
-MXD double reflectivity(double cos_t, double beta, double delta) {
+// |num/den|^2 = |num|^2 / |den|^2, returned as num / den (den > 0) so that
+// the reflectivity test can decide u * den < num without the division.
+MXD void reflectivity_parts(double cos_t, double beta, double delta, double &num, double &den) {
   double nr = 1.0 - delta, ni = beta;
   double sin2 = 1.0 - cos_t * cos_t;                     // sin_theta^2
   double sr = nr * nr - ni * ni, si = 2.0 * nr * ni;     // n^2
@@ -466,31 +467,13 @@ MXD double reflectivity(double cos_t, double beta, double delta) {
   double pr = cos_t * sr, pi_ = cos_t * si;
   double a2 = (pr - rr) * (pr - rr) + (pi_ - ri) * (pi_ - ri);
   double b2 = (pr + rr) * (pr + rr) + (pi_ + ri) * (pi_ + ri);
-  return 0.5 * (a1 * b2 + a2 * b1) / (b1 * b2);
-}
-// The same reflectivity as num / den (den > 0).
-MXD void reflectivity_parts(double cos_t, double beta, double delta, double &num, double &den) {
-  double nr = 1.0 - delta, ni = beta;
-  double sin2 = 1.0 - cos_t * cos_t;
-  double sr = nr * nr - ni * ni, si = 2.0 * nr * ni;
-  double wr = sr - sin2, wi = si;
-  double rr, ri;
-  double r = sqrt(wr * wr + wi * wi);
-  if (r == 0.0) { rr = wr; ri = wi; }
-  else if (wr >= 0.0) {
-    double h = 0.5 * (r + wr), inv = mx_rsqrt(h);
-    rr = h * inv; ri = 0.5 * wi * inv;
-  } else {
-    double h = 0.5 * (r - wr), inv = mx_rsqrt(h);
-    rr = 0.5 * wi * inv; ri = h * inv;
-    if (rr < 0.0) { rr = -rr; ri = -ri; }
-  }
-  double a1 = (cos_t - rr) * (cos_t - rr) + ri * ri, b1 = (cos_t + rr) * (cos_t + rr) + ri * ri;
-  double pr = cos_t * sr, pi_ = cos_t * si;
-  double a2 = (pr - rr) * (pr - rr) + (pi_ - ri) * (pi_ - ri);
-  double b2 = (pr + rr) * (pr + rr) + (pi_ + ri) * (pi_ + ri);
   num = 0.5 * (a1 * b2 + a2 * b1);
   den = b1 * b2;
+}
+MXD double reflectivity(double cos_t, double beta, double delta) {
+  double num, den;
+  reflectivity_parts(cos_t, beta, delta, num, den);
+  return num / den;
 }
 
 // interpolate_theta (wfold.c:304-332) on one fold array.

@@ -48,26 +48,23 @@ extern "C" int mx_trace_static(mx_context *c, const mx_photons *ph, uint32_t sta
                                      std::to_string(MX_STATIC_MAX_PHOTONS) + "); use mx_trace or smaller lists");
   if (!(stages & MX_STAGE_MIRROR)) return mx_fail(c, MX_EINVAL, "mx_trace_static: stages must include the mirror");
   if (ph->n == 0) return MX_OK;
-  if (!ph->energy || !ph->p || !ph->x) return mx_fail(c, MX_EINVAL, "mx_trace_static: energy, x and p are required");
-  const double *U = var ? var->U : nullptr, *N = var ? var->N : nullptr;
-  if ((U == nullptr) != (N == nullptr)) return mx_fail(c, MX_EINVAL, "mx_trace_static: give both U and N or neither");
-  void *scratch = nullptr;
-  int r = static_scratch(c, &scratch);
-  if (r) return r;
-
+  if (!ph->x) return mx_fail(c, MX_EINVAL, "mx_trace_static: x is required");
+  // the context's tables, overrun counter and launch shape belong to its
+  // device; the static array is looked up on the current one
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return mx_cuda_fail(c, e, "mx_trace_static");
+  if (dev != c->device)
+    return mx_fail(c, MX_EINVAL, "mx_trace_static: the current device (" + std::to_string(dev) +
+                                     ") is not the context's (" + std::to_string(c->device) + ")");
+  // the same argument checks and photon view as mx_trace
   TraceIO io;
-  memset(&io, 0, sizeof(io));
-  io.energy = ph->energy; io.x = ph->x; io.p = ph->p; io.t = ph->arrival_time; io.flags = ph->flags;
-  io.tag = ph->tag; io.shell = ph->mirror_shell; io.order = ph->order; io.ccd = ph->ccd_num;
-  io.ypix = ph->y_pixel; io.zpix = ph->z_pixel; io.dith = ph->dither_state;
-  io.support = ph->support_orders; io.pha = ph->pulse_height; io.upix = ph->u_pixel; io.vpix = ph->v_pixel;
-  io.region = ph->detector_region;
-  io.pi = ph->pi;
-  io.ddith = ph->det_dither;
-  io.U = U; io.N = N; io.n = ph->n; io.seed = seed; io.stages = stages; io.fresh = 0;
-  io.stride = ph->stride ? ph->stride : ph->n;
-  if (io.stride < io.n) return mx_fail(c, MX_EINVAL, "mx_trace_static: stride below n");
-  io.overrun = c->d_overrun;
+  int r = mx_trace_io(c, c->T, ph, stages, var ? var->U : nullptr, var ? var->N : nullptr, seed, false, io,
+                      "mx_trace_static");
+  if (r) return r;
+  void *scratch = nullptr;
+  r = static_scratch(c, &scratch);
+  if (r) return r;
   // Every call shares the array, so the queue counters are cleared on the
   // stream before the kernels run (launch_wavefront does it); calls that
   // overlap on the GPU would race on the queues.
@@ -76,7 +73,7 @@ extern "C" int mx_trace_static(mx_context *c, const mx_photons *ph, uint32_t sta
   w.q1 = (MxRec *) scratch;
   w.q2 = (MxRec *) ((char *) scratch + qbytes);
   w.counts = (unsigned int *) ((char *) scratch + 2 * qbytes);
-  cudaError_t e = launch_wavefront(c->T, io, w, c->num_sms * c->wave_blocks, (int) c->shared_bytes, (cudaStream_t) stream);
+  e = launch_wavefront(c->T, io, w, c->num_sms * c->wave_blocks, (int) c->shared_bytes, (cudaStream_t) stream);
   c->launches += MX_WAVE_KERNELS;
   if (e == cudaSuccess && (stages & MX_STAGE_DETECT) && (c->T.acis_fef || c->T.acis_qe)) {
     e = launch_acis_fef(c->T, io, c->num_sms * 8, (cudaStream_t) stream);

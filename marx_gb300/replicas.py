@@ -12,6 +12,8 @@ import numpy as np
 
 
 def rank_photons(workload, n: int, rank: int):
+    if (rank + 1) * n > 1 << 32:
+        raise ValueError(f"rank {rank} x {n} photons: tags beyond 2^32 would repeat another photon's draws")
     ph = workload.photons(n, seed=workload.seed + rank)
     ph.tag[:] = np.arange(n, dtype=np.uint64).astype(np.uint32) + np.uint32(rank * n)
     return ph

@@ -14,7 +14,7 @@ plain_hrci      4e6 photons of plain_scatter's source on the HRC-I.
 letg_hrcs       4e6 photons of plain_hetg's spectrum through the LETG onto
                 the HRC-S behind its Drake flat.
 batched         256 sources (see marx_gb300.batched).
-differentiable  4e6 weighted rays (see marx_gb300.adjoint).
+differentiable  4e6 weighted rays (see marx_gb300.diff).
 
 Every input comes from numpy's PCG64 with a fixed seed per workload; no
 dataset is read.

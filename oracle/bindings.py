@@ -14,7 +14,23 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libmx_oracle.so")
 REF_SLOTS_SO = os.path.join(HERE, "_ref", "libmxref_slots.so")
 REF_NATIVE_SO = os.path.join(HERE, "_ref", "libmxref_native.so")
-REF_ROOT = os.environ.get("MARX_REFERENCE_ROOT", "/root/reference")
+
+
+def _reference_root() -> str:
+    """The reference checkout: MARX_REFERENCE_ROOT, else the one the build
+    recipe (oracle/Makefile, REF) names."""
+    root = os.environ.get("MARX_REFERENCE_ROOT")
+    if root:
+        return root
+    try:
+        r = subprocess.run(["make", "-s", "--no-print-directory", "-C", HERE, "print-ref"], capture_output=True,
+                           text=True, timeout=30)
+        return r.stdout.strip() if r.returncode == 0 else ""
+    except (OSError, subprocess.TimeoutExpired):
+        return ""
+
+
+REF_ROOT = _reference_root()
 
 
 def build_port() -> str:
@@ -23,7 +39,7 @@ def build_port() -> str:
 
 
 def reference_available() -> bool:
-    return os.path.isdir(os.path.join(REF_ROOT, "marx", "libsrc"))
+    return bool(REF_ROOT) and os.path.isdir(os.path.join(REF_ROOT, "marx", "libsrc"))
 
 
 def build_reference() -> bool:
