@@ -227,6 +227,47 @@ int  mx_configure(mx_context *ctx, const mx_config *cfg);
  * MX_OK, or MX_EPACK / MX_EINVAL with the reason in mx_last_error(NULL). */
 int  mx_validate_config(const char *pack_path, const mx_config *cfg);
 void mx_destroy(mx_context *ctx);
+
+/* Marx_Photon_Type.start_time for the photons traced next (the ACIS frame
+ * streak and the aspect solution take start_time + arrival time): a launch
+ * parameter, changed without rebuilding the model (MARX moves it on by each
+ * batch's total time, source.c:285). */
+int  mx_set_start_time(mx_context *ctx, double start_time);
+
+/* ---------------------------------------------------- parameter files --
+ * The marx.par parameters behind mx_config (marx/par/marx.par), grouped by
+ * the module whose *_init reads them: the mirror (mirror.c:48, hrma.c:244-286),
+ * the gratings (grating.c:44, diffract.c:550-614, :1727-1860), the detectors
+ * (detector.c:298, acis-i.c:170-176, hrc-*.c, drake.c:148-246) and the aspect
+ * dither (dither.c:85-160).  A reader returns one parameter's value as text
+ * ("yes"/"no" for booleans), given its name and marx.par type letter
+ * ('r' real, 'i' integer, 'b' boolean, 's' string); 0 when found, -1 when
+ * the parameter is absent. */
+#define MX_PARAMS_MIRROR   0x1u
+#define MX_PARAMS_GRATING  0x2u
+#define MX_PARAMS_DETECTOR 0x4u
+#define MX_PARAMS_DITHER   0x8u
+#define MX_PARAMS_ALL      0xFu
+typedef int (*mx_param_reader)(void *user, const char *name, char type, char *value, size_t len);
+
+/* Read the parameters of the given groups into cfg (fields of other
+ * groups keep their values).  required != 0: an absent parameter is an
+ * error (MX_EINVAL), as a missing parameter is to the reference's *_init;
+ * otherwise it keeps cfg's value.  Unsupported values (MirrorType other than
+ * HRMA, an unknown GratingType, DetectorType or DitherModel, a malformed
+ * number, boolean or shutter string) are MX_EINVAL; the reason is in
+ * mx_last_error(NULL). */
+int  mx_config_read_params(mx_config *cfg, uint32_t groups, mx_param_reader read, void *user, int required);
+
+/* A MARX parameter file (name,type,mode,value,... per line) plus
+ * "Name=value" overrides, as the marx command line takes them (a later
+ * one wins), read into cfg from mx_config_default: every parameter the
+ * engine uses, absent ones at their defaults. */
+int  mx_config_read_par(mx_config *cfg, const char *par_path, const char *const *overrides, int n_overrides);
+
+/* The marx.par type letter and MX_PARAMS_* group of a parameter the engine
+ * reads (MX_EINVAL for any other name). */
+int  mx_param_type(const char *name, char *type, uint32_t *group);
 const char *mx_last_error(const mx_context *ctx);  /* ctx may be NULL */
 
 /* Trace photons in place on the device (pointers in ph are device

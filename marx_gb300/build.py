@@ -18,8 +18,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libmarx_gb300.so")
+# MARX's own stage API over its array-of-structures photon list
+# (include/marx_gb300_compat.h), on top of LIB
+COMPAT_LIB = os.path.join(OUT, "libmarx_gb300_compat.so")
+COMPAT_SOURCES = ["mx_compat.cpp"]
 SOURCES = ["mx_capi.cu", "mx_kernels.cu", "mx_batch.cu", "mx_static.cu", "mx_diff.cu", "mx_model.cpp",
-           "mx_output.cpp", "mx_source.cpp", "mx_events.cu", "mx_user_source.cpp"]
+           "mx_output.cpp", "mx_source.cpp", "mx_events.cu", "mx_user_source.cpp", "mx_par.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -50,9 +54,12 @@ def _flags(src: str, verbose: bool):
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     srcs = [os.path.join(CSRC, s) for s in SOURCES]
-    deps = srcs + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
-    deps.append(os.path.join(os.path.dirname(HERE), "include", "marx_gb300.h"))
-    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
+    compat = [os.path.join(CSRC, s) for s in COMPAT_SOURCES]
+    inc = os.path.join(os.path.dirname(HERE), "include")
+    deps = srcs + compat + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
+    deps += [os.path.join(inc, h) for h in os.listdir(inc)]
+    if (not force and all(os.path.exists(f) for f in (LIB, COMPAT_LIB))
+            and all(min(os.path.getmtime(LIB), os.path.getmtime(COMPAT_LIB)) >= os.path.getmtime(d) for d in deps)):
         return LIB
     cc = nvcc()
 
@@ -66,14 +73,17 @@ def build(verbose: bool = False, force: bool = False) -> str:
             print(r.stderr, file=sys.stderr)
         return obj
 
-    with ThreadPoolExecutor(len(srcs)) as ex:
-        objs = list(ex.map(compile_one, srcs))
-    tmp = LIB + ".tmp"
-    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-ldl"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"link failed:\n{r.stderr}")
-    os.replace(tmp, LIB)
+    with ThreadPoolExecutor(len(srcs) + len(compat)) as ex:
+        objs = list(ex.map(compile_one, srcs + compat))
+    core, shim = objs[:len(srcs)], objs[len(srcs):]
+    for out, cmd in ((LIB, [*ARCH, "-shared", *core, "-lcudart", "-ldl"]),
+                     (COMPAT_LIB, ["-shared", *shim, "-L" + OUT, "-lmarx_gb300", "-lcudart", "-ldl",
+                                   "-Xlinker", "-rpath,$ORIGIN"])):
+        tmp = out + ".tmp"
+        r = subprocess.run([cc, "-o", tmp, *cmd], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link of {os.path.basename(out)} failed:\n{r.stderr}")
+        os.replace(tmp, out)
     return LIB
 
 

@@ -181,6 +181,14 @@ int mx_configure(mx_context *c, const mx_config *cfg) {
   return configure(c, cfg);
 }
 
+int mx_set_start_time(mx_context *c, double start_time) {
+  if (!c) return MX_EINVAL;
+  c->cfg.start_time = start_time;
+  c->T.start_time = start_time;
+  c->hm.T.start_time = start_time;
+  return MX_OK;
+}
+
 int mx_validate_config(const char *pack_path, const mx_config *cfg) {
   if (!pack_path || !cfg) { g_create_err = "mx_validate_config: null argument"; return MX_EINVAL; }
   Pack pk;

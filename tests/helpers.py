@@ -48,12 +48,29 @@ def compare(q, ref, exact_fields=("flags", "mirror_shell", "order", "ccd_num", "
 EXTRA_FIELDS = ("support_orders", "pulse_height", "u_pixel", "v_pixel", "detector_region")
 
 
-def assert_parity(q, ref, where=""):
+def assert_parity(q, ref, where="", pixel_ulps=0):
+    """The parity contract.  pixel_ulps > 0 allows the single-precision chip
+    pixels to differ by that many float steps where the FP64 positions
+    behind them differ in their last bits (well inside the 1e-9 mm position
+    tolerance) and round to neighbouring floats; the whole pixel
+    (floor of y_pixel, z_pixel) must still be equal."""
     keys = getattr(ref, "files", None) or [k for k in EXTRA_FIELDS if hasattr(ref, k)]
     extra = tuple(k for k in EXTRA_FIELDS if k in keys and hasattr(q, k))
-    r = compare(q, ref, exact_fields=("flags", "mirror_shell", "order", "ccd_num", "y_pixel", "z_pixel",
-                                      "dither_state") + extra)
+    exact = ("flags", "mirror_shell", "order", "ccd_num", "dither_state") + extra
+    if not pixel_ulps:
+        exact += ("y_pixel", "z_pixel")
+    r = compare(q, ref, exact_fields=exact)
     assert r["dx"] <= X_TOL_MM, (where, r)
     assert r["dp"] <= P_TOL, (where, r)
     bad = {k: v for k, v in r.items() if k not in ("dx", "dp") and v}
     assert not bad, (where, r)
+    if pixel_ulps:
+        g = lambda o, k: getattr(o, k) if hasattr(o, k) else o[k]  # noqa: E731
+        for k in ("y_pixel", "z_pixel"):
+            a, b = g(q, k), g(ref, k)
+            steps = np.abs(a.view(np.int32).astype(np.int64) - b.view(np.int32).astype(np.int64))
+            assert int(steps.max(initial=0)) <= pixel_ulps, (where, k, int(steps.max()))
+            assert np.array_equal(np.floor(a), np.floor(b)), (where, k, "whole pixel")
+            # a last-bit flip needs a float rounding boundary between the two
+            # FP64 positions: rare
+            assert int((steps != 0).sum()) <= max(8, a.size // 200_000), (where, k, int((steps != 0).sum()))

@@ -8,6 +8,11 @@ directions within 1e-12; flags, shell, order, chip, pixels and dither state
 exact).  At these sizes the index arithmetic, the growth of the wavefront
 queues from a smaller list and, through mx_trace_host, the chunk seams of
 the pipelined host entry are all exercised against an independent result.
+The oracle rounds without fused multiply-add, the GPU with it, so FP64
+positions agree to a few 1e-10 mm; about one detected photon in a million
+then has a single-precision pixel one float step away from the oracle's
+(a rounding boundary between the two positions), with the whole pixel
+equal.
 """
 import numpy as np
 import pytest
@@ -46,7 +51,7 @@ def test_full_size_device_trace_matches_oracle(cuda, name):
     ph = w.photons()
     assert ph.n == w.n
     q = _device(Engine(w.cfg), ph, seed=2718)
-    assert_parity(q, _oracle(w, ph, 2718), f"{name} at {w.n} photons")
+    assert_parity(q, _oracle(w, ph, 2718), f"{name} at {w.n} photons", pixel_ulps=1)
     assert int(((q.flags & BAD_PHOTON_MASK) == 0).sum()) > w.n // 20
 
 
@@ -60,14 +65,14 @@ def test_full_size_hetg_device_and_host_entries_match_oracle(cuda):
     assert ph.n == 20_000_000
     eng = Engine(w.cfg)
     small = w.photons(1_000_000, seed=5)
-    assert_parity(_device(eng, small, 99), _oracle(w, small, 99), "hetg 1e6 before growth")
+    assert_parity(_device(eng, small, 99), _oracle(w, small, 99), "hetg 1e6 before growth", pixel_ulps=1)
     ref = _oracle(w, ph, 1414)
     q = _device(eng, ph, 1414)
-    assert_parity(q, ref, "hetg 2e7 device entry")
+    assert_parity(q, ref, "hetg 2e7 device entry", pixel_ulps=1)
     del q
     h = ph.copy()
     eng.trace_host(h, seed=1414)
-    assert_parity(h, ref, "hetg 2e7 host entry (chunked)")
+    assert_parity(h, ref, "hetg 2e7 host entry (chunked)", pixel_ulps=1)
     det = (h.flags & BAD_PHOTON_MASK) == 0
     assert det.sum() > 1_000_000
     # every order -3..3 reaches the ACIS-S, and both signs of each

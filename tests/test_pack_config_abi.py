@@ -144,3 +144,63 @@ def test_source_direction_matches_reference_live():
             p_ref, _, _ = ref.source_photons(1, np.full((4, 1), 0.5))
             r, p = _source_direction(cfg, ra, dec)
             assert r == 0 and np.abs(p - p_ref).max() <= 1e-15, (ra, dec, roll, dither, p, p_ref)
+
+
+def _read_par_c(L, path, overrides=()):
+    L.mx_config_read_par.argtypes = [C.POINTER(cfgmod.MxConfig), C.c_char_p, C.POINTER(C.c_char_p), C.c_int]
+    c = cfgmod.MxConfig()
+    arr = (C.c_char_p * max(1, len(overrides)))(*[o.encode() for o in overrides])
+    rc = L.mx_config_read_par(C.byref(c), path.encode(), arr, len(overrides))
+    return rc, c
+
+
+@pytest.mark.parametrize("name", list(W.ALL))
+def test_c_par_reader_matches_python_reader(tmp_path, name):
+    """mx_config_read_par (the C ABI's parameter-file reader) gives the same
+    configuration as from_par on a parameter file of every workload, with
+    the marx.par type letter of each parameter."""
+    L = _native().load_library()
+    L.mx_param_type.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_uint32)]
+    c = W.ALL[name]().cfg
+    lines = []
+    for k, v in cfgmod.to_par(c).items():
+        t = C.create_string_buffer(1)
+        if L.mx_param_type(k.encode(), t, None) != 0:
+            continue            # read by no engine module (Verbose, UseGratingEffFiles)
+        lines.append(f'{k},{t.value.decode()},h,"{v}",,,""')
+    p = tmp_path / "w.par"
+    p.write_text("\n".join(lines) + "\n")
+    rc, d = _read_par_c(L, str(p))
+    assert rc == 0, L.mx_last_error(None)
+    e = cfgmod.from_par(str(p))
+    for f, _ in cfgmod.MxConfig._fields_:
+        if f in ("max_order", "aperture_area_uniform", "source_distance", "start_time", "focal_length",
+                 "tstart_mjdsecs"):
+            continue            # engine settings, not marx.par parameters
+        val = lambda o: getattr(o, f)[:] if hasattr(getattr(o, f), "_length_") else getattr(o, f)  # noqa: E731
+        assert repr(val(d)) == repr(val(e)), f
+
+
+def test_c_par_reader_overrides_and_errors(tmp_path):
+    L = _native().load_library()
+    p = tmp_path / "o.par"
+    p.write_text('GratingType,s,h,"HETG",,,""\nHRMA_Use_Blur,b,h,yes,,,""\nShutters3,s,h,"0101",,,""\n')
+    rc, c = _read_par_c(L, str(p), ["GratingType=LETG", "DetectorType=HRC-S", "P3Blur=0.25"])
+    assert rc == 0
+    assert c.grating == cfgmod.GRATING["LETG"] and c.detector == cfgmod.DETECTOR["HRC-S"]
+    assert c.use_blur == 1 and c.shutters[1] == 0b0101 and c.blur_p[1] == 0.25
+    for bad in (["GratingType=XTG"], ["HRMA_Use_Blur=maybe"], ["Shutters1=01"], ["P1Blur=abc"], ["MirrorType=FLATFIELD"],
+                ["DitherModel"]):
+        rc, _ = _read_par_c(L, str(p), bad)
+        assert rc == -1, bad
+
+
+def test_c_par_reader_reads_the_reference_parameter_file():
+    from oracle.bindings import REF_ROOT, reference_available
+    if not reference_available():
+        pytest.skip("the reference checkout is not on this machine")
+    path = os.path.join(REF_ROOT, "marx", "par", "marx.par")
+    L = _native().load_library()
+    rc, d = _read_par_c(L, path)
+    assert rc == 0, L.mx_last_error(None)
+    assert bytes(d) == bytes(cfgmod.from_par(path))
