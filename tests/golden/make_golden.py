@@ -2,8 +2,9 @@
 
     python tests/golden/make_golden.py [workload ...]
 
-Needs the reference sources (MARX_REFERENCE_ROOT, default /root/reference);
-oracle/Makefile compiles them in place into oracle/_ref.  Writes:
+Needs the reference sources (MARX_REFERENCE_ROOT, else the checkout
+oracle/Makefile names); oracle/Makefile compiles them in place into
+oracle/_ref.  Writes:
 
   trace_<workload>.npz   per-photon parity fixtures: seeded inputs, the
                          pre-drawn variates handed to the reference's stage
@@ -40,6 +41,13 @@ oracle/Makefile compiles them in place into oracle/_ref.  Writes:
                          a workload's photons by the reference with
                          DitherModel = FILE reading it (sky and detector
                          dither state recorded) (--aspsol).
+  dispersed_<workload>.npz
+                         dispersed spectra of the reference's own seeded
+                         run of 1e6 photons through the HETG or LETG: the
+                         detected photons' focal-plane coordinate along the
+                         dispersion direction of their grating arm, per arm
+                         and order (-3..3), as samples and histograms
+                         (--dispersed).
   diff_rays.npz          focal-plane positions of the differentiable form's
                          rays traced by the reference's mirror stage, at
                          theta = 0 and at the workload's perturbation written
@@ -700,10 +708,42 @@ def diff_rays():
     np.savez_compressed(os.path.join(HERE, "diff_rays.npz"), **out)
 
 
+N_DISPERSED = 1_000_000
+DISPERSED_WORKLOADS = ("plain_hetg", "plain_letg", "letg_hrcs")
+
+
+def dispersed_fixture(name):
+    """Dispersed spectra of the reference's seeded run (its own generator):
+    per grating arm and order, the detected photons' coordinate along the
+    dispersion direction (tests/helpers.py dispersed_groups)."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    from helpers import dispersed_groups, DISPERSED_BINS
+    w = W.ALL[name](parity=True)
+    ref_n = Reference(w.cfg, native=True, seed=w.seed + 17)
+    ph = w.photons(N_DISPERSED, seed=w.seed + 19)
+    q, secs = ref_n.trace_batch(ph)
+    out = {"n": np.array(N_DISPERSED)}
+    for key, u in dispersed_groups(q, w.cfg).items():
+        u = np.sort(u)
+        out[f"count_{key}"] = np.array(u.size)
+        # histogram over equal-probability bins of the reference's sample
+        edges = np.quantile(u, np.linspace(0.0, 1.0, DISPERSED_BINS + 1)) if u.size >= 10 * DISPERSED_BINS else None
+        if edges is not None:
+            edges[0], edges[-1] = -np.inf, np.inf
+            out[f"edges_{key}"] = edges
+            out[f"hist_{key}"] = np.histogram(u, edges)[0]
+        out[f"sample_{key}"] = u[:: max(1, u.size // 20000)]
+    np.savez_compressed(os.path.join(HERE, f"dispersed_{name}.npz"), **out)
+    print(name, {k: int(v) for k, v in out.items() if k.startswith("count_")}, f"{secs:.1f} s")
+
+
 if __name__ == "__main__":
     sys.path.insert(0, os.path.dirname(HERE))
     names = [a for a in sys.argv[1:] if not a.startswith("-")]
-    if "--diff" in sys.argv:
+    if "--dispersed" in sys.argv:
+        for n in names or DISPERSED_WORKLOADS:
+            dispersed_fixture(n)
+    elif "--diff" in sys.argv:
         diff_rays()
     elif "--fef" in sys.argv:
         fef_fixtures()

@@ -45,6 +45,37 @@ def compare(q, ref, exact_fields=("flags", "mirror_shell", "order", "ccd_num", "
     return out
 
 
+# Dispersed spectra: equal-probability bins per (arm, order) histogram.
+DISPERSED_BINS = 20
+
+
+def dispersed_groups(q, cfg, orders=range(-3, 4)):
+    """The detected photons' focal-plane coordinate along the dispersion
+    direction of their grating arm, per arm and order: {"<arm>_<order>":
+    values (mm)}.  The grating stage turns each photon by -theta (its
+    shell's dispersion angle, plus LETG_ACIS_dTheta for the LETG on an
+    ACIS detector) into the facet frame, where the grating's lines run
+    along z and the dispersion along y (diffract.c:690-740, :1013), so the
+    dispersion coordinate is y cos(theta) + z sin(theta).  HETG arms: MEG
+    (shells 1 and 3), HEG (shells 4 and 6); the LETG has one arm."""
+    good = ((q.flags & 0xFF) == 0) & (q.ccd_num >= 0)
+    shell = q.mirror_shell.astype(int)
+    if cfg.grating == 1:
+        theta = np.asarray(cfg.hetg_theta[:])[shell]
+        arm = np.where(shell < 2, "meg", "heg")
+    else:
+        theta = np.asarray(cfg.letg_theta[:])[shell] + (cfg.letg_acis_dtheta if cfg.detector in (1, 2) else 0.0)
+        arm = np.full(q.n, "leg")
+    th = np.deg2rad(theta)
+    u = q.x[1] * np.cos(th) + q.x[2] * np.sin(th)
+    out = {}
+    for a in np.unique(arm):
+        for m in orders:
+            sel = good & (arm == a) & (q.order.astype(int) == m)
+            out[f"{a}_{m}"] = u[sel]
+    return out
+
+
 EXTRA_FIELDS = ("support_orders", "pulse_height", "u_pixel", "v_pixel", "detector_region")
 
 

@@ -72,3 +72,34 @@ def test_psf_encircled_energy(cuda, name):
     ee = np.array([(r <= a).mean() for a in ref["ee_radii"]])
     assert np.max(np.abs(ee - ref["ee"])) < 0.01, (ee, ref["ee"])
     assert stats.ks_2samp(np.sort(r)[:: max(1, len(r) // 5000)], ref["radius_sample"]).pvalue > 1e-3
+
+
+@pytest.mark.parametrize("name", ["plain_hetg", "plain_letg", "letg_hrcs"])
+def test_dispersed_spectra(cuda, name):
+    """Dispersed spectra: per grating arm (MEG, HEG; LEG) and order -3..3,
+    the detected photons' coordinate along the dispersion direction, from
+    1e6 photons on the GPU (Philox) against the reference's own seeded run
+    of 1e6 (tests/golden/dispersed_*.npz): chi-square over the reference's
+    equal-probability bins, two-sample KS on the values, and the split of
+    the detected photons over (arm, order) by chi-square."""
+    from helpers import dispersed_groups
+    ref = np.load(os.path.join(GOLDEN, f"dispersed_{name}.npz"))
+    n = int(ref["n"])
+    w, q = run_gpu(name, n=n, seed=4242)
+    groups = dispersed_groups(q, w.cfg)
+    keys = sorted(groups)
+    assert keys == sorted(k[len("count_"):] for k in ref.files if k.startswith("count_"))
+    counts = np.array([groups[k].size for k in keys])
+    ref_counts = np.array([int(ref[f"count_{k}"]) for k in keys])
+    assert chi2_p(counts, ref_counts) > 1e-4, dict(zip(keys, zip(counts, ref_counts)))
+    tested = 0
+    for k in keys:
+        u = groups[k]
+        if f"edges_{k}" not in ref.files or u.size < 100:
+            continue
+        h = np.histogram(u, ref[f"edges_{k}"])[0]
+        assert chi2_p(h, ref[f"hist_{k}"]) > 1e-4, (k, h, ref[f"hist_{k}"])
+        p = stats.ks_2samp(u, ref[f"sample_{k}"]).pvalue
+        assert p > 1e-4, (k, p)
+        tested += 1
+    assert tested >= 7
