@@ -80,6 +80,8 @@ class Oracle:
         L.mxo_splat_exp.restype = C.c_float
         L.mxo_splat_exp.argtypes = [C.c_float]
         L.mxo_weighted.argtypes = [C.c_void_p, C.POINTER(MxDiffConfig), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        L.mxo_splat.argtypes = [C.POINTER(MxDiffConfig), C.c_void_p, C.c_uint64, C.c_void_p]
+        L.mxo_philox_slots.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64, C.c_void_p, C.c_void_p]
         if pack is None:
             from marx_gb300.caldb.pack import DEFAULT_PACK
             pack = DEFAULT_PACK
@@ -128,6 +130,22 @@ class Oracle:
         if self.lib.mxo_weighted_flops(self.h, C.byref(dcfg), _p(th), _p(out)) != 0:
             raise RuntimeError("oracle weighted flop count failed")
         return out
+
+    def splat(self, dcfg, yzw):
+        """The engine's fixed-point image of given rays (3, n): y, z (mm),
+        weight."""
+        yzw = np.ascontiguousarray(yzw, dtype=np.float64)
+        img = np.zeros((dcfg.ny, dcfg.nx))
+        if self.lib.mxo_splat(C.byref(dcfg), _p(yzw), yzw.shape[1], _p(img)) != 0:
+            raise RuntimeError("oracle splat failed")
+        return img
+
+    def philox_slots(self, seed, n, first_tag=0):
+        """Slot arrays (U, N) of the Philox variates of n consecutive tags."""
+        U = np.zeros((NUM_U, n))
+        N = np.zeros((NUM_N, n))
+        self.lib.mxo_philox_slots(seed, first_tag, n, _p(U), _p(N))
+        return U, N
 
     def splat_exp(self, x: float) -> float:
         return self.lib.mxo_splat_exp(x)

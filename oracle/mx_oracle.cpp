@@ -511,6 +511,57 @@ extern "C" int mxo_weighted_flops(const mxo_model *m, const mx_diff_config *cfg,
   return 0;
 }
 
+// The engine's fixed-point splat of one ray of weight w at (y, z) into the
+// 64-bit accumulators A (w 2^31 x K 2^31 x K 2^31 >> shift per tap).
+struct SplatGeom {
+  int nx, ny, shift;
+  float knorm, half_inv_s2;
+  double inv_pitch, cxp, czp, cy, cz;
+  SplatGeom(const mx_diff_config *cfg, uint64_t n) {
+    nx = (int) cfg->nx; ny = (int) cfg->ny;
+    knorm = (float) (1.0 / (std::sqrt(2.0 * PI) * cfg->sigma));
+    half_inv_s2 = (float) (0.5 / (cfg->sigma * cfg->sigma));
+    const double kmax = knorm;
+    shift = (int) std::ceil(std::log2((double) n * kmax * kmax / 4.0)) + 1;
+    if (shift < 0) shift = 0;
+    inv_pitch = 1.0 / cfg->pitch; cxp = 0.5 * nx - 0.5; czp = 0.5 * ny - 0.5;
+    cy = cfg->center_y; cz = cfg->center_z;
+  }
+  void add(std::vector<uint64_t> &A, double y, double z, double w) const {
+    const double u = (y - cy) * inv_pitch + cxp, vv = (z - cz) * inv_pitch + czp;
+    if (!(u > -6.0 && u < nx + 5.0 && vv > -6.0 && vv < ny + 5.0)) return;
+    const double uc = std::floor(u + 0.5), vc = std::floor(vv + 0.5);
+    const int ic = (int) uc, jc = (int) vc;
+    const float fu = (float) (u - uc), fv = (float) (vv - vc);
+    const uint32_t wq = (uint32_t) std::nearbyint(std::fmin(w * 2147483648.0, 4294967295.0));
+    uint32_t a[11], b[11];
+    for (int k = 0; k < 11; k++) {
+      float d = (float) (k - 5) - fu;
+      uint32_t gy = (uint32_t) std::nearbyint((double) (knorm * exp_neg_f((d * d) * half_inv_s2) * 2147483648.0f));
+      a[k] = (uint32_t) (((uint64_t) wq * gy) >> 32);
+      float e = (float) (k - 5) - fv;
+      b[k] = (uint32_t) std::nearbyint((double) (knorm * exp_neg_f((e * e) * half_inv_s2) * 2147483648.0f));
+    }
+    for (int kz = 0; kz < 11; kz++) {
+      int row = jc - 5 + kz;
+      if (row < 0 || row >= ny) continue;
+      for (int ky = 0; ky < 11; ky++) {
+        int col = ic - 5 + ky;
+        if (col < 0 || col >= nx) continue;
+        A[(size_t) row * nx + col] += ((uint64_t) a[ky] * b[kz]) >> shift;
+      }
+    }
+  }
+  void finish(const std::vector<std::vector<uint64_t>> &acc, uint64_t n, double *image) const {
+    const double scale = std::ldexp(1.0, shift - 61) / (double) n;
+    for (size_t k = 0; k < (size_t) nx * ny; k++) {
+      uint64_t s = 0;
+      for (const auto &A : acc) s += A[k];
+      image[k] = (double) s * scale;
+    }
+  }
+};
+
 extern "C" int mxo_weighted(const mxo_model *m, const mx_diff_config *cfg, const double *theta, double *yzw,
                             double *image, int nthreads) {
   if (!m || !cfg || !theta || cfg->n_rays < 1 || cfg->n_rays > 0xffffffffull) return MX_EINVAL;
@@ -518,19 +569,13 @@ extern "C" int mxo_weighted(const mxo_model *m, const mx_diff_config *cfg, const
   V3<double> p0;
   perturbed(m, cfg, theta, M, p0);
   const uint64_t n = cfg->n_rays;
-  const int nx = (int) cfg->nx, ny = (int) cfg->ny;
-  const float knorm = (float) (1.0 / (std::sqrt(2.0 * PI) * cfg->sigma));
-  const float half_inv_s2 = (float) (0.5 / (cfg->sigma * cfg->sigma));
-  const double kmax = knorm;
-  int shift = (int) std::ceil(std::log2((double) n * kmax * kmax / 4.0)) + 1;
-  if (shift < 0) shift = 0;
-  const double inv_pitch = 1.0 / cfg->pitch, cxp = 0.5 * nx - 0.5, czp = 0.5 * ny - 0.5;
+  const SplatGeom g(cfg, n);
   unsigned nt = nthreads > 0 ? (unsigned) nthreads : std::max(1u, std::thread::hardware_concurrency());
   nt = (unsigned) std::min<uint64_t>(nt, n / 1024 + 1);
   std::vector<std::vector<uint64_t>> acc(image ? nt : 0);
   auto work = [&](unsigned wk) {
     std::vector<uint64_t> *A = image ? &acc[wk] : nullptr;
-    if (A) A->assign((size_t) nx * ny, 0);
+    if (A) A->assign((size_t) g.nx * g.ny, 0);
     for (uint64_t i = wk; i < n; i += nt) {
       double y = 0, z = 0, w = 0;
       bool hit = weighted_ray<double>(M, cfg->seed, (uint32_t) i, p0, cfg->energy, y, z, w);
@@ -539,30 +584,7 @@ extern "C" int mxo_weighted(const mxo_model *m, const mx_diff_config *cfg, const
         yzw[n + i] = hit ? z : NAN;
         yzw[2 * n + i] = hit ? w : 0.0;
       }
-      if (!A || !hit || !(w > 0.0)) continue;
-      const double u = (y - cfg->center_y) * inv_pitch + cxp, vv = (z - cfg->center_z) * inv_pitch + czp;
-      if (!(u > -6.0 && u < nx + 5.0 && vv > -6.0 && vv < ny + 5.0)) continue;
-      const double uc = std::floor(u + 0.5), vc = std::floor(vv + 0.5);
-      const int ic = (int) uc, jc = (int) vc;
-      const float fu = (float) (u - uc), fv = (float) (vv - vc);
-      const uint32_t wq = (uint32_t) std::nearbyint(std::fmin(w * 2147483648.0, 4294967295.0));
-      uint32_t a[11], b[11];
-      for (int k = 0; k < 11; k++) {
-        float d = (float) (k - 5) - fu;
-        uint32_t gy = (uint32_t) std::nearbyint((double) (knorm * exp_neg_f((d * d) * half_inv_s2) * 2147483648.0f));
-        a[k] = (uint32_t) (((uint64_t) wq * gy) >> 32);
-        float e = (float) (k - 5) - fv;
-        b[k] = (uint32_t) std::nearbyint((double) (knorm * exp_neg_f((e * e) * half_inv_s2) * 2147483648.0f));
-      }
-      for (int kz = 0; kz < 11; kz++) {
-        int row = jc - 5 + kz;
-        if (row < 0 || row >= ny) continue;
-        for (int ky = 0; ky < 11; ky++) {
-          int col = ic - 5 + ky;
-          if (col < 0 || col >= nx) continue;
-          (*A)[(size_t) row * nx + col] += ((uint64_t) a[ky] * b[kz]) >> shift;
-        }
-      }
+      if (A && hit && w > 0.0) g.add(*A, y, z, w);
     }
   };
   if (nt == 1) work(0);
@@ -571,13 +593,36 @@ extern "C" int mxo_weighted(const mxo_model *m, const mx_diff_config *cfg, const
     for (unsigned w = 0; w < nt; w++) th.emplace_back(work, w);
     for (auto &t : th) t.join();
   }
-  if (image) {
-    const double scale = std::ldexp(1.0, shift - 61) / (double) n;
-    for (size_t k = 0; k < (size_t) nx * ny; k++) {
-      uint64_t s = 0;
-      for (unsigned w = 0; w < nt; w++) s += acc[w][k];
-      image[k] = (double) s * scale;
-    }
-  }
+  if (image) g.finish(acc, n, image);
   return 0;
+}
+
+// The image of given rays (yzw: 3 x n, y and z in mm, weight; rays of
+// weight 0 or non-finite position are skipped) with the engine's splat, as
+// mxo_weighted images its own rays: for rays traced elsewhere (the
+// reference's mirror stage).
+extern "C" int mxo_splat(const mx_diff_config *cfg, const double *yzw, uint64_t n, double *image) {
+  if (!cfg || !yzw || !image || n < 1) return MX_EINVAL;
+  const SplatGeom g(cfg, n);
+  std::vector<std::vector<uint64_t>> acc(1);
+  acc[0].assign((size_t) g.nx * g.ny, 0);
+  for (uint64_t i = 0; i < n; i++) {
+    const double y = yzw[i], z = yzw[n + i], w = yzw[2 * n + i];
+    if (w > 0.0 && std::isfinite(y) && std::isfinite(z)) g.add(acc[0], y, z, w);
+  }
+  g.finish(acc, n, image);
+  return 0;
+}
+
+// Pre-drawn slot arrays holding the Philox variates of tags first_tag ..
+// first_tag + n - 1 (U: MX_NUM_U x n, N: MX_NUM_N x n, slot-major): the
+// draws the engine's Philox mode gives those photons.
+extern "C" void mxo_philox_slots(uint64_t seed, uint32_t first_tag, uint64_t n, double *U, double *N) {
+  for (uint64_t i = 0; i < n; i++) {
+    const uint32_t tag = first_tag + (uint32_t) i;
+    if (U)
+      for (uint32_t k = 0; k < MX_NUM_U; k++) U[k * n + i] = philox_uniform(seed, tag, k);
+    if (N)
+      for (uint32_t k = 0; k < MX_NUM_N; k++) N[k * n + i] = philox_normal(seed, tag, k);
+  }
 }

@@ -48,6 +48,15 @@ oracle/_ref.  Writes:
                          dispersion direction of their grating arm, per arm
                          and order (-3..3), as samples and histograms
                          (--dispersed).
+  diff_fd_reference.npz  central finite differences of the reference itself
+                         for the differentiable form: 2e5 rays (Philox
+                         variates of their tags, so common random numbers
+                         at every step) through the reference's ideal mirror
+                         with each of the 18 parameters moved by +-h in the
+                         HRMA geometry file (and the source direction),
+                         imaged with the engine's splat; the MSE to a target
+                         image and the 18-gradient, at theta_true and at a
+                         random theta (--diff-fd).
   diff_rays.npz          focal-plane positions of the differentiable form's
                          rays traced by the reference's mirror stage, at
                          theta = 0 and at the workload's perturbation written
@@ -708,6 +717,75 @@ def diff_rays():
     np.savez_compressed(os.path.join(HERE, "diff_rays.npz"), **out)
 
 
+N_FD = 200_000
+FD_STEP = 2e-3
+
+
+def diff_fd_fixture():
+    """Central differences of the reference's own mirror stage (ideal
+    mirror) for the 18 parameters, with common random numbers: every
+    perturbed run traces the same rays (the Philox variates of tags
+    0 .. N_FD - 1, served as pre-drawn slots), so the differences carry no
+    sampling noise; decisions (which shell, hit or miss of a mirror end or
+    a strut) are the reference's own at every step."""
+    w = diff_workload(n_rays=N_FD)
+    cfg = diff_mirror_config(ideal=True)
+    cfg.use_blur = 0
+    cfg.use_wfold = 0
+    o = Oracle(cfg)
+    U, N = o.philox_slots(w.cfg.seed, N_FD)
+    tags = np.arange(N_FD, dtype=np.uint32)
+
+    def rays(theta):
+        tmp = tempfile.mkdtemp(prefix="mxfd")
+        try:
+            ref = Reference(cfg, datadir=perturbed_datadir(theta, tmp))
+            p0 = source_direction(w.cfg.src_y + theta[16], w.cfg.src_z + theta[17])
+            ph = PhotonList.from_inputs(np.full(N_FD, w.cfg.energy), np.repeat(p0[:, None], N_FD, 1),
+                                        np.zeros(N_FD))
+            ph.tag[:] = tags
+            q, used, bad = ref.trace_slots(ph, U, N, stages=2)
+            assert bad == 0
+        finally:
+            shutil.rmtree(tmp)
+        hit = (q.flags & 0xFF) == 0
+        t = -q.x[0] / q.p[0]
+        return np.stack([np.where(hit, q.x[1] + t * q.p[1], np.nan), np.where(hit, q.x[2] + t * q.p[2], np.nan),
+                         hit.astype(np.float64)])
+
+    dc = w.cfg.copy()
+    r0 = rays(np.zeros(NPARAM))
+    h0 = r0[2] > 0
+    dc.center_y, dc.center_z = float(r0[0][h0].mean()), float(r0[1][h0].mean())
+    # the target: the oracle's image at theta_true from rays of another seed
+    tc = dc.copy()
+    tc.seed = w.target_seed
+    _, target = o.weighted(tc, w.theta_true, rays=False)
+    out = {"n": np.array(N_FD), "seed": np.array(w.cfg.seed), "h": np.array(FD_STEP),
+           "center": np.array([dc.center_y, dc.center_z]), "target": target}
+    points = {"true": w.theta_true, "random": np.random.default_rng(7).normal(0.0, 1.0, NPARAM)}
+    for name, theta in points.items():
+        loss = lambda r: float(np.mean((o.splat(dc, r) - target) ** 2))  # noqa: E731
+        r = rays(theta)
+        L = np.zeros((NPARAM, 2))
+        changed = np.zeros(NPARAM, np.int64)
+        for k in range(NPARAM):
+            rr = []
+            for j, sgn in enumerate((-1.0, 1.0)):
+                t = theta.copy()
+                t[k] += sgn * FD_STEP
+                rr.append(rays(t))
+                L[k, j] = loss(rr[-1])
+            changed[k] = int(np.sum((rr[0][2] > 0) != (rr[1][2] > 0)))
+        out[f"{name}_theta"] = theta
+        out[f"{name}_loss"] = np.array(loss(r))
+        out[f"{name}_losses"] = L
+        out[f"{name}_grad"] = (L[:, 1] - L[:, 0]) / (2.0 * FD_STEP)
+        out[f"{name}_changed"] = changed
+        print(name, "rays that hit on one side of a step and not the other:", changed.tolist())
+    np.savez_compressed(os.path.join(HERE, "diff_fd_reference.npz"), **out)
+
+
 N_DISPERSED = 1_000_000
 DISPERSED_WORKLOADS = ("plain_hetg", "plain_letg", "letg_hrcs")
 
@@ -740,7 +818,9 @@ def dispersed_fixture(name):
 if __name__ == "__main__":
     sys.path.insert(0, os.path.dirname(HERE))
     names = [a for a in sys.argv[1:] if not a.startswith("-")]
-    if "--dispersed" in sys.argv:
+    if "--diff-fd" in sys.argv:
+        diff_fd_fixture()
+    elif "--dispersed" in sys.argv:
         for n in names or DISPERSED_WORKLOADS:
             dispersed_fixture(n)
     elif "--diff" in sys.argv:

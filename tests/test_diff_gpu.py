@@ -205,3 +205,74 @@ def test_argument_checks(engines):
     with pytest.raises(RuntimeError, match="theta"):
         d.forward(t, RECORD, out=img)
     assert isinstance(MxDiffConfig(), MxDiffConfig)
+
+
+def _thetas(w):
+    return {"true": w.theta_true, "random": np.random.default_rng(7).normal(0.0, 1.0, NPARAM)}
+
+
+@pytest.mark.parametrize("at", ["true", "random"])
+def test_adjoint_matches_reference_crn_differences(engines, at):
+    """The adjoint against central differences of the reference itself
+    (tests/golden/diff_fd_reference.npz): 2e5 rays through the reference's
+    ideal mirror with each parameter moved by +-2e-3 in the HRMA geometry
+    file, the same rays (Philox variates of their tags) at every step, the
+    reference's own decisions at every step, imaged with the engine's
+    splat and compared with the same target image by MSE."""
+    import torch
+    z = np.load(os.path.join(HERE, "golden", "diff_fd_reference.npz"))
+    w = diff_workload(n_rays=int(z["n"]))
+    cfg = w.cfg.copy()
+    cfg.center_y, cfg.center_z = (float(v) for v in z["center"])
+    d = DiffImage(engines["ideal"], cfg)
+    target = torch.from_numpy(z["target"]).cuda()
+    theta = z[f"{at}_theta"]
+    img = d.forward(theta, RECORD)
+    loss, dl = d.mse(img, target)
+    assert float(loss) == pytest.approx(float(z[f"{at}_loss"]), rel=1e-9)
+    g_adj = d.adjoint(theta, dl)
+    g_ref = z[f"{at}_grad"]
+    assert int(z[f"{at}_changed"].sum()) == 0      # no ray changed its hit or miss across a step
+    rel, norm = _grad_errors(g_adj, g_ref)
+    table = "\n".join(f"{PARAM_NAMES[k]:>10s} {g_adj[k]: .6e} {g_ref[k]: .6e} {rel[k]:.2e}" for k in range(NPARAM))
+    print(f"\nadjoint vs reference CRN differences, norm-wise rel {norm:.2e}\n{table}")
+    assert np.all(rel <= GRAD_RTOL), table
+    d.close()
+
+
+@pytest.mark.parametrize("at", ["true", "random"])
+def test_adjoint_matches_oracle_crn_differences(engines, at):
+    """The adjoint of the reflecting mirror (reflectivity weights) on 1e6
+    rays against central differences of the oracle's weighted images (the
+    restatement pinned to the reference's perturbed-geometry rays), the
+    same rays at every step and decisions made afresh, as the reference
+    makes them."""
+    from oracle.bindings import Oracle
+    w = diff_workload(n_rays=1_000_000)
+    d = DiffImage.centred(engines["reflect"], w.cfg)
+    tc = d.cfg.copy()
+    tc.seed = w.target_seed
+    dt = DiffImage(engines["reflect"], tc)
+    target = dt.forward(w.theta_true, FRESH).clone()
+    dt.close()
+    theta = _thetas(w)[at]
+    img = d.forward(theta, RECORD)
+    _, dl = d.mse(img, target)
+    g_adj = d.adjoint(theta, dl)
+    o = Oracle(diff_mirror_config(ideal=False))
+    T = target.cpu().numpy()
+    h = 2e-3
+    g_fd = np.zeros(NPARAM)
+    for k in range(NPARAM):
+        L = []
+        for s in (-1.0, 1.0):
+            t = theta.copy()
+            t[k] += s * h
+            _, im = o.weighted(d.cfg, t, rays=False)
+            L.append(np.mean((im - T) ** 2))
+        g_fd[k] = (L[1] - L[0]) / (2.0 * h)
+    rel, norm = _grad_errors(g_adj, g_fd)
+    table = "\n".join(f"{PARAM_NAMES[k]:>10s} {g_adj[k]: .6e} {g_fd[k]: .6e} {rel[k]:.2e}" for k in range(NPARAM))
+    print(f"\nadjoint vs oracle CRN differences, norm-wise rel {norm:.2e}\n{table}")
+    assert np.all(rel <= GRAD_RTOL), table
+    d.close()
