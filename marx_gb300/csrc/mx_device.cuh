@@ -160,6 +160,164 @@ MXD float d2f_trunc(double d) {
   return (float) d;
 #endif
 }
+// d rounded to the nearest float (ties to even), as the cast rounds it,
+// on the integer pipe for results in the normal float range; other
+// magnitudes (and NaN) take the cast.
+MXD float d2f_rn(double d) {
+#ifdef __CUDA_ARCH__
+  const unsigned long long b = (unsigned long long) __double_as_longlong(d);
+  const uint32_t hi = (uint32_t) (b >> 32), e = (hi >> 20) & 0x7ffu;
+  if (e - 897u < 253u) {   // 2^-126 <= |d| < 2^126: the result is a normal float
+    const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+    uint32_t keep = (uint32_t) (m >> 29);                  // 24 bits with the leading one
+    const uint32_t rem = (uint32_t) m & 0x1FFFFFFFu;
+    keep += (rem > 0x10000000u || (rem == 0x10000000u && (keep & 1u))) ? 1u : 0u;
+    // a carry out of the 24 bits lands in the exponent field, as it should
+    const uint32_t r = (hi & 0x80000000u) + ((e - 896u) << 23) + (keep - 0x800000u);
+    return __uint_as_float(r);
+  }
+#endif
+  return (float) d;
+}
+// ------------------------------------------------ sines on the FP32 pipe --
+// GB300 issues FP64 at 1/64 of its FP32 rate, and a double-precision sine
+// or cosine from the math library takes about twenty FP64-pipe
+// instructions.  The angles below are reduced in double (a few exact FP64
+// operations), then sin and cos of the reduced angle r, |r| <= pi/4, are
+// evaluated in double-float arithmetic on the FP32 pipe: a value is the
+// unevaluated sum hi + lo of two floats, sums and products are formed with
+// the error-free transformations of Dekker (1971) and Knuth (TAOCP 4.2.2)
+// using fused multiply-adds.  The polynomials are the Taylor series of sin
+// and cos (truncation error below 5e-17 on |r| <= pi/4); their leading
+// terms carry double-float coefficients (1/n! split into two floats), the
+// last ones are summed in single precision where their size keeps the
+// rounding below 2^-48.  The result is within 2^-44 of the true sine or
+// cosine of the double argument.
+#ifdef __CUDA_ARCH__
+struct F2 { float h, l; };
+__device__ __forceinline__ F2 quick_sum(float a, float b) {   // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ F2 two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b), v = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v))};
+}
+__device__ __forceinline__ F2 df_add(F2 a, F2 b) {
+  const F2 s = two_sum(a.h, b.h);
+  return quick_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ F2 df_mul(F2 a, F2 b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return quick_sum(p, e);
+}
+__device__ __forceinline__ F2 df_mul_f(F2 a, float b) {
+  const float p = __fmul_rn(a.h, b);
+  float e = __fmaf_rn(a.h, b, -p);
+  e = __fmaf_rn(a.l, b, e);
+  return quick_sum(p, e);
+}
+// d as hi + lo: hi the truncation of d to float, lo that of the remainder
+// (exact in double); |d - hi - lo| < 2^-46 |d|.  One FP64 subtraction.
+__device__ __forceinline__ F2 df_from(double d) {
+  const float h = d2f_trunc(d);
+  return {h, d2f_trunc(d - f2d(h))};
+}
+__device__ __forceinline__ double df_to(F2 a) { return f2d(a.h) + f2d(a.l); }
+
+// sin and cos of r (|r| <= pi/4 + a little) in double-float.
+__device__ __forceinline__ void df_sincos(F2 r, F2 &sr, F2 &cr) {
+  const F2 z = df_mul(r, r);
+  const float zf = z.h;
+  // S(z) = (sin r - r) / (r z) = -1/3! + z/5! - z^2/7! + ...: the terms
+  // from z^4/11! on in single precision
+  float g = __fmaf_rn(zf, -0x1.ae7f3ep-41f, 0x1.612462p-33f);
+  g = __fmaf_rn(zf, g, -0x1.ae6456p-26f);
+  F2 P = df_add(F2{0x1.71de3ap-19f, 0x1.55b1ccp-45f}, df_mul_f(z, g));
+  P = df_add(F2{-0x1.a01a02p-13f, 0x1.7f97fap-39f}, df_mul(z, P));
+  P = df_add(F2{0x1.111112p-7f, -0x1.dddddep-32f}, df_mul(z, P));
+  P = df_add(F2{-0x1.555556p-3f, 0x1.555556p-28f}, df_mul(z, P));
+  sr = df_add(r, df_mul(r, df_mul(z, P)));
+  // C(z) = (cos r - 1) / z = -1/2! + z/4! - z^2/6! + ...: from z^5/12! on
+  // in single precision
+  float gc = __fmaf_rn(zf, 0x1.ae7f3ep-45f, -0x1.93974ap-37f);
+  gc = __fmaf_rn(zf, gc, 0x1.1eed8ep-29f);
+  F2 Q = df_add(F2{-0x1.27e4fcp-22f, 0x1.10ec14p-47f}, df_mul_f(z, gc));
+  Q = df_add(F2{0x1.a01a02p-16f, -0x1.7f97fap-42f}, df_mul(z, Q));
+  Q = df_add(F2{-0x1.6c16c2p-10f, 0x1.27d27ep-35f}, df_mul(z, Q));
+  Q = df_add(F2{0x1.555556p-5f, -0x1.555556p-30f}, df_mul(z, Q));
+  Q = df_add(F2{-0.5f, 0.0f}, df_mul(z, Q));
+  cr = df_add(F2{1.0f, 0.0f}, df_mul(z, Q));
+}
+#endif
+
+// sin(pi y) and cos(pi y) within 2^-44 (for angles that set positions and
+// directions, whose tolerance is far wider).  y = q/2 + f with q the
+// nearest integer to 2y, |f| <= 1/4, both exact; pi f in double-float.
+MXD void sincospi_fast(double y, double *s, double *c) {
+#ifdef __CUDA_ARCH__
+  const double magic = 6755399441055744.0;   // 1.5 2^52: the sum rounds to an integer
+  const double t = fma(y, 2.0, magic);
+  const int q = __double2loint(t);
+  const double f = fma(t - magic, -0.5, y);
+  const F2 r = df_mul(F2{0x1.921fb6p+1f, -0x1.777a5cp-24f}, df_from(f));   // pi f
+  F2 sr, cr;
+  df_sincos(r, sr, cr);
+  // sin(q pi/2 + x), cos(q pi/2 + x) from sin x, cos x
+  const double a = df_to(sr), b = df_to(cr);
+  const int k = q & 3;
+  *s = k == 0 ? a : k == 1 ? b : k == 2 ? -a : -b;
+  *c = k == 0 ? b : k == 1 ? -a : k == 2 ? -b : a;
+#else
+  *s = std::sin(PI * y); *c = std::cos(PI * y);
+#endif
+}
+
+// (float) (amp * sin(arg)) exactly as the double-precision expression
+// rounds it (the dither offsets, which Marx_Dither_Type keeps as floats).
+// arg is reduced by pi/2 in three Cody-Waite parts (the first two of 33
+// bits, so k c1 and k c2 are exact for |k| < 2^18), sin in double-float.
+// The double-float value is within amp 2^-44 of amp sin(arg), the double
+// expression within two of its own ulps; when no float rounding boundary
+// lies within twice that distance of the value, both round to the same
+// float.  Otherwise (about one value in 10^4), and for |arg| >= 2^18, the
+// library sine decides.  amp_exp: an integer with amp <= 2^amp_exp.
+MXD float sine_to_float(double amp, int amp_exp, double arg) {
+#ifdef __CUDA_ARCH__
+  const unsigned long long ab = (unsigned long long) __double_as_longlong(arg);
+  if (((ab >> 52) & 0x7ffu) < 1023u + 18u) {
+    const double magic = 6755399441055744.0;
+    const double t = fma(arg, 0x1.45f306dc9c883p-1, magic);   // arg 2/pi + magic
+    const double kd = t - magic;
+    double r = fma(-kd, 0x1.921fb544p+0, arg);
+    r = fma(-kd, 0x1.0b4611a6p-34, r);
+    r = fma(-kd, 0x1.3198a2e037073p-69, r);
+    F2 sr, cr;
+    df_sincos(df_from(r), sr, cr);
+    const int k = __double2loint(t) & 3;
+    const F2 w = (k & 1) ? cr : sr;
+    double v = amp * df_to(w);
+    if (k & 2) v = -v;
+    const unsigned long long vb = (unsigned long long) __double_as_longlong(v);
+    const int e = (int) ((vb >> 52) & 0x7ffu);
+    const int sh = amp_exp + 1031 - e;   // log2 of amp 2^-44 in ulps of v
+    if (e >= 897 && e < 1150 && sh < 26) {
+      const uint32_t low = (uint32_t) vb & 0x1FFFFFFFu;   // the 29 bits the float rounding drops
+      const uint32_t dist = low > 0x10000000u ? low - 0x10000000u : 0x10000000u - low;
+      const uint32_t margin = (2u << (sh > 0 ? sh : 0)) + 8u;
+      if (dist > margin) return d2f_rn(v);
+    }
+  }
+  return (float) (amp * sin(arg));
+#else
+  (void) amp_exp;
+  return (float) (amp * std::sin(arg));
+#endif
+}
+
 // a / b from the correctly rounded reciprocal rb = 1/b by one Markstein
 // correction: q = a rb, r = a - q b (exact with a fused multiply-add),
 // q + r rb rounds to the correctly rounded quotient, as a division does,
@@ -248,7 +406,7 @@ MXD float interp_f(float x, const float *xp, const float *yp, const double *slop
   const float xf0 = xp[n0], xf1 = xp[n1];
   if (xf1 == xf0) return yp[n1];   // the same test in float: the cast is exact
   double q = slope[n0 < n1 ? n0 : n1];
-  return (float) MX_DADD(f2d(yp[n0]), MX_DMUL(q, MX_DADD(f2d(x), -f2d(xf0))));
+  return d2f_rn(MX_DADD(f2d(yp[n0]), MX_DMUL(q, MX_DADD(f2d(x), -f2d(xf0)))));
 }
 
 // ----------------------------------------------------------- variates --
@@ -269,11 +427,23 @@ MXD void philox(uint32_t c[4], uint32_t k0, uint32_t k1) {
     c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
   }
 }
+// m 2^-53 for a 53-bit integer m, built from its bits on the integer pipe
+// (the same value the conversion and the multiplication give, without
+// their two FP64-pipe instructions).
+MXD double unit_from_bits(uint64_t m) {
+#ifdef __CUDA_ARCH__
+  if (m == 0) return 0.0;
+  const int lz = __clzll((long long) m) - 11;   // shift that brings the leading one to bit 52
+  return __longlong_as_double((long long) (((uint64_t) (1022 - lz) << 52) | ((m << lz) & 0xFFFFFFFFFFFFFull)));
+#else
+  return (double) m * (1.0 / 9007199254740992.0);
+#endif
+}
 MXD double philox_uniform(uint64_t seed, uint32_t tag, uint32_t k) {
   uint32_t c[4] = {tag, k, 0x5A5A0001u, 0u};
   philox(c, (uint32_t) seed, (uint32_t) (seed >> 32));
   uint64_t b = ((uint64_t) c[0] << 32) | c[1];
-  return (double) (b >> 11) * (1.0 / 9007199254740992.0);
+  return unit_from_bits(b >> 11);
 }
 // Single-precision natural log and cos(2 pi u) for the normal variates,
 // from their series (ln m = 2 atanh((m-1)/(m+1)); Taylor series of sin and
@@ -336,7 +506,7 @@ MXD double source_uniform(uint64_t seed, uint32_t tag, uint32_t k) {
   uint32_t c[4] = {tag, k, 0x5A5A0003u, 0u};
   philox(c, (uint32_t) seed, (uint32_t) (seed >> 32));
   uint64_t b = ((uint64_t) c[0] << 32) | c[1];
-  return (double) (b >> 11) * (1.0 / 9007199254740992.0);
+  return unit_from_bits(b >> 11);
 }
 
 // Variate source for one photon: fixed per-stage slot windows.
@@ -351,6 +521,12 @@ struct Rng {
     if (upos >= uend) { overrun = true; return 0.5; }
     int k = upos++;
     return U ? MX_LDG(U + (size_t) k * n + i) : philox_uniform(seed, tag, (uint32_t) k);
+  }
+  // Pass over the next uniform slot without drawing it (a test whose
+  // outcome is known: a probability of 1).
+  MXD void skip_uniform() {
+    if (upos >= uend) overrun = true;
+    else upos++;
   }
   MXD double normal() {
     if (npos >= nend) { overrun = true; return 0.0; }
@@ -431,7 +607,7 @@ MXD int conic_intersection(const MxShellDev &h, int o, D3 &x0, D3 p, D3 &normal)
 MXD void blur_normal(D3 &n, double blur_rad, Rng &rng) {
   const double l2 = n.y * n.y + n.z * n.z, inv = mx_rsqrt(l2), len = l2 * inv;
   double s, c;
-  mx_sincospi(2.0 * rng.uniform(), &s, &c);   // phi = 2 pi u
+  sincospi_fast(2.0 * rng.uniform(), &s, &c);   // phi = 2 pi u
   double ang = blur_rad * rng.normal();
   double sa, ca;
   sincos_small(ang, &sa, &ca);
@@ -610,7 +786,9 @@ MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *
                       Rng &rng, MirrorState &m) {
   rng.window(MX_U_MIRROR, 12, MX_N_MIRROR, 2);
   if (!T.ideal) {
-    if (rng.uniform() > T.hrma_vig) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
+    // a uniform in [0, 1) never exceeds a vignetting factor of 1
+    if (T.hrma_vig >= 1.0) rng.skip_uniform();
+    else if (rng.uniform() > T.hrma_vig) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
     if (ph.flags & MX_BAD_PHOTON_MASK) return false;
   }
   D3 x = ph.x, p = ph.p;
@@ -638,7 +816,7 @@ MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *
     if (h.shutter & (1u << quad)) break;
   }
   double st, ct;
-  mx_sincospi(2.0 * (theta - 1.0 / 8.0), &st, &ct);   // angle 2 pi (u - 1/8)
+  sincospi_fast(2.0 * (theta - 1.0 / 8.0), &st, &ct);   // angle 2 pi (u - 1/8)
   x = mk(h.front_position, radius * st - h.to_osac[0][1], radius * ct - h.to_osac[0][2]);
   if (T.source_distance > 0.0) p = normalized(x + T.source_distance * p);
   if (T.use_struts && struts_block(T, 0, x, p)) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
@@ -648,7 +826,7 @@ MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *
   p = mat_mul(h.fwd[0], p);
   m.beta = 0.0f; m.delta = 1.0f; m.corr = 1.0;
   if (T.opt_n) {
-    float fe = (float) ph.e;
+    float fe = d2f_rn(ph.e);
     m.beta = interp_f(fe, optc, optc + T.opt_n, slope, T.opt_n);
     m.delta = interp_f(fe, optc, optc + 2 * T.opt_n, slope + (T.opt_n - 1), T.opt_n);
     if (T.use_scale) {
@@ -764,14 +942,18 @@ MXD void dither_stage(const MxTables &T, Ph &ph, Rng &rng) {
     froll = T.asp_record_only ? 0.0f : s[2];
   } else {
     double t = (2.0 * PI) * (T.start_time + ph.t);
-    // A zero amplitude makes amp * sin(...) zero whatever the sine; skip it.
-    double v[3];
-    for (int k = 0; k < 3; k++)
-      v[k] = T.dith_amp[k] != 0.0 ? T.dith_amp[k] * sin(div_by(t, T.dith_period[k], T.dith_inv_period[k]) +
-                                                        T.dith_phase[k]) : 0.0;
-    fra = (float) v[0];
-    fdec = (float) v[1];
-    froll = (float) (T.nominal_roll + v[2]);
+    // amp * sin(2 pi t / period + phase) rounded to float as the reference
+    // stores it; a zero amplitude makes it zero whatever the sine
+    float f[2];
+    for (int k = 0; k < 2; k++)
+      f[k] = T.dith_amp[k] != 0.0 ? sine_to_float(T.dith_amp[k], T.dith_amp_exp[k],
+                                                  div_by(t, T.dith_period[k], T.dith_inv_period[k]) + T.dith_phase[k])
+                                  : 0.0f;
+    fra = f[0];
+    fdec = f[1];
+    if (T.roll_fixed) froll = T.roll_f;
+    else froll = (float) (T.nominal_roll + T.dith_amp[2] * sin(div_by(t, T.dith_period[2], T.dith_inv_period[2]) +
+                                                                T.dith_phase[2]));
     ph.dith[0] = fra; ph.dith[1] = fdec; ph.dith[2] = froll;
   }
   double ra = f2d(fra) + T.aspect_blur * rng.normal();
@@ -950,7 +1132,7 @@ MXD void grating_stage(const MxTables &T, const MxGratingDev *grs, int kind, Ph 
   if (ph.flags & MX_BAD_PHOTON_MASK) return;
   D3 x = rot_x(ph.x, g.cos_m, g.sin_m), p = rot_x(ph.p, g.cos_m, g.sin_m);
   if (-1 == rowland_intersect(x, p, g.rowland)) ph.flags |= MX_PHOTON_UNDIFFRACTED;
-  float fe = (float) ph.e;
+  float fe = d2f_rn(ph.e);
   int chosen = choose_order(T.geff_energy + g.geff_off, (unsigned) g.nenergy, T.geff_cum + g.cum_off, g.norders,
                             g.monotone != 0, fe, rng.uniform());
   if (chosen < 0) ph.flags |= MX_PHOTON_UNDIFFRACTED;
@@ -1281,8 +1463,8 @@ MXD void detect_stage(const MxTables &T, const MxChipDev *chips, int nchips, Ph 
     const MxChipDev &d = chips[hit];
     x = xh;
     ph.ccd = d.id;
-    ph.ypix = (float) div_by(dx, d.xpix, d.inv_xpix);
-    ph.zpix = (float) div_by(dy, d.ypix, d.inv_ypix);
+    ph.ypix = d2f_rn(div_by(dx, d.xpix, d.inv_xpix));
+    ph.zpix = d2f_rn(div_by(dy, d.ypix, d.inv_ypix));
     // with an FEF or the QE acceptance the response and the streak are a
     // pass of their own over the photons on a chip (mx_acis_fef_kernel)
     if (!T.acis_fef && !T.acis_qe) acis_streak(T, d, ph, x, p, rng);
@@ -1370,7 +1552,7 @@ MXD void drake_reflect(const MxTables &T, const MxHrcDev &h, Ph &ph, Rng &rng) {
     if ((yy < 0.0) || (yy >= r.len2)) continue;
     const bool cr = xx < h.drake_cr_width;
     ph.x = nx;
-    float fe = (float) ph.e;
+    float fe = d2f_rn(ph.e);
     float beta = hrc_interp(T, cr ? h.cr_beta : h.c_beta, fe), delta = hrc_interp(T, cr ? h.cr_delta : h.c_delta, fe);
     double rfl = reflectivity(fabs(pdn), f2d(beta), f2d(delta));
     if (rfl < rng.uniform()) { ph.flags |= MX_PHOTON_DRAKE_BLOCKED; return; }
@@ -1416,7 +1598,7 @@ MXD void hrc_detect_stage(const MxTables &T, const MxChipDev *chips, int nchips,
   }
   x = xh;
   const MxChipDev &d = chips[hit];
-  const float fe = (float) ph.e;
+  const float fe = d2f_rn(ph.e);
   bool ok = true;
   const int m = hrcs ? d.id - 1 : 0;                     // facet index 0..2
   const MxTabDev &mcp = h.mcp[hrcs ? 2 - m : 0];         // HRC-S MCP ids 1, 2, 3 use QE files 2, 1, 0

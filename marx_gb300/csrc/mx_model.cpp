@@ -1072,12 +1072,16 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
     T.dith_phase[k] = cfg.dither_phase[k];
     if (cfg.dither == MX_DITHER_INTERNAL && !(cfg.dither_period[k] > 0)) { err = "dither periods must be > 0"; return false; }
     T.dith_inv_period[k] = cfg.dither_period[k] > 0 ? 1.0 / cfg.dither_period[k] : 0.0;
+    int e = 0;
+    frexp(T.dith_amp[k], &e);   // |amp| = m 2^e, 1/2 <= m < 1
+    T.dith_amp_exp[k] = e;
   }
   double roll = cfg.roll_nom * (PI_ / 180.0);
   double xr = fmod(roll, 2 * PI_);
   if (xr >= PI_) xr -= (2 * PI_);
   if (xr < -PI_) xr += (2 * PI_);
   T.nominal_roll = xr;
+  T.roll_f = (float) (T.nominal_roll + 0.0);
   // With no roll amplitude every photon is rolled by the same float angle
   // (get_internal_dither, dither.c:175): its sine and cosine are taken once
   // here as the per-photon code would take them (series below 1e-3 rad).

@@ -142,6 +142,8 @@ struct MxTables {
   int32_t dither, grating;      // grating: MX_GRATING_* of the configuration
   double dith_amp[3], dith_period[3], dith_phase[3], nominal_roll, aspect_blur, start_time;
   double dith_inv_period[3];    // correctly rounded 1 / dith_period
+  int32_t dith_amp_exp[3];      // dith_amp <= 2^dith_amp_exp (sine_to_float)
+  float roll_f;                 // (float) nominal_roll, the roll of every photon when roll_fixed
   int32_t roll_fixed, roll_zero;// roll amplitude 0: the roll angle is the same for every photon (zero: no roll)
   double roll_cos, roll_sin;    // cos and sin of -(float) nominal_roll, when roll_fixed
   // DitherModel FILE (mx_set_aspect_solution): rows 0 .. asp_n of the
