@@ -150,7 +150,35 @@ def cpu_sample(w, n, threads):
     return n / (time.perf_counter() - t0)
 
 
-def bench_batched(a):
+def batched_flops(sources, n_sample=20_000):
+    """Algorithmic FP64 operations of the batch: the oracle's counting
+    arithmetic on a sample of each (grating, detector) pair's photons, drawn
+    from its sources in proportion to their counts (energies uniform over
+    each source's band, each source's direction), times the pair's photons."""
+    import numpy as np
+    from marx_gb300 import batched as B
+    from marx_gb300.photons import PhotonList
+    from oracle.bindings import Oracle
+    counts = np.array([s.num_photons for s in sources], dtype=np.float64)
+    total = counts.sum()
+    r = np.random.default_rng(12)
+    flops = 0.0
+    for g in sorted({s.grating for s in sources}):
+        for d in sorted({s.detector for s in sources}):
+            idx = [k for k, s in enumerate(sources) if s.grating == g and s.detector == d]
+            if not idx:
+                continue
+            take = [max(1, int(round(n_sample * counts[k] / total))) for k in idx]
+            E = np.concatenate([r.uniform(sources[k].energy_min, sources[k].energy_max, m) for k, m in zip(idx, take)])
+            P = np.concatenate([np.repeat(np.array(sources[k].p[:])[:, None], m, 1) for k, m in zip(idx, take)], 1)
+            cfg = B.batched_config()
+            cfg.grating, cfg.detector = g, d
+            ops, cnt = Oracle(cfg).count_flops(PhotonList.from_inputs(E, P), seed=5)
+            flops += ops / cnt * counts[idx].sum()
+    return flops
+
+
+def bench_batched(a, fp64_peak):
     """256 uneven point sources: one persistent graph launch (after the
     autotuner chose its launch shape) against 256 sequential plain traces
     of the same photons.  Both write identical per-photon results."""
@@ -158,7 +186,8 @@ def bench_batched(a):
     from marx_gb300 import batched as B
     from marx_gb300._native import Engine
     eng = Engine(B.batched_config())
-    b = B.Batch(eng, B.batched_sources())
+    sources = B.batched_sources()
+    b = B.Batch(eng, sources)
     t0 = time.perf_counter()
     params = b.tune(trials=2)
     tune_s = time.perf_counter() - t0
@@ -179,12 +208,20 @@ def bench_batched(a):
     k = max(2, min(a.steps, 5))
     ms_b = timed(b.run, k)
     ms_s = timed(b.run_sequential, k)
+    flops = batched_flops(sources)
+    achieved = flops / (ms_b * 1e-3) / 1e12
+    roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+            "algorithmic_flops_per_photon": flops / b.n,
+            "sequential_frac": flops / (ms_s * 1e-3) / 1e12 / fp64_peak,
+            "note": "graph launch time (generation and trace of every source); per-photon operations from the "
+                    "oracle's counting arithmetic per (grating, detector) pair"}
     return {"workload": "256 point sources, photons log-uniform 1e3-1e6 per source, 0-10 arcmin, 0.3-10 keV, "
                         "grating NONE|HETG and ACIS-I|ACIS-S per source",
             "photons_per_step": b.n, "steps": k,
             "batched_photons_per_s": b.n / (ms_b * 1e-3), "sequential_photons_per_s": b.n / (ms_s * 1e-3),
             "batched_ms": ms_b, "sequential_ms": ms_s, "speedup": ms_s / ms_b,
-            "tuned_params": params, "tune_seconds": tune_s}
+            "tuned_params": params, "tune_seconds": tune_s,
+            "roofline": roof}
 
 
 def bench_diff(a, fp64_peak):
@@ -653,7 +690,7 @@ def main():
     torch.cuda.empty_cache()
     configs = None if a.no_configs else {c: bench_config(a, c, fp64_peak) for c in ("plain_onaxis", "plain_hetg")
                                          if c != a.workload}
-    batched = None if a.no_batched else bench_batched(a)
+    batched = None if a.no_batched else bench_batched(a, fp64_peak)
     differentiable = None if a.no_diff else bench_diff(a, fp64_peak)
     workloads = None if a.no_workloads else bench_workloads(
         a, {a.workload} | (set() if a.no_configs else {"plain_onaxis", "plain_hetg"}))

@@ -773,19 +773,24 @@ int mx_batch_tune(mx_batch *b, int trials, mx_batch_params *best) {
       return MX_OK;
     }
   }
+  // block sizes up to the kernel's bound, warp tiles from one warp's worth
+  // of photons to 1024, and resident blocks per SM from the register limit
+  // down to half of it
   std::vector<mx_batch_params> cand;
-  const int blocks[2] = {128, 256};
-  const int tiles[3] = {64, 256, 1024};
+  const int blocks[4] = {64, 128, 192, 256};
+  const int tiles[5] = {32, 64, 128, 256, 1024};
   for (int bl : blocks) {
     int maxb = 0;
     int r = batch_max_blocks(b, bl, &maxb);
     if (r) return r;
     if (maxb < 1) continue;
-    int per[2] = {maxb, std::max(1, maxb / 2)};
-    for (int k = 0; k < (per[0] == per[1] ? 1 : 2); k++)
+    std::vector<int> per = {maxb};
+    for (int v : {(3 * maxb + 3) / 4, maxb / 2})
+      if (v >= 1 && v != per.back()) per.push_back(v);
+    for (int pb : per)
       for (int t : tiles) {
         mx_batch_params q;
-        q.block = bl; q.tile = t; q.blocks_per_sm = per[k]; q.reserved = 0;
+        q.block = bl; q.tile = t; q.blocks_per_sm = pb; q.reserved = 0;
         cand.push_back(q);
       }
   }
