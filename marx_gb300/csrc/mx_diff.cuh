@@ -35,6 +35,17 @@ struct Dual6 {
   float d[ND];
 };
 
+// A value rounded to single precision for the tangents, which are single
+// precision anyway: on the device by truncation on the integer pipe (a
+// conversion instruction would take an FP64-pipe slot).
+MXG float tof(double x) {
+#ifdef __CUDA_ARCH__
+  return mx::d2f_trunc(x);
+#else
+  return (float) x;
+#endif
+}
+
 MXG double val(double a) { return a; }
 MXG double val(const Dual6 &a) { return a.v; }
 
@@ -60,13 +71,13 @@ MXG Dual6 operator-(const Dual6 &a) {
 }
 MXG Dual6 operator*(const Dual6 &a, const Dual6 &b) {
   Dual6 r; r.v = a.v * b.v;
-  const float av = (float) a.v, bv = (float) b.v;
+  const float av = tof(a.v), bv = tof(b.v);
   for (int k = 0; k < ND; k++) r.d[k] = av * b.d[k] + bv * a.d[k];
   return r;
 }
 MXG Dual6 operator*(double s, const Dual6 &a) {
   Dual6 r; r.v = s * a.v;
-  const float f = (float) s;
+  const float f = tof(s);
   for (int k = 0; k < ND; k++) r.d[k] = f * a.d[k];
   return r;
 }
@@ -81,49 +92,60 @@ MXG Dual6 operator-(double s, const Dual6 &a) {
 }
 MXG Dual6 operator/(const Dual6 &a, const Dual6 &b) {
   Dual6 r; r.v = a.v / b.v;
-  const float ib = (float) (1.0 / b.v), q = (float) r.v;
+  const float ib = 1.0f / tof(b.v), q = tof(r.v);
   for (int k = 0; k < ND; k++) r.d[k] = (a.d[k] - q * b.d[k]) * ib;
   return r;
 }
 MXG Dual6 operator/(double s, const Dual6 &b) {
   Dual6 r; r.v = s / b.v;
-  const float g = (float) (-r.v / b.v);
+  const float g = -tof(r.v) / tof(b.v);
   for (int k = 0; k < ND; k++) r.d[k] = g * b.d[k];
   return r;
 }
 MXG Dual6 operator/(const Dual6 &a, double s) {
   Dual6 r; r.v = a.v / s;
-  const float f = (float) (1.0 / s);
+  const float f = 1.0f / tof(s);
   for (int k = 0; k < ND; k++) r.d[k] = a.d[k] * f;
   return r;
 }
 MXG double dsqrt(double a) { return sqrt(a); }
 MXG Dual6 dsqrt(const Dual6 &a) {
   Dual6 r; r.v = sqrt(a.v);
-  const float h = (float) (0.5 / r.v);
+  const float h = 0.5f / tof(r.v);
   for (int k = 0; k < ND; k++) r.d[k] = h * a.d[k];
   return r;
 }
+// 1 / sqrt(a): one reciprocal square root instead of a square root and a
+// division (normalisations, the Fresnel root).
+MXG double drsqrt(double a) { return mx::mx_rsqrt(a); }
+MXG Dual6 drsqrt(const Dual6 &a) {
+  Dual6 r; r.v = mx::mx_rsqrt(a.v);
+  const float t = tof(r.v), h = -0.5f * t * t * t;
+  for (int k = 0; k < ND; k++) r.d[k] = h * a.d[k];
+  return r;
+}
+MXG double dcopysign(double a, double b) { return copysign(a, b); }
+MXG Dual6 dcopysign(const Dual6 &a, const Dual6 &b) { return (a.v < 0.0) != (b.v < 0.0) ? -a : a; }
 MXG double dabs(double a) { return fabs(a); }
 MXG Dual6 dabs(const Dual6 &a) { return a.v < 0.0 ? -a : a; }
 MXG double dsin(double a) { return sin(a); }
 MXG double dcos(double a) { return cos(a); }
 MXG Dual6 dsin(const Dual6 &a) {
   Dual6 r; r.v = sin(a.v);
-  const float c = (float) cos(a.v);
+  const float c = cosf(tof(a.v));
   for (int k = 0; k < ND; k++) r.d[k] = c * a.d[k];
   return r;
 }
 MXG Dual6 dcos(const Dual6 &a) {
   Dual6 r; r.v = cos(a.v);
-  const float s = (float) -sin(a.v);
+  const float s = -sinf(tof(a.v));
   for (int k = 0; k < ND; k++) r.d[k] = s * a.d[k];
   return r;
 }
 MXG double dtan(double a) { return tan(a); }
 MXG Dual6 dtan(const Dual6 &a) {
   Dual6 r; r.v = tan(a.v);
-  const float s = (float) (1.0 + r.v * r.v);
+  const float t = tof(r.v), s = 1.0f + t * t;
   for (int k = 0; k < ND; k++) r.d[k] = s * a.d[k];
   return r;
 }
@@ -140,7 +162,7 @@ template <class S> MXG V3<S> operator-(const V3<S> &a, const V3<S> &b) { return 
 template <class S> MXG V3<S> scale(const S &s, const V3<S> &a) { return v3<S>(s * a.x, s * a.y, s * a.z); }
 template <class S> MXG S dotp(const V3<S> &a, const V3<S> &b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 template <class S> MXG V3<S> unit(const V3<S> &a) {
-  S inv = 1.0 / dsqrt(dotp(a, a));
+  S inv = drsqrt(dotp(a, a));
   return scale(inv, a);
 }
 template <class S> MXG V3<S> matv(const S *m, const V3<S> &v) {
@@ -198,14 +220,17 @@ template <class S> MXG S fresnel(const S &cos_t, double beta, double delta) {
   S sin2 = 1.0 - cos_t * cos_t;
   S wr = sr - sin2;
   const double wi = si;
+  // the principal square root of wr + i wi: with q^2 = h = (r + |wr|) / 2,
+  // q = h / sqrt(h) and wi / (2 q) = (wi / 2) / sqrt(h), one reciprocal
+  // square root for both
   S r = dsqrt(wr * wr + wi * wi);
   S rr, ri;
   if (val(wr) >= 0.0) {
-    S q = dsqrt(0.5 * (r + wr));
-    rr = q; ri = (0.5 * wi) / q;
+    S h = 0.5 * (r + wr), inv = drsqrt(h);
+    rr = h * inv; ri = (0.5 * wi) * inv;
   } else {
-    S q = dsqrt(0.5 * (r - wr));
-    rr = (0.5 * wi) / q; ri = q;
+    S h = 0.5 * (r - wr), inv = drsqrt(h);
+    rr = (0.5 * wi) * inv; ri = h * inv;
     if (val(rr) < 0.0) { rr = 0.0 - rr; ri = 0.0 - ri; }
   }
   S a1 = (cos_t - rr) * (cos_t - rr) + ri * ri, b1 = (cos_t + rr) * (cos_t + rr) + ri * ri;
@@ -231,8 +256,11 @@ MXG bool conic_hit(const Optic<S> &o, V3<S> &x0, const V3<S> &p, V3<S> &n, int r
   if (val(alpha) == 0.0) return false;
   S bsqr = beta * beta, ac4 = alpha * gamma * 4.0;
   if (!(val(bsqr) > val(ac4))) return false;
-  S factor = 1.0 + dsqrt(1.0 - ac4 / bsqr);
-  S tp = (-2.0 * gamma) / (beta * factor), tm = (0.0 - beta) * factor / (2.0 * alpha);
+  // the roots -2 gamma / (beta f) and -beta f / (2 alpha) of the reference,
+  // f = 1 + sqrt(1 - 4 alpha gamma / beta^2), from b f = beta + sign(beta)
+  // sqrt(beta^2 - 4 alpha gamma) and one reciprocal of alpha b f
+  S bf = beta + dcopysign(dsqrt(bsqr - ac4), beta), inv = 1.0 / (alpha * bf);
+  S tp = (-2.0 * gamma) * alpha * inv, tm = (-0.5 * bf) * bf * inv;
   int pick = root;
   if (root < 0) {
     const double xp = val(p.x) * val(tp), xm = val(p.x) * val(tm);
