@@ -688,13 +688,20 @@ def main():
     cpu_rate = cpu_sample(w, 200_000, os.cpu_count() or 1)
     del d, p0, flags0
     torch.cuda.empty_cache()
-    configs = None if a.no_configs else {c: bench_config(a, c, fp64_peak) for c in ("plain_onaxis", "plain_hetg")
-                                         if c != a.workload}
-    batched = None if a.no_batched else bench_batched(a, fp64_peak)
-    differentiable = None if a.no_diff else bench_diff(a, fp64_peak)
-    workloads = None if a.no_workloads else bench_workloads(
-        a, {a.workload} | (set() if a.no_configs else {"plain_onaxis", "plain_hetg"}))
-    events = None if a.no_events else bench_events(a)
+    def section(fn, *args):
+        # a failing section is reported in its place; the headline line stands
+        try:
+            return fn(*args)
+        except Exception as e:  # noqa: BLE001
+            return {"error": f"{type(e).__name__}: {e}"}
+
+    configs = None if a.no_configs else {c: section(bench_config, a, c, fp64_peak)
+                                         for c in ("plain_onaxis", "plain_hetg") if c != a.workload}
+    batched = None if a.no_batched else section(bench_batched, a, fp64_peak)
+    differentiable = None if a.no_diff else section(bench_diff, a, fp64_peak)
+    workloads = None if a.no_workloads else section(
+        bench_workloads, a, {a.workload} | (set() if a.no_configs else {"plain_onaxis", "plain_hetg"}))
+    events = None if a.no_events else section(bench_events, a)
 
     line = {
         "metric": METRIC, "value": value, "unit": "photons/s", "n_gpus": world, "steps": a.steps,

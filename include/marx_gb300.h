@@ -430,7 +430,7 @@ int mx_generate_source(mx_context *ctx, const mx_source *src, uint32_t first_tag
  * source-table and configuration hash for the life of the process). */
 typedef struct mx_batch mx_batch;
 typedef struct mx_batch_params {
-  int32_t block;            /* threads per block: 128 or 256 */
+  int32_t block;            /* threads per block: 32 to 256 in whole warps */
   int32_t tile;             /* photons a warp claims per visit of the work counter (multiple of 32) */
   int32_t blocks_per_sm;    /* resident blocks per SM (<= the occupancy limit) */
   int32_t reserved;

@@ -685,8 +685,12 @@ void mx_batch_destroy(mx_batch *b) {
 
 int mx_batch_set_params(mx_batch *b, const mx_batch_params *p) {
   if (!b || !p) return MX_EINVAL;
-  if ((p->block != 128 && p->block != 256) || p->tile < 32 || (p->tile % 32) != 0 || p->blocks_per_sm < 1)
-    return mx_fail(b->ctx, MX_EINVAL, "mx_batch_set_params: block must be 128 or 256, tile a positive multiple of 32");
+  // warps claim tiles on their own, so any whole number of warps up to the
+  // kernel's bound of 256 threads works
+  if (p->block < 32 || p->block > 256 || (p->block % 32) != 0 || p->tile < 32 || (p->tile % 32) != 0 ||
+      p->blocks_per_sm < 1)
+    return mx_fail(b->ctx, MX_EINVAL, "mx_batch_set_params: block must be 32 to 256 threads in whole warps, "
+                                      "tile a positive multiple of 32");
   int maxb = 0;
   int r = batch_max_blocks(b, p->block, &maxb);
   if (r) return r;
@@ -753,8 +757,8 @@ int mx_batch_photons(mx_batch *b, mx_photons *dev_view, const uint32_t **source_
 
 uint64_t mx_batch_total_photons(const mx_batch *b) { return b ? b->total : 0; }
 
-// The autotuner: every block size the kernel supports, the largest and
-// half the largest resident block count per SM, and three work-tile sizes,
+// The autotuner: block sizes of 64 to 256 threads, resident block counts
+// per SM from the largest down to half of it, and five work-tile sizes,
 // each timed with CUDA events over `trials` graph launches after one
 // warm-up launch (which also captures that candidate's graph).  The
 // fastest mean wins and is remembered under the batch's hash.

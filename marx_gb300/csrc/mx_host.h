@@ -41,4 +41,14 @@ struct HostModel {
 
 bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string &err);
 
+// The parameters of a MARX parameter file (name,type,mode,value,... per
+// line) plus "Name=value" overrides, a later entry winning (mx_par.cpp).
+struct ParSet {
+  std::vector<std::pair<std::string, std::string>> kv;
+  const std::string *find(const std::string &name) const;
+};
+bool load_par(const char *path, const char *const *overrides, int n_overrides, ParSet &out, std::string &err);
+// An mx_param_reader over a ParSet (user: the ParSet).
+int par_reader(void *user, const char *name, char type, char *value, size_t len);
+
 }  // namespace mx

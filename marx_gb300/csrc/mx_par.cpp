@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "../../include/marx_gb300.h"
+#include "mx_host.h"
 
 extern int mx_fail(struct mx_context *c, int code, const std::string &msg);
 
@@ -223,24 +224,46 @@ std::vector<std::string> csv_fields(const std::string &line) {
   return f;
 }
 
-struct ParFile {
-  std::vector<std::pair<std::string, std::string>> kv;
-  const std::string *find(const std::string &name) const {
-    for (size_t k = kv.size(); k-- > 0;)   // a later line or override wins
-      if (kv[k].first == name) return &kv[k].second;
-    return nullptr;
+}  // namespace
+
+namespace mx {
+
+const std::string *ParSet::find(const std::string &name) const {
+  for (size_t k = kv.size(); k-- > 0;)   // a later line or override wins
+    if (kv[k].first == name) return &kv[k].second;
+  return nullptr;
+}
+
+bool load_par(const char *path, const char *const *overrides, int n_overrides, ParSet &out, std::string &err) {
+  FILE *f = fopen(path, "r");
+  if (!f) { err = std::string("cannot open ") + path; return false; }
+  out.kv.clear();
+  char line[4096];
+  while (fgets(line, sizeof line, f)) {
+    std::string s = trim(line);
+    if (s.empty() || s[0] == '#') continue;
+    std::vector<std::string> fl = csv_fields(s);
+    if (fl.size() >= 4) out.kv.emplace_back(trim(fl[0]), trim(fl[3]));
   }
-};
+  fclose(f);
+  for (int k = 0; k < n_overrides; k++) {
+    const char *o = overrides ? overrides[k] : nullptr;
+    const char *eq = o ? strchr(o, '=') : nullptr;
+    if (!eq) { err = std::string("override without '=': ") + (o ? o : ""); return false; }
+    out.kv.emplace_back(trim(std::string(o, eq - o)), trim(std::string(eq + 1)));
+  }
+  return true;
+}
 
 int par_reader(void *user, const char *name, char type, char *value, size_t len) {
   (void) type;
-  const std::string *v = ((const ParFile *) user)->find(name);
+  const std::string *v = ((const ParSet *) user)->find(name);
   if (!v || len == 0) return -1;
   snprintf(value, len, "%s", v->c_str());
   return 0;
 }
 
-}  // namespace
+}  // namespace mx
 
 extern "C" {
 
@@ -273,25 +296,11 @@ int mx_param_type(const char *name, char *type, uint32_t *group) {
 
 int mx_config_read_par(mx_config *cfg, const char *path, const char *const *overrides, int n_overrides) {
   if (!cfg || !path) return mx_fail(nullptr, MX_EINVAL, "mx_config_read_par: null argument");
-  FILE *f = fopen(path, "r");
-  if (!f) return mx_fail(nullptr, MX_EINVAL, std::string("mx_config_read_par: cannot open ") + path);
-  ParFile pf;
-  char line[4096];
-  while (fgets(line, sizeof line, f)) {
-    std::string s = trim(line);
-    if (s.empty() || s[0] == '#') continue;
-    std::vector<std::string> fl = csv_fields(s);
-    if (fl.size() >= 4) pf.kv.emplace_back(trim(fl[0]), fl[3]);
-  }
-  fclose(f);
-  for (int k = 0; k < n_overrides; k++) {
-    const char *o = overrides ? overrides[k] : nullptr;
-    const char *eq = o ? strchr(o, '=') : nullptr;
-    if (!eq) return mx_fail(nullptr, MX_EINVAL, std::string("mx_config_read_par: override without '=': ") + (o ? o : ""));
-    pf.kv.emplace_back(trim(std::string(o, eq - o)), std::string(eq + 1));
-  }
+  mx::ParSet pf;
+  std::string err;
+  if (!mx::load_par(path, overrides, n_overrides, pf, err)) return mx_fail(nullptr, MX_EINVAL, "mx_config_read_par: " + err);
   mx_config_default(cfg);
-  return mx_config_read_params(cfg, MX_PARAMS_ALL, par_reader, &pf, 0);
+  return mx_config_read_params(cfg, MX_PARAMS_ALL, mx::par_reader, &pf, 0);
 }
 
 }  // extern "C"

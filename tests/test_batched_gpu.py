@@ -35,6 +35,22 @@ def test_batched_equals_sequential(cuda):
     assert ((one.flags & 0xFF) == 0).mean() > 0.05
 
 
+@pytest.mark.parametrize("block,tile", [(64, 32), (192, 128)])
+def test_every_launch_shape_gives_the_same_photons(cuda, block, tile):
+    """The tuner's search space: other block sizes and tiles change who
+    traces which photon, never a photon's result."""
+    import torch
+    eng = engine()
+    b = small_batch(eng, nsrc=12, seed=4)
+    b.run(seed=9)
+    torch.cuda.synchronize()
+    ref = b.to_host()
+    b.set_params(block, tile, 1)
+    b.run(seed=9)
+    torch.cuda.synchronize()
+    assert_parity(b.to_host(), ref, f"block {block} tile {tile}")
+
+
 def test_batched_matches_oracle_per_source(cuda):
     import torch
     from oracle.bindings import Oracle
@@ -65,14 +81,14 @@ def test_batched_matches_oracle_per_source(cuda):
             setattr(part, k, getattr(q, k)[:, n0:n1])
         for k in ("flags", "mirror_shell", "order", "ccd_num", "y_pixel", "z_pixel"):
             setattr(part, k, getattr(q, k)[n0:n1])
-        assert_parity(part, ph, f"source {s}")
+        assert_parity(part, ph, f"source {s}", pixel_ulps=1)
 
 
 def test_tuner_picks_a_valid_shape_and_remembers_it(cuda):
     eng = engine()
     b = small_batch(eng, nsrc=16, seed=1)
     p = b.tune(trials=1)
-    assert p["block"] in (128, 256) and p["tile"] % 32 == 0 and p["blocks_per_sm"] >= 1
+    assert p["block"] in (64, 128, 192, 256) and p["tile"] % 32 == 0 and p["blocks_per_sm"] >= 1
     b2 = small_batch(eng, nsrc=16, seed=1)
     assert b2.params() == p
     assert b2.tune(trials=1) == p
