@@ -546,6 +546,36 @@ void *mx_stream(mx_context *ctx);
 /* Photons flagged MX_PHOTON_VARIATE_OVERRUN since the last reset. */
 int mx_overrun_count(mx_context *ctx, unsigned long long *count, int reset);
 
+/* ------------------------------------------------------------- runs --
+ * marx's main loop (marx/src/marx.c:545-608) on the GPU: the parameter
+ * file par_path (marx.par format) with "Name=value" overrides configures
+ * the engine and the run, as the marx program reads them: SourceType
+ * (POINT, GAUSS, BETA, DISK, LINE) with SourceRA, SourceDEC,
+ * SourceDistance and the model's S-* parameters; SpectrumType FLAT
+ * (MinEnergy, MaxEnergy) or FILE (SpectrumFile) with SourceFlux; NumRays
+ * (photons to create, or with a minus sign to detect) in batches of
+ * dNumRays, or ExposureTime (s) when positive; RandomSeed (-1: from the
+ * clock); OutputDir, OutputVectors, DumpToRayFile and RayFile.  Each batch
+ * is created on the device (energies and directions of the source model,
+ * Poisson arrival times with mean 1 / (SourceFlux x the mirror's open
+ * area), tags from 0 on), traced through every stage and written to
+ * OutputDir (mx_write_photons), or with DumpToRayFile = yes dithered and
+ * written to RayFile (mx_write_rayfile); OutputDir then receives marx.par
+ * (the parameter file with the overrides) and obs.par (the detector's
+ * observation template from the table pack with the run's pointing,
+ * detector, grating and times), as marx leaves them for marx2fits.
+ * Results are statistically, not photon for photon, those of the
+ * reference's marx: its generator differs. */
+typedef struct mx_run_stats {
+  uint64_t collected;      /* photons created */
+  uint64_t detected;       /* photons written (no MX_BAD_PHOTON_MASK bit) */
+  double total_time;       /* simulated exposure (s) */
+  uint32_t iterations;     /* batches */
+  uint32_t reserved;
+} mx_run_stats;
+int mx_run_marx(const char *pack_path, const char *par_path, const char *const *overrides, int n_overrides,
+                mx_run_stats *stats);
+
 /* ------------------------------------------------------------ output --
  * MARX's output directory format (marx_write_photons, marxio.c:395-478):
  * one big-endian column file per attribute (xpos.dat, energy.dat,

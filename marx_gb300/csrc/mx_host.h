@@ -19,6 +19,7 @@ struct Pack {
 // Host copies of every device table, plus the scalar launch parameters.
 struct HostModel {
   MxTables T;
+  double geom_area_cm2 = 0.0;   // Marx_Mirror_Geometric_Area (hrma.c:736): the open aperture area, cm^2
   std::vector<MxShellDev> shells;
   std::vector<float> optc;
   std::vector<double> optc_slope;

@@ -846,6 +846,7 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
     append_slopes(M.optc_slope, corr, corr + h.corr_n, (unsigned) h.corr_n);
   }
   if (total_area <= 0.0) { err = "The mirror geometric area is 0.  Check shutters."; return false; }
+  M.geom_area_cm2 = (total_area * PI_) / 100.0;
   for (auto &h : M.shells) h.area_fraction = h.area_fraction / total_area;
   T.optc_len = (int32_t) M.optc.size();
   if (M.optc_slope.empty()) M.optc_slope.push_back(0.0);
