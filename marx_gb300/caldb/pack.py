@@ -418,7 +418,24 @@ def build_sections(data_dir: str) -> dict:
     for h, c in qe:
         if h.get("EXTNAME") == "AXAF_QE":
             S[f"acis/qe{int(h['CCD_ID'])}"] = np.vstack([c["ENERGY"], c["QE"]]).astype(np.float32)
+    # the observation templates obs.par of a run starts from (write_obs_par,
+    # marx.c:999-1196), as text sections
+    obs_dir = os.path.join(data_dir, "obs")
+    for f in sorted(os.listdir(obs_dir)) if os.path.isdir(obs_dir) else []:
+        if f.endswith(".par"):
+            S[f"obs/{f[:-4]}"] = text_section(open(os.path.join(obs_dir, f), "rb").read())
     return S
+
+
+def text_section(b: bytes) -> np.ndarray:
+    """Bytes as an int32 section: the byte count, then the bytes four to a
+    word (little-endian), zero padded."""
+    pad = b + b"\0" * (-len(b) % 4)
+    return np.concatenate([np.array([len(b)], dtype=np.int32), np.frombuffer(pad, dtype="<i4").astype(np.int32)])
+
+
+def section_text(a: np.ndarray) -> bytes:
+    return a[1:].astype("<i4").tobytes()[: int(a[0])]
 
 
 DEFAULT_PACK = os.path.join(os.path.dirname(os.path.abspath(__file__)), "marx_tables.mxpack")

@@ -406,6 +406,9 @@ extern "C" int mx_run_marx(const char *pack_path, const char *par_path, const ch
   mx_context *c = mx_create(pack_path, &cfg);
   if (!c) return MX_EPACK;
   struct Closer { mx_context *c; ~Closer() { mx_destroy(c); } } closer{c};
+  // errors past this point are reported with no context (it is destroyed
+  // on return): the context's message moves to mx_last_error(NULL)
+  auto ctx_fail = [&](int code) { return mx_fail(nullptr, code, "mx_run_marx: " + c->err); };
   const double mt = 1.0 / flux / c->hm.geom_area_cm2;   // compute_mean_time (source.c:260-264)
   cudaStream_t st = c->stream;
   const uint32_t cap = (uint32_t) drays;
@@ -414,7 +417,7 @@ extern "C" int mx_run_marx(const char *pack_path, const char *par_path, const ch
   cudaError_t e = dev.ensure(cap);
   const uint32_t ntile = (cap + TIME_TILE - 1) / TIME_TILE;
   if (e == cudaSuccess) e = sums.ensure((size_t) ntile * sizeof(double));
-  if (e != cudaSuccess) return mx_cuda_fail(c, e, "mx_run_marx: allocating the photon columns");
+  if (e != cudaSuccess) return mx_cuda_fail(nullptr, e, "mx_run_marx: allocating the photon columns");
   HostList host;
   std::vector<double> times(cap);
   const uint32_t history = mx_output_history(&cfg, MX_STAGE_ALL);
@@ -440,7 +443,7 @@ extern "C" int mx_run_marx(const char *pack_path, const char *par_path, const ch
     mx_photons d = dev.ph;
     d.n = per_iter;
     d.stride = cap;
-    if ((r = mx_generate_source(c, &src, tag_start, seed, &d, st)) != MX_OK) return r;
+    if ((r = mx_generate_source(c, &src, tag_start, seed, &d, st)) != MX_OK) return ctx_fail(r);
     mx_time_tiles<<<(per_iter + TIME_TILE - 1) / TIME_TILE, TIME_THREADS, 0, st>>>(d.arrival_time, per_iter, seed,
                                                                                  tag_start, mt, (double *) sums.ptr);
     mx_time_offsets<<<1, 1024, 0, st>>>((double *) sums.ptr, (per_iter + TIME_TILE - 1) / TIME_TILE);
@@ -449,24 +452,26 @@ extern "C" int mx_run_marx(const char *pack_path, const char *par_path, const ch
     c->launches += 3;
     e = cudaMemcpyAsync(times.data(), d.arrival_time, (size_t) per_iter * 8, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return mx_cuda_fail(c, e, "mx_run_marx: photon times");
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) return mx_cuda_fail(nullptr, e, "mx_run_marx: photon times");
     uint32_t n = per_iter;
     if (exposure > 0.0)   // the first photon at or past the time left ends the batch (source.c:327-333)
       for (uint32_t i = 0; i < per_iter; i++)
         if (times[i] >= left) { n = i + 1; break; }
     d.n = n;
-    if ((r = mx_set_start_time(c, start_time)) != MX_OK) return r;
+    if ((r = mx_set_start_time(c, start_time)) != MX_OK) return ctx_fail(r);
     const uint32_t stages = dump ? MX_STAGE_DITHER : MX_STAGE_ALL;   // the ray file holds the dithered rays
-    if ((r = mx_trace_tables(c, c->T, &d, stages, nullptr, nullptr, seed, st, true)) != MX_OK) return r;
-    if ((e = copy_out(d, cap, n, host, st)) != cudaSuccess) return mx_cuda_fail(c, e, "mx_run_marx: copying photons out");
+    if ((r = mx_trace_tables(c, c->T, &d, stages, nullptr, nullptr, seed, st, true)) != MX_OK) return ctx_fail(r);
+    if ((e = copy_out(d, cap, n, host, st)) != cudaSuccess)
+      return mx_cuda_fail(nullptr, e, "mx_run_marx: copying photons out");
     if (dump) {
       if ((r = mx_write_rayfile(&host.ph, history & (MX_OUT_ENERGY | MX_OUT_TIME | MX_OUT_X | MX_OUT_P | MX_OUT_TAG |
                                                      MX_OUT_SKY_DITHER),
                                 ray_file.c_str(), first ? 0 : 1, total_time)) != MX_OK)
-        return mx_fail(c, r, std::string("mx_run_marx: ") + mx_write_error());
+        return mx_fail(nullptr, r, std::string("mx_run_marx: ") + mx_write_error());
     } else if ((r = mx_write_photons(&host.ph, history, write_mask, cfg.dither != MX_DITHER_NONE, out_dir.c_str(),
                                      first ? 0 : 1, total_time)) != MX_OK)
-      return mx_fail(c, r, std::string("mx_run_marx: ") + mx_write_error());
+      return mx_fail(nullptr, r, std::string("mx_run_marx: ") + mx_write_error());
     first = false;
     uint32_t good = 0;
     for (uint32_t i = 0; i < n; i++) good += (host.flags[i] & MX_BAD_PHOTON_MASK) == 0;
@@ -496,7 +501,7 @@ extern "C" int mx_run_marx(const char *pack_path, const char *par_path, const ch
       const char *o = overrides[k], *eq = strchr(o, '=');
       par_set(lines, std::string(o, eq - o), std::string(eq + 1), 's');
     }
-    if (!write_text(out_dir + "/marx.par", lines)) return mx_fail(c, MX_EINVAL, "mx_run_marx: writing marx.par");
+    if (!write_text(out_dir + "/marx.par", lines)) return mx_fail(nullptr, MX_EINVAL, "mx_run_marx: writing marx.par");
     static const char *det_names[5] = {"NONE", "ACIS-I", "ACIS-S", "HRC-I", "HRC-S"};
     static const char *tmpl[5] = {"generic_obs", "acis_i_obs", "acis_s_obs", "hrc_i_obs", "hrc_s_obs"};
     const std::string det = det_names[cfg.detector], grat = cfg.grating == 1 ? "HETG" : cfg.grating == 2 ? "LETG" : "NONE";
@@ -526,7 +531,7 @@ extern "C" int mx_run_marx(const char *pack_path, const char *par_path, const ch
       par_set(obs, "defocus", fmt(cfg.det_offset[0]), 'r');
       for (const char *k : {"DY_AVG", "DZ_AVG", "DTH_AVG"}) par_set(obs, k, fmt(0.0), 'r');
       for (const char *k : {"LIVETIME", "ONTIME", "EXPOSURE", "TELAPSE"}) par_set(obs, k, fmt(total_time), 'r');
-      if (!write_text(out_dir + "/obs.par", obs)) return mx_fail(c, MX_EINVAL, "mx_run_marx: writing obs.par");
+      if (!write_text(out_dir + "/obs.par", obs)) return mx_fail(nullptr, MX_EINVAL, "mx_run_marx: writing obs.par");
     }
   }
   if (stats) {

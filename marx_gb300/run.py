@@ -1,0 +1,80 @@
+"""marx's main loop on the GPU (mx_run_marx in include/marx_gb300.h).
+
+    write_par("sim.par", cfg, NumRays=100000, SourceType="POINT", ...)
+    stats = run_marx("sim.par", ["OutputDir=out", "RandomSeed=3"])
+
+``write_par`` renders a configuration and run parameters as a MARX
+parameter file (name,type,mode,value,min,max,prompt per line); the run reads
+it as the marx program reads marx.par, overrides as on its command line.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+from .config import MxConfig, to_par
+
+# the run parameters the loop reads besides the engine's (marx.c:789-805,
+# source.c:77-88, spectrum.c:118-274, s-*.c) and their marx.par types
+RUN_PARAMS = {
+    "NumRays": "i", "dNumRays": "i", "ExposureTime": "r", "OutputDir": "f", "OutputVectors": "s",
+    "RandomSeed": "i", "DumpToRayFile": "b", "RayFile": "f", "SourceType": "s", "SourceRA": "r", "SourceDEC": "r",
+    "SourceDistance": "r", "SourceFlux": "r", "SpectrumType": "s", "SpectrumFile": "f", "MinEnergy": "r",
+    "MaxEnergy": "r", "S-GaussSigma": "r", "S-BetaCoreRadius": "r", "S-BetaBeta": "r", "S-DiskTheta0": "r",
+    "S-DiskTheta1": "r", "S-LinePhi": "r", "S-LineTheta": "r", "MirrorType": "s", "Verbose": "i",
+}
+RUN_DEFAULTS = {
+    "NumRays": 100000, "dNumRays": 100000, "ExposureTime": 0.0, "OutputDir": "point", "RandomSeed": -1,
+    "OutputVectors": "ETXYZ123DxyMPOabcdSrB", "DumpToRayFile": "no", "RayFile": "marx.rays", "SourceType": "POINT",
+    "SourceRA": 250.2134679741175, "SourceDEC": -53.75743813458669, "SourceDistance": 0.0, "SourceFlux": 0.02,
+    "SpectrumType": "FLAT", "SpectrumFile": "none", "MinEnergy": 1.775, "MaxEnergy": 1.775, "S-GaussSigma": 0.5,
+    "S-BetaCoreRadius": 0.5, "S-BetaBeta": 0.5, "S-DiskTheta0": 0.0, "S-DiskTheta1": 20.0, "S-LinePhi": 0.0,
+    "S-LineTheta": 30.0, "MirrorType": "HRMA", "Verbose": 0,
+}
+
+
+class MxRunStats(C.Structure):
+    _fields_ = [("collected", C.c_uint64), ("detected", C.c_uint64), ("total_time", C.c_double),
+                ("iterations", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+def _lib():
+    from ._native import load_library
+    L = load_library()
+    if not getattr(L, "_mx_run_bound", False):
+        L.mx_run_marx.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_char_p), C.c_int, C.POINTER(MxRunStats)]
+        L.mx_param_type.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_uint32)]
+        L._mx_run_bound = True
+    return L
+
+
+def write_par(path: str, cfg: MxConfig, **run) -> None:
+    """A MARX parameter file holding cfg's parameters and the run's (the
+    defaults above, updated by the keyword arguments)."""
+    L = _lib()
+    vals = dict(RUN_DEFAULTS)
+    vals.update(run)
+    lines = []
+    for k, v in to_par(cfg).items():
+        t = C.create_string_buffer(1)
+        if L.mx_param_type(k.encode(), t, None) == 0:
+            lines.append((k, t.value.decode(), v))
+    for k, v in vals.items():
+        lines.append((k, RUN_PARAMS[k], v))
+    with open(path, "w") as fh:
+        for k, t, v in lines:
+            s = f'"{v}"' if t in ("s", "f") else (("yes" if v else "no") if isinstance(v, bool) else str(v))
+            fh.write(f'{k},{t},h,{s},,,""\n')
+
+
+def run_marx(par_path: str, overrides=(), pack: str | None = None) -> dict:
+    """Run the main loop; returns the run's counts and exposure."""
+    from .caldb.pack import DEFAULT_PACK
+    L = _lib()
+    ov = [o.encode() for o in overrides]
+    arr = (C.c_char_p * max(1, len(ov)))(*ov)
+    st = MxRunStats()
+    r = L.mx_run_marx((pack or DEFAULT_PACK).encode(), par_path.encode(), arr, len(ov), C.byref(st))
+    if r != 0:
+        raise RuntimeError(f"mx_run_marx: error {r}: " + L.mx_last_error(None).decode())
+    return {"collected": st.collected, "detected": st.detected, "total_time": st.total_time,
+            "iterations": st.iterations}
