@@ -551,7 +551,10 @@ int mx_overrun_count(mx_context *ctx, unsigned long long *count, int reset);
  * file par_path (marx.par format) with "Name=value" overrides configures
  * the engine and the run, as the marx program reads them: SourceType
  * (POINT, GAUSS, BETA, DISK, LINE) with SourceRA, SourceDEC,
- * SourceDistance and the model's S-* parameters; SpectrumType FLAT
+ * SourceDistance and the model's S-* parameters, or SAOSAC with
+ * SAOSACFile (mx_saosac_*: rays past the mirror, traced from the grating
+ * on; a file without RT_TIME gives zero times and clears the rays'
+ * vignetting flags, as marx_create_photons does for it); SpectrumType FLAT
  * (MinEnergy, MaxEnergy) or FILE (SpectrumFile) with SourceFlux; NumRays
  * (photons to create, or with a minus sign to detect) in batches of
  * dNumRays, or ExposureTime (s) when positive; RandomSeed (-1: from the
@@ -611,6 +614,32 @@ const char *mx_write_error(void);   /* message of the last mx_write_photons fail
 /* The history bits a trace of cfg through `stages` makes valid, as the
  * reference's stages set them. */
 uint32_t mx_output_history(const mx_config *cfg, uint32_t stages);
+
+/* The SAOSAC source (s-saosac.c:95-345): rays of an SAO raytrace of the
+ * mirror from the RAYTRACE binary table of a FITS file (RT_X, RT_Y, RT_Z,
+ * RT_COSX, RT_COSY, RT_COSZ, RT_KEV, RT_WGHT and an optional RT_TIME;
+ * scalar E or D columns).  mx_saosac_read makes up to max photons from the next rows,
+ * as saosac_create_photons does: each row draws one uniform against its
+ * weight (MX_PHOTON_MIRROR_VBLOCKED when u >= RT_WGHT), its ray is projected
+ * to the plane x = 0 of the file's frame and placed at x = hrma_cap_x -
+ * 0.01675 mm, its shell follows from the radius there, its energy is
+ * RT_KEV; times are RT_TIME minus the first row's, relative to the end of
+ * the batch before (without RT_TIME: 1, 2, 3, ... per batch).  A row whose
+ * time falls before the start is dropped and its blocked flag passes to
+ * the next photon, as in the reference.  u: one uniform per row of the
+ * file, indexed by row (NULL: the Philox source draw 0 of tag = row under
+ * seed).  Photons get tags first_tag, first_tag + 1, ...; written into HOST
+ * columns energy, x, p (required), arrival_time, flags, mirror_shell, tag.
+ * Trace them with stages MX_STAGE_DITHER | MX_STAGE_GRATING |
+ * MX_STAGE_DETECT: the rays have passed the mirror.  Errors: NULL or
+ * MX_EINVAL, reason in mx_last_error(NULL). */
+typedef struct mx_saosac mx_saosac;
+mx_saosac *mx_saosac_open(const char *file, double hrma_cap_x);
+int mx_saosac_read(mx_saosac *s, const mx_photons *host, uint32_t max, const double *u, uint64_t seed,
+                   uint32_t first_tag, uint32_t *n_read);
+uint64_t mx_saosac_rows(const mx_saosac *s);
+int mx_saosac_has_time(const mx_saosac *s);   /* 1 when the table has RT_TIME */
+void mx_saosac_close(mx_saosac *s);
 
 /* MARX ray files (DumpToRayFile and the RAYFILE source, s-rayfile.c):
  * a native-endian unsigned long magic 0xF8161961 and the history bits, then

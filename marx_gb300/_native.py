@@ -152,6 +152,12 @@ class Engine:
         self._check(self.lib.mx_configure(self.h, C.byref(cfg)))
         self.cfg = cfg
 
+    def set_start_time(self, start_time: float):
+        """Marx_Photon_Type.start_time of the photons traced next
+        (mx_set_start_time)."""
+        self.lib.mx_set_start_time.argtypes = [C.c_void_p, C.c_double]
+        self._check(self.lib.mx_set_start_time(self.h, float(start_time)))
+
     def trace(self, ph: DevicePhotons, stages: int = 15, U=None, N=None, seed: int = 0, stream=None):
         """In-place trace of device photons (U, N: device tensors or None)."""
         s = ph.struct()

@@ -23,7 +23,7 @@ LIB = os.path.join(OUT, "libmarx_gb300.so")
 COMPAT_LIB = os.path.join(OUT, "libmarx_gb300_compat.so")
 COMPAT_SOURCES = ["mx_compat.cpp"]
 SOURCES = ["mx_capi.cu", "mx_kernels.cu", "mx_batch.cu", "mx_static.cu", "mx_diff.cu", "mx_model.cpp",
-           "mx_output.cpp", "mx_source.cpp", "mx_events.cu", "mx_user_source.cpp", "mx_par.cpp", "mx_run.cu"]
+           "mx_output.cpp", "mx_source.cpp", "mx_events.cu", "mx_user_source.cpp", "mx_par.cpp", "mx_run.cu", "mx_saosac.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

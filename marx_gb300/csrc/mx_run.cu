@@ -335,6 +335,23 @@ cudaError_t copy_out(const mx_photons &d, uint32_t cap, uint32_t n, HostList &h,
   return e;
 }
 
+// n photons of a host list (stride n) into a device list laid out for cap
+// photons (stride cap): the columns a trace reads.
+cudaError_t copy_in(const HostList &h, uint32_t n, const mx_photons &d, uint32_t cap, cudaStream_t st) {
+  struct Col { const void *src; void *dst; size_t elem; int comps; };
+  const Col cols[12] = {
+      {h.ph.energy, d.energy, 8, 1}, {h.ph.x, d.x, 8, 3}, {h.ph.p, d.p, 8, 3}, {h.ph.arrival_time, d.arrival_time, 8, 1},
+      {h.ph.flags, d.flags, 4, 1}, {h.ph.tag, d.tag, 4, 1}, {h.ph.mirror_shell, d.mirror_shell, 1, 1},
+      {h.ph.order, d.order, 1, 1}, {h.ph.ccd_num, d.ccd_num, 1, 1}, {h.ph.y_pixel, d.y_pixel, 4, 1},
+      {h.ph.z_pixel, d.z_pixel, 4, 1}, {h.ph.dither_state, d.dither_state, 4, 3}};
+  const size_t hs = h.ph.stride;
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < 12 && e == cudaSuccess; k++)
+    e = cudaMemcpy2DAsync(cols[k].dst, (size_t) cap * cols[k].elem, cols[k].src, hs * cols[k].elem,
+                          (size_t) n * cols[k].elem, cols[k].comps, cudaMemcpyHostToDevice, st);
+  return e;
+}
+
 const char *source_names[] = {"POINT", "GAUSS", "BETA", "DISK", "LINE"};
 
 }  // namespace
@@ -371,10 +388,14 @@ extern "C" int mx_run_marx(const char *pack_path, const char *par_path, const ch
 
   mx_source src;
   memset(&src, 0, sizeof src);
-  int kind = -1;
+  const bool saosac = src_name == "SAOSAC";
+  std::string saosac_file;
+  if (saosac && !R.str("SAOSACFile", saosac_file)) return bad(R.err);
+  int kind = saosac ? 0 : -1;
   for (int k = 0; k < 5; k++)
     if (src_name == source_names[k]) kind = k;
-  if (kind < 0) return bad("SourceType " + src_name + " is not supported here (POINT, GAUSS, BETA, DISK, LINE)");
+  if (kind < 0)
+    return bad("SourceType " + src_name + " is not supported here (POINT, GAUSS, BETA, DISK, LINE, SAOSAC)");
   src.kind = kind;
   const char *model_pars[5][2] = {{nullptr, nullptr}, {"S-GaussSigma", nullptr}, {"S-BetaCoreRadius", "S-BetaBeta"},
                                   {"S-DiskTheta0", "S-DiskTheta1"}, {"S-LinePhi", "S-LineTheta"}};
@@ -384,7 +405,11 @@ extern "C" int mx_run_marx(const char *pack_path, const char *par_path, const ch
   double flux = 0.0;
   std::vector<double> spec_e, spec_f;
   if (!R.num("SourceFlux", flux)) return bad(R.err);
-  if (spec_type == "FLAT") {
+  if (saosac) {
+    // the rays carry their energies; the spectrum's total flux is 0, so
+    // photons of a file without RT_TIME get zero times (source.c:315-337)
+    flux = 0.0;
+  } else if (spec_type == "FLAT") {
     if (!R.num("MinEnergy", src.energy_min) || !R.num("MaxEnergy", src.energy_max)) return bad(R.err);
     if (flux <= 0.0) return bad("SourceFlux for FLAT spectrum must be positive");
     if (src.energy_max - src.energy_min < 0.0 || src.energy_max <= 0.0) return bad("bad MinEnergy, MaxEnergy");
@@ -409,7 +434,12 @@ extern "C" int mx_run_marx(const char *pack_path, const char *par_path, const ch
   // errors past this point are reported with no context (it is destroyed
   // on return): the context's message moves to mx_last_error(NULL)
   auto ctx_fail = [&](int code) { return mx_fail(nullptr, code, "mx_run_marx: " + c->err); };
-  const double mt = 1.0 / flux / c->hm.geom_area_cm2;   // compute_mean_time (source.c:260-264)
+  const double mt = flux > 0.0 ? 1.0 / flux / c->hm.geom_area_cm2 : 0.0;   // compute_mean_time (source.c:260-264)
+  mx_saosac *sa = nullptr;
+  if (saosac && !(sa = mx_saosac_open(saosac_file.c_str(), cfg.hrma_cap_x)))
+    return mx_fail(nullptr, MX_EINVAL, std::string("mx_run_marx: ") + mx_last_error(nullptr));
+  struct SaCloser { mx_saosac *s; ~SaCloser() { mx_saosac_close(s); } } sa_closer{sa};
+  HostList hin;
   cudaStream_t st = c->stream;
   const uint32_t cap = (uint32_t) drays;
   DevList dev;
@@ -443,25 +473,40 @@ extern "C" int mx_run_marx(const char *pack_path, const char *par_path, const ch
     mx_photons d = dev.ph;
     d.n = per_iter;
     d.stride = cap;
-    if ((r = mx_generate_source(c, &src, tag_start, seed, &d, st)) != MX_OK) return ctx_fail(r);
-    mx_time_tiles<<<(per_iter + TIME_TILE - 1) / TIME_TILE, TIME_THREADS, 0, st>>>(d.arrival_time, per_iter, seed,
-                                                                                 tag_start, mt, (double *) sums.ptr);
-    mx_time_offsets<<<1, 1024, 0, st>>>((double *) sums.ptr, (per_iter + TIME_TILE - 1) / TIME_TILE);
-    mx_time_add<<<(per_iter + TIME_TILE - 1) / TIME_TILE, TIME_THREADS, 0, st>>>(d.arrival_time, per_iter,
-                                                                               (const double *) sums.ptr);
-    c->launches += 3;
-    e = cudaMemcpyAsync(times.data(), d.arrival_time, (size_t) per_iter * 8, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e == cudaSuccess) e = cudaGetLastError();
-    if (e != cudaSuccess) return mx_cuda_fail(nullptr, e, "mx_run_marx: photon times");
     uint32_t n = per_iter;
-    if (exposure > 0.0)   // the first photon at or past the time left ends the batch (source.c:327-333)
-      for (uint32_t i = 0; i < per_iter; i++)
-        if (times[i] >= left) { n = i + 1; break; }
+    if (saosac) {
+      // the next rows of the ray file (saosac_create_photons), copied to
+      // the device; the mirror stage is skipped (its history bit is set)
+      hin.resize(per_iter);
+      std::fill(hin.ccd.begin(), hin.ccd.end(), (int8_t) -1);
+      if ((r = mx_saosac_read(sa, &hin.ph, per_iter, nullptr, seed, tag_start, &n)) != MX_OK)
+        return mx_fail(nullptr, r, std::string("mx_run_marx: ") + mx_last_error(nullptr));
+      if (n == 0) break;
+      if (!mx_saosac_has_time(sa))   // marx_create_photons gives them Poisson times of mean 0 and clears the flags
+        for (uint32_t i = 0; i < n; i++) { hin.t[i] = 0.0; hin.flags[i] = 0u; }
+      std::copy(hin.t.begin(), hin.t.begin() + n, times.begin());
+      if ((e = copy_in(hin, n, d, cap, st)) != cudaSuccess) return mx_cuda_fail(nullptr, e, "mx_run_marx: rays");
+    } else {
+      if ((r = mx_generate_source(c, &src, tag_start, seed, &d, st)) != MX_OK) return ctx_fail(r);
+      mx_time_tiles<<<(per_iter + TIME_TILE - 1) / TIME_TILE, TIME_THREADS, 0, st>>>(d.arrival_time, per_iter, seed,
+                                                                                   tag_start, mt, (double *) sums.ptr);
+      mx_time_offsets<<<1, 1024, 0, st>>>((double *) sums.ptr, (per_iter + TIME_TILE - 1) / TIME_TILE);
+      mx_time_add<<<(per_iter + TIME_TILE - 1) / TIME_TILE, TIME_THREADS, 0, st>>>(d.arrival_time, per_iter,
+                                                                                 (const double *) sums.ptr);
+      c->launches += 3;
+      e = cudaMemcpyAsync(times.data(), d.arrival_time, (size_t) per_iter * 8, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e == cudaSuccess) e = cudaGetLastError();
+      if (e != cudaSuccess) return mx_cuda_fail(nullptr, e, "mx_run_marx: photon times");
+      if (exposure > 0.0)   // the first photon at or past the time left ends the batch (source.c:327-333)
+        for (uint32_t i = 0; i < per_iter; i++)
+          if (times[i] >= left) { n = i + 1; break; }
+    }
     d.n = n;
     if ((r = mx_set_start_time(c, start_time)) != MX_OK) return ctx_fail(r);
-    const uint32_t stages = dump ? MX_STAGE_DITHER : MX_STAGE_ALL;   // the ray file holds the dithered rays
-    if ((r = mx_trace_tables(c, c->T, &d, stages, nullptr, nullptr, seed, st, true)) != MX_OK) return ctx_fail(r);
+    // the ray file holds the dithered rays; SAOSAC rays have passed the mirror
+    const uint32_t stages = dump ? MX_STAGE_DITHER : saosac ? (MX_STAGE_ALL & ~MX_STAGE_MIRROR) : MX_STAGE_ALL;
+    if ((r = mx_trace_tables(c, c->T, &d, stages, nullptr, nullptr, seed, st, !saosac)) != MX_OK) return ctx_fail(r);
     if ((e = copy_out(d, cap, n, host, st)) != cudaSuccess)
       return mx_cuda_fail(nullptr, e, "mx_run_marx: copying photons out");
     if (dump) {

@@ -294,6 +294,34 @@ class Reference:
             raise RuntimeError("reference source photons: " + self.lib.mxref_last_error().decode())
         return p0, e, np.ascontiguousarray(p.T)
 
+    def source_batch(self, n: int, U=None):
+        """One create_photons call of up to n photons of the source set up
+        by source_photons or source_open (U: the uniforms in draw order).
+        Returns a PhotonList of the photons made (energy, x, p, arrival time,
+        flags, mirror shell), with the count of uniforms drawn as
+        uniforms_used."""
+        e, t = np.zeros(n), np.zeros(n)
+        x, p = np.zeros((n, 3)), np.zeros((n, 3))
+        flags, shell = np.zeros(n, np.uint32), np.zeros(n, np.int32)
+        num, used = C.c_uint(0), C.c_int(0)
+        u = np.ascontiguousarray(U if U is not None else np.zeros(0), dtype=np.float64)
+        if self.lib.mxref_source_batch(n, _p(u), u.size, _p(e), _p(x), _p(p), _p(t), _p(flags), _p(shell),
+                                       C.byref(num), C.byref(used)) != 0:
+            raise RuntimeError("reference source batch: " + self.lib.mxref_last_error().decode())
+        m = num.value
+        q = PhotonList(m)
+        q.energy[:] = e[:m]; q.arrival_time[:] = t[:m]; q.flags[:] = flags[:m]
+        q.x[:] = x[:m].T; q.p[:] = p[:m].T; q.mirror_shell[:] = shell[:m]
+        q.uniforms_used = used.value
+        return q
+
+    def source_open(self):
+        """Set up and open the source the parameters describe."""
+        p0 = np.zeros(3)
+        if self.lib.mxref_source_setup(_p(p0)) != 0:
+            raise RuntimeError("reference source: " + self.lib.mxref_last_error().decode())
+        return p0
+
     def trace_batch(self, ph: PhotonList, stages: int = 15):
         """Whole batch with the reference's own generator; returns (list, seconds)."""
         assert self.native

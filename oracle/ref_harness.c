@@ -653,3 +653,43 @@ int mxref_source_photons(int n, const double *U, double *energy, double *p)
      }
    return 0;
 }
+
+/* One create_photons call for a batch of up to n photons (the SAOSAC
+ * source reads its rays in batches; its times are relative to the batch
+ * before, s-saosac.c:173-300).  With the slot build the uniforms come from
+ * U[0 .. nu) in the order they are drawn.  Energies, positions and
+ * directions (n x 3), times, flags and shells out; *num the photons made,
+ * *used the uniforms drawn (slot build). */
+int mxref_source_batch(int n, const double *U, int nu, double *energy, double *x, double *p, double *t,
+                       unsigned int *flags, int *shell, unsigned int *num, int *used)
+{
+   Marx_Photon_Type pt;
+   Marx_Photon_Attr_Type *at;
+   unsigned int i;
+   if (Src == NULL) { set_err("no source"); return -1; }
+   if (NULL == (at = (Marx_Photon_Attr_Type *) calloc((size_t) n, sizeof (Marx_Photon_Attr_Type))))
+     { set_err("out of memory"); return -1; }
+   memset(&pt, 0, sizeof(pt));
+   pt.attributes = at; pt.max_n_photons = (unsigned int) n;
+#if MXREF_INTERPOSE
+   rng_window(U, 0, nu, NULL, 0, 0);
+   Rng_Overrun = 0;
+#else
+   (void) U; (void) nu;
+#endif
+   if (-1 == (*Src->create_photons)(Src, &pt, (unsigned int) n, num)) { free(at); set_err("create_photons"); return -1; }
+#if MXREF_INTERPOSE
+   *used = U_pos;
+   rng_window(NULL, 0, 0, NULL, 0, 0);
+   if (Rng_Overrun) { free(at); set_err("source drew more uniforms than given"); return -1; }
+#endif
+   for (i = 0; i < *num; i++)
+     {
+        energy[i] = at[i].energy; t[i] = at[i].arrival_time;
+        x[3 * i] = at[i].x.x; x[3 * i + 1] = at[i].x.y; x[3 * i + 2] = at[i].x.z;
+        p[3 * i] = at[i].p.x; p[3 * i + 1] = at[i].p.y; p[3 * i + 2] = at[i].p.z;
+        flags[i] = at[i].flags; shell[i] = (int) at[i].mirror_shell;
+     }
+   free(at);
+   return 0;
+}

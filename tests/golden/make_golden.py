@@ -48,6 +48,12 @@ oracle/_ref.  Writes:
                          dispersion direction of their grating arm, per arm
                          and order (-3..3), as samples and histograms
                          (--dispersed).
+  saosac_synthetic.fits, saosac_notime.fits, saosac.npz
+                         synthetic SAO raytrace files (RAYTRACE tables of
+                         rays on the four shells' exit annuli toward the
+                         focus, weights, with and without RT_TIME) and the
+                         photons the reference's SAOSAC source makes of them
+                         in batches, fed per-row uniforms (--saosac).
   diff_fd_reference.npz  central finite differences of the reference itself
                          for the differentiable form: 2e5 rays (Philox
                          variates of their tags, so common random numbers
@@ -717,6 +723,53 @@ def diff_rays():
     np.savez_compressed(os.path.join(HERE, "diff_rays.npz"), **out)
 
 
+SAOSAC_ROWS = 3000
+
+
+def saosac_fixture():
+    """Synthetic SAOSAC ray files and the reference's SAOSAC source
+    (s-saosac.c) reading them: rays start 50-250 mm in front of the cap
+    plane of the file's frame on the four shells' exit annuli, head for
+    the focus 10070 mm behind with a few arcsec of scatter, energies
+    0.3-8 keV, weights 0.05-1; RT_TIME increasing from 5e3 s with two rows
+    earlier than the first (dropped by the reader)."""
+    r = np.random.default_rng(77)
+    n = SAOSAC_ROWS
+    radius = r.choice([316.97, 426.35, 482.86, 599.45], n) + r.normal(0.0, 1.5, n)
+    phi = r.uniform(0, 2 * np.pi, n)
+    y, z = radius * np.cos(phi), radius * np.sin(phi)
+    x = r.uniform(50.0, 250.0, n)
+    d = np.stack([-10070.0 - x, -y, -z]) + r.normal(0.0, 0.05, (3, n))
+    k = d / np.linalg.norm(d, axis=0)
+    y0, z0 = y, z
+    t = 5000.0 + np.cumsum(r.exponential(0.2, n))
+    t[[700, 1900]] = 4000.0          # earlier than the first row: dropped
+    e = r.uniform(0.3, 8.0, n)
+    w = r.uniform(0.05, 1.0, n)
+    cols = [("RT_X", "D", x), ("RT_Y", "D", y0), ("RT_Z", "D", z0), ("RT_COSX", "D", k[0]), ("RT_COSY", "D", k[1]),
+            ("RT_COSZ", "D", k[2]), ("RT_KEV", "E", e), ("RT_WGHT", "E", w)]
+    files = {"saosac_synthetic.fits": cols + [("RT_TIME", "D", t)], "saosac_notime.fits": cols}
+    U = r.random(n)
+    out = {"U": U}
+    for fname, c in files.items():
+        path = os.path.join(HERE, fname)
+        write_bintable(path, "RAYTRACE", c)
+        cfg = W.plain_hetg(parity=True).cfg
+        ref = Reference(cfg, extra_par={"SourceType": "SAOSAC", "SAOSACFile": path, "DitherModel": "INTERNAL"})
+        ref.source_open()
+        tag = fname.split("_")[1].split(".")[0]
+        used = 0
+        for b, m in enumerate((1000, 1000, 1500)):
+            q = ref.source_batch(m, U[used:])
+            for col in ("energy", "x", "p", "arrival_time", "flags", "mirror_shell"):
+                out[f"{tag}_{b}_{col}"] = getattr(q, col)
+            out[f"{tag}_{b}_n"] = np.array(q.n)
+            out[f"{tag}_{b}_rows"] = np.array(q.uniforms_used)   # one uniform per row read
+            used += q.uniforms_used
+        print(fname, [int(out[f"{tag}_{b}_n"]) for b in range(3)])
+    np.savez_compressed(os.path.join(HERE, "saosac.npz"), **out)
+
+
 N_FD = 200_000
 FD_STEP = 2e-3
 
@@ -818,7 +871,9 @@ def dispersed_fixture(name):
 if __name__ == "__main__":
     sys.path.insert(0, os.path.dirname(HERE))
     names = [a for a in sys.argv[1:] if not a.startswith("-")]
-    if "--diff-fd" in sys.argv:
+    if "--saosac" in sys.argv:
+        saosac_fixture()
+    elif "--diff-fd" in sys.argv:
         diff_fd_fixture()
     elif "--dispersed" in sys.argv:
         for n in names or DISPERSED_WORKLOADS:
