@@ -228,6 +228,11 @@ int  mx_configure(mx_context *ctx, const mx_config *cfg);
 int  mx_validate_config(const char *pack_path, const mx_config *cfg);
 void mx_destroy(mx_context *ctx);
 
+/* The mirror's open aperture area in cm^2 for cfg (its shells' annuli and
+ * open shutters; Marx_Mirror_Geometric_Area, hrma.c:719-736), which sets
+ * the mean time between a source's photons.  Host only. */
+int  mx_geometric_area(const char *pack_path, const mx_config *cfg, double *cm2);
+
 /* Marx_Photon_Type.start_time for the photons traced next (the ACIS frame
  * streak and the aspect solution take start_time + arrival time): a launch
  * parameter, changed without rebuilding the model (MARX moves it on by each

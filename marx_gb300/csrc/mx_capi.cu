@@ -189,6 +189,17 @@ int mx_set_start_time(mx_context *c, double start_time) {
   return MX_OK;
 }
 
+int mx_geometric_area(const char *pack_path, const mx_config *cfg, double *cm2) {
+  if (!pack_path || !cfg || !cm2) { g_create_err = "mx_geometric_area: null argument"; return MX_EINVAL; }
+  Pack pk;
+  HostModel hm;
+  std::string err;
+  if (!pk.load(pack_path, err)) { g_create_err = err; return MX_EPACK; }
+  if (!build_model(pk, *cfg, hm, err)) { g_create_err = err; return MX_EINVAL; }
+  *cm2 = hm.geom_area_cm2;
+  return MX_OK;
+}
+
 int mx_validate_config(const char *pack_path, const mx_config *cfg) {
   if (!pack_path || !cfg) { g_create_err = "mx_validate_config: null argument"; return MX_EINVAL; }
   Pack pk;

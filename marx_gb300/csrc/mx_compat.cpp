@@ -33,6 +33,16 @@ int pf_get_integer(Param_File_Type *, char *, int *) __attribute__((weak));
 int pf_get_boolean(Param_File_Type *, char *, int *) __attribute__((weak));
 }
 
+// Globals of the reference's mirror module that its other modules read:
+// the aperture area behind a source's photon rate (source.c:260-264) and
+// the cap position the SAOSAC source places its rays at (s-saosac.c:224).
+// marx_mirror_init sets both; a program linking this library instead of
+// those modules gets them from here.
+extern "C" {
+__attribute__((visibility("default"))) double Marx_Mirror_Geometric_Area = 1.0;
+__attribute__((visibility("default"))) double _Marx_HRMA_Cap_Position = 10079.5;
+}
+
 namespace {
 
 // The MARX type ids the *_init functions return (marx.h:364-376).
@@ -319,6 +329,11 @@ int marx_mirror_init(Param_File_Type *pf) {
   if (read_group(s, pf, MX_PARAMS_MIRROR, "marx_mirror_init")) return -1;
   int seed;
   if (pf_get_integer(pf, (char *) "RandomSeed", &seed) == 0 && seed >= 0) s.seed = (uint64_t) seed;
+  double area = 0.0;
+  if (mx_geometric_area(pack_path().c_str(), &s.cfg, &area) != MX_OK)
+    return error(s, "marx_mirror_init: %s", mx_last_error(nullptr));
+  Marx_Mirror_Geometric_Area = area;
+  _Marx_HRMA_Cap_Position = s.cfg.hrma_cap_x;
   s.mirror = MIRROR_HRMA;
   return s.mirror;
 }

@@ -1,7 +1,8 @@
 """The compatibility shim without a GPU: the layout of the reference's
 photon types in include/marx_gb300_compat.h against the reference's own
-marx.h, the library's exports, and the host-side pieces (allocation,
-marx_prune_photons, errors before initialisation)."""
+marx.h, the library's exports, the host-side pieces (allocation,
+marx_prune_photons, errors before initialisation), and the reference's
+unmodified marx program linked against the shim."""
 import ctypes as C
 import os
 import re
@@ -139,3 +140,36 @@ def test_stages_refuse_before_init_and_without_a_parameter_library():
     assert b"parameter-file library" in L.marx_gb300_compat_last_error()
     assert L.marx_gb300_compat_set_variates(C.c_void_p(8), None, 4) == -1
     L.marx_dealloc_photon_type(pt)
+
+
+def test_stock_marx_binds_its_stage_calls_to_the_shim(tmp_path):
+    """The reference's own marx program (marx/src/marx.c, unmodified),
+    compiled and linked with libmarx_gb300_compat ahead of the reference's
+    modules (oracle/Makefile target marx): its stage calls and the
+    mirror-module globals the source reads bind to the shim, and a run gets
+    through the parameter file, the shim's *_init functions and the
+    reference's source up to the first stage, which asks the engine for a
+    GPU (on a machine without one it stops there with the shim's error)."""
+    from oracle.bindings import REF_ROOT, reference_available
+    if not reference_available():
+        pytest.skip("the reference checkout is not on this machine")
+    _compat()
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "marx", f"REF={REF_ROOT}"], check=True)
+    exe = os.path.join(ROOT, "oracle", "_ref", "marx_gb300")
+    par = tmp_path / "marx.par"
+    par.write_text(open(os.path.join(REF_ROOT, "marx", "par", "marx.par")).read())
+    env = dict(os.environ, MARX_DATA_DIR=os.path.join(REF_ROOT, "marx", "data"), LD_DEBUG="bindings",
+               LD_BIND_NOW="1", LD_DEBUG_OUTPUT=str(tmp_path / "ld"))
+    r = subprocess.run([exe, "NumRays=1000", "dNumRays=1000", f"OutputDir={tmp_path / 'out'}", "DetectorType=ACIS-I",
+                        "GratingType=NONE", f"DataDirectory={os.path.join(REF_ROOT, 'marx', 'data')}"],
+                       cwd=tmp_path, env=env, capture_output=True, text=True, timeout=120)
+    log = "".join(open(os.path.join(tmp_path, f)).read() for f in os.listdir(tmp_path) if f.startswith("ld"))
+    for sym in ("marx_mirror_reflect", "marx_grating_diffract", "marx_detect", "marx_prune_photons",
+                "marx_mirror_init", "marx_detector_init", "Marx_Mirror_Geometric_Area"):
+        binds = [ln for ln in log.splitlines() if f"symbol `{sym}'" in ln]
+        assert binds and all("libmarx_gb300_compat.so" in ln.split(" to ")[1] for ln in binds), sym
+    out = r.stdout + r.stderr
+    assert "1000 photons collected" in out
+    import torch
+    if not torch.cuda.is_available():
+        assert "(gb300 compat) error: creating the engine" in out
