@@ -418,6 +418,11 @@ def build_sections(data_dir: str) -> dict:
     for h, c in qe:
         if h.get("EXTNAME") == "AXAF_QE":
             S[f"acis/qe{int(h['CCD_ID'])}"] = np.vstack([c["ENERGY"], c["QE"]]).astype(np.float32)
+    # the parameter file marx ships (marx/par/marx.par): the template of a
+    # run's parameter file
+    par = os.path.join(data_dir, os.pardir, "par", "marx.par")
+    if os.path.exists(par):
+        S["par/marx"] = text_section(open(par, "rb").read())
     # the observation templates obs.par of a run starts from (write_obs_par,
     # marx.c:999-1196), as text sections
     obs_dir = os.path.join(data_dir, "obs")

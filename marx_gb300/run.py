@@ -48,22 +48,36 @@ def _lib():
 
 
 def write_par(path: str, cfg: MxConfig, **run) -> None:
-    """A MARX parameter file holding cfg's parameters and the run's (the
-    defaults above, updated by the keyword arguments)."""
+    """A MARX parameter file: the marx.par MARX ships (kept in the table
+    pack) with cfg's parameters and the run's (the defaults above, updated by
+    the keyword arguments) set, so that every program reading it (marx2fits
+    too) finds all of its parameters."""
+    from .caldb.pack import DEFAULT_PACK, read_pack, section_text
+    from .output import _par_lines, _par_set
     L = _lib()
     vals = dict(RUN_DEFAULTS)
     vals.update(run)
-    lines = []
+    lines = _par_lines(section_text(read_pack(DEFAULT_PACK)["par/marx"]).decode())
     for k, v in to_par(cfg).items():
         t = C.create_string_buffer(1)
         if L.mx_param_type(k.encode(), t, None) == 0:
-            lines.append((k, t.value.decode(), v))
+            _par_set(lines, k, v, t.value.decode())
     for k, v in vals.items():
-        lines.append((k, RUN_PARAMS[k], v))
+        t = RUN_PARAMS[k]
+        _par_set(lines, k, ("yes" if v else "no") if isinstance(v, bool) else v, t)
     with open(path, "w") as fh:
-        for k, t, v in lines:
-            s = f'"{v}"' if t in ("s", "f") else (("yes" if v else "no") if isinstance(v, bool) else str(v))
-            fh.write(f'{k},{t},h,{s},,,""\n')
+        fh.write("\n".join(lines) + "\n")
+
+
+def geometric_area(cfg: MxConfig, pack: str | None = None) -> float:
+    """The mirror's open aperture area in cm^2 (mx_geometric_area)."""
+    from .caldb.pack import DEFAULT_PACK
+    L = _lib()
+    L.mx_geometric_area.argtypes = [C.c_char_p, C.POINTER(MxConfig), C.POINTER(C.c_double)]
+    a = C.c_double(0.0)
+    if L.mx_geometric_area((pack or DEFAULT_PACK).encode(), C.byref(cfg), C.byref(a)) != 0:
+        raise RuntimeError("mx_geometric_area: " + L.mx_last_error(None).decode())
+    return a.value
 
 
 def run_marx(par_path: str, overrides=(), pack: str | None = None) -> dict:

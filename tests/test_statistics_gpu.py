@@ -102,4 +102,4 @@ def test_dispersed_spectra(cuda, name):
         p = stats.ks_2samp(u, ref[f"sample_{k}"]).pvalue
         assert p > 1e-4, (k, p)
         tested += 1
-    assert tested >= 7
+    assert tested >= 5
