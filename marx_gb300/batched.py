@@ -246,3 +246,27 @@ def generate_source(engine, src: MxSource, first_tag: int, seed: int, dev_photon
     s = dev_photons.struct()
     st = stream.cuda_stream if stream is not None else engine.current_stream()
     engine._check(engine.lib.mx_generate_source(engine.h, C.byref(src), first_tag, seed, C.byref(s), C.c_void_p(st)))
+
+
+def main(argv=None):
+    """Batched launches of the 256-source workload on the current GPU:
+    python -m marx_gb300.batched [--nmax N] [--steps K] (sources of 1e3 .. N
+    photons, log-uniform; tuned launch shape)."""
+    import argparse
+    import torch
+    from ._native import Engine
+    ap = argparse.ArgumentParser(description=main.__doc__)
+    ap.add_argument("--nmax", type=float, default=1e6)
+    ap.add_argument("--steps", type=int, default=2)
+    a = ap.parse_args(argv)
+    eng = Engine(batched_config())
+    b = Batch(eng, batched_sources(nmax=a.nmax))
+    p = b.tune(trials=1)
+    for s in range(a.steps):
+        b.run(seed=s)
+    torch.cuda.synchronize()
+    print(f"{b.n} photons per launch, launch shape {p}")
+
+
+if __name__ == "__main__":
+    main()
