@@ -250,18 +250,25 @@ def generate_source(engine, src: MxSource, first_tag: int, seed: int, dev_photon
 
 def main(argv=None):
     """Batched launches of the 256-source workload on the current GPU:
-    python -m marx_gb300.batched [--nmax N] [--steps K] (sources of 1e3 .. N
-    photons, log-uniform; tuned launch shape)."""
+    python -m marx_gb300.batched [--nmax N] [--steps K] [--shape B T P]
+    (sources of 1e3 .. N photons, log-uniform; the autotuner's launch shape
+    unless one is given)."""
     import argparse
     import torch
     from ._native import Engine
     ap = argparse.ArgumentParser(description=main.__doc__)
     ap.add_argument("--nmax", type=float, default=1e6)
     ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--shape", type=int, nargs=3, metavar=("BLOCK", "TILE", "PER_SM"),
+                    help="launch shape instead of the autotuner's choice")
     a = ap.parse_args(argv)
     eng = Engine(batched_config())
     b = Batch(eng, batched_sources(nmax=a.nmax))
-    p = b.tune(trials=1)
+    if a.shape:
+        b.set_params(*a.shape)
+        p = b.params()
+    else:
+        p = b.tune(trials=1)
     for s in range(a.steps):
         b.run(seed=s)
     torch.cuda.synchronize()
