@@ -728,18 +728,21 @@ SAOSAC_ROWS = 3000
 
 def saosac_fixture():
     """Synthetic SAOSAC ray files and the reference's SAOSAC source
-    (s-saosac.c) reading them: rays start 50-250 mm in front of the cap
-    plane of the file's frame on the four shells' exit annuli, head for
-    the focus 10070 mm behind with a few arcsec of scatter, energies
-    0.3-8 keV, weights 0.05-1; RT_TIME increasing from 5e3 s with two rows
-    earlier than the first (dropped by the reader)."""
+    (s-saosac.c) reading them: rays start 0-2 mm in front of the cap plane
+    of the file's frame on the four shells' exit annuli, head for the focus
+    with a few arcsec of scatter, energies 0.3-8 keV, weights 0.05-1;
+    RT_TIME increasing from 5e3 s with two rows earlier than the first
+    (dropped by the reader)."""
     r = np.random.default_rng(77)
     n = SAOSAC_ROWS
     radius = r.choice([316.97, 426.35, 482.86, 599.45], n) + r.normal(0.0, 1.5, n)
     phi = r.uniform(0, 2 * np.pi, n)
     y, z = radius * np.cos(phi), radius * np.sin(phi)
-    x = r.uniform(50.0, 250.0, n)
-    d = np.stack([-10070.0 - x, -y, -z]) + r.normal(0.0, 0.05, (3, n))
+    # the file's x = 0 plane is the cap's (the reader places rays there);
+    # rays 0-2 mm in front of it head for the focus at MARX's origin
+    x = r.uniform(0.0, 2.0, n)
+    cap = W.plain_hetg(parity=True).cfg.hrma_cap_x - 0.016750
+    d = np.stack([-(cap + x), -y, -z]) + r.normal(0.0, 0.05, (3, n))
     k = d / np.linalg.norm(d, axis=0)
     y0, z0 = y, z
     t = 5000.0 + np.cumsum(r.exponential(0.2, n))
