@@ -25,10 +25,11 @@ def _rays(cfg):
 
 
 def _config():
-    # no roll: the dither turns the rays' directions about the axis, not
-    # their positions on the cap (as _marx_dither_photons does), so a roll
-    # would send rays that converge on the focus elsewhere
-    w = W.plain_hetg()
+    # every order of the efficiency tables (a parameter file cannot limit
+    # them) and no roll: the dither turns the rays' directions about the
+    # axis, not their positions on the cap (as _marx_dither_photons does),
+    # so a roll would send rays that converge on the focus elsewhere
+    w = W.plain_hetg(parity=True)
     w.cfg.roll_nom = 0.0
     return w
 
