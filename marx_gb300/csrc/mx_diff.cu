@@ -16,8 +16,12 @@
 // the decisions recorded by the forward pass; dL/dimage over the ray's
 // 11 x 11 window gives dL/d(u, v, w), and the ray's derivative of
 // (u, v, w) turns that into six parameter contributions.  Nothing per ray
-// is stored between the passes except the decision byte.  Sums are
-// deterministic: fixed warp order, fixed block order, one final reduction.
+// is stored between the passes except the decision byte.  A block takes
+// the rays of a tile whose decision byte says they reached the focal plane
+// (a ballot and prefix sum into shared memory, in ascending order) and
+// traces only those, so that its lanes do not idle through the rays that
+// were lost.  Sums are deterministic: fixed tiles per block, fixed warp
+// order, fixed block order, one final reduction.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -37,6 +41,7 @@ constexpr int WIN = 64;                             // shared window side, pixel
 constexpr int STAGE_W = 2 + 2 * mxd::TAPS;          // ic, jc, 11 y taps x w, 11 z taps
 constexpr int STAGE_STRIDE = STAGE_W + 1;           // odd stride: conflict-free per-lane rows
 constexpr int ADJ_STAGE = 9;                        // 6 contributions, shell, 2 pad
+constexpr int ADJ_TILE = 8 * DBLOCK;                // rays a block sorts its hits out of at a time
 constexpr int NP = MX_DIFF_NPARAM;
 
 struct ImageGeom {
@@ -104,7 +109,7 @@ __device__ __forceinline__ bool aperture(const Aperture &ap, uint64_t seed, uint
     const double r = rng.uniform();
     if (rng.overrun) return false;
     for (int i = 0; i < 4; i++)
-      if (r < ap.area[i]) { si = i; break; }
+      if (mx::lt_pos(r, ap.area[i])) { si = i; break; }
   }
   if (si < 0) return false;
   double radius;
@@ -114,7 +119,7 @@ __device__ __forceinline__ bool aperture(const Aperture &ap, uint64_t seed, uint
   double theta;
   for (int guard = 0;; guard++) {
     theta = rng.uniform();
-    const unsigned quad = (unsigned) (4.0 * theta);
+    const unsigned quad = mx::quarter_of(theta);
     if (rng.overrun || guard >= 64) return false;
     if (ap.shutter[si] & (1u << quad)) break;
   }
@@ -342,78 +347,105 @@ __global__ void __launch_bounds__(DBLOCK) diff_adjoint_kernel(const __grid_const
   const ImageGeom &g = A.g;
   const mxd::V3<Dual6> p0 = mxd::v3<Dual6>(A.p0[0], A.p0[1], A.p0[2]);
   const StrutTest none{nullptr};   // decisions are replayed: the strut test is never called
+  uint32_t *list = reinterpret_cast<uint32_t *>(rw + WIN * (WIN + 1) + DWARPS * 32 * ADJ_STAGE);   // ADJ_TILE entries
+  uint32_t *wcnt = list + ADJ_TILE;                                                 // DWARPS entries
   double pacc = 0.0;               // lane p < NP: this warp's sum for parameter p
-  const uint64_t step = (uint64_t) gridDim.x * DWARPS * 32;
-  for (uint64_t base = ((uint64_t) blockIdx.x * DWARPS + warp) * 32; base < n; base += step) {
-    const uint64_t i = base + lane;
-    float c6[mxd::ND];
-#pragma unroll
-    for (int k = 0; k < mxd::ND; k++) c6[k] = 0.f;
-    int si = -1;
-    uint8_t code = i < n ? codes[i] : 0;
-    double ry, rz;
-    if ((code & mxd::RAY_HIT) && aperture(A.ap, seed, (uint32_t) i, si, ry, rz)) {
-      Dual6 y, z, w;
-      int ic, jc;
-      float fu, fv;
-      if (mxd::weighted_ray<Dual6>(A.opt[si][0], A.opt[si][1], A.rc[si], ry, rz, p0, true, code, none, y, z, w) &&
-          w.v > 0.0 && splat_origin(g, y.v, z.v, ic, jc, fu, fv)) {
-        float ky[mxd::TAPS], kyd[mxd::TAPS], kz[mxd::TAPS], kzd[mxd::TAPS];
-#pragma unroll
-        for (int k = 0; k < mxd::TAPS; k++) {
-          ky[k] = tap(g, k, fu);
-          kyd[k] = ((float) (k - mxd::HALF) - fu) * g.inv_s2 * ky[k];
-          kz[k] = tap(g, k, fv);
-          kzd[k] = ((float) (k - mxd::HALF) - fv) * g.inv_s2 * kz[k];
-        }
-        float sw = 0.f, su = 0.f, sv = 0.f;
-        const bool inside = ic - mxd::HALF >= g.wx0 && ic + mxd::HALF < g.wx0 + g.wnx &&
-                            jc - mxd::HALF >= g.wy0 && jc + mxd::HALF < g.wy0 + g.wny;
-        if (inside) {
-          const float *base_row = rw + (jc - mxd::HALF - g.wy0) * (WIN + 1) + (ic - mxd::HALF - g.wx0);
-#pragma unroll
-          for (int a = 0; a < mxd::TAPS; a++) {
-            const float *q = base_row + a * (WIN + 1);
-            float t = 0.f, td = 0.f;
-#pragma unroll
-            for (int b = 0; b < mxd::TAPS; b++) { t += q[b] * ky[b]; td += q[b] * kyd[b]; }
-            sw += kz[a] * t; su += kz[a] * td; sv += kzd[a] * t;
-          }
-        } else {
-#pragma unroll
-          for (int a = 0; a < mxd::TAPS; a++) {
-            float t = 0.f, td = 0.f;
-#pragma unroll
-            for (int b = 0; b < mxd::TAPS; b++) {
-              const float r = resid_at(g, rw, dl, jc - mxd::HALF + a, ic - mxd::HALF + b);
-              t += r * ky[b]; td += r * kyd[b];
-            }
-            sw += kz[a] * t; su += kz[a] * td; sv += kzd[a] * t;
-          }
-        }
-        const float vig = (float) A.vig, wv = (float) w.v * vig, ip = (float) g.inv_pitch;
-#pragma unroll
-        for (int k = 0; k < mxd::ND; k++) c6[k] = vig * sw * w.d[k] + wv * ip * (su * y.d[k] + sv * z.d[k]);
-      } else
-        si = -1;
-    }
-    float *row = stage + lane * ADJ_STAGE;
-#pragma unroll
-    for (int k = 0; k < mxd::ND; k++) row[k] = c6[k];
-    row[mxd::ND] = __int_as_float(si);
-    __syncwarp();
-    if (lane < NP) {
-      // lanes 0..15: shell lane/4, slot lane%4; lanes 16, 17: source slots 4, 5
-      const int want = lane < 16 ? (lane >> 2) : -2, slot = lane < 16 ? (lane & 3) : lane - 12;
-      float s = 0.f;
-      for (int r = 0; r < 32; r++) {
-        const float *q = stage + r * ADJ_STAGE;
-        const int sr = __float_as_int(q[mxd::ND]);
-        if (sr == want || (want == -2 && sr >= 0)) s += q[slot];
+  for (uint64_t tile = (uint64_t) blockIdx.x * ADJ_TILE; tile < n; tile += (uint64_t) gridDim.x * ADJ_TILE) {
+    // The rays of the tile that reached the focal plane, in ascending order:
+    // only they contribute, and lanes given the others would idle through
+    // the whole ray.
+    uint32_t nh = 0;
+    for (int j = 0; j < ADJ_TILE / DBLOCK; j++) {
+      const uint64_t i = tile + (uint64_t) j * DBLOCK + threadIdx.x;
+      const bool hit = i < n && (codes[i] & mxd::RAY_HIT);
+      const unsigned m = __ballot_sync(0xffffffffu, hit);
+      if (lane == 0) wcnt[warp] = (uint32_t) __popc(m);
+      __syncthreads();
+      uint32_t off = nh, tot = nh;
+      for (int k = 0; k < DWARPS; k++) {
+        const uint32_t c = wcnt[k];
+        off += k < warp ? c : 0u;
+        tot += c;
       }
-      pacc += (double) s;
+      if (hit) list[off + __popc(m & ((1u << lane) - 1u))] = (uint32_t) (i - tile);
+      __syncthreads();
+      nh = tot;
     }
-    __syncwarp();
+    for (uint32_t b0 = 0; b0 < nh; b0 += DBLOCK) {
+      const uint32_t kk = b0 + threadIdx.x;
+      const bool valid = kk < nh;
+      if (!__any_sync(0xffffffffu, valid)) continue;   // the warp has no ray in this round
+      const uint64_t i = valid ? tile + list[kk] : 0;
+      float c6[mxd::ND];
+#pragma unroll
+      for (int k = 0; k < mxd::ND; k++) c6[k] = 0.f;
+      int si = -1;
+      uint8_t code = valid ? codes[i] : 0;
+      double ry, rz;
+      if (valid && aperture(A.ap, seed, (uint32_t) i, si, ry, rz)) {
+        Dual6 y, z, w;
+        int ic, jc;
+        float fu, fv;
+        if (mxd::weighted_ray<Dual6>(A.opt[si][0], A.opt[si][1], A.rc[si], ry, rz, p0, true, code, none, y, z, w) &&
+            w.v > 0.0 && splat_origin(g, y.v, z.v, ic, jc, fu, fv)) {
+          float ky[mxd::TAPS], kyd[mxd::TAPS], kz[mxd::TAPS], kzd[mxd::TAPS];
+#pragma unroll
+          for (int k = 0; k < mxd::TAPS; k++) {
+            ky[k] = tap(g, k, fu);
+            kyd[k] = ((float) (k - mxd::HALF) - fu) * g.inv_s2 * ky[k];
+            kz[k] = tap(g, k, fv);
+            kzd[k] = ((float) (k - mxd::HALF) - fv) * g.inv_s2 * kz[k];
+          }
+          float sw = 0.f, su = 0.f, sv = 0.f;
+          const bool inside = ic - mxd::HALF >= g.wx0 && ic + mxd::HALF < g.wx0 + g.wnx &&
+                              jc - mxd::HALF >= g.wy0 && jc + mxd::HALF < g.wy0 + g.wny;
+          if (inside) {
+            const float *base_row = rw + (jc - mxd::HALF - g.wy0) * (WIN + 1) + (ic - mxd::HALF - g.wx0);
+#pragma unroll
+            for (int a = 0; a < mxd::TAPS; a++) {
+              const float *q = base_row + a * (WIN + 1);
+              float t = 0.f, td = 0.f;
+#pragma unroll
+              for (int b = 0; b < mxd::TAPS; b++) { t += q[b] * ky[b]; td += q[b] * kyd[b]; }
+              sw += kz[a] * t; su += kz[a] * td; sv += kzd[a] * t;
+            }
+          } else {
+#pragma unroll
+            for (int a = 0; a < mxd::TAPS; a++) {
+              float t = 0.f, td = 0.f;
+#pragma unroll
+              for (int b = 0; b < mxd::TAPS; b++) {
+                const float r = resid_at(g, rw, dl, jc - mxd::HALF + a, ic - mxd::HALF + b);
+                t += r * ky[b]; td += r * kyd[b];
+              }
+              sw += kz[a] * t; su += kz[a] * td; sv += kzd[a] * t;
+            }
+          }
+          const float vig = (float) A.vig, wv = (float) w.v * vig, ip = (float) g.inv_pitch;
+#pragma unroll
+          for (int k = 0; k < mxd::ND; k++) c6[k] = vig * sw * w.d[k] + wv * ip * (su * y.d[k] + sv * z.d[k]);
+        } else
+          si = -1;
+      }
+      float *row = stage + lane * ADJ_STAGE;
+#pragma unroll
+      for (int k = 0; k < mxd::ND; k++) row[k] = c6[k];
+      row[mxd::ND] = __int_as_float(si);
+      __syncwarp();
+      if (lane < NP) {
+        // lanes 0..15: shell lane/4, slot lane%4; lanes 16, 17: source slots 4, 5
+        const int want = lane < 16 ? (lane >> 2) : -2, slot = lane < 16 ? (lane & 3) : lane - 12;
+        float s = 0.f;
+        for (int r = 0; r < 32; r++) {
+          const float *q = stage + r * ADJ_STAGE;
+          const int sr = __float_as_int(q[mxd::ND]);
+          if (sr == want || (want == -2 && sr >= 0)) s += q[slot];
+        }
+        pacc += (double) s;
+      }
+      __syncwarp();
+    }
+    __syncthreads();   // the list is refilled for the next tile
   }
   __syncthreads();
   double *red = reinterpret_cast<double *>(rw);   // the window is no longer read
@@ -616,7 +648,8 @@ mx_diff *mx_diff_create(mx_context *c, const mx_diff_config *cfg) {
   if (e == cudaSuccess) {
     d->fwd_smem = align_up(sizeof(FwdArgs)) + sizeof(unsigned long long) * WIN * WIN + 4 * DWARPS * 32 * STAGE_STRIDE;
     d->rays_smem = align_up(sizeof(FwdArgs)) + 4 * DWARPS * 32 * STAGE_STRIDE;
-    d->adj_smem = align_up(sizeof(AdjArgs)) + 4 * WIN * (WIN + 1) + 4 * DWARPS * 32 * ADJ_STAGE;
+    d->adj_smem = align_up(sizeof(AdjArgs)) + 4 * WIN * (WIN + 1) + 4 * DWARPS * 32 * ADJ_STAGE + 4 * ADJ_TILE +
+                  4 * DWARPS;
     e = occupancy(diff_forward_kernel<true>, d->fwd_smem, c->num_sms, &d->fwd_blocks);
   }
   if (e == cudaSuccess) e = occupancy(diff_forward_kernel<false>, d->rays_smem, c->num_sms, &d->rays_blocks);

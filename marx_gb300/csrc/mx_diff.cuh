@@ -17,6 +17,7 @@
 #include <stdint.h>
 
 #include <cmath>
+#include <type_traits>
 
 #include "mx_device.cuh"
 
@@ -108,6 +109,12 @@ MXG Dual6 operator/(const Dual6 &a, double s) {
   for (int k = 0; k < ND; k++) r.d[k] = a.d[k] * f;
   return r;
 }
+// 1 / a: for the double rays the Newton-Raphson reciprocal (within one ulp)
+MXG double drcp(double a) { return mx::rcp_fast(a); }
+MXG Dual6 drcp(const Dual6 &a) { return 1.0 / a; }
+// a < b and a == 0 on the values, on the integer pipe
+MXG bool vlt(double a, double b) { return mx::dkey(a) < mx::dkey(b); }
+MXG bool vzero(double a) { return mx::is_zero(a); }
 MXG double dsqrt(double a) { return sqrt(a); }
 MXG Dual6 dsqrt(const Dual6 &a) {
   Dual6 r; r.v = sqrt(a.v);
@@ -215,6 +222,15 @@ template <class S> MXG void yaw_pitch(S fwd[9], S bwd[9], const S &az, const S &
 // Fresnel reflectivity averaged over polarisations (reflect.c:39-77) for a
 // grazing cosine cos_t and refractive index 1 - delta + i beta.
 template <class S> MXG S fresnel(const S &cos_t, double beta, double delta) {
+#ifdef __CUDA_ARCH__
+  if constexpr (std::is_same<S, double>::value) {
+    // the value alone: in double-float on the FP32 pipe (mx::reflectivity_df,
+    // beta and delta are floats), within about 2^-40 of the expression below
+    mx::F2 num, den;
+    mx::reflectivity_df(cos_t, mx::d2f_trunc(beta), mx::d2f_trunc(delta), num, den);
+    return mx::df_to(mx::df_div(num, den));
+  }
+#endif
   const double nr = 1.0 - delta, ni = beta;
   const double sr = nr * nr - ni * ni, si = 2.0 * nr * ni;
   S sin2 = 1.0 - cos_t * cos_t;
@@ -248,24 +264,24 @@ template <class S> MXG S fresnel(const S &cos_t, double beta, double delta) {
 // stays on the same branch while the optic moves.  Returns false on a miss.
 template <class S>
 MXG bool conic_hit(const Optic<S> &o, V3<S> &x0, const V3<S> &p, V3<S> &n, int root, int *chosen) {
-  S t_plus = (0.0 - x0.x) / p.x;
+  S t_plus = (0.0 - x0.x) * drcp(p.x);
   S x_y = x0.y + t_plus * p.y, x_z = x0.z + t_plus * p.z;
   S alpha = o.a * (p.x * p.x) - 1.0;
   S beta = o.b * p.x - 2.0 * (p.y * x_y + p.z * x_z);
   S gamma = o.c - x_z * x_z - x_y * x_y;
-  if (val(alpha) == 0.0) return false;
+  if (vzero(val(alpha))) return false;
   S bsqr = beta * beta, ac4 = alpha * gamma * 4.0;
-  if (!(val(bsqr) > val(ac4))) return false;
+  if (!vlt(val(ac4), val(bsqr))) return false;
   // the roots -2 gamma / (beta f) and -beta f / (2 alpha) of the reference,
   // f = 1 + sqrt(1 - 4 alpha gamma / beta^2), from b f = beta + sign(beta)
   // sqrt(beta^2 - 4 alpha gamma) and one reciprocal of alpha b f
-  S bf = beta + dcopysign(dsqrt(bsqr - ac4), beta), inv = 1.0 / (alpha * bf);
+  S bf = beta + dcopysign(dsqrt(bsqr - ac4), beta), inv = drcp(alpha * bf);
   S tp = (-2.0 * gamma) * alpha * inv, tm = (-0.5 * bf) * bf * inv;
   int pick = root;
   if (root < 0) {
     const double xp = val(p.x) * val(tp), xm = val(p.x) * val(tm);
-    const bool okp = xp >= o.xmin && xp < o.xmax, okm = xm >= o.xmin && xm < o.xmax;
-    if (okp) pick = (okm && xm > xp) ? 1 : 0;
+    const bool okp = !vlt(xp, o.xmin) && vlt(xp, o.xmax), okm = !vlt(xm, o.xmin) && vlt(xm, o.xmax);
+    if (okp) pick = (okm && vlt(xp, xm)) ? 1 : 0;
     else if (okm) pick = 1;
     else return false;
     *chosen = pick;
@@ -330,7 +346,7 @@ MXG bool weighted_ray(const Optic<S> &P, const Optic<S> &H, const RayConst &rc, 
   x = matv(H.bwd, x);
   x = x - v3<S>(H.to[0], H.to[1], H.to[2]);
   if (!replay && blocked(2, x, p)) return false;
-  S t = (0.0 - x.x) / p.x;
+  S t = (0.0 - x.x) * drcp(p.x);
   y = x.y + t * p.y;
   z = x.z + t * p.z;
   w = wt;
