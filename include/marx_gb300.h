@@ -735,6 +735,21 @@ int mx_event_bad_count(mx_context *ctx, unsigned long long *count, int reset);
  * (TFLOP/s), the denominator of the trace kernels' roofline. */
 int mx_probe_fp64(double *tflops, double *ms);
 
+/* The engine's own arithmetic helpers evaluated on the current device, for
+ * tests that hold them to their stated error bounds (no counterpart in the
+ * reference).  x and y are device pointers; n values in, n results out
+ * (2n for fn 1):
+ *   fn 0  y = 1/x by Newton-Raphson from a float seed (within one ulp)
+ *   fn 1  y[2i], y[2i+1] = sin(pi x), cos(pi x) in double-float (within 2^-44)
+ *   fn 2  y = x rounded to the nearest float (as the cast rounds it)
+ *   fn 3  y = (float) sin(x), as the cast of the double sine rounds it
+ *   fn 4  y = x truncated toward zero to float
+ *   fn 5  x holds n triples (cos of the grazing angle, beta, delta), y gets
+ *         n quadruples: the Fresnel numerator and denominator of the mirror
+ *         reflectivity in double-float, then in double precision
+ * Synchronises the device.  MX_EINVAL for an unknown fn or null pointers. */
+int mx_math_check(int fn, const double *x, double *y, size_t n);
+
 #ifdef __cplusplus
 }
 #endif

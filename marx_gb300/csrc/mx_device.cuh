@@ -47,10 +47,46 @@ MXD void mx_sincos(double x, double *s, double *c) {
   *s = std::sin(x); *c = std::cos(x);
 #endif
 }
+// Comparisons of doubles on the integer pipe.  On GB300 a DSETP issues on
+// the FP64 pipe, the one this trace is bound by; the order of IEEE doubles
+// is the order of their bit patterns read as sign-magnitude integers.
+// None of the helpers is meant for NaN.
+MXD unsigned long long dbits(double x) {
+#ifdef __CUDA_ARCH__
+  return (unsigned long long) __double_as_longlong(x);
+#else
+  unsigned long long u;
+  memcpy(&u, &x, 8);
+  return u;
+#endif
+}
+// a < b for a, b >= +0 (no -0): the bit patterns compare as unsigned integers
+MXD bool lt_pos(double a, double b) { return dbits(a) < dbits(b); }
+// a signed integer key with key(a) < key(b) exactly when a < b, and
+// key(-0) = key(+0) = 0
+MXD long long dkey(double x) {
+  const unsigned long long b = dbits(x);
+  return (long long) ((long long) b < 0 ? 0x8000000000000000ull - b : b);
+}
+MXD bool is_zero(double x) { return (dbits(x) << 1) == 0; }   // x = +0 or -0
+MXD bool neg_bit(double x) { return (long long) dbits(x) < 0; }   // sign bit: x < 0 or x = -0
+// (unsigned) (4 x) for 0 <= x < 1 from the bits of x: the integer part of
+// 1.m 2^(e+2).
+MXD unsigned quarter_of(double x) {
+#ifdef __CUDA_ARCH__
+  const unsigned long long b = dbits(x);
+  const int e = (int) ((b >> 52) & 0x7ff) - 1023 + 2;   // 4x = 1.m 2^e
+  if (e < 0) return 0u;
+  if (e > 2) return (unsigned) (4.0 * x);
+  return (unsigned) (((b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull) >> (52 - e));
+#else
+  return (unsigned) (4.0 * x);
+#endif
+}
 // JDMv_normalize (vector.c:99): a / |a|, a unchanged when |a| = 0.
 MXD D3 normalized(D3 a) {
   double d = dot(a, a);
-  if (d == 0.0) return a;
+  if (is_zero(d)) return a;
   return mx_rsqrt(d) * a;
 }
 // a / |a| for a vector whose length is 1 to within 1e-8 (a rotation of a
@@ -59,7 +95,8 @@ MXD D3 normalized(D3 a) {
 // shorter vectors take the full reciprocal square root.
 MXD D3 normalized_unit(D3 a) {
   double d = dot(a, a);
-  if (fabs(d - 1.0) < 1e-8) return (1.5 - 0.5 * d) * a;
+  // |d - 1| < 1e-8 exactly when 0x1.ffffffaa19c47p-1 < d < 0x1.0000002af31ddp+0
+  if (lt_pos(0x1.ffffffaa19c47p-1, d) && lt_pos(d, 0x1.0000002af31ddp+0)) return (1.5 - 0.5 * d) * a;
   return normalized(a);
 }
 // JDMv_rotate_unit_vector1 (vector.c:198): Rodrigues rotation of p about
@@ -70,19 +107,22 @@ MXD D3 rotate_unit(D3 p, D3 n, double c, double s) {
   return normalized_unit(u);
 }
 // sin and cos of an angle that is usually tiny (mirror blur, aspect blur,
-// dither offsets, facet misalignment, scattering): below 1e-3 rad the Taylor
-// series to x^7 / x^6 is exact to the last bit (the next terms are below
-// 1e-24 relative); larger angles take the library sincos.
+// dither offsets, facet misalignment, scattering).  Below 2^-5 rad the
+// Taylor series of sin to x^7 and of cos to x^8 leave out terms below
+// 3e-18 (sin, relative) and 3e-22 (cos): under a tenth of an ulp; below
+// 1e-4 rad the series to x^3 and x^2 already do (the next terms are below
+// 5e-18 relative).  Larger angles, rare in a warp, take the library
+// sincos.
 MXD void sincos_small(double x, double *s, double *c) {
-  if (fabs(x) < 1e-4) {
-    // the x^5 and x^4 terms are below 1e-18 relative: under a tenth of an ulp
+  const double ax = fabs(x);
+  if (lt_pos(ax, 1e-4)) {
     double x2 = x * x;
     *s = x + x * x2 * (-1.0 / 6.0);
     *c = 1.0 + x2 * -0.5;
-  } else if (fabs(x) < 1e-3) {
+  } else if (lt_pos(ax, 0x1p-5)) {
     double x2 = x * x;
     *s = x + x * x2 * (-1.0 / 6.0 + x2 * (1.0 / 120.0 + x2 * (-1.0 / 5040.0)));
-    *c = 1.0 + x2 * (-0.5 + x2 * (1.0 / 24.0 + x2 * (-1.0 / 720.0)));
+    *c = 1.0 + x2 * (-0.5 + x2 * (1.0 / 24.0 + x2 * (-1.0 / 720.0 + x2 * (1.0 / 40320.0))));
   } else
     mx_sincos(x, s, c);
 }
@@ -179,6 +219,26 @@ MXD float d2f_rn(double d) {
 #endif
   return (float) d;
 }
+// 1 / d by Newton-Raphson iteration (y <- y + y (1 - d y)) from a
+// single-precision seed: the float reciprocal of d is good to about 2^-23,
+// each step squares the relative error, so two steps leave only the
+// rounding of the last fused multiply-add (within one ulp of the quotient,
+// not always the correctly rounded one).  Two MUFU/integer operations and
+// four DFMA instead of the division's longer FP64 sequence.  Magnitudes
+// outside [2^-125, 2^125), zeros, infinities and NaN take the division.
+MXD double rcp_fast(double d) {
+#ifdef __CUDA_ARCH__
+  const unsigned e = (unsigned) (dbits(d) >> 52) & 0x7ffu;
+  if (e - 898u < 250u) {
+    double y = f2d(__frcp_rn(d2f_trunc(d)));
+    double r = fma(-d, y, 1.0);
+    y = fma(y, r, y);
+    r = fma(-d, y, 1.0);
+    return fma(y, r, y);
+  }
+#endif
+  return 1.0 / d;
+}
 // ------------------------------------------------ sines on the FP32 pipe --
 // GB300 issues FP64 at 1/64 of its FP32 rate, and a double-precision sine
 // or cosine from the math library takes about twenty FP64-pipe
@@ -251,6 +311,75 @@ __device__ __forceinline__ void df_sincos(F2 r, F2 &sr, F2 &cr) {
   Q = df_add(F2{0x1.555556p-5f, -0x1.555556p-30f}, df_mul(z, Q));
   Q = df_add(F2{-0.5f, 0.0f}, df_mul(z, Q));
   cr = df_add(F2{1.0f, 0.0f}, df_mul(z, Q));
+}
+
+__device__ __forceinline__ F2 df_neg(F2 a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ F2 df_sub(F2 a, F2 b) { return df_add(a, df_neg(b)); }
+__device__ __forceinline__ F2 df_sqr(F2 a) { return df_mul(a, a); }
+// sqrt(a), a > 0: the float root s corrected by (a - s^2) / (2 s), the
+// residual from a fused multiply-add (one Newton step; Karp and Markstein
+// 1997).
+__device__ __forceinline__ F2 df_sqrt(F2 a) {
+  const float s = __fsqrt_rn(a.h);
+  const float e = __fadd_rn(__fmaf_rn(-s, s, a.h), a.l);
+  return quick_sum(s, __fmul_rn(e, __fdiv_rn(0.5f, s)));
+}
+// 1 / sqrt(a), a > 0: the float estimate y and one Newton step
+// y (1 + (1 - a y^2) / 2), with 1 - a y^2 formed in double-float.
+__device__ __forceinline__ F2 df_rsqrt(F2 a) {
+  const float y = __frsqrt_rn(a.h);
+  const float p = __fmul_rn(y, y);
+  const F2 q = df_mul(a, F2{p, __fmaf_rn(y, y, -p)});
+  const float e = __fsub_rn(__fsub_rn(1.0f, q.h), q.l);
+  return quick_sum(y, __fmul_rn(__fmul_rn(0.5f, y), e));
+}
+// a / b: the float quotient corrected by the remainder a - q b.
+__device__ __forceinline__ F2 df_div(F2 a, F2 b) {
+  const float q = __fdiv_rn(a.h, b.h);
+  const F2 r = df_sub(a, df_mul_f(b, q));
+  return quick_sum(q, __fdiv_rn(r.h, b.h));
+}
+
+// The Fresnel numerator and denominator of reflectivity_parts in
+// double-float arithmetic on the FP32 pipe (beta, delta are floats), with
+// the same branches.  n^2 - sin^2 is formed without cancelling two numbers
+// near 1 (where the double evaluation loses up to 2^-28 near the critical
+// angle).  Within 2^-30 of the exact values over grazing angles of
+// 0.05-3 degrees and beta, delta of 1e-9..1e-2, typically 2^-42; the worst
+// case is the numerator of a reflectivity near 1e-7, which cancels in
+// cos - root as the double evaluation does.
+__device__ __forceinline__ void reflectivity_df(double cos_t, float beta, float delta, F2 &num, F2 &den) {
+  const F2 c = df_from(cos_t);
+  const F2 nr = two_sum(1.0f, -delta);
+  const float b2 = __fmul_rn(beta, beta);
+  const F2 bsq = {b2, __fmaf_rn(beta, beta, -b2)};
+  const F2 sr = df_sub(df_sqr(nr), bsq);
+  const F2 si = df_mul_f(nr, 2.0f * beta);
+  // wr = sr - (1 - c^2) as c^2 - (delta (2 - delta) + beta^2): the same
+  // value without the cancellation of two numbers near 1
+  const F2 k = df_add(df_mul_f(two_sum(2.0f, -delta), delta), bsq);
+  const F2 wr = df_sub(df_sqr(c), k), wi = si;
+  const F2 r = df_sqrt(df_add(df_sqr(wr), df_sqr(wi)));
+  F2 rr, ri;
+  const F2 half_wi = {0.5f * wi.h, 0.5f * wi.l};
+  if (wr.h >= 0.0f) {
+    const F2 h = df_add(r, wr);
+    const F2 hh = {0.5f * h.h, 0.5f * h.l}, inv = df_rsqrt(hh);
+    rr = df_mul(hh, inv); ri = df_mul(half_wi, inv);
+  } else {
+    const F2 h = df_sub(r, wr);
+    const F2 hh = {0.5f * h.h, 0.5f * h.l}, inv = df_rsqrt(hh);
+    rr = df_mul(half_wi, inv); ri = df_mul(hh, inv);
+    if (rr.h < 0.0f) { rr = df_neg(rr); ri = df_neg(ri); }
+  }
+  const F2 ri2 = df_sqr(ri);
+  const F2 a1 = df_add(df_sqr(df_sub(c, rr)), ri2), bb1 = df_add(df_sqr(df_add(c, rr)), ri2);
+  const F2 pr = df_mul(c, sr), pi_ = df_mul(c, si);
+  const F2 a2 = df_add(df_sqr(df_sub(pr, rr)), df_sqr(df_sub(pi_, ri)));
+  const F2 bb2 = df_add(df_sqr(df_add(pr, rr)), df_sqr(df_add(pi_, ri)));
+  const F2 t = df_add(df_mul(a1, bb2), df_mul(a2, bb1));
+  num = {0.5f * t.h, 0.5f * t.l};
+  den = df_mul(bb1, bb2);
 }
 #endif
 
@@ -408,6 +537,22 @@ MXD float interp_f(float x, const float *xp, const float *yp, const double *slop
   double q = slope[n0 < n1 ? n0 : n1];
   return d2f_rn(MX_DADD(f2d(yp[n0]), MX_DMUL(q, MX_DADD(f2d(x), -f2d(xf0)))));
 }
+// Two tables over the same abscissae (the optical constants beta and
+// delta): interp_f of each with one binary search.
+MXD void interp2_f(float x, const float *xp, const float *ya, const float *yb, const double *sa, const double *sb,
+                   unsigned n, float &a, float &b) {
+  if (n == 1) { a = ya[0]; b = yb[0]; return; }
+  unsigned n1 = bsearch_f(x, xp, n), n0 = n1 - 1;
+  if (n1 < n && x == xp[n1]) { a = ya[n1]; b = yb[n1]; return; }
+  if (n1 == n) { n1--; n0--; }
+  if (n1 == 0) n0 = 1;
+  const float xf0 = xp[n0], xf1 = xp[n1];
+  if (xf1 == xf0) { a = ya[n1]; b = yb[n1]; return; }
+  const unsigned k = n0 < n1 ? n0 : n1;
+  const double dx = MX_DADD(f2d(x), -f2d(xf0));
+  a = d2f_rn(MX_DADD(f2d(ya[n0]), MX_DMUL(sa[k], dx)));
+  b = d2f_rn(MX_DADD(f2d(yb[n0]), MX_DMUL(sb[k], dx)));
+}
 
 // ----------------------------------------------------------- variates --
 // Philox4x32-10 (Salmon et al., SC'11).  Uniform slot k of photon `tag`
@@ -559,36 +704,38 @@ struct Ph {
 // ------------------------------------------------------------- mirror --
 // JDMquadratic_root (qroot.c:36-70), same cancellation-free form.
 MXD int quadratic_root(double a, double b, double c, double &rp, double &rm) {
-  if (a == 0.0) return -1;
+  if (is_zero(a)) return -1;
   double bsqr = b * b, ac4 = a * c * 4;
-  if (bsqr > ac4) {
+  const long long kb = dkey(bsqr), ka = dkey(ac4);
+  if (kb > ka) {
     // rp = -2c / (b f), rm = -b f / (2a) from one reciprocal of a b f,
     // with b f = b (1 + sqrt(1 - 4ac/b^2)) = b + sign(b) sqrt(b^2 - 4ac)
-    double bf = b + copysign(sqrt(bsqr - ac4), b), inv = 1.0 / (a * bf);
+    double bf = b + copysign(sqrt(bsqr - ac4), b), inv = rcp_fast(a * bf);
     rp = -2.0 * c * a * inv;
     rm = -0.5 * bf * bf * inv;
     return 1;
   }
-  if (bsqr == ac4) { rp = rm = -b / (2.0 * a); return 1; }
+  if (kb == ka) { rp = rm = -b / (2.0 * a); return 1; }
   return 0;
 }
 
 // compute_conic_intersection (hrma.c:411-478) for x^2+y^2+z^2 = a x^2+b x+c.
 MXD int conic_intersection(const MxShellDev &h, int o, D3 &x0, D3 p, D3 &normal) {
   double a = h.a[o], b = h.b[o];
-  double t_plus = -x0.x / p.x, t_minus;
+  double t_plus = -x0.x * rcp_fast(p.x), t_minus;
   double x_y = x0.y + t_plus * p.y, x_z = x0.z + t_plus * p.z;
   double alpha = a * p.x * p.x - 1.0;
   double beta = b * p.x - 2.0 * (p.y * x_y + p.z * x_z);
   double gamma = h.c[o] - x_z * x_z - x_y * x_y;
-  if (alpha == 0.0) {
-    if (beta == 0.0) return -1;
+  if (is_zero(alpha)) {
+    if (is_zero(beta)) return -1;
     t_plus = t_minus = -gamma / beta;
   } else if (0 >= quadratic_root(alpha, beta, gamma, t_plus, t_minus)) return -1;
   double x_plus = p.x * t_plus, x_minus = p.x * t_minus;
   double xmin = h.xmin[o], xmax = h.xmax[o], t;
-  bool okp = (x_plus >= xmin) && (x_plus < xmax), okm = (x_minus >= xmin) && (x_minus < xmax);
-  if (okp) t = (okm && x_minus > x_plus) ? t_minus : t_plus;
+  const long long kp = dkey(x_plus), km = dkey(x_minus), kmin = dkey(xmin), kmax = dkey(xmax);
+  bool okp = (kp >= kmin) && (kp < kmax), okm = (km >= kmin) && (km < kmax);
+  if (okp) t = (okm && km > kp) ? t_minus : t_plus;
   else if (okm) t = t_minus;
   else return -1;
   x0 = mk(p.x * t, x_y + p.y * t, x_z + p.z * t);
@@ -628,14 +775,14 @@ MXD void reflectivity_parts(double cos_t, double beta, double delta, double &num
   // principal square root, branches as JDMc_sqrt (complex.c:201)
   double rr, ri;
   double r = sqrt(wr * wr + wi * wi);
-  if (r == 0.0) { rr = wr; ri = wi; }
-  else if (wr >= 0.0) {
+  if (is_zero(r)) { rr = wr; ri = wi; }
+  else if (!neg_bit(wr) || is_zero(wr)) {
     double h = 0.5 * (r + wr), inv = mx_rsqrt(h);
     rr = h * inv; ri = 0.5 * wi * inv;
   } else {
     double h = 0.5 * (r - wr), inv = mx_rsqrt(h);
     rr = 0.5 * wi * inv; ri = h * inv;
-    if (rr < 0.0) { rr = -rr; ri = -ri; }
+    if (neg_bit(rr) && !is_zero(rr)) { rr = -rr; ri = -ri; }
   }
   // e_perp = (cos - root) / (cos + root)
   double a1 = (cos_t - rr) * (cos_t - rr) + ri * ri, b1 = (cos_t + rr) * (cos_t + rr) + ri * ri;
@@ -656,9 +803,11 @@ MXD double reflectivity(double cos_t, double beta, double delta) {
 MXD double fold_theta(const MxTables &T, int table, unsigned a, double p) {
   const double *hd = T.fold_hdr + ((size_t) table * MX_FOLD_MAX + a) * 8;
   double p_min = MX_LDG(hd + 1), p_max = MX_LDG(hd + 3);
-  if (p < p_min) return 0.0;
+  if (dkey(p) < dkey(p_min)) return 0.0;
 #ifdef __CUDA_ARCH__
-  if (p > p_max) return pow(MX_LDG(hd + 4) * (1.0 - p), MX_LDG(hd + 5));
+  // the power law of the tail as exp(b log(a (1 - p))), a (1 - p) > 0: within
+  // about 1e-14 relative of pow, and about half its FP64 instructions
+  if (dkey(p_max) < dkey(p)) return exp(MX_LDG(hd + 5) * log(MX_LDG(hd + 4) * (1.0 - p)));
 #else
   if (p > p_max) return std::pow(MX_LDG(hd + 4) * (1.0 - p), MX_LDG(hd + 5));
 #endif
@@ -695,11 +844,22 @@ MXD bool reflect_test(const MxTables &T, const MxShellDev &h, int o, D3 p, D3 &n
   pdn = dot(p, n);
   if (!T.ideal) {
     double r = rng.uniform();
+#ifdef __CUDA_ARCH__
+    // decided in double-float, unless r * den and num * corr lie within
+    // 2^-24 of each other (far wider than the two evaluations' difference):
+    // then the double-precision values decide, as below
+    {
+      F2 fn, fd;
+      reflectivity_df(fabs(pdn), d2f_trunc(beta), d2f_trunc(delta), fn, fd);
+      const double x = r * df_to(fd), y = df_to(fn) * corr, gap = x - y, ag = fabs(gap);
+      if (lt_pos(0x1p-100, y) && lt_pos(0x1p-24 * y, ag) && lt_pos(ag, 0x1p+100)) return neg_bit(gap);
+    }
+#endif
     double num, den;
     reflectivity_parts(fabs(pdn), beta, delta, num, den);
     // r >= rfl * corr with rfl = num / den, den > 0, decided without the
     // division (the two differ only for r within an ulp of the threshold)
-    if (r * den >= num * corr) return false;
+    if (dkey(r * den) >= dkey(num * corr)) return false;
   }
   return true;
 }
@@ -712,8 +872,8 @@ MXD int reflect_finish(const MxTables &T, const MxShellDev &h, int o, int table,
   if (!T.use_wfold) return 0;
   double r = rng.uniform();
   double dg = wfold_interp(T, table, energy, -pdn, r) * h.scat[o];
-  if (dg > PI / 4) return -1;
-  if (rng.uniform() < 0.5) dg = -dg;
+  if (dkey(dg) > dkey(PI / 4)) return -1;
+  if (lt_pos(rng.uniform(), 0.5)) dg = -dg;
   // JDMv_rotate_unit_vector(p, p x n, dg): with a = p x n, p.a = 0 and
   // a x p = n - (p.n) p for unit p, so p becomes cos(dg) p + sin(dg) (n - (p.n) p)
   double sg, cg;
@@ -788,7 +948,7 @@ MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *
   if (!T.ideal) {
     // a uniform in [0, 1) never exceeds a vignetting factor of 1
     if (T.hrma_vig >= 1.0) rng.skip_uniform();
-    else if (rng.uniform() > T.hrma_vig) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
+    else if (lt_pos(T.hrma_vig, rng.uniform())) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
     if (ph.flags & MX_BAD_PHOTON_MASK) return false;
   }
   D3 x = ph.x, p = ph.p;
@@ -797,7 +957,7 @@ MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *
     double r = rng.uniform();
     if (rng.overrun) return false;
     for (int i = 0; i < 4; i++)
-      if (r < shells[i].area_fraction) { si = i; break; }
+      if (lt_pos(r, shells[i].area_fraction)) { si = i; break; }
   }
   if (si < 0) { rng.overrun = true; return false; }
   const MxShellDev &h = shells[si];
@@ -811,7 +971,7 @@ MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *
   double theta;
   for (int guard = 0;; guard++) {
     theta = rng.uniform();
-    unsigned quad = (unsigned) (4.0 * theta);
+    unsigned quad = quarter_of(theta);
     if (rng.overrun || guard >= 64) { rng.overrun = true; return false; }
     if (h.shutter & (1u << quad)) break;
   }
@@ -827,8 +987,7 @@ MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *
   m.beta = 0.0f; m.delta = 1.0f; m.corr = 1.0;
   if (T.opt_n) {
     float fe = d2f_rn(ph.e);
-    m.beta = interp_f(fe, optc, optc + T.opt_n, slope, T.opt_n);
-    m.delta = interp_f(fe, optc, optc + 2 * T.opt_n, slope + (T.opt_n - 1), T.opt_n);
+    interp2_f(fe, optc, optc + T.opt_n, optc + 2 * T.opt_n, slope, slope + (T.opt_n - 1), T.opt_n, m.beta, m.delta);
     if (T.use_scale) {
       const float *ce = optc + 3 * T.opt_n + h.corr_off;
       m.corr = sqrt(f2d(interp_f(fe, ce, ce + h.corr_n, slope + h.corr_slope_off, h.corr_n)));
@@ -973,7 +1132,7 @@ MXD void dither_stage(const MxTables &T, Ph &ph, Rng &rng) {
   double cos_theta = cd * cr;
   D3 n = mk(0, sd, -cd * sr);
   double s2 = n.y * n.y + n.z * n.z;
-  if (!(s2 > 1e-40)) { ph.p = p; return; }
+  if (!lt_pos(1e-40, s2)) { ph.p = p; return; }
   // rotate_unit(p, n / s, cos_theta, s) with s = |n| written without the
   // unit axis: cos p + ((p.n)(1 - cos) / s^2) n + n x p, n.x = 0.  With
   // s^2 = sin^2 the factor (1 - cos) / s^2 is 1 / (1 + cos) = 1 / (2 - d),
@@ -981,7 +1140,7 @@ MXD void dither_stage(const MxTables &T, Ph &ph, Rng &rng) {
   // 1/2 + d/4 + d^2/8 is exact to 1e-19 and saves the division.
   const double pn = p.y * n.y + p.z * n.z;
   const double d = 1.0 - cos_theta;
-  const double k = d < 1e-6 ? pn * (0.5 + d * (0.25 + d * 0.125)) : pn * d / s2;
+  const double k = lt_pos(d, 1e-6) ? pn * (0.5 + d * (0.25 + d * 0.125)) : pn * d / s2;
   ph.p = normalized_unit(mk(cos_theta * p.x + (n.y * p.z - n.z * p.y), cos_theta * p.y + k * n.y + n.z * p.x,
                        cos_theta * p.z + k * n.z - n.y * p.x));
 }
@@ -1163,14 +1322,14 @@ MXD void grating_stage(const MxTables &T, const MxGratingDev *grs, int kind, Ph 
 MXD int chip_plane(const MxChipDev &g, D3 x0, D3 p, D3 &x, double &dx, double &dy, bool must_hit) {
   D3 nrm = mk(g.normal[0], g.normal[1], g.normal[2]), ll = mk(g.x_ll[0], g.x_ll[1], g.x_ll[2]);
   double pdn = dot(p, nrm);
-  if (pdn == 0) return -1;
+  if (is_zero(pdn)) return -1;
   D3 r = x0 - ll;
   r = r + (-1.0 * dot(r, nrm) / pdn) * p;
   int hit = 1;
   double rx = r.x * g.xhat[0] + r.y * g.xhat[1] + r.z * g.xhat[2];
-  if ((rx < 0.0) || (rx >= g.xlen)) { if (must_hit) return 0; hit = 0; }
+  if ((dkey(rx) < 0) || (dkey(rx) >= dkey(g.xlen))) { if (must_hit) return 0; hit = 0; }
   double ry = r.x * g.yhat[0] + r.y * g.yhat[1] + r.z * g.yhat[2];
-  if ((ry < 0.0) || (ry >= g.ylen)) { if (must_hit) return 0; hit = 0; }
+  if ((dkey(ry) < 0) || (dkey(ry) >= dkey(g.ylen))) { if (must_hit) return 0; hit = 0; }
   x = r + ll; dx = rx; dy = ry;
   return hit;
 }
@@ -1193,6 +1352,17 @@ MXD int chip_screen(const MxChipDev &g, float x0, float x1, float x2, float p0, 
       ry > g.f_ylen + MX_CHIP_MARGIN)
     return 0;
   return 1;
+}
+// The first chip from k on that the screen does not rule out (nchips if
+// none).  Stepping from one candidate to the next keeps a warp's lanes
+// together: each runs the double-precision test once, on its own candidate
+// chip, in the same iteration, instead of at the loop index where its chip
+// happens to come.
+MXD int next_chip(const MxChipDev *chips, int nchips, int k, float x0, float x1, float x2, float p0, float p1,
+                  float p2) {
+  for (; k < nchips; k++)
+    if (chip_screen(chips[k], x0, x1, x2, p0, p1, p2)) break;
+  return k;
 }
 
 // The detector frame of a photon: _marx_dither_detector then
@@ -1440,13 +1610,13 @@ MXD void detect_stage(const MxTables &T, const MxChipDev *chips, int nchips, Ph 
 #ifdef __CUDA_ARCH__
   const float fx0 = d2f_trunc(x.x), fx1 = d2f_trunc(x.y), fx2 = d2f_trunc(x.z);
   const float fp0 = d2f_trunc(p.x), fp1 = d2f_trunc(p.y), fp2 = d2f_trunc(p.z);
-#endif
-  for (int k = 0; k < nchips; k++) {
-#ifdef __CUDA_ARCH__
-    if (!chip_screen(chips[k], fx0, fx1, fx2, fp0, fp1, fp2)) continue;
-#endif
+  for (int k = next_chip(chips, nchips, 0, fx0, fx1, fx2, fp0, fp1, fp2); k < nchips;
+       k = next_chip(chips, nchips, k + 1, fx0, fx1, fx2, fp0, fp1, fp2))
     if (1 == chip_plane(chips[k], x, p, xh, dx, dy, true)) { hit = k; break; }
-  }
+#else
+  for (int k = 0; k < nchips; k++)
+    if (1 == chip_plane(chips[k], x, p, xh, dx, dy, true)) { hit = k; break; }
+#endif
   if (hit < 0 && T.det_extend) {
     double best = -1;
     for (int k = 0; k < nchips; k++) {
@@ -1578,8 +1748,18 @@ MXD void hrc_detect_stage(const MxTables &T, const MxChipDev *chips, int nchips,
   int hit = -1;
   D3 xh = x;
   double dx = 0, dy = 0;
+#ifdef __CUDA_ARCH__
+  {
+    const float fx0 = d2f_trunc(x.x), fx1 = d2f_trunc(x.y), fx2 = d2f_trunc(x.z);
+    const float fp0 = d2f_trunc(p.x), fp1 = d2f_trunc(p.y), fp2 = d2f_trunc(p.z);
+    for (int k = next_chip(chips, nchips, 0, fx0, fx1, fx2, fp0, fp1, fp2); k < nchips;
+         k = next_chip(chips, nchips, k + 1, fx0, fx1, fx2, fp0, fp1, fp2))
+      if (1 == chip_plane(chips[k], x, p, xh, dx, dy, true)) { hit = k; break; }
+  }
+#else
   for (int k = 0; k < nchips; k++)
     if (1 == chip_plane(chips[k], x, p, xh, dx, dy, true)) { hit = k; break; }
+#endif
   if (hit < 0 && T.det_extend) {
     double best = -1;
     for (int k = 0; k < nchips; k++) {

@@ -443,6 +443,50 @@ cudaError_t launch_compact(const uint32_t *flags, uint32_t n, uint32_t *idx_out,
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------- arithmetic check --
+// The trace's own arithmetic helpers evaluated on the device, so that a
+// test can hold them to their error bounds: fn 0 rcp_fast (y = 1/x),
+// 1 sincospi_fast (y[2i], y[2i+1] = sin, cos of pi x), 2 d2f_rn
+// (y = the float nearest x), 3 sine_to_float with amp 1, amp_exp 0
+// (y = (float) sin x), 4 f2d of d2f_trunc (y = x truncated to float),
+// 5 the Fresnel numerator and denominator in double-float and in double.
+__global__ void __launch_bounds__(256) mx_math_kernel(int fn, const double *x, double *y, size_t n) {
+  const size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = fn == 5 ? 0.0 : x[i];
+  if (fn == 0) y[i] = mx::rcp_fast(v);
+  else if (fn == 1) {
+    double sn, cs;
+    mx::sincospi_fast(v, &sn, &cs);
+    y[2 * i] = sn;
+    y[2 * i + 1] = cs;
+  } else if (fn == 2) y[i] = (double) mx::d2f_rn(v);
+  else if (fn == 3) y[i] = (double) mx::sine_to_float(1.0, 0, v);
+  else if (fn == 4) y[i] = mx::f2d(mx::d2f_trunc(v));
+  else {
+    // x: n triples (cos, beta, delta); y: n quadruples, the double-float
+    // numerator and denominator, then the double-precision ones
+#ifdef __CUDA_ARCH__
+    const double c = x[3 * i], b = x[3 * i + 1], d = x[3 * i + 2];
+    mx::F2 fn, fd;
+    mx::reflectivity_df(c, mx::d2f_trunc(b), mx::d2f_trunc(d), fn, fd);
+    double num, den;
+    mx::reflectivity_parts(c, b, d, num, den);
+    y[4 * i] = mx::df_to(fn); y[4 * i + 1] = mx::df_to(fd);
+    y[4 * i + 2] = num; y[4 * i + 3] = den;
+#endif
+  }
+}
+
+cudaError_t math_check(int fn, const double *x, double *y, size_t n) {
+  if (n == 0) return cudaSuccess;
+  const unsigned blocks = (unsigned) ((n + 255) / 256);
+  mx_math_kernel<<<blocks, 256>>>(fn, x, y, n);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  return e;
+}
+
 // ----------------------------------------------------------- FP64 probe --
 // Dependent-free DFMA chains: 8 accumulators per thread, so the FP64 pipe
 // rather than latency bounds the rate.

@@ -67,3 +67,4 @@ cudaError_t launch_trace(const MxTables &T, const TraceIO &io, int grid, int sha
 cudaError_t launch_compact(const uint32_t *flags, uint32_t n, uint32_t *idx_out, uint32_t *scan, uint32_t nblk,
                            cudaStream_t st);
 cudaError_t probe_fp64(double *tflops, double *ms);
+cudaError_t math_check(int fn, const double *x, double *y, size_t n);
