@@ -69,6 +69,15 @@ MXD long long dkey(double x) {
   return (long long) ((long long) b < 0 ? 0x8000000000000000ull - b : b);
 }
 MXD bool is_zero(double x) { return (dbits(x) << 1) == 0; }   // x = +0 or -0
+// -x when neg, else x: a sign-bit flip on the integer pipe (a negation that
+// is not folded into the next operation issues as a DADD)
+MXD double flip_sign(double x, bool neg) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double(__double_as_longlong(x) ^ ((long long) neg << 63));
+#else
+  return neg ? -x : x;
+#endif
+}
 MXD bool neg_bit(double x) { return (long long) dbits(x) < 0; }   // sign bit: x < 0 or x = -0
 // (unsigned) (4 x) for 0 <= x < 1 from the bits of x: the integer part of
 // 1.m 2^(e+2).
@@ -81,6 +90,29 @@ MXD unsigned quarter_of(double x) {
   return (unsigned) (((b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull) >> (52 - e));
 #else
   return (unsigned) (4.0 * x);
+#endif
+}
+// (unsigned) x and (double) u on the integer pipe (the conversions issue
+// on the FP64 pipe): x >= 0 below 2^32, u below 2^32.
+MXD unsigned trunc_to_unsigned(double x) {
+#ifdef __CUDA_ARCH__
+  const unsigned long long b = dbits(x);
+  const int e = (int) ((b >> 52) & 0x7ff) - 1023;   // x = 1.m 2^e
+  if (e < 0) return 0u;
+  if (e > 31) return (unsigned) x;
+  return (unsigned) (((b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull) >> (52 - e));
+#else
+  return (unsigned) x;
+#endif
+}
+MXD double u2d(unsigned u) {
+#ifdef __CUDA_ARCH__
+  if (u == 0u) return 0.0;
+  const int lz = __clz((int) u);                      // u = 1.m 2^(31 - lz)
+  const unsigned long long m = ((unsigned long long) u << (lz + 21)) & 0xFFFFFFFFFFFFFull;
+  return __longlong_as_double((long long) (((unsigned long long) (1023 + 31 - lz) << 52) | m));
+#else
+  return (double) u;
 #endif
 }
 // JDMv_normalize (vector.c:99): a / |a|, a unchanged when |a| = 0.
@@ -398,8 +430,8 @@ MXD void sincospi_fast(double y, double *s, double *c) {
   // sin(q pi/2 + x), cos(q pi/2 + x) from sin x, cos x
   const double a = df_to(sr), b = df_to(cr);
   const int k = q & 3;
-  *s = k == 0 ? a : k == 1 ? b : k == 2 ? -a : -b;
-  *c = k == 0 ? b : k == 1 ? -a : k == 2 ? -b : a;
+  *s = flip_sign((k & 1) ? b : a, (k & 2) != 0);
+  *c = flip_sign((k & 1) ? a : b, ((k + 1) & 2) != 0);
 #else
   *s = std::sin(PI * y); *c = std::cos(PI * y);
 #endif
@@ -407,8 +439,9 @@ MXD void sincospi_fast(double y, double *s, double *c) {
 
 // (float) (amp * sin(arg)) exactly as the double-precision expression
 // rounds it (the dither offsets, which Marx_Dither_Type keeps as floats).
-// arg is reduced by pi/2 in three Cody-Waite parts (the first two of 33
-// bits, so k c1 and k c2 are exact for |k| < 2^18), sin in double-float.
+// arg is reduced by pi/2 in two Cody-Waite parts of 33 bits (k c1 and k c2
+// are exact for |k| < 2^18; the part left out, k 2.3e-21, stays below
+// 4e-16), sin in double-float.
 // The double-float value is within amp 2^-44 of amp sin(arg), the double
 // expression within two of its own ulps; when no float rounding boundary
 // lies within twice that distance of the value, both round to the same
@@ -423,13 +456,11 @@ MXD float sine_to_float(double amp, int amp_exp, double arg) {
     const double kd = t - magic;
     double r = fma(-kd, 0x1.921fb544p+0, arg);
     r = fma(-kd, 0x1.0b4611a6p-34, r);
-    r = fma(-kd, 0x1.3198a2e037073p-69, r);
     F2 sr, cr;
     df_sincos(df_from(r), sr, cr);
     const int k = __double2loint(t) & 3;
     const F2 w = (k & 1) ? cr : sr;
-    double v = amp * df_to(w);
-    if (k & 2) v = -v;
+    const double v = flip_sign(amp * df_to(w), (k & 2) != 0);
     const unsigned long long vb = (unsigned long long) __double_as_longlong(v);
     const int e = (int) ((vb >> 52) & 0x7ffu);
     const int sh = amp_exp + 1031 - e;   // log2 of amp 2^-44 in ulps of v
@@ -445,6 +476,17 @@ MXD float sine_to_float(double amp, int amp_exp, double arg) {
   (void) amp_exp;
   return (float) (amp * std::sin(arg));
 #endif
+}
+
+// sqrt of a float: in double-float on the FP32 pipe (within 2^-46 of the
+// double root; it scales the reflectivity, whose test leaves values within
+// 2^-24 of the threshold to a double comparison that a last-bit difference
+// of the root cannot reach but with a probability near 1e-16).
+MXD double sqrt_of_float(float f) {
+#ifdef __CUDA_ARCH__
+  if (f > 0.0f && f < 3.0e38f) return df_to(df_sqrt(F2{f, 0.0f}));
+#endif
+  return sqrt((double) f);
 }
 
 // a / b from the correctly rounded reciprocal rb = 1/b by one Markstein
@@ -812,12 +854,12 @@ MXD double fold_theta(const MxTables &T, int table, unsigned a, double p) {
   if (p > p_max) return std::pow(MX_LDG(hd + 4) * (1.0 - p), MX_LDG(hd + 5));
 #endif
   double di = (p - p_min) * MX_LDG(hd + 7);
-  unsigned i = (unsigned) di;
-  unsigned num = (unsigned) MX_LDG(hd + 6);
+  unsigned i = trunc_to_unsigned(di);
+  unsigned num = trunc_to_unsigned(MX_LDG(hd + 6));
   const float *t = T.fold_theta + ((size_t) table * MX_FOLD_MAX + a) * MX_FOLD_THETA;
   if (i + 1 >= num) return (double) MX_LDG(t + num - 1);
-  di -= (double) i;
-  return (1.0 - di) * (double) MX_LDG(t + i) + di * (double) MX_LDG(t + i + 1);
+  di -= u2d(i);
+  return (1.0 - di) * f2d(MX_LDG(t + i)) + di * f2d(MX_LDG(t + i + 1));
 }
 // marx_wfold_table_interp (wfold.c:334-363).
 MXD double wfold_interp(const MxTables &T, int table, double energy, double sin_alpha, double r) {
@@ -990,7 +1032,7 @@ MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *
     interp2_f(fe, optc, optc + T.opt_n, optc + 2 * T.opt_n, slope, slope + (T.opt_n - 1), T.opt_n, m.beta, m.delta);
     if (T.use_scale) {
       const float *ce = optc + 3 * T.opt_n + h.corr_off;
-      m.corr = sqrt(f2d(interp_f(fe, ce, ce + h.corr_n, slope + h.corr_slope_off, h.corr_n)));
+      m.corr = sqrt_of_float(interp_f(fe, ce, ce + h.corr_n, slope + h.corr_slope_off, h.corr_n));
     }
   }
   D3 n;
@@ -1141,8 +1183,10 @@ MXD void dither_stage(const MxTables &T, Ph &ph, Rng &rng) {
   const double pn = p.y * n.y + p.z * n.z;
   const double d = 1.0 - cos_theta;
   const double k = lt_pos(d, 1e-6) ? pn * (0.5 + d * (0.25 + d * 0.125)) : pn * d / s2;
-  ph.p = normalized_unit(mk(cos_theta * p.x + (n.y * p.z - n.z * p.y), cos_theta * p.y + k * n.y + n.z * p.x,
-                       cos_theta * p.z + k * n.z - n.y * p.x));
+  // a rotation of a unit vector: unit to the last bits without the
+  // reference's renormalisation, which moves it by less than 1e-15
+  ph.p = mk(cos_theta * p.x + (n.y * p.z - n.z * p.y), cos_theta * p.y + k * n.y + n.z * p.x,
+            cos_theta * p.z + k * n.z - n.y * p.x);
 }
 
 // ------------------------------------------------------------ grating --
@@ -1166,8 +1210,8 @@ MXD int rowland_intersect(D3 &x0, D3 p, double rowland) {
     double tt = t0 * t0;
     double num = tt * (3.0 * tt + a2 * t0 + b) - d;
     double den = tt * (4.0 * t0 + a3) + b2 * t0 + c;
-    t = num / den;
-    if (fabs(t - t0) < 1.0e-4) { x0 = x0 + t * p; return 0; }
+    t = num * rcp_fast(den);
+    if (lt_pos(fabs(t - t0), 1.0e-4)) { x0 = x0 + t * p; return 0; }
     t0 = t;
   }
   return -1;
@@ -1177,19 +1221,38 @@ MXD int rowland_intersect(D3 &x0, D3 p, double rowland) {
 // with facet sectors when the grating has them.
 MXD int diffract_photon(const MxTables &T, const MxGratingDev &g, int order_idx, double energy,
                         D3 x, D3 &P, Rng &rng) {
-  double nlod = MX_LDG(T.order_k + g.order_off + order_idx) / energy;
+  double nlod = MX_LDG(T.order_k + g.order_off + order_idx) * rcp_fast(energy);
   D3 n = -1.0 * normalized(x);
   D3 l = normalized(mk(n.z, 0.0, -n.x));
   D3 d = cross(n, l);
   double dtheta, dpp;
   if (g.nsec > 0) {
-    double sector = atan2(x.y, x.z);
-    if (sector < 0) sector = 2 * PI + sector;
     const double *smin = T.sectors + g.sec_off;          // [6][nsec]: min max dth dthb dpp dppb
-    unsigned sn = bsearch_d(sector, smin, (unsigned) g.nsec);
-    if (sn == 0) return -1;
-    sn -= 1;
-    if ((MX_LDG(smin + g.nsec + sn) <= sector) || (MX_LDG(smin + sn) > sector)) return -1;
+    const unsigned ns = (unsigned) g.nsec;
+    unsigned sn = ns;   // ns: not settled by the screen
+#ifdef __CUDA_ARCH__
+    {
+      // single-precision screen: the azimuth from atan2f is within 2e-6 rad
+      // of the double one; a photon more than 1e-5 rad inside a sector
+      // (from its two edges and the next sector's start) is in that sector
+      // in double precision too.  Others take the double-precision search.
+      float af = atan2f(d2f_trunc(x.y), d2f_trunc(x.z));
+      if (af < 0.0f) af += 6.28318531f;
+      const double a = f2d(af);
+      const unsigned k = bsearch_d(a, smin, ns);
+      if (k > 0 && lt_pos(MX_LDG(smin + k - 1) + 1e-5, a) && lt_pos(a + 1e-5, MX_LDG(smin + ns + k - 1)) &&
+          (k == ns || lt_pos(a + 1e-5, MX_LDG(smin + k))))
+        sn = k - 1;
+    }
+#endif
+    if (sn == ns) {
+      double sector = atan2(x.y, x.z);
+      if (sector < 0) sector = 2 * PI + sector;
+      sn = bsearch_d(sector, smin, ns);
+      if (sn == 0) return -1;
+      sn -= 1;
+      if ((MX_LDG(smin + g.nsec + sn) <= sector) || (MX_LDG(smin + sn) > sector)) return -1;
+    }
     dtheta = MX_LDG(smin + 2 * g.nsec + sn) + MX_LDG(smin + 3 * g.nsec + sn) * rng.normal();
     dpp = MX_LDG(smin + 4 * g.nsec + sn) + MX_LDG(smin + 5 * g.nsec + sn) * rng.normal();
   } else {
@@ -1197,7 +1260,7 @@ MXD int diffract_photon(const MxTables &T, const MxGratingDev &g, int order_idx,
     dpp = g.dp_over_p * rng.normal();
   }
   double theta = 0.0 - dtheta;
-  if (theta != 0.0) {
+  if (!is_zero(theta)) {
     double s, c;
     sincos_small(theta, &s, &c);
     D3 lt = l, dt = d;
@@ -1207,10 +1270,10 @@ MXD int diffract_photon(const MxTables &T, const MxGratingDev &g, int order_idx,
   D3 p = P;
   double p_d = nlod + dot(p, d), p_l = dot(p, l);
   double p_n = 1.0 - p_l * p_l - p_d * p_d;
-  if (p_n < 0.0) return -1;
+  if (neg_bit(p_n) && !is_zero(p_n)) return -1;
   p_n = sqrt(p_n);
   P = p_d * d + p_n * n + p_l * l;
-  if (dpp == 0) return 0;
+  if (is_zero(dpp)) return 0;
   double f = nlod * dpp;
   P = normalized(P + (-f) * d + (f * (p_d / p_n)) * n);
   return 0;
@@ -1225,30 +1288,36 @@ MXD int choose_order(const float *ge, unsigned n, const float *cum, int norders,
   unsigned lo = 1, hi = n - 1;
   while (lo < hi) {
     unsigned mid = (lo + hi) >> 1;
-    if ((double) fe > (double) MX_LDG(ge + mid)) lo = mid + 1; else hi = mid;
+    if (fe > MX_LDG(ge + mid)) lo = mid + 1; else hi = mid;   // floats compare as their doubles do
   }
   unsigned idx = lo;
-  double x0 = MX_LDG(ge + idx - 1), x1 = MX_LDG(ge + idx), dx = MX_DADD(x1, -x0);
-  double w = MX_DADD((double) fe, -x0);
+  double x0 = f2d(MX_LDG(ge + idx - 1)), x1 = f2d(MX_LDG(ge + idx)), dx = MX_DADD(x1, -x0);
+  double w = MX_DADD(f2d(fe), -x0);
   const float *c0 = cum + (size_t) (idx - 1) * norders;
+  const bool flat = is_zero(dx);
+  // the quotient by dx from one correctly rounded reciprocal: a Markstein
+  // division (div_by) rounds as the division does
+  const double rdx = flat ? 0.0 : MX_DDIV(1.0, dx);
   auto ck = [&](int k) -> float {
-    if (dx == 0.0) return MX_LDG(c0 + k);
-    double y0 = MX_LDG(c0 + k), y1 = MX_LDG(c0 + norders + k);
-    return (float) MX_DADD(y0, MX_DDIV(MX_DMUL(MX_DADD(y1, -y0), w), dx));
+    if (flat) return MX_LDG(c0 + k);
+    double y0 = f2d(MX_LDG(c0 + k)), y1 = f2d(MX_LDG(c0 + norders + k));
+    return d2f_rn(MX_DADD(y0, div_by(MX_DMUL(MX_DADD(y1, -y0), w), dx, rdx)));
   };
-  if (monotone && (dx == 0.0 || (w >= 0.0 && w <= dx))) {
+  // r <= c for r >= 0 and a cumulative efficiency c >= 0
+  auto reaches = [&](float c) { return !lt_pos(f2d(c), r); };
+  if (monotone && (flat || (!neg_bit(w) && dkey(w) <= dkey(dx)))) {
     // Between two rows that are non-decreasing in the order index the
     // interpolated row is too (rounding to float keeps the order), so the
     // first index reaching r is found by bisection over the same values.
     int a = 0, b = norders;
     while (a < b) {
       int m = (a + b) >> 1;
-      if (r <= (double) ck(m)) b = m; else a = m + 1;
+      if (reaches(ck(m))) b = m; else a = m + 1;
     }
     return a < norders ? a : -1;
   }
   for (int k = 0; k < norders; k++)
-    if (r <= (double) ck(k)) return k;
+    if (reaches(ck(k))) return k;
   return -1;
 }
 
@@ -1258,7 +1327,7 @@ MXD int choose_order(const float *ge, unsigned n, const float *cum, int norders,
 // drawn), the facet basis rotated about n by the support's fixed angle.
 MXD int diffract_support(const MxTables &T, const MxSupportDev &g, int order_idx, double energy, D3 x, D3 &P,
                          Rng &rng) {
-  double nlod = MX_LDG(T.support_k + g.order_off + order_idx) / energy;
+  double nlod = MX_LDG(T.support_k + g.order_off + order_idx) * rcp_fast(energy);
   D3 n = -1.0 * normalized(x);
   D3 l = normalized(mk(n.z, 0.0, -n.x));
   D3 d = cross(n, l);
@@ -1287,7 +1356,7 @@ MXD void grating_stage(const MxTables &T, const MxGratingDev *grs, int kind, Ph 
   if (letg) rng.window(MX_U_LETG, 6, MX_N_LETG, 10);
   else rng.window(MX_U_GRATING, 2, MX_N_GRATING, 2);
   const MxGratingDev &g = grs[(letg ? 4 : 0) + ph.shell];
-  if (rng.uniform() > g.vig) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
+  if (lt_pos(g.vig, rng.uniform())) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
   if (ph.flags & MX_BAD_PHOTON_MASK) return;
   D3 x = rot_x(ph.x, g.cos_m, g.sin_m), p = rot_x(ph.p, g.cos_m, g.sin_m);
   if (-1 == rowland_intersect(x, p, g.rowland)) ph.flags |= MX_PHOTON_UNDIFFRACTED;
