@@ -92,6 +92,16 @@ MXD unsigned quarter_of(double x) {
   return (unsigned) (4.0 * x);
 #endif
 }
+// sqrt(x) for geometry: x times the library's reciprocal square root (within
+// two ulps; six FP64 instructions and a multiply instead of the correctly
+// rounded root's nine).  x = 0, infinities and NaN take sqrt.
+MXD double sqrt_fast(double x) {
+#ifdef __CUDA_ARCH__
+  const unsigned e = (unsigned) (dbits(x) >> 52);   // sign and exponent
+  if (e - 1u < 0x7feu) return x * rsqrt(x);         // positive, normal, finite
+#endif
+  return sqrt(x);
+}
 // (unsigned) x and (double) u on the integer pipe (the conversions issue
 // on the FP64 pipe): x >= 0 below 2^32, u below 2^32.
 MXD unsigned trunc_to_unsigned(double x) {
@@ -752,7 +762,7 @@ MXD int quadratic_root(double a, double b, double c, double &rp, double &rm) {
   if (kb > ka) {
     // rp = -2c / (b f), rm = -b f / (2a) from one reciprocal of a b f,
     // with b f = b (1 + sqrt(1 - 4ac/b^2)) = b + sign(b) sqrt(b^2 - 4ac)
-    double bf = b + copysign(sqrt(bsqr - ac4), b), inv = rcp_fast(a * bf);
+    double bf = b + copysign(sqrt_fast(bsqr - ac4), b), inv = rcp_fast(a * bf);
     rp = -2.0 * c * a * inv;
     rm = -0.5 * bf * bf * inv;
     return 1;
@@ -802,7 +812,9 @@ MXD void blur_normal(D3 &n, double blur_rad, Rng &rng) {
   sincos_small(ang, &sa, &ca);
   const double nxy = n.x * n.y, nxz = n.x * n.z;
   const D3 w = mk(c * len, (s * n.z - c * nxy) * inv, (-s * n.y - c * nxz) * inv);   // perp x n
-  n = normalized_unit(ca * n + sa * w);
+  // a rotation of a unit vector: unit to the last bits without the
+  // reference's renormalisation, which moves it by less than 1e-15
+  n = ca * n + sa * w;
 }
 
 // marx_reflectivity (reflect.c:39-77): polarisation-averaged Fresnel
@@ -1007,7 +1019,7 @@ MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *
   double radius;
   if (T.area_uniform) {
     double r0 = h.min_radius, r1 = h.max_radius;
-    radius = sqrt(r0 * r0 + (r1 * r1 - r0 * r0) * rng.uniform());
+    radius = sqrt_fast(r0 * r0 + (r1 * r1 - r0 * r0) * rng.uniform());
   } else
     radius = h.min_radius + (h.max_radius - h.min_radius) * rng.uniform();
   double theta;
@@ -1023,8 +1035,14 @@ MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *
   if (T.source_distance > 0.0) p = normalized(x + T.source_distance * p);
   if (T.use_struts && struts_block(T, 0, x, p)) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
 
-  x = x + mk(h.to_osac[0][0], h.to_osac[0][1], h.to_osac[0][2]);
-  x = mat_mul(h.fwd[0], x);
+  // fwd (x + to_osac): (r sin - t1) + t1 is r sin to within an ulp of t1,
+  // and the first column's product with the front plane is a constant
+  {
+    const double y = radius * st, z = radius * ct;
+    const double *f = h.fwd[0];
+    x = mk(h.front_fwd[0] + f[1] * y + f[2] * z, h.front_fwd[1] + f[4] * y + f[5] * z,
+           h.front_fwd[2] + f[7] * y + f[8] * z);
+  }
   p = mat_mul(h.fwd[0], p);
   m.beta = 0.0f; m.delta = 1.0f; m.corr = 1.0;
   if (T.opt_n) {
@@ -1204,7 +1222,7 @@ MXD int rowland_intersect(D3 &x0, D3 p, double rowland) {
   double b = 2.0 * x2 + a * pdotx - r2 * pxpz;
   double c = a * x2 - 2.0 * r2 * p.z * x0.z;
   double d = x2 * x2 - r2 * x0.z * x0.z;
-  double t0 = -rowland * sqrt(pxpz);
+  double t0 = -rowland * sqrt_fast(pxpz);
   double a2 = 2.0 * a, a3 = 3.0 * a, b2 = 2.0 * b;
   for (int it = 0; it < 10; it++) {
     double tt = t0 * t0;
@@ -1271,7 +1289,7 @@ MXD int diffract_photon(const MxTables &T, const MxGratingDev &g, int order_idx,
   double p_d = nlod + dot(p, d), p_l = dot(p, l);
   double p_n = 1.0 - p_l * p_l - p_d * p_d;
   if (neg_bit(p_n) && !is_zero(p_n)) return -1;
-  p_n = sqrt(p_n);
+  p_n = sqrt_fast(p_n);
   P = p_d * d + p_n * n + p_l * l;
   if (is_zero(dpp)) return 0;
   double f = nlod * dpp;
@@ -1342,7 +1360,7 @@ MXD int diffract_support(const MxTables &T, const MxSupportDev &g, int order_idx
   double p_d = nlod + dot(p, d), p_l = dot(p, l);
   double p_n = 1.0 - p_l * p_l - p_d * p_d;
   if (p_n < 0.0) return -1;
-  p_n = sqrt(p_n);
+  p_n = sqrt_fast(p_n);
   P = p_d * d + p_n * n + p_l * l;
   return 0;
 }

@@ -826,6 +826,7 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
     }
     const double *qp = rdb + i * 9;
     h.front_position = cap_pos - qp[2] + h.xmax[0];
+    for (int r = 0; r < 3; r++) h.front_fwd[r] = h.fwd[0][3 * r] * (h.front_position + h.to_osac[0][0]);
     auto radius = [](double a, double b, double c, double x) { return sqrt(c + x * (b + x * (a - 1))); };
     h.min_radius = radius(h.a[0], h.b[0], h.c[0], h.xmin[0]);
     h.max_radius = radius(h.a[0], h.b[0], h.c[0], h.xmax[0]);

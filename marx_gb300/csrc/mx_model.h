@@ -21,6 +21,7 @@ struct MxShellDev {
   int32_t corr_off, corr_n;                    // correction-factor table (floats after the optical constants)
   uint32_t shutter;                            // open-quadrant bitmap
   int32_t corr_slope_off;                      // its interval slopes in optc_slope
+  double front_fwd[3];                         // fwd[0] (front_position + to_osac[0][0], 0, 0)
 };
 
 // One HETG grating (per mirror shell, diffract.c:51-77).
