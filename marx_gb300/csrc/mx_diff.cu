@@ -114,7 +114,7 @@ __device__ __forceinline__ bool aperture(const Aperture &ap, uint64_t seed, uint
   if (si < 0) return false;
   double radius;
   const double r0 = ap.rmin[si], r1 = ap.rmax[si];
-  if (ap.area_uniform) radius = sqrt(r0 * r0 + (r1 * r1 - r0 * r0) * rng.uniform());
+  if (ap.area_uniform) radius = mx::sqrt_fast(r0 * r0 + (r1 * r1 - r0 * r0) * rng.uniform());
   else radius = r0 + (r1 - r0) * rng.uniform();
   double theta;
   for (int guard = 0;; guard++) {
@@ -511,6 +511,7 @@ int build_optics(mx_diff *d, const double *theta, mxd::Optic<Dual6> opt[4][2], D
       Dual6 el = mxd::mkd(-(q[7] + theta[4 * s + 1] / 3600.0) * (PI_D / 180.0));
       el.d[1] = (float) -ARCSEC;
       mxd::yaw_pitch<Dual6>(op.fwd, op.bwd, az, el);
+      for (int r = 0; r < 3; r++) op.ff[r] = op.fwd[3 * r] * (h.front_position + op.to[0]);
     }
   }
   Dual6 ay = mxd::mkd((d->cfg.src_y + theta[16]) * ARCSEC);
@@ -543,6 +544,7 @@ int fill_fwd(mx_diff *d, const double *theta, FwdArgs &F) {
       b.a = a.a; b.b = a.b; b.c = a.c; b.xmin = a.xmin; b.xmax = a.xmax;
       for (int k = 0; k < 3; k++) b.to[k] = a.to[k].v;
       for (int k = 0; k < 9; k++) { b.fwd[k] = a.fwd[k].v; b.bwd[k] = a.bwd[k].v; }
+      for (int k = 0; k < 3; k++) b.ff[k] = a.ff[k].v;
     }
   for (int s = 0; s < 4; s++) F.rc[s] = d->rc[s];
   F.ap = d->ap;

@@ -185,6 +185,7 @@ template <class S> struct Optic {
   double a, b, c, xmin, xmax;
   S to[3];
   S fwd[9], bwd[9];
+  S ff[3];   // fwd (front + to[0], 0, 0): the aperture plane's part of fwd (x + to)
 };
 
 // The rotation builders of init_yaw_pitch (hrma.c:842-880), over S.
@@ -317,11 +318,12 @@ MXG bool weighted_ray(const Optic<S> &P, const Optic<S> &H, const RayConst &rc, 
   int rootH = replay ? ((code & RAY_ROOT_H) ? 1 : 0) : -1;
   if (replay && !(code & RAY_HIT)) return false;
   if (!replay) code = 0;
-  V3<S> x = v3<S>(cst<S>(rc.front), ry - P.to[1], rz - P.to[2]);
   V3<S> p = p0;
-  if (!replay && blocked(0, x, p)) return false;
-  x = x + v3<S>(P.to[0], P.to[1], P.to[2]);
-  x = matv(P.fwd, x);
+  if (!replay && blocked(0, v3<S>(cst<S>(rc.front), ry - P.to[1], rz - P.to[2]), p)) return false;
+  // fwd (x + to) with x + to = (front + to[0], ry, rz): (ry - to[1]) + to[1]
+  // is ry to within an ulp of to[1]
+  V3<S> x = v3<S>(P.ff[0] + P.fwd[1] * ry + P.fwd[2] * rz, P.ff[1] + P.fwd[4] * ry + P.fwd[5] * rz,
+                  P.ff[2] + P.fwd[7] * ry + P.fwd[8] * rz);
   p = matv(P.fwd, p);
   V3<S> n;
   int ch = 0;
