@@ -327,7 +327,7 @@ int mx_trace_static(mx_context *ctx, const mx_photons *ph, uint32_t stages, cons
                     uint64_t seed, void *stream);
 
 /* Same trace on HOST buffers: copies inputs to the device, traces and
- * copies results back; blocks until done.  A list of 2^21 photons or more
+ * copies results back; blocks until done.  A list of 2^19 photons or more
  * (tracing the mirror) is cut into chunks on several streams, so that the
  * copies of one chunk overlap the trace of another (pinned host memory lets
  * them run asynchronously); the results are those of one pass. */

@@ -405,7 +405,8 @@ static int trace_host_pipelined(mx_context *c, const mx_photons *h, uint32_t sta
   cudaEventRecord(ready, c->stream);
   for (int s = 0; s < MX_PIPE_STREAMS; s++) cudaStreamWaitEvent(c->pipe[s], ready, 0);
   cudaEventDestroy(ready);
-  const size_t chunk = ((n + MX_PIPE_CHUNKS - 1) / MX_PIPE_CHUNKS + 255) & ~(size_t) 255;
+  const size_t nch = std::max<size_t>(4, std::min<size_t>(MX_PIPE_CHUNKS, n >> 17));
+  const size_t chunk = ((n + nch - 1) / nch + 255) & ~(size_t) 255;
   for (size_t i0 = 0, j = 0; i0 < n; i0 += chunk, j++) {
     const size_t m = std::min(chunk, n - i0);
     cudaStream_t st = c->pipe[j % MX_PIPE_STREAMS];

@@ -58,8 +58,8 @@ struct mx_context {
   int asp_record_only = 0;
 };
 #define MX_PIPE_STREAMS 3
-#define MX_PIPE_CHUNKS 16
-#define MX_PIPE_MIN_PHOTONS (2u << 20)
+#define MX_PIPE_CHUNKS 16           // at most; about 2^17 photons per chunk, at least 4 chunks
+#define MX_PIPE_MIN_PHOTONS (1u << 19)
 
 // Record an error on the context (or as the creation error when c is null)
 // and return code.

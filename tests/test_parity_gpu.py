@@ -173,14 +173,14 @@ def test_launch_count_tracks_kernels(cuda):
     assert eng.launch_count() == before + 1 + 4   # phases A, T, B and C
 
 
-@pytest.mark.parametrize("slots", [False, True])
-def test_pipelined_host_entry_equals_device_trace(cuda, slots):
+@pytest.mark.parametrize("slots,n", [(False, (1 << 21) + 12345), (True, (1 << 21) + 12345), (False, (1 << 19) + 333)])
+def test_pipelined_host_entry_equals_device_trace(cuda, slots, n):
     """mx_trace_host on a list large enough to be cut into chunks on
-    several streams (copies overlapping the trace): every column equals the
-    one-pass device trace of the same photons, with Philox draws and with
-    pre-drawn variates (packed per chunk)."""
+    several streams (copies overlapping the trace; 16 chunks, and 4 at the
+    smallest size that is cut): every column equals the one-pass device
+    trace of the same photons, with Philox draws and with pre-drawn
+    variates (packed per chunk)."""
     w = W.ALL["plain_scatter"]()
-    n = (1 << 21) + 12345
     ph = w.photons(n, seed=9)
     U, N = predraw_variates(n, 3) if slots else (None, None)
     eng = engine(w.cfg)
