@@ -747,6 +747,9 @@ int mx_probe_fp64(double *tflops, double *ms);
  *   fn 5  x holds n triples (cos of the grazing angle, beta, delta), y gets
  *         n quadruples: the Fresnel numerator and denominator of the mirror
  *         reflectivity in double-float, then in double precision
+ *   fn 6  y = (double) (unsigned) x, 0 <= x < 2^32, on the integer pipe
+ *   fn 7  y = sqrt(x) from the reciprocal square root (within two ulps)
+ *   fn 8  y = (unsigned) (4 x), 0 <= x < 1, from the bits of x
  * Synchronises the device.  MX_EINVAL for an unknown fn or null pointers. */
 int mx_math_check(int fn, const double *x, double *y, size_t n);
 

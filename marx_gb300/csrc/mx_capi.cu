@@ -542,7 +542,7 @@ int mx_probe_fp64(double *tflops, double *ms) {
 }
 
 int mx_math_check(int fn, const double *x, double *y, size_t n) {
-  if (fn < 0 || fn > 5 || (n && (!x || !y))) return MX_EINVAL;
+  if (fn < 0 || fn > 8 || (n && (!x || !y))) return MX_EINVAL;
   if (n > ((size_t) 1 << 32)) return MX_ERANGE;
   return math_check(fn, x, y, n) == cudaSuccess ? MX_OK : MX_ECUDA;
 }

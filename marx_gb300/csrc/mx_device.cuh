@@ -102,6 +102,16 @@ MXD double sqrt_fast(double x) {
 #endif
   return sqrt(x);
 }
+// sqrt(x) and 1 / sqrt(x) from one reciprocal square root (x positive,
+// normal, finite); other x take sqrt and a division.
+MXD void sqrt_rsqrt(double x, double &s, double &rs) {
+#ifdef __CUDA_ARCH__
+  const unsigned e = (unsigned) (dbits(x) >> 52);
+  if (e - 1u < 0x7feu) { rs = rsqrt(x); s = x * rs; return; }
+#endif
+  s = sqrt(x);
+  rs = 1.0 / s;
+}
 // (unsigned) x and (double) u on the integer pipe (the conversions issue
 // on the FP64 pipe): x >= 0 below 2^32, u below 2^32.
 MXD unsigned trunc_to_unsigned(double x) {
@@ -725,6 +735,12 @@ struct Rng {
     if (upos >= uend) overrun = true;
     else upos++;
   }
+  // Pass over the next normal slot without drawing it (a normal that is
+  // multiplied by zero).
+  MXD void skip_normal() {
+    if (npos >= nend) overrun = true;
+    else npos++;
+  }
   MXD double normal() {
     if (npos >= nend) { overrun = true; return 0.0; }
     int k = npos++;
@@ -1040,8 +1056,8 @@ MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *
   {
     const double y = radius * st, z = radius * ct;
     const double *f = h.fwd[0];
-    x = mk(h.front_fwd[0] + f[1] * y + f[2] * z, h.front_fwd[1] + f[4] * y + f[5] * z,
-           h.front_fwd[2] + f[7] * y + f[8] * z);
+    x = mk(fma(f[2], z, fma(f[1], y, h.front_fwd[0])), fma(f[5], z, fma(f[4], y, h.front_fwd[1])),
+           fma(f[8], z, fma(f[7], y, h.front_fwd[2])));
   }
   p = mat_mul(h.fwd[0], p);
   m.beta = 0.0f; m.delta = 1.0f; m.corr = 1.0;
@@ -1210,6 +1226,13 @@ MXD void dither_stage(const MxTables &T, Ph &ph, Rng &rng) {
 // ------------------------------------------------------------ grating --
 MXD D3 rot_x(D3 a, double c, double s) { return mk(a.x, c * a.y - s * a.z, s * a.y + c * a.z); }
 
+// a l + b d + c n with a fixed order of fused multiply-adds, so that every
+// kernel that inlines it rounds it alike (left to the compiler, the
+// contraction of a sum of products may differ from one kernel to another).
+MXD D3 comb3(double a, D3 l, double b, D3 d, double c, D3 n) {
+  return mk(fma(a, l.x, fma(b, d.x, MX_DMUL(c, n.x))), fma(a, l.y, fma(b, d.y, MX_DMUL(c, n.y))),
+            fma(a, l.z, fma(b, d.z, MX_DMUL(c, n.z))));
+}
 // intersect + newtons_quartic (diffract.c:622-687): Rowland torus.
 MXD int rowland_intersect(D3 &x0, D3 p, double rowland) {
   double t = -x0.x / p.x;
@@ -1240,7 +1263,8 @@ MXD int rowland_intersect(D3 &x0, D3 p, double rowland) {
 MXD int diffract_photon(const MxTables &T, const MxGratingDev &g, int order_idx, double energy,
                         D3 x, D3 &P, Rng &rng) {
   double nlod = MX_LDG(T.order_k + g.order_off + order_idx) * rcp_fast(energy);
-  D3 n = -1.0 * normalized(x);
+  const double xx = dot(x, x);
+  const D3 n = is_zero(xx) ? -1.0 * x : (-mx_rsqrt(xx)) * x;   // -x / |x|
   D3 l = normalized(mk(n.z, 0.0, -n.x));
   D3 d = cross(n, l);
   double dtheta, dpp;
@@ -1278,22 +1302,26 @@ MXD int diffract_photon(const MxTables &T, const MxGratingDev &g, int order_idx,
     dpp = g.dp_over_p * rng.normal();
   }
   double theta = 0.0 - dtheta;
-  if (!is_zero(theta)) {
-    double s, c;
-    sincos_small(theta, &s, &c);
-    D3 lt = l, dt = d;
-    l = c * lt + s * dt;
-    d = (-s) * lt + c * dt;
+  // the facet basis turned by theta, l' = c l + s d and d' = c d - s l,
+  // enters through its components only: p.l', p.d' from p.l, p.d, and the
+  // new direction p_d d' + p_n n + p_l l' (and the dP/P term -f d') as
+  // coefficients of l, d and n
+  double sn = 0.0, cs = 1.0;
+  if (!is_zero(theta)) sincos_small(theta, &sn, &cs);
+  const double pl0 = dot(P, l), pd0 = dot(P, d);
+  const double p_l = fma(cs, pl0, MX_DMUL(sn, pd0)), p_d = nlod + fma(cs, pd0, -MX_DMUL(sn, pl0));
+  const double pn2 = fma(-p_d, p_d, fma(-p_l, p_l, 1.0));
+  if (neg_bit(pn2) && !is_zero(pn2)) return -1;
+  double p_n, inv_pn;
+  sqrt_rsqrt(pn2, p_n, inv_pn);
+  double cl = fma(p_l, cs, -MX_DMUL(p_d, sn)), cd = fma(p_l, sn, MX_DMUL(p_d, cs)), cn = p_n;
+  if (is_zero(dpp)) {
+    P = comb3(cl, l, cd, d, cn, n);
+    return 0;
   }
-  D3 p = P;
-  double p_d = nlod + dot(p, d), p_l = dot(p, l);
-  double p_n = 1.0 - p_l * p_l - p_d * p_d;
-  if (neg_bit(p_n) && !is_zero(p_n)) return -1;
-  p_n = sqrt_fast(p_n);
-  P = p_d * d + p_n * n + p_l * l;
-  if (is_zero(dpp)) return 0;
-  double f = nlod * dpp;
-  P = normalized(P + (-f) * d + (f * (p_d / p_n)) * n);
+  const double f = MX_DMUL(nlod, dpp);
+  cl = fma(f, sn, cl); cd = fma(-f, cs, cd); cn = fma(f, MX_DMUL(p_d, inv_pn), cn);
+  P = normalized(comb3(cl, l, cd, d, cn, n));
   return 0;
 }
 
@@ -1346,22 +1374,21 @@ MXD int choose_order(const float *ge, unsigned n, const float *cum, int norders,
 MXD int diffract_support(const MxTables &T, const MxSupportDev &g, int order_idx, double energy, D3 x, D3 &P,
                          Rng &rng) {
   double nlod = MX_LDG(T.support_k + g.order_off + order_idx) * rcp_fast(energy);
-  D3 n = -1.0 * normalized(x);
+  const double xx = dot(x, x);
+  const D3 n = is_zero(xx) ? -1.0 * x : (-mx_rsqrt(xx)) * x;   // -x / |x|
   D3 l = normalized(mk(n.z, 0.0, -n.x));
   D3 d = cross(n, l);
-  (void) rng.normal();   // dtheta = 0 x N
-  (void) rng.normal();   // dP/P = 0 x N
-  if (g.rotate) {
-    D3 lt = l, dt = d;
-    l = g.cos_t * lt + g.sin_t * dt;
-    d = (-g.sin_t) * lt + g.cos_t * dt;
-  }
-  D3 p = P;
-  double p_d = nlod + dot(p, d), p_l = dot(p, l);
-  double p_n = 1.0 - p_l * p_l - p_d * p_d;
-  if (p_n < 0.0) return -1;
-  p_n = sqrt_fast(p_n);
-  P = p_d * d + p_n * n + p_l * l;
+  rng.skip_normal();   // dtheta = 0 x N
+  rng.skip_normal();   // dP/P = 0 x N
+  // the basis turned by the support's angle enters through its components,
+  // as in diffract_photon
+  const double cs = g.rotate ? g.cos_t : 1.0, sn = g.rotate ? g.sin_t : 0.0;
+  const double pl0 = dot(P, l), pd0 = dot(P, d);
+  const double p_l = fma(cs, pl0, MX_DMUL(sn, pd0)), p_d = nlod + fma(cs, pd0, -MX_DMUL(sn, pl0));
+  const double pn2 = fma(-p_d, p_d, fma(-p_l, p_l, 1.0));
+  if (neg_bit(pn2) && !is_zero(pn2)) return -1;
+  const double p_n = sqrt_fast(pn2);
+  P = comb3(fma(p_l, cs, -MX_DMUL(p_d, sn)), l, fma(p_l, sn, MX_DMUL(p_d, cs)), d, p_n, n);
   return 0;
 }
 
@@ -1811,8 +1838,20 @@ MXD void drake_reflect(const MxTables &T, const MxHrcDev &h, Ph &ph, Rng &rng) {
     ph.x = nx;
     float fe = d2f_rn(ph.e);
     float beta = hrc_interp(T, cr ? h.cr_beta : h.c_beta, fe), delta = hrc_interp(T, cr ? h.cr_delta : h.c_delta, fe);
-    double rfl = reflectivity(fabs(pdn), f2d(beta), f2d(delta));
-    if (rfl < rng.uniform()) { ph.flags |= MX_PHOTON_DRAKE_BLOCKED; return; }
+    const double u = rng.uniform();
+    int blocked = -1;   // -1: left to the double-precision test
+#ifdef __CUDA_ARCH__
+    {
+      // the double-float reflectivity decides unless u den and num lie
+      // within 2^-24 of each other, as in reflect_test
+      F2 fn, fd;
+      reflectivity_df(fabs(pdn), beta, delta, fn, fd);
+      const double y = df_to(fn), gap = y - u * df_to(fd), ag = fabs(gap);
+      if (lt_pos(0x1p-100, y) && lt_pos(0x1p-24 * y, ag) && lt_pos(ag, 0x1p+100)) blocked = neg_bit(gap) ? 1 : 0;
+    }
+#endif
+    if (blocked < 0) blocked = reflectivity(fabs(pdn), f2d(beta), f2d(delta)) < u ? 1 : 0;
+    if (blocked) { ph.flags |= MX_PHOTON_DRAKE_BLOCKED; return; }
     ph.p = p + (-2.0 * pdn) * nrm;
     ph.flags |= MX_PHOTON_DRAKE_REFLECTED;
     return;

@@ -449,7 +449,8 @@ cudaError_t launch_compact(const uint32_t *flags, uint32_t n, uint32_t *idx_out,
 // 1 sincospi_fast (y[2i], y[2i+1] = sin, cos of pi x), 2 d2f_rn
 // (y = the float nearest x), 3 sine_to_float with amp 1, amp_exp 0
 // (y = (float) sin x), 4 f2d of d2f_trunc (y = x truncated to float),
-// 5 the Fresnel numerator and denominator in double-float and in double.
+// 5 the Fresnel numerator and denominator in double-float and in double,
+// 6 (double) (unsigned) x on the integer pipe, 7 sqrt_fast, 8 quarter_of.
 __global__ void __launch_bounds__(256) mx_math_kernel(int fn, const double *x, double *y, size_t n) {
   const size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -463,6 +464,9 @@ __global__ void __launch_bounds__(256) mx_math_kernel(int fn, const double *x, d
   } else if (fn == 2) y[i] = (double) mx::d2f_rn(v);
   else if (fn == 3) y[i] = (double) mx::sine_to_float(1.0, 0, v);
   else if (fn == 4) y[i] = mx::f2d(mx::d2f_trunc(v));
+  else if (fn == 6) y[i] = mx::u2d(mx::trunc_to_unsigned(v));
+  else if (fn == 7) y[i] = mx::sqrt_fast(v);
+  else if (fn == 8) y[i] = mx::quarter_of(v);
   else {
     // x: n triples (cos, beta, delta); y: n quadruples, the double-float
     // numerator and denominator, then the double-precision ones

@@ -153,3 +153,22 @@ def test_double_float_reflectivity(cuda):
     e = np.maximum(rel(num_df, en), rel(den_df, ed))
     assert float(e.max()) <= 2.0 ** -30 and float(np.median(e)) <= 2.0 ** -42
     assert float(max(rel(num_df, num.astype(np.longdouble)).max(), rel(den_df, den.astype(np.longdouble)).max())) <= 2.0 ** -26
+
+
+def test_integer_pipe_truncations_and_fast_root(cuda):
+    """(double) (unsigned) x and (unsigned) (4 x) built from the bits of x,
+    exactly the casts; sqrt from the reciprocal square root within two
+    ulps of the correctly rounded root."""
+    rng = np.random.default_rng(16)
+    x = np.concatenate([rng.uniform(0, 4.29e9, 20000), rng.uniform(0, 2, 5000), np.arange(0, 70) / 3.0,
+                        [0.0, 0.999999, 1.0, 2.0 ** 31, 2.0 ** 32 - 1.0, 4294967295.5, 1e-300]])
+    assert np.array_equal(_run(6, x), np.floor(x))
+    u = np.concatenate([rng.uniform(0, 1, 20000), [0.0, 0.25, 0.5, 0.75, np.nextafter(0.25, 0), np.nextafter(1.0, 0),
+                                                   1e-300, 5e-324]])
+    assert np.array_equal(_run(8, u), np.floor(4 * u))
+    r = np.concatenate([np.exp(rng.uniform(-700, 700, 20000)), rng.uniform(0, 1e6, 5000)])
+    got = _run(7, r)
+    want = np.sqrt(r)
+    assert np.all(np.abs(got - want) <= 2 * np.spacing(want))
+    edge = np.array([0.0, -0.0, np.inf, 5e-324, 1e-310])
+    assert np.array_equal(_run(7, edge), np.sqrt(edge))
