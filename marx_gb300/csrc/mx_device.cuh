@@ -1160,6 +1160,38 @@ MXD bool aspsol_state(const MxTables &T, double t, float s[6]) {
   return true;
 }
 
+#ifdef __CUDA_ARCH__
+// apply_dither's rotation (below) for offsets ra, dec under 1e-4 rad, as the
+// change it makes: p' = p + D with
+//   D = -d p + k n + n x p,  n = (0, sin dec, -cos dec sin ra),
+//   d = 1 - cos dec cos ra,  k = (p.n) (1/2 + d/4 + d^2/8),
+// the terms of D (below 1e-4) in double-float on the FP32 pipe and the sum
+// with p in double.  sin and cos go to x^3 and x^2 (the next terms are
+// below 1e-18 relative) as in sincos_small, and d is formed as
+// (ra^2 + dec^2)/2 - ra^2 dec^2/4, without the cancellation that costs the
+// double evaluation seven digits of d.  Eleven FP64 operations (the
+// splits, the sums back to double and the additions to p) instead of about
+// thirty-five; the result is within an ulp or two of the double evaluation.
+__device__ __forceinline__ D3 dither_rotate_df(D3 p, double ra, double dec) {
+  const F2 sixth = {0x1.555556p-3f, -0x1.555556p-28f};   // 1/6
+  const F2 r = df_from(ra), e = df_from(dec);
+  const F2 r2 = df_sqr(r), e2 = df_sqr(e);
+  const F2 sr = df_sub(r, df_mul(df_mul(r, r2), sixth)), sd = df_sub(e, df_mul(df_mul(e, e2), sixth));
+  const F2 cd = df_add(F2{1.0f, 0.0f}, F2{-0.5f * e2.h, -0.5f * e2.l});
+  const F2 ny = sd, nz = df_neg(df_mul(cd, sr));
+  const F2 h = df_add(r2, e2), q = df_mul(r2, e2);
+  const F2 d = df_sub(F2{0.5f * h.h, 0.5f * h.l}, F2{0.25f * q.h, 0.25f * q.l});
+  const F2 px = df_from(p.x), py = df_from(p.y), pz = df_from(p.z);
+  const F2 pn = df_add(df_mul(py, ny), df_mul(pz, nz));
+  const F2 k = df_mul(pn, df_add(F2{0.5f, 0.0f}, df_mul(d, df_add(F2{0.25f, 0.0f}, df_mul_f(d, 0.125f)))));
+  const F2 md = df_neg(d);
+  const F2 dx = df_add(df_mul(md, px), df_sub(df_mul(ny, pz), df_mul(nz, py)));
+  const F2 dy = df_add(df_add(df_mul(md, py), df_mul(k, ny)), df_mul(nz, px));
+  const F2 dz = df_sub(df_add(df_mul(md, pz), df_mul(k, nz)), df_mul(ny, px));
+  return mk(p.x + df_to(dx), p.y + df_to(dy), p.z + df_to(dz));
+}
+#endif
+
 // get_internal_dither / get_aspsol_dither + dither_ray + apply_dither
 // (dither.c:167-182, 350-389, 551-581, 609-628).  The dither angles pass
 // through float as they do in Marx_Dither_Type.
@@ -1202,6 +1234,14 @@ MXD void dither_stage(const MxTables &T, Ph &ph, Rng &rng) {
     p = rotate_x(p, cr, sr);
   } else if (!T.roll_zero)
     p = rotate_x(p, T.roll_cos, T.roll_sin);
+#ifdef __CUDA_ARCH__
+  // arcsecond offsets (the usual case): the same rotation in double-float
+  const double ara = fabs(ra), adec = fabs(dec);
+  if (lt_pos(ara, 1e-4) && lt_pos(adec, 1e-4) && (lt_pos(1e-19, ara) || lt_pos(1e-19, adec))) {
+    ph.p = dither_rotate_df(p, ra, dec);
+    return;
+  }
+#endif
   double sr, cr, sd, cd;
   sincos_small(ra, &sr, &cr);
   sincos_small(dec, &sd, &cd);
