@@ -1370,6 +1370,18 @@ MXD int diffract_photon(const MxTables &T, const MxGratingDev &g, int order_idx,
 // capped at n-1; each order's value rounded to float) and the order choice
 // of diffract_photon_from_grating (diffract.c:828-849): the first index
 // whose cumulative efficiency reaches r, or -1.  cum is [energy][order].
+// Whether the cumulative efficiency of order index k, interpolated at w
+// into the energy bin of width dx (rdx = 1/dx) and rounded to float,
+// reaches r (r <= c; r and c are not negative).
+MXD bool order_reaches(const float *c0, int norders, int k, bool flat, double w, double dx, double rdx, double r) {
+  float c;
+  if (flat) c = MX_LDG(c0 + k);
+  else {
+    const double y0 = f2d(MX_LDG(c0 + k)), y1 = f2d(MX_LDG(c0 + norders + k));
+    c = d2f_rn(MX_DADD(y0, div_by(MX_DMUL(MX_DADD(y1, -y0), w), dx, rdx)));
+  }
+  return !lt_pos(f2d(c), r);
+}
 MXD int choose_order(const float *ge, unsigned n, const float *cum, int norders, bool monotone, float fe, double r) {
   unsigned lo = 1, hi = n - 1;
   while (lo < hi) {
@@ -1384,13 +1396,6 @@ MXD int choose_order(const float *ge, unsigned n, const float *cum, int norders,
   // the quotient by dx from one correctly rounded reciprocal: a Markstein
   // division (div_by) rounds as the division does
   const double rdx = flat ? 0.0 : MX_DDIV(1.0, dx);
-  auto ck = [&](int k) -> float {
-    if (flat) return MX_LDG(c0 + k);
-    double y0 = f2d(MX_LDG(c0 + k)), y1 = f2d(MX_LDG(c0 + norders + k));
-    return d2f_rn(MX_DADD(y0, div_by(MX_DMUL(MX_DADD(y1, -y0), w), dx, rdx)));
-  };
-  // r <= c for r >= 0 and a cumulative efficiency c >= 0
-  auto reaches = [&](float c) { return !lt_pos(f2d(c), r); };
   if (monotone && (flat || (!neg_bit(w) && dkey(w) <= dkey(dx)))) {
     // Between two rows that are non-decreasing in the order index the
     // interpolated row is too (rounding to float keeps the order), so the
@@ -1398,12 +1403,12 @@ MXD int choose_order(const float *ge, unsigned n, const float *cum, int norders,
     int a = 0, b = norders;
     while (a < b) {
       int m = (a + b) >> 1;
-      if (reaches(ck(m))) b = m; else a = m + 1;
+      if (order_reaches(c0, norders, m, flat, w, dx, rdx, r)) b = m; else a = m + 1;
     }
     return a < norders ? a : -1;
   }
   for (int k = 0; k < norders; k++)
-    if (reaches(ck(k))) return k;
+    if (order_reaches(c0, norders, k, flat, w, dx, rdx, r)) return k;
   return -1;
 }
 
