@@ -23,6 +23,10 @@ struct DevBuf {
   void release() { if (ptr) cudaFree(ptr); ptr = nullptr; bytes = 0; }
 };
 
+#define MX_PIPE_STREAMS 6
+#define MX_PIPE_CHUNKS 16           // at most; about 2^17 photons per chunk, at least 4 chunks
+#define MX_PIPE_MIN_PHOTONS (1u << 19)
+
 struct mx_context {
   int device = 0;
   int num_sms = 0;
@@ -50,16 +54,14 @@ struct mx_context {
   unsigned long long *d_event_bad = nullptr;
   // mx_trace_host on large lists: chunks on MX_PIPE_STREAMS streams so that
   // copies in, kernels and copies out of different chunks overlap
-  cudaStream_t pipe[3] = {nullptr, nullptr, nullptr};
-  DevBuf pipe_wave[3];
+  cudaStream_t pipe[MX_PIPE_STREAMS] = {};
+  DevBuf pipe_wave[MX_PIPE_STREAMS];
   // DitherModel FILE: the converted aspect solution (mx_set_aspect_solution)
   DevBuf asp;
   uint32_t asp_n = 0;
   int asp_record_only = 0;
 };
-#define MX_PIPE_STREAMS 3
-#define MX_PIPE_CHUNKS 16           // at most; about 2^17 photons per chunk, at least 4 chunks
-#define MX_PIPE_MIN_PHOTONS (1u << 19)
+
 
 // Record an error on the context (or as the creation error when c is null)
 // and return code.
