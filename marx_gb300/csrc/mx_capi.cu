@@ -331,7 +331,7 @@ int mx_trace_queues(mx_context *c, const MxTables &T, const mx_photons *ph, uint
     w.q2 = (MxRec *) ((char *) queues.ptr + qbytes);
     w.counts = (unsigned int *) ((char *) queues.ptr + 2 * qbytes);
     e = launch_wavefront(T, io, w, c->num_sms * c->wave_blocks, (int) c->shared_bytes, st);
-    c->launches += MX_WAVE_KERNELS;
+    c->launches += wave_kernels(T, stages);
   } else {
     e = launch_trace(T, io, c->num_sms * c->trace_blocks[slots ? 0 : 1], (int) c->shared_bytes, slots != 0, st);
     c->launches++;

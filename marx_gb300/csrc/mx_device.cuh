@@ -1437,28 +1437,47 @@ MXD int diffract_support(const MxTables &T, const MxSupportDev &g, int order_idx
   return 0;
 }
 
-// diffract (diffract.c:974-1130) for one photon: vignetting, rotation into
-// the grating frame, Rowland torus, the primary grating's order and
-// diffraction, for the LETG the four support gratings (fine, then coarse
-// at 60, 120 and 0 degrees), and the rotation back.
-MXD void grating_stage(const MxTables &T, const MxGratingDev *grs, int kind, Ph &ph, Rng &rng) {
+// diffract (diffract.c:974-1130) for one photon, in two parts: vignetting,
+// rotation into the grating frame, Rowland torus, the primary grating's
+// order; then its diffraction, for the LETG the four support gratings, and
+// the rotation back.
+// grating_front: the grating's vignetting, the Rowland torus and the order
+// choice.  Returns the chosen order index, with the photon at the torus in
+// the grating's frame in x, p, or -1 when the photon's grating stage ends
+// here (vignetted: ph unchanged; no order chosen: ph.x, ph.p rotated back
+// from the torus).  Most photons that reach the gratings end here (no
+// order), so the wavefront diffracts the others in a phase of their own.
+MXD int grating_front(const MxTables &T, const MxGratingDev *grs, int kind, Ph &ph, Rng &rng, D3 &x, D3 &p) {
   const bool letg = kind == MX_GRATING_LETG;
   if (letg) rng.window(MX_U_LETG, 6, MX_N_LETG, 10);
   else rng.window(MX_U_GRATING, 2, MX_N_GRATING, 2);
   const MxGratingDev &g = grs[(letg ? 4 : 0) + ph.shell];
   if (lt_pos(g.vig, rng.uniform())) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
-  if (ph.flags & MX_BAD_PHOTON_MASK) return;
-  D3 x = rot_x(ph.x, g.cos_m, g.sin_m), p = rot_x(ph.p, g.cos_m, g.sin_m);
+  if (ph.flags & MX_BAD_PHOTON_MASK) return -1;
+  x = rot_x(ph.x, g.cos_m, g.sin_m);
+  p = rot_x(ph.p, g.cos_m, g.sin_m);
   if (-1 == rowland_intersect(x, p, g.rowland)) ph.flags |= MX_PHOTON_UNDIFFRACTED;
-  float fe = d2f_rn(ph.e);
-  int chosen = choose_order(T.geff_energy + g.geff_off, (unsigned) g.nenergy, T.geff_cum + g.cum_off, g.norders,
-                            g.monotone != 0, fe, rng.uniform());
-  if (chosen < 0) ph.flags |= MX_PHOTON_UNDIFFRACTED;
-  else {
-    ph.order = chosen - g.max_order;
-    if (-1 == diffract_photon(T, g, chosen, ph.e, x, p, rng)) ph.flags |= MX_PHOTON_UNDIFFRACTED;
+  const int chosen = choose_order(T.geff_energy + g.geff_off, (unsigned) g.nenergy, T.geff_cum + g.cum_off, g.norders,
+                                  g.monotone != 0, d2f_rn(ph.e), rng.uniform());
+  if (chosen < 0) {
+    // no order: the LETG's supports are skipped (the photon is flagged)
+    ph.flags |= MX_PHOTON_UNDIFFRACTED;
+    ph.x = rot_x(x, g.cos_p, g.sin_p);
+    ph.p = rot_x(p, g.cos_p, g.sin_p);
+    return -1;
   }
+  ph.order = chosen - g.max_order;
+  return chosen;
+}
+// grating_back: the diffraction into the chosen order, for the LETG its
+// four support gratings (fine, then coarse at 60, 120 and 0 degrees), and
+// the rotation back; the rng window is grating_front's.
+MXD void grating_back(const MxTables &T, const MxGratingDev *grs, int kind, Ph &ph, Rng &rng, D3 x, D3 p, int chosen) {
+  const bool letg = kind == MX_GRATING_LETG;
+  const MxGratingDev &g = grs[(letg ? 4 : 0) + ph.shell];
+  if (-1 == diffract_photon(T, g, chosen, ph.e, x, p, rng)) ph.flags |= MX_PHOTON_UNDIFFRACTED;
   if (letg) {
+    const float fe = d2f_rn(ph.e);
     for (int s = 0; s < 4; s++) {
       const MxSupportDev &sg = T.supports[s];
       if (!sg.norders) continue;
@@ -1474,6 +1493,12 @@ MXD void grating_stage(const MxTables &T, const MxGratingDev *grs, int kind, Ph 
   }
   ph.x = rot_x(x, g.cos_p, g.sin_p);
   ph.p = rot_x(p, g.cos_p, g.sin_p);
+}
+// diffract (diffract.c:974-1130) for one photon, both parts.
+MXD void grating_stage(const MxTables &T, const MxGratingDev *grs, int kind, Ph &ph, Rng &rng) {
+  D3 x, p;
+  const int chosen = grating_front(T, grs, kind, ph, rng, x, p);
+  if (chosen >= 0) grating_back(T, grs, kind, ph, rng, x, p, chosen);
 }
 
 // ----------------------------------------------------------- detector --

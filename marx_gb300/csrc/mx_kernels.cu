@@ -286,43 +286,113 @@ __global__ void __launch_bounds__(MX_WAVE_BLOCK, MX_WAVE_MIN_BLOCKS) mx_wave_b(M
             [&](Ph &q, Rng &r, MirrorState &m) { return mirror_middle(T, sh, q, r, m); });
 }
 
-__global__ void __launch_bounds__(MX_WAVE_BLOCK, MX_WAVE_MIN_BLOCKS) mx_wave_c(MxTables T, TraceIO io, WaveBufs w) {
-  MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
-  stage_tables(T, sh, gr, ch, optc, slope);
-  const uint32_t count = *(volatile unsigned int *) &w.counts[2];
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += stride) {
-    const MxRec rec = w.q1[k];
-    const uint32_t i = rec.i;
-    Ph q; MirrorState m; Rng r;
-    from_rec(rec, q, m, r, io);
-    const int unset = 0x7fff;
-    q.order = unset; q.ccd = unset;
-    if (T.grating == MX_GRATING_LETG)   // supports skipped by this photon keep their values
-      for (int s = 0; s < 4; s++) q.sup[s] = io.support ? io.support[s * (size_t) io.stride + i] : 0;
-    mirror_back(T, sh, q, r, m);
-    if (!r.overrun && (io.stages & MX_STAGE_GRATING) && T.grating && !(q.flags & MX_BAD_PHOTON_MASK))
-      grating_stage(T, gr, T.grating, q, r);
-    if (!r.overrun && (io.stages & MX_STAGE_DETECT) && T.nchips && !(q.flags & MX_BAD_PHOTON_MASK))
-      any_detect_stage(T, ch + T.chip_off, T.nchips, q, r);
-    store_core(io, i, q, r.overrun);
-    store_extra(io, i, q);
-    if (q.order != unset && io.order) io.order[i] = (int8_t) q.order;
-    if (q.ccd != unset) {
-      if (io.ccd) io.ccd[i] = (int8_t) q.ccd;
-      if (q.ccd >= 0) {
-        if (io.ypix) io.ypix[i] = q.ypix;
-        if (io.zpix) io.zpix[i] = q.zpix;
-      }
+// The end of a photon's trace in phases C and D: the detector (when the
+// photon is still good), then its output columns.
+__device__ __forceinline__ void finish_photon(const MxTables &T, const MxChipDev *ch, const TraceIO &io, uint32_t i,
+                                              Ph &q, Rng &r) {
+  const int unset = 0x7fff;
+  if (!r.overrun && (io.stages & MX_STAGE_DETECT) && T.nchips && !(q.flags & MX_BAD_PHOTON_MASK))
+    any_detect_stage(T, ch + T.chip_off, T.nchips, q, r);
+  store_core(io, i, q, r.overrun);
+  store_extra(io, i, q);
+  if (q.order != unset && io.order) io.order[i] = (int8_t) q.order;
+  if (q.ccd != unset) {
+    if (io.ccd) io.ccd[i] = (int8_t) q.ccd;
+    if (q.ccd >= 0) {
+      if (io.ypix) io.ypix[i] = q.ypix;
+      if (io.zpix) io.zpix[i] = q.zpix;
     }
   }
 }
 
+// The photons a grating diffracts, between phases C and D: at the Rowland
+// torus in the grating's frame (x, p), with the chosen order index in the
+// record's pdn field (n, corr, beta and delta are unused here).
+__device__ __forceinline__ void to_rec_d(MxRec &r, D3 x, D3 p, const Ph &q, const Rng &rng, uint32_t i, int chosen) {
+  r.x[0] = x.x; r.x[1] = x.y; r.x[2] = x.z;
+  r.p[0] = p.x; r.p[1] = p.y; r.p[2] = p.z;
+  r.e = q.e; r.t = q.t;
+  r.i = i; r.tag = rng.tag; r.flags = q.flags;
+  r.shell = (uint8_t) q.shell; r.upos = (uint8_t) rng.upos; r.npos = (uint8_t) rng.npos;
+  r.overrun = rng.overrun ? 1 : 0;
+  r.pdn = (double) chosen;
+}
+
+__device__ __forceinline__ void load_supports(const MxTables &T, const TraceIO &io, uint32_t i, Ph &q) {
+  if (T.grating == MX_GRATING_LETG)   // supports skipped by this photon keep their values
+    for (int s = 0; s < 4; s++) q.sup[s] = io.support ? io.support[s * (size_t) io.stride + i] : 0;
+}
+
+// Phase C: the hyperboloid's reflection and the post-collimator struts, then
+// with a grating its vignetting, Rowland torus and order choice, sending the
+// photons given an order to phase D; every other photon runs the detector
+// (without a grating) and is stored here.
+__global__ void __launch_bounds__(MX_WAVE_BLOCK, MX_WAVE_MIN_BLOCKS) mx_wave_c(MxTables T, TraceIO io, WaveBufs w) {
+  MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
+  stage_tables(T, sh, gr, ch, optc, slope);
+  const uint32_t count = *(volatile unsigned int *) &w.counts[2];
+  const bool grating = (io.stages & MX_STAGE_GRATING) && T.grating;
+  const uint32_t lane = threadIdx.x & 31, warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t base = warp * 32; base < count; base += nwarps * 32) {
+    const uint32_t k = base + lane;
+    bool to_d = false;
+    MxRec rec;
+    if (k < count) {
+      rec = w.q1[k];
+      const uint32_t i = rec.i;
+      Ph q; MirrorState m; Rng r;
+      from_rec(rec, q, m, r, io);
+      const int unset = 0x7fff;
+      q.order = unset; q.ccd = unset;
+      load_supports(T, io, i, q);
+      mirror_back(T, sh, q, r, m);
+      if (!r.overrun && grating && !(q.flags & MX_BAD_PHOTON_MASK)) {
+        D3 gx, gp;
+        const int chosen = grating_front(T, gr, T.grating, q, r, gx, gp);
+        if (chosen >= 0) {
+          to_d = true;
+          to_rec_d(rec, gx, gp, q, r, i, chosen);
+        }
+      }
+      if (!to_d) finish_photon(T, ch, io, i, q, r);
+    }
+    if (grating) append(to_d, rec, w.q2, &w.counts[3]);
+  }
+}
+
+// Phase D (with a grating): the diffraction into the chosen order (and the
+// LETG's supports), the detector and the output columns.
+__global__ void __launch_bounds__(MX_WAVE_BLOCK, MX_WAVE_MIN_BLOCKS) mx_wave_d(MxTables T, TraceIO io, WaveBufs w) {
+  MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
+  stage_tables(T, sh, gr, ch, optc, slope);
+  const uint32_t count = *(volatile unsigned int *) &w.counts[3];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += stride) {
+    const MxRec rec = w.q2[k];
+    const uint32_t i = rec.i;
+    Ph q;
+    q.e = rec.e; q.t = rec.t; q.flags = rec.flags; q.shell = rec.shell; q.set = 0;
+    const int unset = 0x7fff;
+    q.ccd = unset;
+    load_supports(T, io, i, q);
+    Rng r;
+    r.U = io.U; r.N = io.N; r.seed = io.seed; r.n = io.n; r.i = i; r.tag = rec.tag;
+    if (T.grating == MX_GRATING_LETG) r.window(MX_U_LETG, 6, MX_N_LETG, 10);
+    else r.window(MX_U_GRATING, 2, MX_N_GRATING, 2);
+    r.upos = rec.upos; r.npos = rec.npos; r.overrun = rec.overrun != 0;
+    const int chosen = (int) rec.pdn;
+    q.order = chosen - gr[(T.grating == MX_GRATING_LETG ? 4 : 0) + q.shell].max_order;
+    grating_back(T, gr, T.grating, q, r, mk(rec.x[0], rec.x[1], rec.x[2]), mk(rec.p[0], rec.p[1], rec.p[2]), chosen);
+    finish_photon(T, ch, io, i, q, r);
+  }
+}
+
 cudaError_t wave_occupancy(int shared_bytes, int *blocks_per_sm) {
-  const void *f[4] = {(const void *) mx_wave_a, (const void *) mx_wave_t, (const void *) mx_wave_b,
-                      (const void *) mx_wave_c};
+  const void *f[5] = {(const void *) mx_wave_a, (const void *) mx_wave_t, (const void *) mx_wave_b,
+                      (const void *) mx_wave_c, (const void *) mx_wave_d};
   int best = 1 << 30;
-  for (int k = 0; k < 4; k++) {
+  for (int k = 0; k < 5; k++) {
     int b = 0;
     cudaError_t e = cudaFuncSetAttribute(f[k], cudaFuncAttributeMaxDynamicSharedMemorySize, shared_bytes);
     if (e != cudaSuccess) return e;
@@ -339,12 +409,13 @@ cudaError_t launch_wavefront(const MxTables &T, const TraceIO &io, const WaveBuf
   uint32_t need = (io.n + MX_WAVE_BLOCK - 1) / MX_WAVE_BLOCK;
   int ga = (uint32_t) grid > need ? (int) need : grid;
   if (ga < 1) ga = 1;
-  cudaError_t e = cudaMemsetAsync(w.counts, 0, 3 * sizeof(unsigned int), st);
+  cudaError_t e = cudaMemsetAsync(w.counts, 0, 4 * sizeof(unsigned int), st);
   if (e != cudaSuccess) return e;
   mx_wave_a<<<ga, MX_WAVE_BLOCK, shared_bytes, st>>>(T, io, w);
   mx_wave_t<<<ga, MX_WAVE_BLOCK, shared_bytes, st>>>(T, io, w);
   mx_wave_b<<<ga, MX_WAVE_BLOCK, shared_bytes, st>>>(T, io, w);
   mx_wave_c<<<ga, MX_WAVE_BLOCK, shared_bytes, st>>>(T, io, w);
+  if (wave_kernels(T, io.stages) == 5) mx_wave_d<<<ga, MX_WAVE_BLOCK, shared_bytes, st>>>(T, io, w);
   return cudaGetLastError();
 }
 

@@ -9,7 +9,7 @@
 #define MX_TRACE_BLOCK 256
 #define MX_WAVE_BLOCK 256         // threads per block of the wavefront kernels
 #define MX_WAVE_MIN_BLOCKS 2     // resident blocks per SM they are compiled for: up to 128 registers, no spills (256 x 3 with 80 registers and 256 x 4, 128 x 5 and 128 x 7 measured no faster)
-#define MX_WAVE_KERNELS 4        // kernels of one wavefront trace
+#define MX_WAVE_KERNELS 4        // kernels of one wavefront trace without a grating (5 with one)
 #define MX_COMPACT_THREADS 256
 #define MX_COMPACT_ITEMS 16
 #define MX_COMPACT_TILE (MX_COMPACT_THREADS * MX_COMPACT_ITEMS)
@@ -46,11 +46,16 @@ struct __align__(16) MxRec {
 
 // Wavefront scratch: two record queues of n entries and their fill counts.
 // Phase A appends to q1, the paraboloid test moves survivors to q2, phase B
-// appends to q1 again (its first use is over), phase C reads it.
+// appends to q1 again (its first use is over), phase C reads it and, with a
+// grating, appends the photons given an order to q2 for phase D.
 struct WaveBufs {
   MxRec *q1, *q2;
-  unsigned int *counts;         // [0]: first q1 fill, [1]: q2 fill, [2]: second q1 fill
+  unsigned int *counts;         // [0]: first q1 fill, [1]: q2 fill, [2]: second q1 fill, [3]: second q2 fill
 };
+// Kernels of one wavefront trace: a, t, b, c and, with a grating stage, d.
+__host__ __device__ inline int wave_kernels(const MxTables &T, uint32_t stages) {
+  return (T.grating && (stages & MX_STAGE_GRATING)) ? 5 : 4;
+}
 
 size_t trace_shared_bytes(const MxTables &T);
 cudaError_t wave_occupancy(int shared_bytes, int *blocks_per_sm);

@@ -74,7 +74,7 @@ extern "C" int mx_trace_static(mx_context *c, const mx_photons *ph, uint32_t sta
   w.q2 = (MxRec *) ((char *) scratch + qbytes);
   w.counts = (unsigned int *) ((char *) scratch + 2 * qbytes);
   e = launch_wavefront(c->T, io, w, c->num_sms * c->wave_blocks, (int) c->shared_bytes, (cudaStream_t) stream);
-  c->launches += MX_WAVE_KERNELS;
+  c->launches += wave_kernels(c->T, stages);
   if (e == cudaSuccess && (stages & MX_STAGE_DETECT) && (c->T.acis_fef || c->T.acis_qe)) {
     e = launch_acis_fef(c->T, io, c->num_sms * 8, (cudaStream_t) stream);
     c->launches++;
