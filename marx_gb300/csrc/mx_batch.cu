@@ -43,6 +43,7 @@ struct BatchIO {
   MxRec *q1, *q2;
   unsigned int *ctr;            // [0] q1 entries [1] q2 entries [2..4] work counters of phases A, B, C
                                 // [5] q1 entries of phase B (q1 reused) [6] work counter of phase T
+                                // [7] q2 entries of phase C (q2 reused) [8] work counter of phase D
   const uint64_t *seed;         // device scalar, written before each graph launch
   const double *spec;           // FILE spectra of the sources (energies then cumulative flux, per source)
 };
@@ -176,8 +177,27 @@ __device__ __forceinline__ int source_of(uint32_t i, const uint32_t *start, int 
   return lo;
 }
 
-// The whole batch in one persistent cooperative launch.  The four phases
-// of the wavefront trace are separated by grid-wide barriers; inside a
+// The end of a photon in phases C and D: the source's detector (when the
+// photon is still good), then the output columns.
+__device__ __forceinline__ void batch_finish(const MxTables &T, const MxChipDev *ch, const MxSourceDev &S,
+                                             const TraceIO &io, uint32_t i, Ph &q, Rng &r) {
+  const int unset = 0x7fff;
+  if (!r.overrun && S.nchips && !(q.flags & MX_BAD_PHOTON_MASK)) detect_stage(T, ch + S.chip_off, S.nchips, q, r);
+  store_core(io, i, q, r.overrun);
+  store_extra(io, i, q);
+  if (q.order != unset && io.order) io.order[i] = (int8_t) q.order;
+  if (q.ccd != unset) {
+    if (io.ccd) io.ccd[i] = (int8_t) q.ccd;
+    if (q.ccd >= 0) {
+      if (io.ypix) io.ypix[i] = q.ypix;
+      if (io.zpix) io.zpix[i] = q.zpix;
+    }
+  }
+}
+
+// The whole batch in one persistent cooperative launch.  The five phases
+// of the wavefront trace (A, T, B, C and the gratings' D) are separated by
+// grid-wide barriers; inside a
 // phase warps claim tiles of work from a counter, so uneven sources and
 // uneven survivor counts spread over every SM.  Every thread reaches every
 // barrier: the claim loops end for a whole warp at once and nothing
@@ -289,33 +309,65 @@ __global__ void __launch_bounds__(256) mx_batch_kernel(MxTables T, BatchIO b) {
   }
   grid.sync();
 
-  // Phase C: hyperboloid reflection, the source's grating and detector.
+  // Phase C: hyperboloid reflection, the source's grating up to its order
+  // choice; the photons given an order go on to phase D (q2 is free again),
+  // the others run the detector (without a grating) and are stored.
   const uint32_t nc = __ldcg(&b.ctr[5]);
   for (;;) {
     const uint32_t base = claim(&b.ctr[4], b.tile);
     if (base >= nc) break;
     const uint32_t end = min(base + (uint32_t) b.tile, nc);
-    for (uint32_t k = base + lane; k < end; k += 32) {
-      const MxRec rec = b.q1[k];
-      const MxSourceDev &S = ssrc[source_of(rec.i, sstart, b.nsrc)];
-      const uint32_t i = rec.i;
-      Ph q; MirrorState m; Rng r;
-      from_rec(rec, q, m, r, io);
-      const int unset = 0x7fff;
-      q.order = unset; q.ccd = unset;
-      mirror_back(T, sh, q, r, m);
-      if (!r.overrun && S.grating && !(q.flags & MX_BAD_PHOTON_MASK)) grating_stage(T, gr, S.grating, q, r);
-      if (!r.overrun && S.nchips && !(q.flags & MX_BAD_PHOTON_MASK)) detect_stage(T, ch + S.chip_off, S.nchips, q, r);
-      store_core(io, i, q, r.overrun);
-      store_extra(io, i, q);
-      if (q.order != unset && io.order) io.order[i] = (int8_t) q.order;
-      if (q.ccd != unset) {
-        if (io.ccd) io.ccd[i] = (int8_t) q.ccd;
-        if (q.ccd >= 0) {
-          if (io.ypix) io.ypix[i] = q.ypix;
-          if (io.zpix) io.zpix[i] = q.zpix;
+    for (uint32_t j = base; j < end; j += 32) {
+      const uint32_t k = j + lane;
+      bool to_d = false;
+      MxRec rec;
+      if (k < end) {
+        rec = b.q1[k];
+        const MxSourceDev &S = ssrc[source_of(rec.i, sstart, b.nsrc)];
+        const uint32_t i = rec.i;
+        Ph q; MirrorState m; Rng r;
+        from_rec(rec, q, m, r, io);
+        const int unset = 0x7fff;
+        q.order = unset; q.ccd = unset;
+        mirror_back(T, sh, q, r, m);
+        if (!r.overrun && S.grating && !(q.flags & MX_BAD_PHOTON_MASK)) {
+          D3 gx, gp;
+          const int chosen = grating_front(T, gr, S.grating, q, r, gx, gp);
+          if (chosen >= 0) {
+            to_d = true;
+            to_rec_d(rec, gx, gp, q, r, i, chosen);
+          }
         }
+        if (!to_d) batch_finish(T, ch, S, io, i, q, r);
       }
+      append(to_d, rec, b.q2, &b.ctr[7]);
+    }
+  }
+  grid.sync();
+
+  // Phase D: the diffraction into the chosen order, the detector, the
+  // output columns.
+  const uint32_t nd = __ldcg(&b.ctr[7]);
+  for (;;) {
+    const uint32_t base = claim(&b.ctr[8], b.tile);
+    if (base >= nd) break;
+    const uint32_t end = min(base + (uint32_t) b.tile, nd);
+    for (uint32_t k = base + lane; k < end; k += 32) {
+      const MxRec rec = b.q2[k];
+      const uint32_t i = rec.i;
+      const MxSourceDev &S = ssrc[source_of(i, sstart, b.nsrc)];
+      Ph q;
+      q.e = rec.e; q.t = rec.t; q.flags = rec.flags; q.shell = rec.shell; q.set = 0;
+      q.ccd = 0x7fff;
+      Rng r;
+      r.U = nullptr; r.N = nullptr; r.seed = seed; r.n = io.n; r.i = i; r.tag = rec.tag;
+      if (S.grating == MX_GRATING_LETG) r.window(MX_U_LETG, 6, MX_N_LETG, 10);
+      else r.window(MX_U_GRATING, 2, MX_N_GRATING, 2);
+      r.upos = rec.upos; r.npos = rec.npos; r.overrun = rec.overrun != 0;
+      const int chosen = (int) rec.pdn;
+      q.order = chosen - gr[(S.grating == MX_GRATING_LETG ? 4 : 0) + q.shell].max_order;
+      grating_back(T, gr, S.grating, q, r, mk(rec.x[0], rec.x[1], rec.x[2]), mk(rec.p[0], rec.p[1], rec.p[2]), chosen);
+      batch_finish(T, ch, S, io, i, q, r);
     }
   }
 }
@@ -332,7 +384,7 @@ struct mx_batch {
   DevBuf d_src;                 // sources then starts
   DevBuf cols[12];              // photon list columns
   DevBuf queues;                // two record queues
-  DevBuf ctr;                   // 7 counters + seed
+  DevBuf ctr;                   // 9 counters, the seed at byte 64
   uint64_t *h_seed = nullptr;   // pinned, copied into the graph's seed slot
   mx_batch_params params;
   bool have_params = false;
@@ -403,7 +455,7 @@ static int build_graph(mx_batch *b) {
   cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
   if (e != cudaSuccess) return mx_cuda_fail(c, e, "batch capture stream");
   e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
-  if (e == cudaSuccess) e = cudaMemsetAsync(b->ctr.ptr, 0, 7 * sizeof(unsigned int), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->ctr.ptr, 0, 9 * sizeof(unsigned int), st);
   if (e == cudaSuccess) e = cudaMemcpyAsync((char *) b->ctr.ptr + 64, b->h_seed, sizeof(uint64_t), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
     cudaLaunchConfig_t lc;

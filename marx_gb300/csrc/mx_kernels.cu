@@ -305,19 +305,6 @@ __device__ __forceinline__ void finish_photon(const MxTables &T, const MxChipDev
   }
 }
 
-// The photons a grating diffracts, between phases C and D: at the Rowland
-// torus in the grating's frame (x, p), with the chosen order index in the
-// record's pdn field (n, corr, beta and delta are unused here).
-__device__ __forceinline__ void to_rec_d(MxRec &r, D3 x, D3 p, const Ph &q, const Rng &rng, uint32_t i, int chosen) {
-  r.x[0] = x.x; r.x[1] = x.y; r.x[2] = x.z;
-  r.p[0] = p.x; r.p[1] = p.y; r.p[2] = p.z;
-  r.e = q.e; r.t = q.t;
-  r.i = i; r.tag = rng.tag; r.flags = q.flags;
-  r.shell = (uint8_t) q.shell; r.upos = (uint8_t) rng.upos; r.npos = (uint8_t) rng.npos;
-  r.overrun = rng.overrun ? 1 : 0;
-  r.pdn = (double) chosen;
-}
-
 __device__ __forceinline__ void load_supports(const MxTables &T, const TraceIO &io, uint32_t i, Ph &q) {
   if (T.grating == MX_GRATING_LETG)   // supports skipped by this photon keep their values
     for (int s = 0; s < 4; s++) q.sup[s] = io.support ? io.support[s * (size_t) io.stride + i] : 0;
