@@ -193,9 +193,11 @@ cudaError_t launch_acis_fef(const MxTables &T, const TraceIO &io, int grid, cuda
 // normal blur and reflectivity test and moves the photons it reflects to
 // queue 2; phase B finishes that reflection, intersects the hyperboloid and
 // applies its reflectivity test, appending survivors to queue 1 again;
-// phase C finishes the hyperboloid reflection and runs the grating and the
-// detector.  Appends are warp-aggregated (one atomic per warp); the order
-// of records in a queue does not affect any photon's result.
+// phase C finishes the hyperboloid reflection and runs the detector, or,
+// with a grating, the grating up to its order choice, appending the photons
+// given an order to queue 2 for phase D (diffraction and detector).
+// Appends are warp-aggregated (one atomic per warp); the order of records
+// in a queue does not affect any photon's result.
 
 __global__ void __launch_bounds__(MX_WAVE_BLOCK, MX_WAVE_MIN_BLOCKS) mx_wave_a(MxTables T, TraceIO io, WaveBufs w) {
   MxShellDev *sh; MxGratingDev *gr; MxChipDev *ch; float *optc; double *slope;
