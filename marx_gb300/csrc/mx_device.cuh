@@ -807,7 +807,7 @@ MXD int conic_intersection(const MxShellDev &h, int o, D3 &x0, D3 p, D3 &normal)
   else if (okm) t = t_minus;
   else return -1;
   x0 = mk(p.x * t, x_y + p.y * t, x_z + p.z * t);
-  normal = normalized(mk((a - 1) * x0.x + 0.5 * b, -x0.y, -x0.z));
+  normal = normalized(mk(fma(h.am1[o], x0.x, h.hb[o]), -x0.y, -x0.z));   // ((a - 1) x + b/2, -y, -z)
   return 0;
 }
 
@@ -1017,7 +1017,7 @@ MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *
   rng.window(MX_U_MIRROR, 12, MX_N_MIRROR, 2);
   if (!T.ideal) {
     // a uniform in [0, 1) never exceeds a vignetting factor of 1
-    if (T.hrma_vig >= 1.0) rng.skip_uniform();
+    if (dkey(T.hrma_vig) >= dkey(1.0)) rng.skip_uniform();
     else if (lt_pos(T.hrma_vig, rng.uniform())) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
     if (ph.flags & MX_BAD_PHOTON_MASK) return false;
   }
@@ -1048,7 +1048,7 @@ MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *
   double st, ct;
   sincospi_fast(2.0 * (theta - 1.0 / 8.0), &st, &ct);   // angle 2 pi (u - 1/8)
   x = mk(h.front_position, radius * st - h.to_osac[0][1], radius * ct - h.to_osac[0][2]);
-  if (T.source_distance > 0.0) p = normalized(x + T.source_distance * p);
+  if (dkey(T.source_distance) > 0) p = normalized(x + T.source_distance * p);
   if (T.use_struts && struts_block(T, 0, x, p)) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;
 
   // fwd (x + to_osac): (r sin - t1) + t1 is r sin to within an ulp of t1,
@@ -1596,7 +1596,7 @@ MXD void det_leave(const MxTables &T, const DetFrame &f, D3 &x, D3 &p) {
 // frame transfer lands on a random row of its column.  x, p in the
 // detector frame.
 MXD void acis_streak(const MxTables &T, const MxChipDev &d, Ph &ph, D3 &x, D3 &p, Rng &rng) {
-  if (!(T.frame_transfer > 0.0)) return;
+  if (!(dkey(T.frame_transfer) > 0)) return;
   double t = fmod_pos(T.start_time + ph.t, T.frame_time, T.inv_frame_time);
   if (t > T.exposure) {
     ph.zpix = (float) (1.0 + 1022.0 * rng.uniform());

@@ -807,6 +807,7 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
       const double *q = rdb + (4 * o + i) * 9;   // x0 y0 z0 p k rho0 az el l
       len[o] = q[8];
       h.c[o] = q[5] * q[5]; h.b[o] = -2.0 * q[4]; h.a[o] = 1.0 - q[3];
+      h.am1[o] = h.a[o] - 1.0; h.hb[o] = 0.5 * h.b[o];
       h.xmin[o] = -0.5 * q[8]; h.xmax[o] = 0.5 * q[8];
       h.to_osac[o][0] = -(-q[2]) - cap_pos;
       h.to_osac[o][1] = (-q[0]);
