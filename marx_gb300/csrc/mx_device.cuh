@@ -1037,7 +1037,7 @@ MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *
     double r0 = h.min_radius, r1 = h.max_radius;
     radius = sqrt_fast(r0 * r0 + (r1 * r1 - r0 * r0) * rng.uniform());
   } else
-    radius = h.min_radius + (h.max_radius - h.min_radius) * rng.uniform();
+    radius = h.min_radius + h.dr * rng.uniform();
   double theta;
   for (int guard = 0;; guard++) {
     theta = rng.uniform();
@@ -1208,14 +1208,18 @@ MXD void dither_stage(const MxTables &T, Ph &ph, Rng &rng) {
     fdec = T.asp_record_only ? 0.0f : s[1];
     froll = T.asp_record_only ? 0.0f : s[2];
   } else {
-    double t = (2.0 * PI) * (T.start_time + ph.t);
+    // (a zero start time or phase is added exactly: skipped)
+    double t = (2.0 * PI) * (is_zero(T.start_time) ? ph.t : T.start_time + ph.t);
     // amp * sin(2 pi t / period + phase) rounded to float as the reference
     // stores it; a zero amplitude makes it zero whatever the sine
     float f[2];
     for (int k = 0; k < 2; k++)
-      f[k] = T.dith_amp[k] != 0.0 ? sine_to_float(T.dith_amp[k], T.dith_amp_exp[k],
-                                                  div_by(t, T.dith_period[k], T.dith_inv_period[k]) + T.dith_phase[k])
-                                  : 0.0f;
+      f[k] = !is_zero(T.dith_amp[k])
+                 ? sine_to_float(T.dith_amp[k], T.dith_amp_exp[k],
+                                 is_zero(T.dith_phase[k]) ? div_by(t, T.dith_period[k], T.dith_inv_period[k])
+                                                          : div_by(t, T.dith_period[k], T.dith_inv_period[k]) +
+                                                                T.dith_phase[k])
+                 : 0.0f;
     fra = f[0];
     fdec = f[1];
     if (T.roll_fixed) froll = T.roll_f;

@@ -832,6 +832,7 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
     h.min_radius = radius(h.a[0], h.b[0], h.c[0], h.xmin[0]);
     h.max_radius = radius(h.a[0], h.b[0], h.c[0], h.xmax[0]);
     h.min_radius -= len[0] * tan(0.67 * PI_ / 180);
+    h.dr = h.max_radius - h.min_radius;
     h.shutter = cfg.shutters[i] & 0xF;
     unsigned nopen = (unsigned) __builtin_popcount(h.shutter);
     if (nopen) total_area += (nopen / 4.0) * (h.max_radius - h.min_radius) * (h.max_radius + h.min_radius);

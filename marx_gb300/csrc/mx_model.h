@@ -23,6 +23,7 @@ struct MxShellDev {
   int32_t corr_slope_off;                      // its interval slopes in optc_slope
   double front_fwd[3];                         // fwd[0] (front_position + to_osac[0][0], 0, 0)
   double am1[2], hb[2];                        // a - 1 and b / 2 (the conic's normal)
+  double dr;                                   // max_radius - min_radius
 };
 
 // One HETG grating (per mirror shell, diffract.c:51-77).
