@@ -47,7 +47,7 @@ METRIC = "photons/s HRMA+grating+ACIS trace"
 # DRAM bytes the four wavefront kernels move per photon of plain_scatter
 # (dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of 2e6
 # photons); the traffic of a step grows with its photon count.
-TRAFFIC_BYTES_PER_PHOTON = 558.0
+TRAFFIC_BYTES_PER_PHOTON = 557.0
 
 
 def parse():

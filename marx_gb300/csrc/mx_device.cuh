@@ -1046,7 +1046,7 @@ MXD bool mirror_front(const MxTables &T, const MxShellDev *shells, const float *
     if (h.shutter & (1u << quad)) break;
   }
   double st, ct;
-  sincospi_fast(2.0 * (theta - 1.0 / 8.0), &st, &ct);   // angle 2 pi (u - 1/8)
+  sincospi_fast(fma(theta, 2.0, -0.25), &st, &ct);   // angle 2 pi (u - 1/8)
   x = mk(h.front_position, radius * st - h.to_osac[0][1], radius * ct - h.to_osac[0][2]);
   if (dkey(T.source_distance) > 0) p = normalized(x + T.source_distance * p);
   if (T.use_struts && struts_block(T, 0, x, p)) ph.flags |= MX_PHOTON_MIRROR_VBLOCKED;

@@ -124,7 +124,7 @@ __device__ __forceinline__ bool aperture(const Aperture &ap, uint64_t seed, uint
     if (ap.shutter[si] & (1u << quad)) break;
   }
   double st, ct;
-  mx::sincospi_fast(2.0 * (theta - 1.0 / 8.0), &st, &ct);
+  mx::sincospi_fast(fma(theta, 2.0, -0.25), &st, &ct);   // angle 2 pi (u - 1/8)
   ry = radius * st;
   rz = radius * ct;
   return true;
