@@ -328,8 +328,9 @@ int mx_trace_static(mx_context *ctx, const mx_photons *ph, uint32_t stages, cons
 
 /* Same trace on HOST buffers: copies inputs to the device, traces and
  * copies results back; blocks until done.  A list of 2^19 photons or more
- * (tracing the mirror) is cut into chunks on several streams, so that the
- * copies of one chunk overlap the trace of another (pinned host memory lets
+ * (tracing the mirror) is cut into chunks: copies in on one stream, copies
+ * out on another and the traces on two more, ordered by events, so that the
+ * copies of some chunks overlap the trace of others (pinned host memory lets
  * them run asynchronously); the results are those of one pass. */
 int mx_trace_host(mx_context *ctx, const mx_photons *host, uint32_t stages,
                   const mx_variates *host_var, uint64_t seed);

@@ -226,6 +226,11 @@ void mx_destroy(mx_context *c) {
     c->pipe_wave[k].release();
     if (c->pipe[k]) cudaStreamDestroy(c->pipe[k]);
   }
+  if (c->pipe_in) cudaStreamDestroy(c->pipe_in);
+  if (c->pipe_out) cudaStreamDestroy(c->pipe_out);
+  for (auto &row : c->pipe_ev)
+    for (auto &ev : row)
+      if (ev) cudaEventDestroy(ev);
   if (c->d_overrun) cudaFree(c->d_overrun);
   if (c->d_event_bad) cudaFree(c->d_event_bad);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -369,11 +374,36 @@ static int host_columns(const mx_photons *h, HostCol cols[19]) {
   return 19;
 }
 
+// Chunk boundaries of a pipelined mx_trace_host over n >= MX_PIPE_MIN_PHOTONS
+// photons: chunk j is start[j] .. start[j + 1]; returns the number of chunks.
+// The nominal chunk is a 1/nch share (nch = n / 2^17 within 4..MX_PIPE_CHUNKS);
+// the first two chunks are a quarter and a half of it and so are the last
+// two, so that the first kernels start after a short copy in and the step
+// ends with a short copy out.  Every boundary but n is a multiple of 256.
+// With u a quarter chunk (n <= 4 nch u) the middle takes at most nch - 1
+// chunks, so there are at most nch + 3 <= MX_PIPE_MAX_CHUNKS.
+static int pipe_chunks(size_t n, size_t start[MX_PIPE_MAX_CHUNKS + 1]) {
+  const size_t nch = std::max<size_t>(4, std::min<size_t>(MX_PIPE_CHUNKS, n >> 17));
+  const size_t u = ((n + 4 * nch - 1) / (4 * nch) + 255) & ~(size_t) 255;
+  const size_t last = (n - u) & ~(size_t) 255, before = last - 2 * u;
+  const size_t r = before - 3 * u, mid = (r + 4 * u - 1) / (4 * u);
+  const size_t each = ((r + mid - 1) / mid + 255) & ~(size_t) 255;
+  int k = 0;
+  start[k++] = 0;
+  start[k++] = u;
+  for (size_t i0 = 3 * u; i0 < before; i0 += each) start[k++] = i0;
+  start[k++] = before;
+  start[k++] = last;
+  start[k] = n;
+  return k;
+}
+
 // mx_trace_host for a large list: MX_PIPE_CHUNKS chunks of consecutive
-// photons, chunk j on stream j % MX_PIPE_STREAMS with its own wavefront
-// queues, each chunk's copies in, trace and copies out queued in order on
-// its stream; the copy engines then move one chunk while the SMs trace
-// another.  Photons are independent and draw by tag, so the results equal
+// photons.  The copies in run back to back on one stream and the copies out
+// on another (the two directions of the host link at once); chunk j is
+// traced on compute stream j % MX_PIPE_STREAMS with its own wavefront
+// queues as soon as its copy is in, so the kernels of neighbouring chunks
+// fill each other's tails and no copy waits behind a trace.  Photons are independent and draw by tag, so the results equal
 // the single-pass trace's.  Multi-component columns keep the list's own
 // component stride on the device; a chunk's pre-drawn variates are packed
 // slot-major for its own length.
@@ -398,33 +428,55 @@ static int trace_host_pipelined(mx_context *c, const mx_photons *h, uint32_t sta
   if (slots && ((e = c->io[NC].ensure(n * MX_NUM_U * 8)) != cudaSuccess ||
                 (e = c->io[NC + 1].ensure(n * MX_NUM_N * 8)) != cudaSuccess))
     return cuda_fail(c, e, "allocating variate buffers");
-  // the queues are per stream; the photons' own columns were written before
-  // by whatever last used them, so wait for the context's stream first
+  if (!c->pipe_in && (e = cudaStreamCreateWithFlags(&c->pipe_in, cudaStreamNonBlocking)) != cudaSuccess)
+    return cuda_fail(c, e, "creating the copy streams");
+  if (!c->pipe_out && (e = cudaStreamCreateWithFlags(&c->pipe_out, cudaStreamNonBlocking)) != cudaSuccess)
+    return cuda_fail(c, e, "creating the copy streams");
+  for (int j = 0; j < MX_PIPE_MAX_CHUNKS && e == cudaSuccess; j++)
+    for (int q = 0; q < 2 && e == cudaSuccess; q++)
+      if (!c->pipe_ev[q][j]) e = cudaEventCreateWithFlags(&c->pipe_ev[q][j], cudaEventDisableTiming);
+  if (e != cudaSuccess) return cuda_fail(c, e, "creating the chunk events");
+  // the staging buffers and queues were last used on the context's stream
+  // or by an earlier call: every stream of this call waits for it first
   cudaEvent_t ready;
   if ((e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming)) != cudaSuccess) return cuda_fail(c, e, "event");
   cudaEventRecord(ready, c->stream);
   for (int s = 0; s < MX_PIPE_STREAMS; s++) cudaStreamWaitEvent(c->pipe[s], ready, 0);
+  cudaStreamWaitEvent(c->pipe_in, ready, 0);
+  cudaStreamWaitEvent(c->pipe_out, ready, 0);
   cudaEventDestroy(ready);
-  const size_t nch = std::max<size_t>(4, std::min<size_t>(MX_PIPE_CHUNKS, n >> 17));
-  const size_t chunk = ((n + nch - 1) / nch + 255) & ~(size_t) 255;
-  for (size_t i0 = 0, j = 0; i0 < n; i0 += chunk, j++) {
-    const size_t m = std::min(chunk, n - i0);
-    cudaStream_t st = c->pipe[j % MX_PIPE_STREAMS];
+  size_t start[MX_PIPE_MAX_CHUNKS + 1];
+  const int nch = pipe_chunks(n, start);
+  // copies in: every chunk back to back on one stream, at the link's rate,
+  // chunk j's completion marked by pipe_ev[0][j]
+  for (int j = 0; j < nch; j++) {
+    const size_t i0 = start[j], m = start[j + 1] - start[j];
     for (int k = 0; k < NC && e == cudaSuccess; k++) {
       if (!cols[k].host || !cols[k].in) continue;
       const size_t el = cols[k].elem;
       e = cudaMemcpy2DAsync(dev[k] + i0 * el, n * el, (const char *) cols[k].host + i0 * el, n * el, m * el,
-                            cols[k].comps, cudaMemcpyHostToDevice, st);
+                            cols[k].comps, cudaMemcpyHostToDevice, c->pipe_in);
     }
-    const double *dU = nullptr, *dN = nullptr;
     if (slots && e == cudaSuccess) {
       double *u = (double *) c->io[NC].ptr + i0 * MX_NUM_U, *v = (double *) c->io[NC + 1].ptr + i0 * MX_NUM_N;
-      e = cudaMemcpy2DAsync(u, m * 8, hv->U + i0, n * 8, m * 8, MX_NUM_U, cudaMemcpyHostToDevice, st);
+      e = cudaMemcpy2DAsync(u, m * 8, hv->U + i0, n * 8, m * 8, MX_NUM_U, cudaMemcpyHostToDevice, c->pipe_in);
       if (e == cudaSuccess)
-        e = cudaMemcpy2DAsync(v, m * 8, hv->N + i0, n * 8, m * 8, MX_NUM_N, cudaMemcpyHostToDevice, st);
-      dU = u; dN = v;
+        e = cudaMemcpy2DAsync(v, m * 8, hv->N + i0, n * 8, m * 8, MX_NUM_N, cudaMemcpyHostToDevice, c->pipe_in);
     }
+    if (e == cudaSuccess) e = cudaEventRecord(c->pipe_ev[0][j], c->pipe_in);
     if (e != cudaSuccess) return cuda_fail(c, e, "copying photons to the device");
+  }
+  // traces: chunk j on compute stream j % MX_PIPE_STREAMS (its own queues)
+  // once its copy is in; pipe_ev[1][j] marks it traced
+  for (int j = 0; j < nch; j++) {
+    const size_t i0 = start[j], m = start[j + 1] - start[j];
+    cudaStream_t st = c->pipe[j % MX_PIPE_STREAMS];
+    if ((e = cudaStreamWaitEvent(st, c->pipe_ev[0][j], 0)) != cudaSuccess) return cuda_fail(c, e, "trace");
+    const double *dU = nullptr, *dN = nullptr;
+    if (slots) {
+      dU = (double *) c->io[NC].ptr + i0 * MX_NUM_U;
+      dN = (double *) c->io[NC + 1].ptr + i0 * MX_NUM_N;
+    }
     mx_photons d;
     memset(&d, 0, sizeof(d));
     d.n = (uint32_t) m;
@@ -439,15 +491,23 @@ static int trace_host_pipelined(mx_context *c, const mx_photons *h, uint32_t sta
     d.det_dither = (float *) at(18);
     int r = mx_trace_queues(c, c->T, &d, stages, dU, dN, seed, st, true, c->pipe_wave[j % MX_PIPE_STREAMS], true);
     if (r) return r;
+    if ((e = cudaEventRecord(c->pipe_ev[1][j], st)) != cudaSuccess) return cuda_fail(c, e, "trace");
+  }
+  // copies out: in chunk order on one stream, each after its chunk's trace
+  for (int j = 0; j < nch; j++) {
+    const size_t i0 = start[j], m = start[j + 1] - start[j];
+    e = cudaStreamWaitEvent(c->pipe_out, c->pipe_ev[1][j], 0);
     for (int k = 0; k < NC && e == cudaSuccess; k++) {
       if (!cols[k].host || !cols[k].out) continue;
       const size_t el = cols[k].elem;
       e = cudaMemcpy2DAsync((char *) cols[k].host + i0 * el, n * el, dev[k] + i0 * el, n * el, m * el,
-                            cols[k].comps, cudaMemcpyDeviceToHost, st);
+                            cols[k].comps, cudaMemcpyDeviceToHost, c->pipe_out);
     }
     if (e != cudaSuccess) return cuda_fail(c, e, "copying photons to the host");
   }
   for (int s = 0; s < MX_PIPE_STREAMS && e == cudaSuccess; s++) e = cudaStreamSynchronize(c->pipe[s]);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->pipe_in);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->pipe_out);
   if (e != cudaSuccess) return cuda_fail(c, e, "trace");
   return MX_OK;
 }

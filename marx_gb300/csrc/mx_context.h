@@ -23,8 +23,9 @@ struct DevBuf {
   void release() { if (ptr) cudaFree(ptr); ptr = nullptr; bytes = 0; }
 };
 
-#define MX_PIPE_STREAMS 6
-#define MX_PIPE_CHUNKS 16           // at most; about 2^17 photons per chunk, at least 4 chunks
+#define MX_PIPE_STREAMS 2
+#define MX_PIPE_CHUNKS 16           // nominal chunks: about 2^17 photons each, 4 to 16
+#define MX_PIPE_MAX_CHUNKS (MX_PIPE_CHUNKS + 4)   // with the shorter chunks at both ends
 #define MX_PIPE_MIN_PHOTONS (1u << 19)
 
 struct mx_context {
@@ -52,10 +53,13 @@ struct mx_context {
   alignas(16) char ev_geom[2048];   // the launch copy of the facet geometry
   DevBuf ev_tab, ev_scan, ev_io;
   unsigned long long *d_event_bad = nullptr;
-  // mx_trace_host on large lists: chunks on MX_PIPE_STREAMS streams so that
-  // copies in, kernels and copies out of different chunks overlap
+  // mx_trace_host on large lists: chunks traced on MX_PIPE_STREAMS streams,
+  // copied in on pipe_in and out on pipe_out; pipe_ev[0][j] marks chunk j
+  // copied in, pipe_ev[1][j] traced
   cudaStream_t pipe[MX_PIPE_STREAMS] = {};
   DevBuf pipe_wave[MX_PIPE_STREAMS];
+  cudaStream_t pipe_in = nullptr, pipe_out = nullptr;
+  cudaEvent_t pipe_ev[2][MX_PIPE_MAX_CHUNKS] = {};
   // DitherModel FILE: the converted aspect solution (mx_set_aspect_solution)
   DevBuf asp;
   uint32_t asp_n = 0;
