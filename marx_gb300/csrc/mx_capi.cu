@@ -447,9 +447,8 @@ static int trace_host_pipelined(mx_context *c, const mx_photons *h, uint32_t sta
   cudaEventDestroy(ready);
   size_t start[MX_PIPE_MAX_CHUNKS + 1];
   const int nch = pipe_chunks(n, start);
-  // copies in: every chunk back to back on one stream, at the link's rate,
-  // chunk j's completion marked by pipe_ev[0][j]
-  for (int j = 0; j < nch; j++) {
+  // chunk j's copies in on pipe_in, marked done by pipe_ev[0][j]
+  auto copy_in = [&](int j) -> int {
     const size_t i0 = start[j], m = start[j + 1] - start[j];
     for (int k = 0; k < NC && e == cudaSuccess; k++) {
       if (!cols[k].host || !cols[k].in) continue;
@@ -464,11 +463,11 @@ static int trace_host_pipelined(mx_context *c, const mx_photons *h, uint32_t sta
         e = cudaMemcpy2DAsync(v, m * 8, hv->N + i0, n * 8, m * 8, MX_NUM_N, cudaMemcpyHostToDevice, c->pipe_in);
     }
     if (e == cudaSuccess) e = cudaEventRecord(c->pipe_ev[0][j], c->pipe_in);
-    if (e != cudaSuccess) return cuda_fail(c, e, "copying photons to the device");
-  }
-  // traces: chunk j on compute stream j % MX_PIPE_STREAMS (its own queues)
-  // once its copy is in; pipe_ev[1][j] marks it traced
-  for (int j = 0; j < nch; j++) {
+    return e == cudaSuccess ? MX_OK : cuda_fail(c, e, "copying photons to the device");
+  };
+  // chunk j traced on compute stream j % MX_PIPE_STREAMS (with its own
+  // queues) once its copy is in, marked done by pipe_ev[1][j]
+  auto trace = [&](int j) -> int {
     const size_t i0 = start[j], m = start[j + 1] - start[j];
     cudaStream_t st = c->pipe[j % MX_PIPE_STREAMS];
     if ((e = cudaStreamWaitEvent(st, c->pipe_ev[0][j], 0)) != cudaSuccess) return cuda_fail(c, e, "trace");
@@ -492,9 +491,10 @@ static int trace_host_pipelined(mx_context *c, const mx_photons *h, uint32_t sta
     int r = mx_trace_queues(c, c->T, &d, stages, dU, dN, seed, st, true, c->pipe_wave[j % MX_PIPE_STREAMS], true);
     if (r) return r;
     if ((e = cudaEventRecord(c->pipe_ev[1][j], st)) != cudaSuccess) return cuda_fail(c, e, "trace");
-  }
-  // copies out: in chunk order on one stream, each after its chunk's trace
-  for (int j = 0; j < nch; j++) {
+    return MX_OK;
+  };
+  // chunk j's copies out on pipe_out (in chunk order) after its trace
+  auto copy_out = [&](int j) -> int {
     const size_t i0 = start[j], m = start[j + 1] - start[j];
     e = cudaStreamWaitEvent(c->pipe_out, c->pipe_ev[1][j], 0);
     for (int k = 0; k < NC && e == cudaSuccess; k++) {
@@ -503,7 +503,15 @@ static int trace_host_pipelined(mx_context *c, const mx_photons *h, uint32_t sta
       e = cudaMemcpy2DAsync((char *) cols[k].host + i0 * el, n * el, dev[k] + i0 * el, n * el, m * el,
                             cols[k].comps, cudaMemcpyDeviceToHost, c->pipe_out);
     }
-    if (e != cudaSuccess) return cuda_fail(c, e, "copying photons to the host");
+    return e == cudaSuccess ? MX_OK : cuda_fail(c, e, "copying photons to the host");
+  };
+  // issued chunk by chunk, so that the first kernels are queued as soon as
+  // their copies are (the streams and events order the work, not the calls)
+  for (int j = 0; j < nch; j++) {
+    int r = copy_in(j);
+    if (!r) r = trace(j);
+    if (!r) r = copy_out(j);
+    if (r) return r;
   }
   for (int s = 0; s < MX_PIPE_STREAMS && e == cudaSuccess; s++) e = cudaStreamSynchronize(c->pipe[s]);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->pipe_in);
