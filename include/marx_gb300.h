@@ -186,7 +186,8 @@ typedef struct mx_photons {
   double   *p;             /* 3n, unit direction (input and output) */
   double   *arrival_time;  /* s, relative to start_time */
   uint32_t *flags;         /* MX_PHOTON_* */
-  uint32_t *tag;           /* per-photon generator counter (Philox mode) */
+  uint32_t *tag;           /* per-photon generator counter (Philox mode); NULL: photon i
+                              draws with counter i (its index in the list) */
   int8_t   *mirror_shell;  /* 0..3 */
   int8_t   *order;         /* grating order */
   int8_t   *ccd_num;       /* chip id, -1 if missed */
@@ -279,7 +280,11 @@ const char *mx_last_error(const mx_context *ctx);  /* ctx may be NULL */
  * pointers).  Stages run back to back per photon inside one fused kernel;
  * a photon whose flags carry a MX_BAD_PHOTON_MASK bit is left untouched, as
  * marx_prune_photons leaves it out of sorted_index.  Asynchronous on
- * stream (a cudaStream_t, NULL = default stream). */
+ * stream (a cudaStream_t, NULL = default stream): a list of 2^18 photons or
+ * more traced with Philox draws by the wavefront kernels runs as two halves
+ * at once on two streams of the context, forked from stream and joined back
+ * into it, so that work queued on stream after the call starts after the
+ * whole trace. */
 int mx_trace(mx_context *ctx, const mx_photons *ph, uint32_t stages,
              const mx_variates *var, uint64_t seed, void *stream);
 

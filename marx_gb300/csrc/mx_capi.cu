@@ -231,6 +231,8 @@ void mx_destroy(mx_context *c) {
   for (auto &row : c->pipe_ev)
     for (auto &ev : row)
       if (ev) cudaEventDestroy(ev);
+  for (auto &ev : c->split_ev)
+    if (ev) cudaEventDestroy(ev);
   if (c->d_overrun) cudaFree(c->d_overrun);
   if (c->d_event_bad) cudaFree(c->d_event_bad);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -285,9 +287,61 @@ int mx_set_trace_mode(mx_context *c, int mode) {
   return MX_OK;
 }
 
+// Photons i0 .. i0 + m of a list, in place (the 3-vector columns keep the
+// list's component stride).
+static mx_photons slice_photons(const mx_photons *ph, size_t i0, size_t m) {
+  mx_photons d = *ph;
+  d.n = (uint32_t) m;
+  d.stride = ph->stride ? ph->stride : ph->n;
+  auto at = [&](auto *&col) {
+    if (col) col += i0;
+  };
+  at(d.energy); at(d.x); at(d.p); at(d.arrival_time); at(d.flags); at(d.tag); at(d.mirror_shell); at(d.order);
+  at(d.ccd_num); at(d.reserved8); at(d.y_pixel); at(d.z_pixel); at(d.dither_state); at(d.support_orders);
+  at(d.pulse_height); at(d.u_pixel); at(d.v_pixel); at(d.detector_region); at(d.pi); at(d.det_dither);
+  return d;
+}
+
+static int pipe_streams(mx_context *c) {
+  cudaError_t e = cudaSuccess;
+  for (int s = 0; s < MX_PIPE_STREAMS && e == cudaSuccess; s++)
+    if (!c->pipe[s]) e = cudaStreamCreateWithFlags(&c->pipe[s], cudaStreamNonBlocking);
+  for (int q = 0; q < 1 + MX_PIPE_STREAMS && e == cudaSuccess; q++)
+    if (!c->split_ev[q]) e = cudaEventCreateWithFlags(&c->split_ev[q], cudaEventDisableTiming);
+  return e == cudaSuccess ? MX_OK : cuda_fail(c, e, "creating the trace streams");
+}
+
+// A device trace that takes the wavefront kernels with Philox draws, from
+// MX_SPLIT_MIN_PHOTONS photons, runs as MX_PIPE_STREAMS consecutive parts
+// traced at once on the context's pipeline streams (each with its own
+// queues), forked from and joined back into the caller's stream: the launch,
+// ramp and tail of one part's kernels overlap the other's work.  Photons
+// are independent and draw by tag (a part without a tag column counts from
+// its first photon's index), so the results equal the one-pass trace's.
 int mx_trace_tables(mx_context *c, const MxTables &T, const mx_photons *ph, uint32_t stages, const double *U,
                     const double *N, uint64_t seed, cudaStream_t st, bool fresh) {
-  return mx_trace_queues(c, T, ph, stages, U, N, seed, st, fresh, c->wave);
+  const bool wave = ph && (stages & MX_STAGE_MIRROR) &&
+                    (c->mode == MX_MODE_WAVEFRONT || (c->mode == MX_MODE_AUTO && ph->n >= MX_WAVEFRONT_MIN_PHOTONS));
+  if (!wave || U || N || ph->n < MX_SPLIT_MIN_PHOTONS)
+    return mx_trace_queues(c, T, ph, stages, U, N, seed, st, fresh, c->wave);
+  TraceIO io;   // the argument checks, before anything is queued
+  int r = mx_trace_io(c, T, ph, stages, U, N, seed, fresh, io, "mx_trace");
+  if (r) return r;
+  if ((r = pipe_streams(c))) return r;
+  cudaError_t e = cudaEventRecord(c->split_ev[0], st);
+  const size_t n = ph->n, part = ((n + MX_PIPE_STREAMS - 1) / MX_PIPE_STREAMS + 255) & ~(size_t) 255;
+  for (int s = 0; s < MX_PIPE_STREAMS && e == cudaSuccess; s++) {
+    const size_t i0 = std::min(n, s * part), m = std::min(part, n - i0);
+    if ((e = cudaStreamWaitEvent(c->pipe[s], c->split_ev[0], 0)) != cudaSuccess) break;
+    if (m) {
+      const mx_photons d = slice_photons(ph, i0, m);
+      if ((r = mx_trace_queues(c, T, &d, stages, U, N, seed, c->pipe[s], fresh, c->pipe_wave[s], true, (uint32_t) i0)))
+        return r;
+    }
+    if ((e = cudaEventRecord(c->split_ev[1 + s], c->pipe[s])) == cudaSuccess)
+      e = cudaStreamWaitEvent(st, c->split_ev[1 + s], 0);
+  }
+  return e == cudaSuccess ? MX_OK : cuda_fail(c, e, "trace");
 }
 
 }  // extern "C"
@@ -317,12 +371,14 @@ int mx_trace_io(mx_context *c, const MxTables &T, const mx_photons *ph, uint32_t
 }
 
 int mx_trace_queues(mx_context *c, const MxTables &T, const mx_photons *ph, uint32_t stages, const double *U,
-                    const double *N, uint64_t seed, cudaStream_t st, bool fresh, DevBuf &queues, bool force_wave) {
+                    const double *N, uint64_t seed, cudaStream_t st, bool fresh, DevBuf &queues, bool force_wave,
+                    uint32_t tag0) {
   if (!ph) return fail(c, MX_EINVAL, "mx_trace: null photon list");
   if (ph->n == 0) return MX_OK;
   TraceIO io;
   int r = mx_trace_io(c, T, ph, stages, U, N, seed, fresh, io, "mx_trace");
   if (r) return r;
+  io.tag0 = tag0;
   int slots = U != nullptr;
   bool wave = (stages & MX_STAGE_MIRROR) &&
               (c->mode == MX_MODE_WAVEFRONT || (c->mode == MX_MODE_AUTO && (force_wave || ph->n >= MX_WAVEFRONT_MIN_PHOTONS)));
@@ -412,10 +468,8 @@ static int trace_host_pipelined(mx_context *c, const mx_photons *h, uint32_t sta
   const size_t n = h->n;
   HostCol cols[19];
   const int NC = host_columns(h, cols);
+  if (int r = pipe_streams(c)) return r;
   cudaError_t e = cudaSuccess;
-  for (int s = 0; s < MX_PIPE_STREAMS && e == cudaSuccess; s++)
-    if (!c->pipe[s]) e = cudaStreamCreateWithFlags(&c->pipe[s], cudaStreamNonBlocking);
-  if (e != cudaSuccess) return cuda_fail(c, e, "creating the copy-overlap streams");
   char *dev[19];
   for (int k = 0; k < NC; k++) {
     dev[k] = nullptr;
@@ -488,7 +542,8 @@ static int trace_host_pipelined(mx_context *c, const mx_photons *h, uint32_t sta
     d.support_orders = (int8_t *) at(12); d.pulse_height = (int16_t *) at(13); d.u_pixel = (float *) at(14);
     d.v_pixel = (float *) at(15); d.detector_region = (uint8_t *) at(16); d.pi = (float *) at(17);
     d.det_dither = (float *) at(18);
-    int r = mx_trace_queues(c, c->T, &d, stages, dU, dN, seed, st, true, c->pipe_wave[j % MX_PIPE_STREAMS], true);
+    int r = mx_trace_queues(c, c->T, &d, stages, dU, dN, seed, st, true, c->pipe_wave[j % MX_PIPE_STREAMS], true,
+                            (uint32_t) i0);
     if (r) return r;
     if ((e = cudaEventRecord(c->pipe_ev[1][j], st)) != cudaSuccess) return cuda_fail(c, e, "trace");
     return MX_OK;

@@ -27,6 +27,7 @@ struct DevBuf {
 #define MX_PIPE_CHUNKS 16           // nominal chunks: about 2^17 photons each, 4 to 16
 #define MX_PIPE_MAX_CHUNKS (MX_PIPE_CHUNKS + 4)   // with the shorter chunks at both ends
 #define MX_PIPE_MIN_PHOTONS (1u << 19)
+#define MX_SPLIT_MIN_PHOTONS (1u << 18)   // a device trace from here runs in MX_PIPE_STREAMS parts at once
 
 struct mx_context {
   int device = 0;
@@ -60,6 +61,9 @@ struct mx_context {
   DevBuf pipe_wave[MX_PIPE_STREAMS];
   cudaStream_t pipe_in = nullptr, pipe_out = nullptr;
   cudaEvent_t pipe_ev[2][MX_PIPE_MAX_CHUNKS] = {};
+  // a device trace cut in parts on the pipe streams: the fork from the
+  // caller's stream, then each part's end
+  cudaEvent_t split_ev[1 + MX_PIPE_STREAMS] = {};
   // DitherModel FILE: the converted aspect solution (mx_set_aspect_solution)
   DevBuf asp;
   uint32_t asp_n = 0;
@@ -80,11 +84,14 @@ extern "C" __attribute__((visibility("hidden"))) int mx_trace_tables(mx_context 
                                const double *U, const double *N, uint64_t seed, cudaStream_t st, bool fresh);
 // The same with the wavefront queues in `queues` instead of the context's
 // own; force_wave: the wavefront kernels whatever the list's length (the
-// chunks of a list that one pass would trace with them).
+// chunks of a list that one pass would trace with them); tag0: the
+// generator counter of the list's photon 0 when it has no tag column (a
+// chunk starting at photon i0 of a longer list passes i0, so that photon i
+// draws as photon i0 + i of the whole list).
 __attribute__((visibility("hidden"))) int mx_trace_queues(mx_context *c, const MxTables &T, const mx_photons *ph,
                                                           uint32_t stages, const double *U, const double *N,
                                                           uint64_t seed, cudaStream_t st, bool fresh, DevBuf &queues,
-                                                          bool force_wave = false);
+                                                          bool force_wave = false, uint32_t tag0 = 0);
 
 // The checks every trace entry point makes on its arguments, and the kernel
 // view of the photon list built from them (who: the entry point's name for

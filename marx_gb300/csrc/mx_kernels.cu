@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(MX_TRACE_BLOCK) mx_trace_kernel(MxTables T, Tr
     }
     Rng r;
     r.U = io.U; r.N = io.N; r.seed = io.seed; r.n = io.n; r.i = i;
-    r.tag = io.tag ? io.tag[i] : i;
+    r.tag = io.tag ? io.tag[i] : io.tag0 + i;
     r.upos = r.uend = r.npos = r.nend = 0;
     r.overrun = false;
     trace_photon(T, sh, optc, slope, gr, ch, io.stages, q, r);
@@ -109,7 +109,7 @@ __device__ void acis_response(const MxTables &T, const TraceIO &io, uint32_t i, 
   q.zpix = io.zpix[i];
   Rng r;
   r.U = io.U; r.N = io.N; r.seed = seed; r.n = io.n; r.i = i;
-  r.tag = io.tag ? io.tag[i] : i;
+  r.tag = io.tag ? io.tag[i] : io.tag0 + i;
   r.overrun = false;
   r.window(MX_U_DETECT, 2, MX_N_DETECT, 2);
   if (T.acis_qe && !acis_qe_accept(T, ccd, q, r)) {
@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(MX_WAVE_BLOCK, MX_WAVE_MIN_BLOCKS) mx_wave_a(M
       }
       Rng r;
       r.U = io.U; r.N = io.N; r.seed = io.seed; r.n = io.n; r.i = i;
-      r.tag = io.tag ? io.tag[i] : i;
+      r.tag = io.tag ? io.tag[i] : io.tag0 + i;
       r.upos = r.uend = r.npos = r.nend = 0;
       r.overrun = false;
       if ((io.stages & MX_STAGE_DITHER) && T.dither) dither_stage(T, q, r);

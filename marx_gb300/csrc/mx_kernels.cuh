@@ -28,7 +28,7 @@ struct TraceIO {
   const double *U, *N;          // pre-drawn variates (slot-major) or null
   uint32_t n, stages;
   uint32_t stride;              // component stride of x, p and dither_state (>= n)
-  uint32_t pad_stride;
+  uint32_t tag0;                // generator counter of photon 0 when tag is null (photon i: tag0 + i)
   uint64_t seed;
   int32_t fresh;                // 1: output columns start from their defaults instead of being read
   unsigned long long *overrun;  // count of photons that ran out of variate slots

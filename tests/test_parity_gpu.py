@@ -175,8 +175,8 @@ def test_launch_count_tracks_kernels(cuda):
 
 @pytest.mark.parametrize("slots,n", [(False, (1 << 21) + 12345), (True, (1 << 21) + 12345), (False, (1 << 19) + 333)])
 def test_pipelined_host_entry_equals_device_trace(cuda, slots, n):
-    """mx_trace_host on a list large enough to be cut into chunks on
-    several streams (copies overlapping the trace; 16 chunks, and 4 at the
+    """mx_trace_host on a list large enough to be cut into chunks
+    (copies overlapping the traces of other chunks; 19 chunks, and 7 at the
     smallest size that is cut): every column equals the one-pass device
     trace of the same photons, with Philox draws and with pre-drawn
     variates (packed per chunk)."""
@@ -187,6 +187,56 @@ def test_pipelined_host_entry_equals_device_trace(cuda, slots, n):
     a = ph.copy()
     eng.trace_host(a, U=U, N=N, seed=5)
     b = device_trace(eng, ph, U, N, seed=5)
+    for k in ("x", "p", "flags", "mirror_shell", "order", "ccd_num", "y_pixel", "z_pixel", "dither_state"):
+        assert np.array_equal(getattr(a, k), getattr(b, k)), k
+    assert int(((a.flags & BAD_PHOTON_MASK) == 0).sum()) > n // 10
+
+
+def _take(ph, idx):
+    """The photons idx of a list (every column, tags included)."""
+    from marx_gb300.photons import COLUMNS
+    q = ph.copy()
+    for k in COLUMNS:
+        setattr(q, k, np.ascontiguousarray(getattr(ph, k)[..., idx]))
+    q.n = len(idx)
+    return q
+
+
+def test_split_device_trace_is_independent_of_the_partition(cuda):
+    """From 2^18 photons a device trace runs in two parts at once on two
+    streams.  Photons are independent and draw by tag, so the list traced
+    reversed (split at another photon) gives the reversed result, and its
+    first 2^17 photons traced alone (one pass) give the same columns."""
+    n = (1 << 19) + 4321
+    w = W.ALL["plain_scatter"]()
+    ph = w.photons(n, seed=12)
+    eng = engine(w.cfg)
+    a = device_trace(eng, ph, seed=8)
+    rev = np.arange(n)[::-1]
+    b = device_trace(eng, _take(ph, rev), seed=8)
+    head = np.arange(1 << 17)
+    c = device_trace(eng, _take(ph, head), seed=8)
+    for k in ("x", "p", "flags", "mirror_shell", "order", "ccd_num", "y_pixel", "z_pixel", "dither_state"):
+        va = getattr(a, k)
+        assert np.array_equal(va, getattr(b, k)[..., rev]), k
+        assert np.array_equal(va[..., head], getattr(c, k)), k
+    assert int(((a.flags & BAD_PHOTON_MASK) == 0).sum()) > n // 10
+
+
+def test_pipelined_host_entry_without_tags(cuda):
+    """A list without a tag column draws photon i with generator counter i
+    (its index in the list): each chunk of the pipelined host entry counts
+    from its first photon's index in the whole list, so the trace equals
+    the one-pass device trace of the same photons tagged 0 .. n - 1."""
+    n = (1 << 20) + 777
+    w = W.ALL["plain_scatter"]()
+    ph = w.photons(n, seed=10)
+    ph.tag = np.arange(n, dtype=np.uint32)
+    eng = engine(w.cfg)
+    a = ph.copy()
+    a.tag = None
+    eng.trace_host(a, seed=6)
+    b = device_trace(eng, ph, seed=6)
     for k in ("x", "p", "flags", "mirror_shell", "order", "ccd_num", "y_pixel", "z_pixel", "dither_state"):
         assert np.array_equal(getattr(a, k), getattr(b, k)), k
     assert int(((a.flags & BAD_PHOTON_MASK) == 0).sum()) > n // 10
