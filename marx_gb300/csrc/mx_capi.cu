@@ -432,14 +432,14 @@ static int host_columns(const mx_photons *h, HostCol cols[19]) {
 
 // Chunk boundaries of a pipelined mx_trace_host over n >= MX_PIPE_MIN_PHOTONS
 // photons: chunk j is start[j] .. start[j + 1]; returns the number of chunks.
-// The nominal chunk is a 1/nch share (nch = n / 2^17 within 4..MX_PIPE_CHUNKS);
+// The nominal chunk is a 1/nch share (nch = n / 2^19 within 4..MX_PIPE_CHUNKS);
 // the first two chunks are a quarter and a half of it and so are the last
 // two, so that the first kernels start after a short copy in and the step
 // ends with a short copy out.  Every boundary but n is a multiple of 256.
 // With u a quarter chunk (n <= 4 nch u) the middle takes at most nch - 1
 // chunks, so there are at most nch + 3 <= MX_PIPE_MAX_CHUNKS.
 static int pipe_chunks(size_t n, size_t start[MX_PIPE_MAX_CHUNKS + 1]) {
-  const size_t nch = std::max<size_t>(4, std::min<size_t>(MX_PIPE_CHUNKS, n >> 17));
+  const size_t nch = std::max<size_t>(4, std::min<size_t>(MX_PIPE_CHUNKS, n >> 19));
   const size_t u = ((n + 4 * nch - 1) / (4 * nch) + 255) & ~(size_t) 255;
   const size_t last = (n - u) & ~(size_t) 255, before = last - 2 * u;
   const size_t r = before - 3 * u, mid = (r + 4 * u - 1) / (4 * u);

@@ -24,7 +24,7 @@ struct DevBuf {
 };
 
 #define MX_PIPE_STREAMS 2
-#define MX_PIPE_CHUNKS 16           // nominal chunks: about 2^17 photons each, 4 to 16
+#define MX_PIPE_CHUNKS 16           // nominal chunks: about 2^19 photons each, 4 to 16
 #define MX_PIPE_MAX_CHUNKS (MX_PIPE_CHUNKS + 4)   // with the shorter chunks at both ends
 #define MX_PIPE_MIN_PHOTONS (1u << 19)
 #define MX_SPLIT_MIN_PHOTONS (1u << 18)   // a device trace from here runs in MX_PIPE_STREAMS parts at once

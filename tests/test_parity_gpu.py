@@ -176,8 +176,9 @@ def test_launch_count_tracks_kernels(cuda):
 @pytest.mark.parametrize("slots,n", [(False, (1 << 21) + 12345), (True, (1 << 21) + 12345), (False, (1 << 19) + 333)])
 def test_pipelined_host_entry_equals_device_trace(cuda, slots, n):
     """mx_trace_host on a list large enough to be cut into chunks
-    (copies overlapping the traces of other chunks; 19 chunks, and 7 at the
-    smallest size that is cut): every column equals the one-pass device
+    (copies overlapping the traces of other chunks; 7 chunks at these
+    sizes, 19 from 2^23 photons, which the 2e7-photon HETG test in
+    test_full_size_gpu.py takes): every column equals the one-pass device
     trace of the same photons, with Philox draws and with pre-drawn
     variates (packed per chunk)."""
     w = W.ALL["plain_scatter"]()
