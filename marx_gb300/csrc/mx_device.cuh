@@ -976,10 +976,8 @@ MXD bool struts_block_exact(const MxTables &T, int set, D3 x, D3 p) {
 // a coordinate within the margin of an edge, or not finite, take the
 // double-precision test.
 #define MX_STRUT_MARGIN 0.05f
-MXD bool struts_block(const MxTables &T, int set, D3 x, D3 p) {
-#ifdef __CUDA_ARCH__
-  const float xx = d2f_trunc(x.x), xy = d2f_trunc(x.y), xz = d2f_trunc(x.z);
-  const float px = d2f_trunc(p.x), py = d2f_trunc(p.y), pz = d2f_trunc(p.z);
+// The screen on float coordinates: 1 blocked, 0 clear, -1 unsure.
+MXD int struts_screen(const MxTables &T, int set, float xx, float xy, float xz, float px, float py, float pz) {
   const float inv = 1.0f / px;
   bool unsure = false;
   for (int k = 0; k < 2; k++) {
@@ -989,13 +987,49 @@ MXD bool struts_block(const MxTables &T, int set, D3 x, D3 p) {
     for (int i = 0; i < 3; i++) {
       if (i != 0) { float tmp = T.cos30f * y - T.sin30f * z; z = T.sin30f * y + T.cos30f * z; y = tmp; }
       const float dy = fabsf(y) - hw, dz = fabsf(z) - hw;
-      if (dy < -MX_STRUT_MARGIN || dz < -MX_STRUT_MARGIN) return true;
+      if (dy < -MX_STRUT_MARGIN || dz < -MX_STRUT_MARGIN) return 1;
       if (!(dy > MX_STRUT_MARGIN && dz > MX_STRUT_MARGIN)) unsure = true;
     }
   }
-  if (!unsure) return false;
+  return unsure ? -1 : 0;
+}
+MXD bool struts_block(const MxTables &T, int set, D3 x, D3 p) {
+#ifdef __CUDA_ARCH__
+  const int s = struts_screen(T, set, d2f_trunc(x.x), d2f_trunc(x.y), d2f_trunc(x.z), d2f_trunc(p.x),
+                              d2f_trunc(p.y), d2f_trunc(p.z));
+  if (s >= 0) return s == 1;
 #endif
   return struts_block_exact(T, set, x, p);
+}
+// The photon between the mirrors, from the paraboloid's frame to the MARX
+// frame (JDM3m_vector_mul by bwd[0], less to_osac[0]), where the reference
+// tests the cap struts and leaves a blocked photon.
+MXD void paraboloid_to_marx(const MxShellDev &h, D3 &x, D3 &p) {
+  p = mat_mul(h.bwd[0], p);
+  x = mat_mul(h.bwd[0], x);
+  x = x - mk(h.to_osac[0][0], h.to_osac[0][1], h.to_osac[0][2]);
+}
+// The cap struts (set 1) for a photon given in the paraboloid's frame: the
+// screen runs on its MARX-frame coordinates formed in single precision
+// (bwd[0] and to_osac[0] in float).  The frame change adds a few float
+// roundings of the 1e4 mm positions, under 4e-3 mm in all with the
+// conversions, and under 1e-4 mm at the bars for directions within a few
+// degrees of the axis: far inside MX_STRUT_MARGIN.  Near an edge the
+// double-precision coordinates decide, as in struts_block.
+MXD bool cap_struts_block(const MxTables &T, const MxShellDev &h, D3 x, D3 p) {
+#ifdef __CUDA_ARCH__
+  const float xx = d2f_trunc(x.x), xy = d2f_trunc(x.y), xz = d2f_trunc(x.z);
+  const float px = d2f_trunc(p.x), py = d2f_trunc(p.y), pz = d2f_trunc(p.z);
+  const float *m = h.bwd0f;
+  const int s = struts_screen(T, 1, fmaf(m[0], xx, fmaf(m[1], xy, m[2] * xz)) - h.osac0f[0],
+                              fmaf(m[3], xx, fmaf(m[4], xy, m[5] * xz)) - h.osac0f[1],
+                              fmaf(m[6], xx, fmaf(m[7], xy, m[8] * xz)) - h.osac0f[2],
+                              fmaf(m[0], px, fmaf(m[1], py, m[2] * pz)), fmaf(m[3], px, fmaf(m[4], py, m[5] * pz)),
+                              fmaf(m[6], px, fmaf(m[7], py, m[8] * pz)));
+  if (s >= 0) return s == 1;
+#endif
+  paraboloid_to_marx(h, x, p);
+  return struts_block_exact(T, 1, x, p);
 }
 
 // Mirror state carried between the three parts of the HRMA trace: the
@@ -1093,13 +1127,20 @@ MXD bool mirror_middle(const MxTables &T, const MxShellDev *shells, Ph &ph, Rng 
   if (0 != reflect_finish(T, h, 0, 2 * ph.shell, p, m.n, m.pdn, ph.e, rng)) {
     ph.flags |= MX_PHOTON_UNREFLECTED; ph.x = x; ph.p = p; return false;
   }
-  p = mat_mul(h.bwd[0], p);
-  x = mat_mul(h.bwd[0], x);
-  x = x - mk(h.to_osac[0][0], h.to_osac[0][1], h.to_osac[0][2]);
-  if (T.use_struts && struts_block(T, 1, x, p)) { ph.flags |= MX_PHOTON_MIRROR_VBLOCKED; ph.x = x; ph.p = p; return false; }
-  x = x + mk(h.to_osac[1][0], h.to_osac[1][1], h.to_osac[1][2]);
-  p = mat_mul(h.fwd[1], p);
-  x = mat_mul(h.fwd[1], x);
+  if (T.use_struts && cap_struts_block(T, h, x, p)) {
+    paraboloid_to_marx(h, x, p);   // a blocked photon stays in the MARX frame
+    ph.flags |= MX_PHOTON_MIRROR_VBLOCKED; ph.x = x; ph.p = p; return false;
+  }
+  // into the hyperboloid's frame: bwd[0], less to_osac[0], plus to_osac[1],
+  // fwd[1] as one matrix and offset (18 operations instead of 42; within a
+  // few ulps of the two steps), with a fixed order of multiply-adds
+  {
+    const double *M = h.mid, *c = h.mid_off;
+    p = mk(fma(M[0], p.x, fma(M[1], p.y, MX_DMUL(M[2], p.z))), fma(M[3], p.x, fma(M[4], p.y, MX_DMUL(M[5], p.z))),
+           fma(M[6], p.x, fma(M[7], p.y, MX_DMUL(M[8], p.z))));
+    x = mk(fma(M[0], x.x, fma(M[1], x.y, fma(M[2], x.z, c[0]))), fma(M[3], x.x, fma(M[4], x.y, fma(M[5], x.z, c[1]))),
+           fma(M[6], x.x, fma(M[7], x.y, fma(M[8], x.z, c[2]))));
+  }
   D3 n;
   if (-1 == conic_intersection(h, 1, x, p, n)) { ph.flags |= MX_PHOTON_UNREFLECTED; ph.x = x; ph.p = p; return false; }
   if (!reflect_test(T, h, 1, p, n, m.pdn, m.beta, m.delta, m.corr, rng)) {

@@ -825,6 +825,15 @@ bool build_model(const Pack &pk, const mx_config &cfg, HostModel &M, std::string
       rot_z(rz, az);
       mat3_mul(h.bwd[o], rz, ry);
     }
+    mat3_mul(h.mid, h.fwd[1], h.bwd[0]);
+    {
+      const double dt[3] = {h.to_osac[1][0] - h.to_osac[0][0], h.to_osac[1][1] - h.to_osac[0][1],
+                            h.to_osac[1][2] - h.to_osac[0][2]};
+      for (int r = 0; r < 3; r++)
+        h.mid_off[r] = h.fwd[1][3 * r] * dt[0] + h.fwd[1][3 * r + 1] * dt[1] + h.fwd[1][3 * r + 2] * dt[2];
+      for (int k = 0; k < 9; k++) h.bwd0f[k] = (float) h.bwd[0][k];
+      for (int r = 0; r < 3; r++) h.osac0f[r] = (float) h.to_osac[0][r];
+    }
     const double *qp = rdb + i * 9;
     h.front_position = cap_pos - qp[2] + h.xmax[0];
     for (int r = 0; r < 3; r++) h.front_fwd[r] = h.fwd[0][3 * r] * (h.front_position + h.to_osac[0][0]);

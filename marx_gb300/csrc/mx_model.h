@@ -24,6 +24,11 @@ struct MxShellDev {
   double front_fwd[3];                         // fwd[0] (front_position + to_osac[0][0], 0, 0)
   double am1[2], hb[2];                        // a - 1 and b / 2 (the conic's normal)
   double dr;                                   // max_radius - min_radius
+  // paraboloid frame -> MARX frame -> hyperboloid frame as one change:
+  // x' = mid x + mid_off, p' = mid p (mid = fwd[1] bwd[0], mid_off =
+  // fwd[1] (to_osac[1] - to_osac[0]))
+  double mid[9], mid_off[3];
+  float bwd0f[9], osac0f[3];                   // bwd[0] and to_osac[0] in float (the cap struts' screen)
 };
 
 // One HETG grating (per mirror shell, diffract.c:51-77).
