@@ -29,7 +29,13 @@ struct MxShellDev {
   // fwd[1] (to_osac[1] - to_osac[0]))
   double mid[9], mid_off[3];
   float bwd0f[9], osac0f[3];                   // bwd[0] and to_osac[0] in float (the cap struts' screen)
+  // Padding to 736 bytes (184 words): the four shells' copies in shared
+  // memory start on banks 0, 24, 16 and 8, so lanes of a warp that load
+  // one field of different shells do not conflict (at 704 bytes shells 0
+  // and 2, and 1 and 3, shared their banks).
+  double bank_pad[4];
 };
+static_assert(sizeof(MxShellDev) % 128 == 96, "shell records of 736 + 128 k bytes: four distinct bank offsets");
 
 // One HETG grating (per mirror shell, diffract.c:51-77).
 struct MxGratingDev {
@@ -112,7 +118,12 @@ struct MxChipDev {
   double inv_xpix, inv_ypix;                   // correctly rounded 1/xpix, 1/ypix
   float f_ll[3], f_xhat[3], f_yhat[3], f_normal[3], f_xlen, f_ylen;   // single-precision screen copies
   int32_t id, pad;
+  // Padding to 232 bytes (58 words): up to ten chips' copies in shared
+  // memory start on distinct even banks, so lanes of a warp on different
+  // chips do not conflict (at 224 bytes chips k and k + 4 shared banks).
+  double bank_pad;
 };
+static_assert(sizeof(MxChipDev) == 232, "chip records of 58 words: distinct bank offsets for ten chips");
 
 // Everything the kernels read, passed by value as a launch parameter.
 struct MxTables {
