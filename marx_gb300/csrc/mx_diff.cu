@@ -65,6 +65,7 @@ struct Aperture {
 
 struct FwdArgs {
   mxd::Optic<double> opt[4][2];
+  mxd::Between<double> mid[4];
   mxd::RayConst rc[4];
   Aperture ap;
   double p0[3];
@@ -74,6 +75,7 @@ struct FwdArgs {
 
 struct AdjArgs {
   mxd::Optic<Dual6> opt[4][2];
+  mxd::Between<Dual6> mid[4];
   mxd::RayConst rc[4];
   Aperture ap;
   Dual6 p0[3];
@@ -92,6 +94,25 @@ struct StrutTest {
     if (!T->use_struts) return false;
     return mx::struts_block(*T, set, mx::mk(mxd::val(x.x), mxd::val(x.y), mxd::val(x.z)),
                             mx::mk(mxd::val(p.x), mxd::val(p.y), mxd::val(p.z)));
+  }
+  // The cap struts for a ray in the paraboloid's frame: screened on its
+  // MARX-frame coordinates formed in single precision (as the trace's
+  // cap_struts_block does), decided in double near a bar edge.
+  template <class S>
+  __device__ bool cap(const mxd::Optic<S> &P, const mxd::Between<S> &B, const mxd::V3<S> &x, const mxd::V3<S> &p) const {
+    if (!T->use_struts) return false;
+    const float xx = mx::d2f_trunc(mxd::val(x.x)), xy = mx::d2f_trunc(mxd::val(x.y)), xz = mx::d2f_trunc(mxd::val(x.z));
+    const float px = mx::d2f_trunc(mxd::val(p.x)), py = mx::d2f_trunc(mxd::val(p.y)), pz = mx::d2f_trunc(mxd::val(p.z));
+    const float *m = B.bwdf;
+    const int s = mx::struts_screen(*T, 1, fmaf(m[0], xx, fmaf(m[1], xy, m[2] * xz)) - B.tof[0],
+                                    fmaf(m[3], xx, fmaf(m[4], xy, m[5] * xz)) - B.tof[1],
+                                    fmaf(m[6], xx, fmaf(m[7], xy, m[8] * xz)) - B.tof[2],
+                                    fmaf(m[0], px, fmaf(m[1], py, m[2] * pz)), fmaf(m[3], px, fmaf(m[4], py, m[5] * pz)),
+                                    fmaf(m[6], px, fmaf(m[7], py, m[8] * pz)));
+    if (s >= 0) return s == 1;
+    mxd::V3<S> pm = mxd::matv(P.bwd, p), xm = mxd::matv(P.bwd, x) - mxd::v3<S>(P.to[0], P.to[1], P.to[2]);
+    return mx::struts_block_exact(*T, 1, mx::mk(mxd::val(xm.x), mxd::val(xm.y), mxd::val(xm.z)),
+                                  mx::mk(mxd::val(pm.x), mxd::val(pm.y), mxd::val(pm.z)));
   }
 };
 
@@ -232,7 +253,8 @@ __global__ void __launch_bounds__(DBLOCK) diff_forward_kernel(const __grid_const
       int si;
       double ry, rz;
       if (aperture(A.ap, seed, (uint32_t) i, si, ry, rz))
-        hit = mxd::weighted_ray<double>(A.opt[si][0], A.opt[si][1], A.rc[si], ry, rz, p0, replay, code, struts, y, z, w);
+        hit = mxd::weighted_ray<double>(A.opt[si][0], A.opt[si][1], A.mid[si], A.rc[si], ry, rz, p0, replay, code, struts,
+                                        y, z, w);
       else
         code = 0;
       if (mode == MX_DIFF_RECORD) codes[i] = code;
@@ -386,7 +408,8 @@ __global__ void __launch_bounds__(DBLOCK) diff_adjoint_kernel(const __grid_const
         Dual6 y, z, w;
         int ic, jc;
         float fu, fv;
-        if (mxd::weighted_ray<Dual6>(A.opt[si][0], A.opt[si][1], A.rc[si], ry, rz, p0, true, code, none, y, z, w) &&
+        if (mxd::weighted_ray<Dual6>(A.opt[si][0], A.opt[si][1], A.mid[si], A.rc[si], ry, rz, p0, true, code, none, y,
+                                     z, w) &&
             w.v > 0.0 && splat_origin(g, y.v, z.v, ic, jc, fu, fv)) {
           float ky[mxd::TAPS], kyd[mxd::TAPS], kz[mxd::TAPS], kzd[mxd::TAPS];
 #pragma unroll
@@ -486,7 +509,8 @@ int diff_fail(mx_diff *d, int code, const std::string &msg) { return mx_fail(d ?
 // and el_mis (degrees in the geometry file) and decenters x0 and y0 (mm),
 // as read_hrma_geometry_file (hrma.c:319-391) and init_hrma_shells take
 // them; the rotations are rebuilt as init_yaw_pitch does.
-int build_optics(mx_diff *d, const double *theta, mxd::Optic<Dual6> opt[4][2], Dual6 p0[3]) {
+int build_optics(mx_diff *d, const double *theta, mxd::Optic<Dual6> opt[4][2], mxd::Between<Dual6> mid[4],
+                 Dual6 p0[3]) {
   mx_context *c = d->ctx;
   std::string err;
   size_t cnt = 0;
@@ -513,6 +537,13 @@ int build_optics(mx_diff *d, const double *theta, mxd::Optic<Dual6> opt[4][2], D
       mxd::yaw_pitch<Dual6>(op.fwd, op.bwd, az, el);
       for (int r = 0; r < 3; r++) op.ff[r] = op.fwd[3 * r] * (h.front_position + op.to[0]);
     }
+    const mxd::Optic<Dual6> &P = opt[s][0], &H = opt[s][1];
+    mxd::Between<Dual6> &B = mid[s];
+    mxd::mat3_mul<Dual6>(B.m, H.fwd, P.bwd);
+    const Dual6 dt[3] = {H.to[0] - P.to[0], H.to[1] - P.to[1], H.to[2] - P.to[2]};
+    for (int r = 0; r < 3; r++) B.c[r] = H.fwd[3 * r] * dt[0] + H.fwd[3 * r + 1] * dt[1] + H.fwd[3 * r + 2] * dt[2];
+    for (int k = 0; k < 9; k++) B.bwdf[k] = (float) P.bwd[k].v;
+    for (int r = 0; r < 3; r++) B.tof[r] = (float) P.to[r].v;
   }
   Dual6 ay = mxd::mkd((d->cfg.src_y + theta[16]) * ARCSEC);
   ay.d[4] = (float) ARCSEC;
@@ -533,10 +564,17 @@ int check_theta(mx_diff *d, const double *theta) {
 
 int fill_fwd(mx_diff *d, const double *theta, FwdArgs &F) {
   mxd::Optic<Dual6> opt[4][2];
+  mxd::Between<Dual6> mid[4];
   Dual6 p0[3];
-  int r = build_optics(d, theta, opt, p0);
+  int r = build_optics(d, theta, opt, mid, p0);
   if (r) return r;
   memset(&F, 0, sizeof(F));
+  for (int s = 0; s < 4; s++) {
+    for (int k = 0; k < 9; k++) F.mid[s].m[k] = mid[s].m[k].v;
+    for (int k = 0; k < 3; k++) F.mid[s].c[k] = mid[s].c[k].v;
+    for (int k = 0; k < 9; k++) F.mid[s].bwdf[k] = mid[s].bwdf[k];
+    for (int k = 0; k < 3; k++) F.mid[s].tof[k] = mid[s].tof[k];
+  }
   for (int s = 0; s < 4; s++)
     for (int o = 0; o < 2; o++) {
       const mxd::Optic<Dual6> &a = opt[s][o];
@@ -556,7 +594,7 @@ int fill_fwd(mx_diff *d, const double *theta, FwdArgs &F) {
 
 int fill_adj(mx_diff *d, const double *theta, AdjArgs &A) {
   memset(&A, 0, sizeof(A));
-  int r = build_optics(d, theta, A.opt, A.p0);
+  int r = build_optics(d, theta, A.opt, A.mid, A.p0);
   if (r) return r;
   for (int s = 0; s < 4; s++) A.rc[s] = d->rc[s];
   A.ap = d->ap;

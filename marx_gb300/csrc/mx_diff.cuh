@@ -188,6 +188,16 @@ template <class S> struct Optic {
   S ff[3];   // fwd (front + to[0], 0, 0): the aperture plane's part of fwd (x + to)
 };
 
+// A shell's way from the paraboloid's frame to the hyperboloid's: back to
+// the MARX frame (P.bwd, less P.to), then in (plus H.to, H.fwd) as one
+// matrix and offset, x' = m x + c, p' = m p, with m = H.fwd P.bwd and
+// c = H.fwd (H.to - P.to); and P.bwd, P.to in float for the cap struts'
+// screen in that frame.
+template <class S> struct Between {
+  S m[9], c[3];
+  float bwdf[9], tof[3];
+};
+
 // The rotation builders of init_yaw_pitch (hrma.c:842-880), over S.
 template <class S> MXG void rot_z(S m[9], const S &theta) {
   S c = dcos(theta), s = 0.0 - dsin(theta);
@@ -310,10 +320,13 @@ struct RayConst {
 // paraboloid P and hyperboloid H of its shell, to the focal plane.
 // replay: code holds the decisions to follow; otherwise they are made here
 // and written to code (0 when the ray is lost).  blocked(set, x, p) is the
-// strut test at the pre-collimator (0), cap (1) and post-collimator (2).
+// strut test at the pre-collimator (0) and post-collimator (2), and
+// blocked.cap(P, B, x, p) at the cap for a ray given in the paraboloid's
+// frame.  B takes the ray from the paraboloid's frame to the hyperboloid's.
 template <class S, class Struts>
-MXG bool weighted_ray(const Optic<S> &P, const Optic<S> &H, const RayConst &rc, double ry, double rz,
-                      const V3<S> &p0, bool replay, uint8_t &code, const Struts &blocked, S &y, S &z, S &w) {
+MXG bool weighted_ray(const Optic<S> &P, const Optic<S> &H, const Between<S> &B, const RayConst &rc, double ry,
+                      double rz, const V3<S> &p0, bool replay, uint8_t &code, const Struts &blocked, S &y, S &z,
+                      S &w) {
   int rootP = replay ? ((code & RAY_ROOT_P) ? 1 : 0) : -1;
   int rootH = replay ? ((code & RAY_ROOT_H) ? 1 : 0) : -1;
   if (replay && !(code & RAY_HIT)) return false;
@@ -332,13 +345,9 @@ MXG bool weighted_ray(const Optic<S> &P, const Optic<S> &H, const RayConst &rc, 
   S pdn = dotp(p, n);
   S wt = rc.weighted ? fresnel(dabs(pdn), rc.beta, rc.delta) * rc.corr : cst<S>(1.0);
   p = p - scale(2.0 * pdn, n);
-  p = matv(P.bwd, p);
-  x = matv(P.bwd, x);
-  x = x - v3<S>(P.to[0], P.to[1], P.to[2]);
-  if (!replay && blocked(1, x, p)) return false;
-  x = x + v3<S>(H.to[0], H.to[1], H.to[2]);
-  p = matv(H.fwd, p);
-  x = matv(H.fwd, x);
+  if (!replay && blocked.cap(P, B, x, p)) return false;
+  p = matv(B.m, p);
+  x = matv(B.m, x) + v3<S>(B.c[0], B.c[1], B.c[2]);
   if (!conic_hit(H, x, p, n, rootH, &ch)) return false;
   if (!replay) rootH = ch;
   pdn = dotp(p, n);
