@@ -1320,7 +1320,7 @@ MXD D3 comb3(double a, D3 l, double b, D3 d, double c, D3 n) {
 }
 // intersect + newtons_quartic (diffract.c:622-687): Rowland torus.
 MXD int rowland_intersect(D3 &x0, D3 p, double rowland) {
-  double t = -x0.x / p.x;
+  double t = -x0.x * rcp_fast(p.x);
   x0 = mk(0.0, x0.y + p.y * t, x0.z + p.z * t);
   double pxpz = p.x * p.x + p.z * p.z;
   double x2 = x0.z * x0.z + x0.y * x0.y;
@@ -1553,7 +1553,7 @@ MXD int chip_plane(const MxChipDev &g, D3 x0, D3 p, D3 &x, double &dx, double &d
   double pdn = dot(p, nrm);
   if (is_zero(pdn)) return -1;
   D3 r = x0 - ll;
-  r = r + (-1.0 * dot(r, nrm) / pdn) * p;
+  r = r + (-dot(r, nrm) * rcp_fast(pdn)) * p;
   int hit = 1;
   double rx = r.x * g.xhat[0] + r.y * g.xhat[1] + r.z * g.xhat[2];
   if ((dkey(rx) < 0) || (dkey(rx) >= dkey(g.xlen))) { if (must_hit) return 0; hit = 0; }
