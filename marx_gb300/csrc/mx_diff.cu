@@ -347,8 +347,12 @@ __device__ __forceinline__ float resid_at(const ImageGeom &g, const float *rw, c
 }
 
 // part[block][NP] = sum over the block's rays of dl/dimage . d(image)/dtheta
-// (before the 1/n_rays factor).
-__global__ void __launch_bounds__(DBLOCK) diff_adjoint_kernel(const __grid_constant__ AdjArgs args, uint64_t n,
+// (before the 1/n_rays factor).  Compiled for two resident blocks per SM
+// (128 registers): the tangents then spill about 600 bytes per thread to
+// local memory, but twice the warps hide the FP64 and load latencies that
+// left one block of 248 registers 43 % FP64-busy (2.45 -> 1.83 ms per 4e6
+// rays).
+__global__ void __launch_bounds__(DBLOCK, 2) diff_adjoint_kernel(const __grid_constant__ AdjArgs args, uint64_t n,
                                                                uint64_t seed, const uint8_t *codes,
                                                                const double *dl, double *part) {
   extern __shared__ __align__(16) unsigned char smem[];
