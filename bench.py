@@ -32,6 +32,8 @@ batch (no collective on the data path) and value = all photons / max time.
 from __future__ import annotations
 
 import argparse
+import contextlib
+import gc
 import json
 import os
 import statistics
@@ -299,13 +301,14 @@ def bench_diff(a, fp64_peak):
         d.mse(img, target, loss=loss)
         d.adjoint(theta, dl)
     torch.cuda.synchronize()
-    h0 = time.perf_counter()
-    for _ in range(k):
-        d.forward(theta, D.RECORD, out=img)
-        d.L.mx_diff_mse(d.h, img.data_ptr(), target.data_ptr(), dl.data_ptr(), loss.data_ptr(), stream.cuda_stream)
-        g_host = d.adjoint(theta, dl)
-        _ = float(loss.item())
-    e2e_s = (time.perf_counter() - h0) / k
+    with no_gc():
+        h0 = time.perf_counter()
+        for _ in range(k):
+            d.forward(theta, D.RECORD, out=img)
+            d.L.mx_diff_mse(d.h, img.data_ptr(), target.data_ptr(), dl.data_ptr(), loss.data_ptr(), stream.cuda_stream)
+            g_host = d.adjoint(theta, dl)
+            _ = float(loss.item())
+        e2e_s = (time.perf_counter() - h0) / k
     ops = Oracle(D.diff_mirror_config()).weighted_flops(D.diff_workload(n_rays=20000).cfg, theta)
     flops_per_ray = ops[0] / ops[1]
     n = w.cfg.n_rays
@@ -505,6 +508,21 @@ def run_reference(a):
     print(json.dumps(line))
 
 
+@contextlib.contextmanager
+def no_gc():
+    """Python's cyclic garbage collector off around a wall-clock timed loop
+    (as timeit does): a collection pause belongs to the harness, not to the
+    call being timed."""
+    gc.collect()
+    was = gc.isenabled()
+    gc.disable()
+    try:
+        yield
+    finally:
+        if was:
+            gc.enable()
+
+
 def e2e_host(eng, host, w, n, steps, warmup, world=1):
     """The metric through mx_trace_host: pinned host buffers in, every
     output column back in host memory, wall clock around each blocking
@@ -533,20 +551,22 @@ def e2e_host(eng, host, w, n, steps, warmup, world=1):
         eng.trace_host(hp, stages=w.stages, seed=2000 + s)
     barrier(world)
     e2e_s = 0.0
-    for s in range(steps):
-        # the step's inputs are put back in the pinned buffers outside the
-        # timed region; each timed call copies them in, traces and copies
-        # every output column back
-        pin["p"].copy_(p_in); pin["flags"].zero_()
-        t0 = time.perf_counter()
-        eng.trace_host(hp, stages=w.stages, seed=s)
-        e2e_s += time.perf_counter() - t0
+    with no_gc():
+        for s in range(steps):
+            # the step's inputs are put back in the pinned buffers outside the
+            # timed region; each timed call copies them in, traces and copies
+            # every output column back
+            pin["p"].copy_(p_in); pin["flags"].zero_()
+            t0 = time.perf_counter()
+            eng.trace_host(hp, stages=w.stages, seed=s)
+            e2e_s += time.perf_counter() - t0
     e2e_s = max_over_ranks(e2e_s, world)
     barrier(world)
     return {"value": world * n * steps / e2e_s, "unit": "photons/s",
             "h2d_bytes_per_step": in_b, "d2h_bytes_per_step": out_b,
             "note": "pinned host buffers; wall clock around each blocking mx_trace_host call (copies in, "
-                    "trace, copies out; the host-side reset of the step's inputs is not timed)"}
+                    "trace, copies out; the host-side reset of the step's inputs is not timed; Python's "
+                    "garbage collector off during the timed steps)"}
 
 
 def flops_per_photon(w):
